@@ -1,0 +1,320 @@
+"""Benchmark: Mrays/s of one rendered frame of the 1M-triangle spectral icosphere field on one GB300.
+
+Workload (one "step" = one frame): 800 icospheres x 1,280 triangles (1,024,000 triangles, seeded), 1920 x 1080,
+16 samples per pixel, path depth 12 (Russian roulette from depth 4), hero-wavelength spectral transport with 4
+wavelengths over 360-830 nm through a device-generated rgb2spec table (res 64), 1024 x 512 FP32 sky map with a
+5e3-radiance 0.5-degree sun, environment importance sampling with MIS, PCG32 seed 1. Synthetic, seeded data.
+
+value : rays (primary + extension + shadow, counted on the device) / device time of the render kernels, scene
+        resident in HBM, L2 flushed (256 MiB write) before every timed frame.
+e2e   : the same rays through the C ABI with host buffers: SceneData in from pinned host memory, the accumulation
+        image (RGBA32F) read back to pinned host memory every frame, timed on the host clock.
+--impl reference : the CPU restatement of vkrt's integrator (the oracle, a port: vkrt's own renderer needs Vulkan
+        and is unavailable here) on all host cores, on a bounded block of rows of the same frame per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s"
+WORKLOAD = "icosphere-field-1M-tris 1920x1080 16spp depth12 hero-spectral env-IS"
+
+
+def _config(width, height, spp, depth, tris, extra=None):
+    c = {"workload": WORKLOAD, "triangles": tris, "width": width, "height": height, "spp": spp, "max_depth": depth,
+         "render_mode": "spectral-hero-4", "rng": "pcg32 seed 1", "environment": "1024x512 fp32 sky + sun, IS+MIS",
+         "l2": "flushed before every timed frame (256 MiB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_launch():
+    """DRAM bytes per render-kernel launch from the committed ncu summary, when one exists."""
+    p = ROOT / "profiles" / "megakernel_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def build_scene(spp=16, depth=12, width=1920, height=1080, n_spheres=800):
+    from vkrt_gb300 import scenes
+    return scenes.icosphere_field(n_spheres=n_spheres, width=width, height=height, spp=spp, max_depth=depth, seed=1,
+                                  spectral=True)
+
+
+def run_ours(args) -> dict | None:
+    import torch
+    from vkrt_gb300 import RenderContext, abi
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    scene = build_scene()
+    ctx = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE)
+    table, info = ctx.generate_rgb2spec(64)  # device rgb2spec fit (setup, not timed)
+    scene.rgb2spec = table
+    scene.scene_data["rgb2specSRGB"] = info
+    ctx.upload_scene(scene)
+    sd = scene.scene_data.copy()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    frame = [rank * 100000]
+
+    def render_one(timed_events=None):
+        sd["frameNumber"] = frame[0]
+        frame[0] += 1
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            if timed_events is not None:
+                timed_events[0].record(stream)
+            ctx.render_frame(sd)
+            if timed_events is not None:
+                timed_events[1].record(stream)
+
+    # algorithmic bytes per frame (node + triangle fetches) from one counting frame of the same workload
+    cctx = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE,
+                         count_rays=True)
+    cctx.upload_scene(scene)
+    csd = scene.scene_data.copy()
+    csd["frameNumber"] = 999999
+    cctx.render_frame(csd)
+    cctx.sync()
+    cst = cctx.stats()
+    cctx.close()
+
+    for _ in range(args.warmup):
+        render_one()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    rays = 0
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        render_one(events[k])
+        ctx.sync()
+        st = ctx.stats()
+        rays += st["primaryRays"] + st["extensionRays"] + st["shadowRays"]
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in events]
+    total_ms = float(sum(ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        rt = torch.tensor([float(rays)], device=f"cuda:{local}")
+        torch.distributed.all_reduce(rt)
+        rays_all = int(rt.item())
+    else:
+        rays_all = rays
+    value = rays_all / (total_ms * 1e-3) / 1e6
+
+    # end to end through the C ABI: SceneData from pinned host memory in, accumulation to pinned host memory out
+    host_sd = torch.empty(abi.SCENE_DATA.itemsize, dtype=torch.uint8, pin_memory=True)
+    sd_view = np.frombuffer(host_sd.numpy(), dtype=abi.SCENE_DATA)
+    sd_view[:] = sd
+    out = torch.empty((ctx.height, ctx.width, 4), dtype=torch.float32, pin_memory=True)
+    out_np = out.numpy()
+    e2e_steps = max(1, min(args.steps, 5))
+    ctx.sync()
+    t0 = time.perf_counter()
+    e2e_rays = 0
+    for k in range(e2e_steps):
+        sd_view["frameNumber"] = frame[0]
+        frame[0] += 1
+        ctx.render_frame(sd_view)
+        ctx.read_accumulation(out_np)
+        st = ctx.stats()
+        e2e_rays += st["primaryRays"] + st["extensionRays"] + st["shadowRays"]
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_rays / e2e_s / 1e6
+
+    peak, peak_kind = _peaks()
+    frame_rays = cst["primaryRays"] + cst["extensionRays"] + cst["shadowRays"]
+    alg_bytes = cst["nodeFetchBytes"] + cst["triFetchBytes"]
+    mean_ms = total_ms / args.steps
+    achieved = alg_bytes / (mean_ms * 1e-3) / 1e9
+    result = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True,
+        "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded icosphere field, procedural sky)",
+        "config": _config(1920, 1080, 16, 12, scene.triangle_count,
+                          {"parallelism": f"replicas x{world} (independent sample sets)",
+                           "rays_per_frame": int(rays / args.steps), "bvh_nodes": cst["bvhNodeCount"],
+                           "bvh_mbytes": round(cst["bvhBytes"] / 2 ** 20, 1)}),
+        "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": abi.SCENE_DATA.itemsize,
+                "d2h_bytes_per_step": int(out.numel() * 4), "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": _traffic_per_launch(),
+                     "kernel": "kRenderMega<spectral>", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": int(alg_bytes),
+                     "note": "node (80 B) + triangle (48 B) fetches per launch / launch time; BVH is L2-resident"},
+        "clocks": clk,
+        "gpu_launches": args.steps,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(scene, budget_s=args.cpu_seconds)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return result if rank == 0 else None
+
+
+def cpu_baseline(scene, budget_s: float = 12.0, threads: int = 0) -> dict:
+    """The oracle (CPU restatement of vkrt's integrator, FP32) on all host cores, rows of the same frame."""
+    from oracle import cpu
+    from vkrt_gb300 import abi
+
+    sd = scene.scene_data.copy()
+    if scene.rgb2spec is None:
+        # no device table on this path: the oracle's own fit (the per-lookup cost does not depend on res)
+        scene.rgb2spec = cpu.rgb2spec_generate(16, threads)
+        sd["rgb2specSRGB"] = (16, 0, 16)
+    orc = cpu.OracleScene(scene, environment_sampling=abi.ENV_IMPORTANCE)
+    ncores = threads or os.cpu_count() or 1
+    rows = 2
+    acc = None
+    t0 = time.perf_counter()
+    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(540, 540 + rows), threads=threads)
+    dt = time.perf_counter() - t0
+    rows = int(max(2, min(1080 - 540, rows * budget_s / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(540 - rows // 2, 540 - rows // 2 + rows), threads=threads)
+    dt = time.perf_counter() - t0
+    rays = st["primaryRays"] + st["extensionRays"] + st["shadowRays"]
+    orc.close()
+    return {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": ncores, "kind": "port",
+            "sample": f"{rows} rows x 1920 px x 16 spp of the same frame ({rays} rays, {dt:.1f} s)"}
+
+
+def run_reference(args) -> dict | None:
+    rank, world, _ = _dist()
+    if rank != 0:
+        return None
+    scene = build_scene()
+    steps = []
+    res = None
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(scene, budget_s=args.cpu_seconds)
+        if k >= args.warmup:
+            steps.append(r)
+        res = r
+    value = float(np.mean([s["value"] for s in steps]))
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere field, procedural sky)",
+            "config": _config(1920, 1080, 16, 12, scene.triangle_count),
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": res["cores"], "kind": "port",
+                             "sample": res["sample"]},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "vkrt's own renderer needs Vulkan ray tracing (no graphics stack on this box): the CPU "
+                    "restatement of its integrator stands in"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,174 @@
+/*
+ * vkrt_cuda.h — C ABI of the GB300 (sm_103a) path-tracing backend for vkrt.
+ *
+ * The backend replaces vkrt's Vulkan ray-tracing dispatch: the body of recordMainTracePass
+ * (src/core/runtime/command/record.c:448-486, vkCmdTraceRaysKHR(W,H,1)), the per-mesh BLAS / TLAS builds it
+ * traverses (src/core/render/accel/blas.c:14-262, tlas.c:291-346) and the descriptor bindings the ray-generation
+ * shader reads (src/shaders/scene/resources.slang:7-59). Everything here takes plain host pointers and counts;
+ * records use the vkrt layouts from vkrt_cuda_types.h. One context = one device, one CUDA stream, one film.
+ * Like vkrt's API (src/core/api/vkrt.h), calls on a context are not thread-safe: the caller serialises them.
+ *
+ * Results are vkrt's VKRT_Result codes (src/core/api/vkrt_types.h:16-26).
+ */
+#ifndef VKRT_CUDA_H
+#define VKRT_CUDA_H
+
+#include "vkrt_cuda_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* VKRT_Result values (vkrt_types.h:16-26) */
+#define VKRT_CUDA_SUCCESS 0
+#define VKRT_CUDA_ERROR_INVALID_ARGUMENT (-1)
+#define VKRT_CUDA_ERROR_OPERATION_FAILED (-2)
+#define VKRT_CUDA_ERROR_OUT_OF_MEMORY (-3)
+#define VKRT_CUDA_ERROR_DEVICE_LOST (-4)
+#define VKRT_CUDA_ERROR_INITIALIZATION_FAILED (-5)
+
+/* random-number stream of the path sampler */
+#define VKRT_CUDA_RNG_REFERENCE 0u /* vkrt's Wellons-hash stream, seed = f(pixel, frame, sample): random.slang:7-27 */
+#define VKRT_CUDA_RNG_PCG32 1u     /* PCG32 (O'Neill 2014), one stream per (pixel, sample), state from rngSeed */
+
+/* environment-light estimator */
+#define VKRT_CUDA_ENV_BSDF_ONLY 0u   /* vkrt: environment only on BSDF-sampled misses (environment.slang:16-27) */
+#define VKRT_CUDA_ENV_IMPORTANCE 1u  /* equirect luminance*sin(theta) importance sampling + MIS with the BSDF */
+
+typedef struct VKRT_CudaContext VKRT_CudaContext;
+
+typedef struct VKRT_CudaConfig {
+    int32_t deviceIndex;          /* CUDA device ordinal */
+    uint32_t rngMode;             /* VKRT_CUDA_RNG_* */
+    uint64_t rngSeed;             /* PCG32 seed (ignored by the reference stream) */
+    uint32_t environmentSampling; /* VKRT_CUDA_ENV_* */
+    uint32_t countRays;           /* 1: keep per-frame ray counters (primary / extension / shadow) */
+    uint32_t threadsPerBlock;     /* megakernel block size, 0 = default (128) */
+    uint32_t blocksPerSM;         /* persistent megakernel residency, 0 = default */
+    uint32_t reserved[8];
+} VKRT_CudaConfig;
+
+typedef struct VKRT_CudaStats {
+    uint64_t primaryRays;    /* camera rays traced by the last render call */
+    uint64_t extensionRays;  /* closest-hit rays after the first bounce */
+    uint64_t shadowRays;     /* any-hit (occlusion) rays */
+    uint64_t pathSamples;    /* pixel samples started */
+    uint64_t nodeFetchBytes; /* BVH node bytes fetched (only with countRays) */
+    uint64_t triFetchBytes;  /* triangle bytes fetched (only with countRays) */
+    uint32_t bvhNodeCount;   /* 8-wide nodes */
+    uint32_t bvhTriangleCount;
+    uint64_t bvhBytes;       /* nodes + triangle records resident in HBM */
+    float bvhBuildMs;        /* device time of the last BVH build */
+    uint32_t errorFlags;     /* device-side error word (bit 0: traversal stack overflow guard hit) */
+} VKRT_CudaStats;
+
+/* ray record for the trace entry points: origin/tMin, direction/tMax (32 bytes, 16-byte aligned) */
+typedef struct VKRT_CudaRay {
+    float origin[3];
+    float tMin;
+    float direction[3];
+    float tMax;
+} VKRT_CudaRay;
+
+/* closest-hit record: the payload vkrt's closest-hit shader stores (entry/path/closest_hit.slang:3-5,
+ * rt/payloads/scene_payload.slang:6-43). Misses report instanceIndex = primitiveIndex = VKRT_CUDA_INVALID_INDEX. */
+typedef struct VKRT_CudaHit {
+    uint32_t instanceIndex;  /* mesh index (TLAS instance) */
+    uint32_t primitiveIndex; /* triangle index within the mesh */
+    float t;
+    float u; /* barycentric weight of vertex 1 */
+    float v; /* barycentric weight of vertex 2 */
+    uint32_t reserved[3];
+} VKRT_CudaHit;
+
+void vkrt_cuda_default_config(VKRT_CudaConfig* config);
+
+/* Creates a context on config->deviceIndex (NULL config = defaults). Replaces VKRT_initWithCreateInfo's device and
+ * pipeline setup (src/core/api/lifecycle.c:586-610) for the tracing path. */
+int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** outContext);
+void vkrt_cuda_destroy(VKRT_CudaContext* context);
+
+/* Uploads the global vertex/index buffers and mesh records and builds the BVH on the device (Morton codes, radix
+ * sort, LBVH, treelet refinement, 8-wide compressed collapse). Indices are mesh-relative, addressed through
+ * MeshInfo.indexBase and offset by MeshInfo.vertexBase, exactly as loadTriangleVertices reads them
+ * (geometry/surface/interpolation.slang:8-25). Replaces the BLAS/TLAS builds (record.c:124-168). */
+int32_t vkrt_cuda_upload_geometry(VKRT_CudaContext* context, const VKRT_CudaShaderVertex* vertices,
+                                  uint32_t vertexCount, const uint32_t* indices, uint32_t indexCount,
+                                  const VKRT_CudaMeshInfo* meshes, uint32_t meshCount);
+
+/* Replaces the mesh records only (transform / material / lightPdfArea edits); rebuilds the BVH when a transform
+ * changed. Counts must match the last upload. */
+int32_t vkrt_cuda_update_meshes(VKRT_CudaContext* context, const VKRT_CudaMeshInfo* meshes, uint32_t meshCount);
+
+int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* context, const VKRT_CudaMaterial* materials, uint32_t count);
+
+/* Emissive-light tables for NEE (lighting.c:496-544 builds them; light_sampling.slang:9-37 reads them). */
+int32_t vkrt_cuda_upload_lights(VKRT_CudaContext* context, const VKRT_CudaEmissiveMesh* meshes, uint32_t meshCount,
+                                const VKRT_CudaEmissiveTriangle* triangles, uint32_t triangleCount,
+                                const float* meshAliasQ, const uint32_t* meshAliasIdx, const float* triAliasQ,
+                                const uint32_t* triAliasIdx);
+
+/* Bindless texture slot `textureIndex` (< VKRT_CUDA_MAX_TEXTURES), sampled bilinearly without mips as vkrt's
+ * samplers do (src/core/scene/textures.c:141-164). format: VKRT_CUDA_TEXTURE_FORMAT_*; colorSpace SRGB decodes
+ * 8/16-bit UNORM texels to linear. */
+int32_t vkrt_cuda_upload_texture(VKRT_CudaContext* context, uint32_t textureIndex, const void* pixels,
+                                 uint32_t width, uint32_t height, uint32_t format, uint32_t colorSpace);
+
+/* Selects the environment texture used for importance sampling and builds its 2D CDF (FP64 prefix sums) on the
+ * device; VKRT_CUDA_INVALID_INDEX = constant environment colour. The texture index and rotation that shading
+ * uses still come from SceneData.environmentTextureIndex / environmentRotation each frame. */
+int32_t vkrt_cuda_set_environment(VKRT_CudaContext* context, uint32_t textureIndex);
+
+/* rgb2spec coefficient table in vkrt's buffer layout: `res` z-scale floats followed by 3*res^3*3 coefficients
+ * (src/core/scene/rgb2spec.c:17-89). */
+int32_t vkrt_cuda_upload_rgb2spec(VKRT_CudaContext* context, const float* table, uint32_t floatCount,
+                                  const VKRT_CudaRGB2SpecTableInfo* info);
+
+/* Generates the sRGB rgb2spec table on the device (Jakob & Hanika 2019 Gauss-Newton fit against the CIE 1931
+ * analytic fits under illuminant E, the colour space of vkrt's spectral output transform) and installs it.
+ * Returns the table layout in outInfo; the table stays resident. */
+int32_t vkrt_cuda_generate_rgb2spec(VKRT_CudaContext* context, uint32_t res, VKRT_CudaRGB2SpecTableInfo* outInfo);
+int32_t vkrt_cuda_download_rgb2spec(VKRT_CudaContext* context, float* table, uint32_t floatCount);
+
+/* (Re)allocates the film: accumulation RGBA32F ping-pong (.w = sample count) and the RGBA16 UNORM output; clears. */
+int32_t vkrt_cuda_resize(VKRT_CudaContext* context, uint32_t width, uint32_t height);
+
+/* Clears the accumulation film (the accumulationNeedsReset clear, record.c:300-446). */
+int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* context);
+
+/* Renders one frame: SceneData.samplesPerPixel samples per pixel blended into the running mean, then swaps the
+ * ping-pong accumulation images (VKRT_trace -> recordMainTracePass plus the swap in VKRT_endFrame,
+ * src/core/api/frame.c:267-337,380-390). Asynchronous on the context stream; SceneData is copied at call time. */
+int32_t vkrt_cuda_render_frame(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData);
+
+/* Waits for all work on the context stream, polling up to timeoutMs (0 = wait without limit). Returns
+ * VKRT_CUDA_ERROR_OPERATION_FAILED on timeout, VKRT_CUDA_ERROR_DEVICE_LOST on a CUDA error. */
+int32_t vkrt_cuda_sync(VKRT_CudaContext* context, uint32_t timeoutMs);
+
+/* Copies the latest accumulation (RGBA32F, .w = samples; linear sRGB in RGB mode, CIE XYZ in spectral mode) or
+ * the tone-mapped RGBA16 UNORM output to host memory; `bytes` must be >= width*height*16 (resp. *8). */
+int32_t vkrt_cuda_read_accumulation(VKRT_CudaContext* context, float* rgba, size_t bytes);
+int32_t vkrt_cuda_read_output(VKRT_CudaContext* context, uint16_t* rgba, size_t bytes);
+
+int32_t vkrt_cuda_get_stats(VKRT_CudaContext* context, VKRT_CudaStats* stats);
+
+/* CUDA stream (cudaStream_t) the context launches on, for callers that time or order work around it. */
+void* vkrt_cuda_stream(VKRT_CudaContext* context);
+
+/* Traces `count` rays against the current BVH: anyHit = 0 gives the closest hit (vkrt's scene query,
+ * rt/queries/scene_query.slang:10-42), anyHit = 1 stops at the first accepted hit (shadow query,
+ * rt/queries/shadow_query.slang:8-28; the record then carries that hit). Host arrays; synchronous. */
+int32_t vkrt_cuda_trace_rays(VKRT_CudaContext* context, const VKRT_CudaRay* rays, uint32_t count, uint32_t anyHit,
+                             VKRT_CudaHit* hits);
+/* Same on device arrays, asynchronous on the context stream. */
+int32_t vkrt_cuda_trace_rays_device(VKRT_CudaContext* context, const VKRT_CudaRay* deviceRays, uint32_t count,
+                                    uint32_t anyHit, VKRT_CudaHit* deviceHits);
+
+/* Last error message of this context (never NULL). */
+const char* vkrt_cuda_last_error(VKRT_CudaContext* context);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VKRT_CUDA_H */

@@ -1,0 +1,59 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares; record layouts match vkrt's."""
+import json
+import re
+from pathlib import Path
+
+import numpy as np
+
+from vkrt_gb300 import abi
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b(vkrt_(?:cuda|host)_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = abi.load(build_if_missing=False)
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert names <= set(abi.EXPORTS), sorted(names - set(abi.EXPORTS))
+
+
+def test_record_sizes_match_vkrt():
+    ref = json.loads((ROOT / "tests/golden/layouts.json").read_text())
+    assert abi.VERTEX.itemsize == ref["Vertex"]
+    assert abi.SHADER_VERTEX.itemsize == ref["ShaderVertex"]
+    assert abi.MESH_INFO.itemsize == ref["MeshInfo"]
+    assert abi.MATERIAL.itemsize == ref["Material"]
+    assert abi.EMISSIVE_MESH.itemsize == ref["EmissiveMesh"]
+    assert abi.EMISSIVE_TRIANGLE.itemsize == ref["EmissiveTriangle"]
+    assert abi.SCENE_DATA.itemsize == ref["SceneData"]
+
+
+def test_host_defaults_read_through_the_layouts(built):
+    """vkrt defaults written by the C host library land on the numpy field offsets (vkrt_types.h:79-121,
+    uniform.c:93-174)."""
+    lib = abi.load()
+    m = np.zeros(1, abi.MATERIAL)
+    lib.vkrt_host_default_material(abi.ptr(m))
+    assert np.allclose(m["baseColor"], 0.8) and m["roughness"] == np.float32(0.5) and m["ior"] == np.float32(1.5)
+    assert m["baseColorTextureIndex"] == abi.INVALID_INDEX and m["emissiveTextureIndex"] == abi.INVALID_INDEX
+    assert np.allclose(m["baseColorTextureTransform"], [1, 1, 0, 0]) and m["opacity"] == 1.0
+    sd = np.zeros(1, abi.SCENE_DATA)
+    lib.vkrt_host_default_scene_data(640, 480, abi.ptr(sd))
+    assert sd["samplesPerPixel"] == 8 and sd["rrMaxDepth"] == 8 and sd["rrMinDepth"] == 4
+    assert list(sd["viewportRect"][0]) == [0, 0, 640, 480]
+    assert sd["environmentTextureIndex"] == abi.INVALID_INDEX and sd["misNeeEnabled"] == 1
+    assert np.allclose(sd["environmentLight"][0], [0.25, 0.25, 0.25, 1.0])
+    assert sd["packedRenderSettings"] == abi.pack_render_settings(1, 0, 1)
+    # camera at (-0.5, 0.2, -0.2): the inverse view's translation column is the eye position
+    assert np.allclose(sd["viewInverse"][0][3, :3], [-0.5, 0.2, -0.2], atol=1e-6)

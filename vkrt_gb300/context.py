@@ -1,0 +1,228 @@
+"""Python host mirror of the backend's C ABI: one RenderContext per CUDA context.
+
+This is the operator interface a Python caller (tests, bench, tools) uses; every call goes straight to
+libvkrt_gb300.so. There is no CPU path: a missing or failing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+
+class VkrtError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"VKRT_Result {code}: {message}")
+        self.code = code
+
+
+@dataclass
+class Scene:
+    """All host arrays of one scene, in vkrt's record layouts (see abi.py)."""
+    vertices: np.ndarray                  # VERTEX (authoring vertices)
+    indices: np.ndarray                   # uint32, mesh-relative
+    meshes: np.ndarray                    # MESH_INFO
+    materials: np.ndarray                 # MATERIAL
+    scene_data: np.ndarray                # SCENE_DATA, shape (1,)
+    textures: dict = field(default_factory=dict)   # slot -> float32 (H, W, 4) linear RGBA
+    env_texture: int = abi.INVALID_INDEX  # slot used for importance sampling
+    shader_vertices: np.ndarray | None = None
+    emissive_meshes: np.ndarray | None = None
+    emissive_triangles: np.ndarray | None = None
+    mesh_alias_q: np.ndarray | None = None
+    mesh_alias_idx: np.ndarray | None = None
+    tri_alias_q: np.ndarray | None = None
+    tri_alias_idx: np.ndarray | None = None
+    rgb2spec: np.ndarray | None = None    # float32 table in vkrt's layout
+    name: str = ""
+
+    @property
+    def triangle_count(self) -> int:
+        return int(self.meshes["indexCount"].sum() // 3)
+
+    @property
+    def width(self) -> int:
+        return int(self.scene_data["viewportRect"][0][2])
+
+    @property
+    def height(self) -> int:
+        return int(self.scene_data["viewportRect"][0][3])
+
+
+def pack_vertices(vertices: np.ndarray) -> np.ndarray:
+    lib = abi.load()
+    v = np.ascontiguousarray(vertices, dtype=abi.VERTEX)
+    out = np.zeros(len(v), dtype=abi.SHADER_VERTEX)
+    lib.vkrt_host_pack_shader_vertices(abi.ptr(v), len(v), abi.ptr(out))
+    return out
+
+
+def build_light_tables(scene: Scene) -> None:
+    """Fills the emissive-light tables and MeshInfo.lightPdfArea with the host library (vkrt's lighting.c rules)."""
+    lib = abi.load()
+    tri_cap = max(1, scene.triangle_count)
+    mesh_cap = max(1, len(scene.meshes))
+    em = np.zeros(mesh_cap, dtype=abi.EMISSIVE_MESH)
+    et = np.zeros(tri_cap, dtype=abi.EMISSIVE_TRIANGLE)
+    mq = np.zeros(mesh_cap, dtype=np.float32)
+    mi = np.zeros(mesh_cap, dtype=np.uint32)
+    tq = np.zeros(tri_cap, dtype=np.float32)
+    ti = np.zeros(tri_cap, dtype=np.uint32)
+    nm = C.c_uint32(0)
+    nt = C.c_uint32(0)
+    r = lib.vkrt_host_build_light_tables(
+        abi.ptr(scene.meshes), len(scene.meshes), abi.ptr(scene.materials), len(scene.materials),
+        abi.ptr(scene.vertices), abi.ptr(scene.indices), abi.ptr(em), mesh_cap, abi.ptr(et), tri_cap, abi.ptr(mq),
+        abi.ptr(mi), abi.ptr(tq), abi.ptr(ti), C.byref(nm), C.byref(nt))
+    if r != 0:
+        raise VkrtError(r, "building light tables")
+    scene.emissive_meshes = em[: nm.value].copy()
+    scene.emissive_triangles = et[: nt.value].copy()
+    scene.mesh_alias_q, scene.mesh_alias_idx = mq[: nm.value].copy(), mi[: nm.value].copy()
+    scene.tri_alias_q, scene.tri_alias_idx = tq[: nt.value].copy(), ti[: nt.value].copy()
+    scene.scene_data["emissiveMeshCount"] = nm.value
+    scene.scene_data["emissiveTriangleCount"] = nt.value
+
+
+class RenderContext:
+    """A CUDA context of the backend: scene buffers, BVH, film and one stream."""
+
+    def __init__(self, device: int = 0, rng_mode: int = abi.RNG_REFERENCE, rng_seed: int = 1,
+                 environment_sampling: int = abi.ENV_BSDF_ONLY, count_rays: bool = False):
+        self.lib = abi.load()
+        cfg = np.zeros(1, dtype=abi.CONFIG)
+        self.lib.vkrt_cuda_default_config(abi.ptr(cfg))
+        cfg["deviceIndex"] = device
+        cfg["rngMode"] = rng_mode
+        cfg["rngSeed"] = rng_seed
+        cfg["environmentSampling"] = environment_sampling
+        cfg["countRays"] = 1 if count_rays else 0
+        handle = C.c_void_p()
+        r = self.lib.vkrt_cuda_create(abi.ptr(cfg), C.byref(handle))
+        if r != abi.SUCCESS:
+            raise VkrtError(r, "vkrt_cuda_create (is a CUDA device visible?)")
+        self.handle = handle
+        self.width = 0
+        self.height = 0
+        self.scene: Scene | None = None
+
+    # -- plumbing ----------------------------------------------------------------------------------------------
+    def _check(self, r: int, what: str) -> None:
+        if r != abi.SUCCESS:
+            msg = self.lib.vkrt_cuda_last_error(self.handle)
+            raise VkrtError(r, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.vkrt_cuda_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.vkrt_cuda_stream(self.handle) or 0)
+
+    # -- scene -------------------------------------------------------------------------------------------------
+    def upload_scene(self, scene: Scene, generate_rgb2spec_res: int | None = None) -> None:
+        if scene.shader_vertices is None:
+            scene.shader_vertices = pack_vertices(scene.vertices)
+        sv, idx = scene.shader_vertices, np.ascontiguousarray(scene.indices, dtype=np.uint32)
+        self._check(self.lib.vkrt_cuda_upload_materials(self.handle, abi.ptr(scene.materials), len(scene.materials)),
+                    "upload materials")
+        self._check(self.lib.vkrt_cuda_upload_geometry(self.handle, abi.ptr(sv), len(sv), abi.ptr(idx), len(idx),
+                                                       abi.ptr(scene.meshes), len(scene.meshes)), "upload geometry")
+        if scene.emissive_meshes is not None and len(scene.emissive_meshes):
+            self._check(self.lib.vkrt_cuda_upload_lights(
+                self.handle, abi.ptr(scene.emissive_meshes), len(scene.emissive_meshes),
+                abi.ptr(scene.emissive_triangles), len(scene.emissive_triangles), abi.ptr(scene.mesh_alias_q),
+                abi.ptr(scene.mesh_alias_idx), abi.ptr(scene.tri_alias_q), abi.ptr(scene.tri_alias_idx)),
+                "upload lights")
+        for slot, tex in scene.textures.items():
+            self.upload_texture(slot, tex)
+        if scene.env_texture != abi.INVALID_INDEX:
+            self._check(self.lib.vkrt_cuda_set_environment(self.handle, scene.env_texture), "set environment")
+        if scene.rgb2spec is not None:
+            info = np.array([scene.scene_data["rgb2specSRGB"][0]], dtype=np.uint32).reshape(3)
+            self._check(self.lib.vkrt_cuda_upload_rgb2spec(self.handle, abi.ptr(scene.rgb2spec), len(scene.rgb2spec),
+                                                           abi.ptr(info)), "upload rgb2spec")
+        elif generate_rgb2spec_res:
+            info = np.zeros(3, dtype=np.uint32)
+            self._check(self.lib.vkrt_cuda_generate_rgb2spec(self.handle, generate_rgb2spec_res, abi.ptr(info)),
+                        "generate rgb2spec")
+            scene.scene_data["rgb2specSRGB"] = info
+        self.resize(scene.width, scene.height)
+        self.scene = scene
+
+    def upload_texture(self, slot: int, rgba: np.ndarray, fmt: int = abi.TEXTURE_FORMAT_RGBA32_SFLOAT,
+                       color_space: int = abi.COLOR_SPACE_LINEAR) -> None:
+        a = np.ascontiguousarray(rgba)
+        h, w = a.shape[0], a.shape[1]
+        self._check(self.lib.vkrt_cuda_upload_texture(self.handle, slot, abi.ptr(a), w, h, fmt, color_space),
+                    "upload texture")
+
+    def update_meshes(self, meshes: np.ndarray) -> None:
+        self._check(self.lib.vkrt_cuda_update_meshes(self.handle, abi.ptr(meshes), len(meshes)), "update meshes")
+
+    def generate_rgb2spec(self, res: int) -> tuple[np.ndarray, np.ndarray]:
+        info = np.zeros(3, dtype=np.uint32)
+        self._check(self.lib.vkrt_cuda_generate_rgb2spec(self.handle, res, abi.ptr(info)), "generate rgb2spec")
+        table = np.zeros(res + 9 * res ** 3, dtype=np.float32)
+        self._check(self.lib.vkrt_cuda_download_rgb2spec(self.handle, abi.ptr(table), len(table)), "download rgb2spec")
+        return table, info
+
+    # -- film / frames -----------------------------------------------------------------------------------------
+    def resize(self, width: int, height: int) -> None:
+        self._check(self.lib.vkrt_cuda_resize(self.handle, width, height), "resize")
+        self.width, self.height = width, height
+
+    def reset_accumulation(self) -> None:
+        self._check(self.lib.vkrt_cuda_reset_accumulation(self.handle), "reset accumulation")
+
+    def render_frame(self, scene_data: np.ndarray) -> None:
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA)
+        self._check(self.lib.vkrt_cuda_render_frame(self.handle, abi.ptr(sd)), "render frame")
+
+    def sync(self, timeout_ms: int = 0) -> None:
+        self._check(self.lib.vkrt_cuda_sync(self.handle, timeout_ms), "sync")
+
+    def read_accumulation(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 4), dtype=np.float32)
+        self._check(self.lib.vkrt_cuda_read_accumulation(self.handle, abi.ptr(out), out.nbytes), "read accumulation")
+        return out
+
+    def read_output(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), dtype=np.uint16)
+        self._check(self.lib.vkrt_cuda_read_output(self.handle, abi.ptr(out), out.nbytes), "read output")
+        return out
+
+    def stats(self) -> dict:
+        st = np.zeros(1, dtype=abi.STATS)
+        self._check(self.lib.vkrt_cuda_get_stats(self.handle, abi.ptr(st)), "stats")
+        return {k: st[k][0].item() for k in abi.STATS.names}
+
+    def trace_rays(self, rays: np.ndarray, any_hit: bool = False) -> np.ndarray:
+        r = np.ascontiguousarray(rays, dtype=abi.RAY)
+        hits = np.zeros(len(r), dtype=abi.HIT)
+        self._check(self.lib.vkrt_cuda_trace_rays(self.handle, abi.ptr(r), len(r), 1 if any_hit else 0,
+                                                  abi.ptr(hits)), "trace rays")
+        return hits
+
+    def trace_rays_device(self, rays_ptr: int, count: int, hits_ptr: int, any_hit: bool = False) -> None:
+        self._check(self.lib.vkrt_cuda_trace_rays_device(self.handle, C.c_void_p(rays_ptr), count,
+                                                         1 if any_hit else 0, C.c_void_p(hits_ptr)),
+                    "trace rays (device)")

@@ -1,0 +1,651 @@
+// capi.cu — the extern "C" boundary declared in include/vkrt_cuda.h.
+//
+// A context owns one CUDA stream and every device buffer of one scene; uploads copy caller arrays (vkrt copies at
+// upload too, src/core/scene/geometry.c:411-429) and kernels read only context memory. Errors follow VKRT_Result:
+// invalid arguments -1, other failures -2, allocation failures -3, CUDA faults that poison the context -4.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "bvh_build.h"
+#include "render.h"
+#include "scene.cuh"
+#include "vkrt_cuda.h"
+#include "vkrt_cuda_host.h"
+
+using namespace vkrt;
+
+namespace {
+
+template <class T>
+struct DeviceArray {
+    T* ptr = nullptr;
+    size_t count = 0;
+    cudaError_t assign(const T* host, size_t n, cudaStream_t s) {
+        cudaError_t e = reserve(n);
+        if (e != cudaSuccess || n == 0) return e;
+        return cudaMemcpyAsync(ptr, host, sizeof(T) * n, cudaMemcpyHostToDevice, s);
+    }
+    cudaError_t reserve(size_t n) {
+        if (n <= count && ptr) return cudaSuccess;
+        release();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&ptr, sizeof(T) * n);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return e;
+        }
+        count = n;
+        return cudaSuccess;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+};
+
+}  // namespace
+
+struct VKRT_CudaContext {
+    VKRT_CudaConfig cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string lastError = "";
+
+    // geometry
+    DeviceArray<VKRT_CudaShaderVertex> vertices;
+    DeviceArray<uint32_t> indices;
+    DeviceArray<VKRT_CudaMeshInfo> meshes;
+    std::vector<VKRT_CudaMeshInfo> hostMeshes;
+    uint32_t vertexCount = 0, indexCount = 0, triCount = 0;
+    BvhBuffers bvh;
+    BvhBuildStats bvhStats{};
+
+    // materials, lights
+    DeviceArray<VKRT_CudaMaterial> materials;
+    uint32_t materialCount = 0;
+    DeviceArray<VKRT_CudaEmissiveMesh> emissiveMeshes;
+    DeviceArray<VKRT_CudaEmissiveTriangle> emissiveTriangles;
+    DeviceArray<float> meshAliasQ, triAliasQ;
+    DeviceArray<uint32_t> meshAliasIdx, triAliasIdx;
+    uint32_t emissiveMeshCount = 0, emissiveTriangleCount = 0;
+
+    // textures: one RGBA32F buffer per bound slot and the descriptor table the kernels index
+    std::vector<DeviceArray<float4>> textureData;
+    std::vector<TextureDesc> textureDescs;
+    DeviceArray<TextureDesc> textureTable;
+    bool textureTableDirty = true;
+
+    // spectral table
+    DeviceArray<float> rgb2spec;
+    uint32_t rgb2specFloats = 0;
+    VKRT_CudaRGB2SpecTableInfo rgb2specInfo{};
+
+    // environment distribution
+    DeviceArray<float> envMarginal, envConditional, envTexelPdf;
+    DeviceArray<double> envScratch;
+    uint32_t envWidth = 0, envHeight = 0, envTexture = VKRT_CUDA_INVALID_INDEX;
+
+    // film
+    DeviceArray<float4> accum[2];
+    DeviceArray<ushort4> output;
+    uint32_t width = 0, height = 0;
+    int readIndex = 0;
+
+    // counters
+    RenderCounters* counters = nullptr;
+    RenderCounters lastCounters{};
+    bool countersPending = false;
+};
+
+namespace {
+
+int32_t fail(VKRT_CudaContext* c, cudaError_t e, const char* what) {
+    if (c) c->lastError = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return VKRT_CUDA_ERROR_OUT_OF_MEMORY;
+    // errors that leave the context unusable
+    if (e == cudaErrorIllegalAddress || e == cudaErrorLaunchFailure || e == cudaErrorIllegalInstruction ||
+        e == cudaErrorMisalignedAddress || e == cudaErrorHardwareStackError || e == cudaErrorAssert ||
+        e == cudaErrorLaunchTimeout || e == cudaErrorECCUncorrectable)
+        return VKRT_CUDA_ERROR_DEVICE_LOST;
+    return VKRT_CUDA_ERROR_OPERATION_FAILED;
+}
+
+int32_t invalid(VKRT_CudaContext* c, const char* what) {
+    if (c) c->lastError = std::string("invalid argument: ") + what;
+    return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+}
+
+#define VKRT_TRY(ctx, expr, what)                      \
+    do {                                               \
+        cudaError_t _e = (expr);                       \
+        if (_e != cudaSuccess) return fail(ctx, _e, what); \
+    } while (0)
+
+bool isIdentityTRS(const VKRT_CudaMeshInfo& m) {
+    return m.position[0] == 0.0f && m.position[1] == 0.0f && m.position[2] == 0.0f && m.rotation[0] == 0.0f &&
+           m.rotation[1] == 0.0f && m.rotation[2] == 0.0f && m.scale[0] == 1.0f && m.scale[1] == 1.0f &&
+           m.scale[2] == 1.0f;
+}
+
+cudaError_t rebuildBvh(VKRT_CudaContext* c) {
+    std::vector<float> world(size_t(c->hostMeshes.size()) * 16);
+    std::vector<uint32_t> ident(c->hostMeshes.size());
+    for (size_t i = 0; i < c->hostMeshes.size(); ++i) {
+        const VKRT_CudaMeshInfo& m = c->hostMeshes[i];
+        vkrt_host_mesh_transform(m.position, m.rotation, m.scale, &world[i * 16]);
+        ident[i] = isIdentityTRS(m) ? 1u : 0u;
+    }
+    BvhBuildInput in;
+    in.vertices = c->vertices.ptr;
+    in.indices = c->indices.ptr;
+    in.meshes = c->meshes.ptr;
+    in.hostMeshes = c->hostMeshes.data();
+    in.hostWorld = world.data();
+    in.hostIdentity = ident.data();
+    in.meshCount = uint32_t(c->hostMeshes.size());
+    in.triCount = c->triCount;
+    return buildBvh(in, c->bvh, &c->bvhStats, c->stream);
+}
+
+DeviceScene makeDeviceScene(VKRT_CudaContext* c) {
+    if (c->textureTableDirty) {
+        c->textureTable.assign(c->textureDescs.data(), c->textureDescs.size(), c->stream);
+        c->textureTableDirty = false;
+    }
+    DeviceScene s{};
+    s.nodes = c->bvh.nodes;
+    s.tris = c->bvh.tris;
+    s.nodeCount = c->bvh.nodeCount;
+    s.triCount = c->bvh.triCount;
+    s.vertices = c->vertices.ptr;
+    s.indices = c->indices.ptr;
+    s.meshes = c->meshes.ptr;
+    s.meshCount = uint32_t(c->hostMeshes.size());
+    s.materials = c->materials.ptr;
+    s.materialCount = c->materialCount;
+    s.emissiveMeshes = c->emissiveMeshes.ptr;
+    s.emissiveTriangles = c->emissiveTriangles.ptr;
+    s.meshAliasQ = c->meshAliasQ.ptr;
+    s.meshAliasIdx = c->meshAliasIdx.ptr;
+    s.triAliasQ = c->triAliasQ.ptr;
+    s.triAliasIdx = c->triAliasIdx.ptr;
+    s.emissiveMeshCount = c->emissiveMeshCount;
+    s.emissiveTriangleCount = c->emissiveTriangleCount;
+    s.textures = c->textureTable.ptr;
+    s.rgb2spec = c->rgb2spec.ptr;
+    s.rgb2specFloatCount = c->rgb2specFloats;
+    s.env.marginal = c->envMarginal.ptr;
+    s.env.conditional = c->envConditional.ptr;
+    s.env.texelPdf = c->envTexelPdf.ptr;
+    s.env.width = c->envWidth;
+    s.env.height = c->envHeight;
+    s.env.textureIndex = c->envTexture;
+    return s;
+}
+
+uint16_t halfToFloatBits(uint16_t h, float& out) {
+    uint32_t sign = (h >> 15) & 1u, exp = (h >> 10) & 0x1Fu, man = h & 0x3FFu;
+    float v;
+    if (exp == 0) v = std::ldexp(float(man), -24);
+    else if (exp == 31) v = man ? NAN : INFINITY;
+    else v = std::ldexp(float(man | 0x400u), int(exp) - 25);
+    out = sign ? -v : v;
+    return 0;
+}
+
+float srgbToLinear(float c) { return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f); }
+
+}  // namespace
+
+extern "C" {
+
+void vkrt_cuda_default_config(VKRT_CudaConfig* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->deviceIndex = 0;
+    cfg->rngMode = VKRT_CUDA_RNG_REFERENCE;
+    cfg->rngSeed = 1u;
+    cfg->environmentSampling = VKRT_CUDA_ENV_BSDF_ONLY;
+    cfg->countRays = 0u;
+    cfg->threadsPerBlock = 0u;
+    cfg->blocksPerSM = 0u;
+}
+
+int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** out) {
+    if (!out) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    VKRT_CudaConfig cfg;
+    if (config) cfg = *config;
+    else vkrt_cuda_default_config(&cfg);
+    if (cfg.rngMode > VKRT_CUDA_RNG_PCG32 || cfg.environmentSampling > VKRT_CUDA_ENV_IMPORTANCE)
+        return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0 || cfg.deviceIndex < 0 || cfg.deviceIndex >= count)
+        return VKRT_CUDA_ERROR_INITIALIZATION_FAILED;
+    if (cudaSetDevice(cfg.deviceIndex) != cudaSuccess) return VKRT_CUDA_ERROR_INITIALIZATION_FAILED;
+    VKRT_CudaContext* c = new VKRT_CudaContext();
+    c->cfg = cfg;
+    c->device = cfg.deviceIndex;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c->counters, sizeof(RenderCounters)) != cudaSuccess) {
+        if (c->stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return VKRT_CUDA_ERROR_INITIALIZATION_FAILED;
+    }
+    cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream);
+    c->textureData.resize(VKRT_CUDA_MAX_TEXTURES);
+    c->textureDescs.assign(VKRT_CUDA_MAX_TEXTURES, TextureDesc{nullptr, 0u, 0u});
+    *out = c;
+    return VKRT_CUDA_SUCCESS;
+}
+
+void vkrt_cuda_destroy(VKRT_CudaContext* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    c->vertices.release();
+    c->indices.release();
+    c->meshes.release();
+    c->bvh.release();
+    c->materials.release();
+    c->emissiveMeshes.release();
+    c->emissiveTriangles.release();
+    c->meshAliasQ.release();
+    c->meshAliasIdx.release();
+    c->triAliasQ.release();
+    c->triAliasIdx.release();
+    for (auto& t : c->textureData) t.release();
+    c->textureTable.release();
+    c->rgb2spec.release();
+    c->envMarginal.release();
+    c->envConditional.release();
+    c->envTexelPdf.release();
+    c->envScratch.release();
+    c->accum[0].release();
+    c->accum[1].release();
+    c->output.release();
+    if (c->counters) cudaFree(c->counters);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int32_t vkrt_cuda_upload_geometry(VKRT_CudaContext* c, const VKRT_CudaShaderVertex* vertices, uint32_t vertexCount,
+                                  const uint32_t* indices, uint32_t indexCount, const VKRT_CudaMeshInfo* meshes,
+                                  uint32_t meshCount) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if ((vertexCount && !vertices) || (indexCount && !indices) || (meshCount && !meshes))
+        return invalid(c, "null array with a non-zero count");
+    if (indexCount % 3u) return invalid(c, "indexCount is not a multiple of 3");
+    // every mesh's triangles must address valid indices and vertices (vkrt validates the same ranges)
+    uint64_t tris = 0;
+    for (uint32_t i = 0; i < meshCount; ++i) {
+        const VKRT_CudaMeshInfo& m = meshes[i];
+        if (m.indexCount % 3u) return invalid(c, "MeshInfo.indexCount is not a multiple of 3");
+        if (uint64_t(m.indexBase) + m.indexCount > indexCount) return invalid(c, "MeshInfo index range out of bounds");
+        if (uint64_t(m.vertexBase) + m.vertexCount > vertexCount) return invalid(c, "MeshInfo vertex range out of bounds");
+        for (uint32_t k = 0; k < m.indexCount; ++k)
+            if (indices[m.indexBase + k] >= m.vertexCount) return invalid(c, "index outside its mesh's vertex range");
+        tris += m.indexCount / 3u;
+    }
+    if (tris >= 0xFFFFFFF0ull) return invalid(c, "too many triangles");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->vertices.assign(vertices, vertexCount, c->stream), "upload vertices");
+    VKRT_TRY(c, c->indices.assign(indices, indexCount, c->stream), "upload indices");
+    VKRT_TRY(c, c->meshes.assign(meshes, meshCount, c->stream), "upload meshes");
+    c->hostMeshes.assign(meshes, meshes + meshCount);
+    c->vertexCount = vertexCount;
+    c->indexCount = indexCount;
+    c->triCount = uint32_t(tris);
+    VKRT_TRY(c, rebuildBvh(c), "BVH build");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_update_meshes(VKRT_CudaContext* c, const VKRT_CudaMeshInfo* meshes, uint32_t meshCount) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (meshCount != c->hostMeshes.size() || (meshCount && !meshes)) return invalid(c, "mesh count mismatch");
+    bool geometryChanged = false;
+    for (uint32_t i = 0; i < meshCount; ++i) {
+        const VKRT_CudaMeshInfo &a = c->hostMeshes[i], &b = meshes[i];
+        if (std::memcmp(a.position, b.position, sizeof(a.position)) || std::memcmp(a.rotation, b.rotation, sizeof(a.rotation)) ||
+            std::memcmp(a.scale, b.scale, sizeof(a.scale)) || a.vertexBase != b.vertexBase || a.indexBase != b.indexBase ||
+            a.indexCount != b.indexCount || a.vertexCount != b.vertexCount)
+            geometryChanged = true;
+    }
+    if (geometryChanged) {
+        for (uint32_t i = 0; i < meshCount; ++i) {
+            const VKRT_CudaMeshInfo& m = meshes[i];
+            if (m.indexCount % 3u || uint64_t(m.indexBase) + m.indexCount > c->indexCount ||
+                uint64_t(m.vertexBase) + m.vertexCount > c->vertexCount)
+                return invalid(c, "MeshInfo range out of bounds");
+        }
+    }
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->meshes.assign(meshes, meshCount, c->stream), "upload meshes");
+    c->hostMeshes.assign(meshes, meshes + meshCount);
+    if (geometryChanged) {
+        uint64_t tris = 0;
+        for (auto& m : c->hostMeshes) tris += m.indexCount / 3u;
+        c->triCount = uint32_t(tris);
+        VKRT_TRY(c, rebuildBvh(c), "BVH build");
+    }
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* c, const VKRT_CudaMaterial* materials, uint32_t count) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (count && !materials) return invalid(c, "null materials");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->materials.assign(materials, count, c->stream), "upload materials");
+    c->materialCount = count;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_upload_lights(VKRT_CudaContext* c, const VKRT_CudaEmissiveMesh* meshes, uint32_t meshCount,
+                                const VKRT_CudaEmissiveTriangle* triangles, uint32_t triangleCount,
+                                const float* meshAliasQ, const uint32_t* meshAliasIdx, const float* triAliasQ,
+                                const uint32_t* triAliasIdx) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (meshCount && (!meshes || !meshAliasQ || !meshAliasIdx)) return invalid(c, "null emissive mesh arrays");
+    if (triangleCount && (!triangles || !triAliasQ || !triAliasIdx)) return invalid(c, "null emissive triangle arrays");
+    for (uint32_t i = 0; i < meshCount; ++i) {
+        if (uint64_t(meshes[i].triOffset) + meshes[i].triCount > triangleCount)
+            return invalid(c, "EmissiveMesh triangle range out of bounds");
+        if (meshAliasIdx[i] >= meshCount) return invalid(c, "mesh alias index out of range");
+    }
+    for (uint32_t i = 0; i < meshCount; ++i)
+        for (uint32_t t = 0; t < meshes[i].triCount; ++t)
+            if (triAliasIdx[meshes[i].triOffset + t] >= meshes[i].triCount)
+                return invalid(c, "triangle alias index out of range");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->emissiveMeshes.assign(meshes, meshCount, c->stream), "upload emissive meshes");
+    VKRT_TRY(c, c->emissiveTriangles.assign(triangles, triangleCount, c->stream), "upload emissive triangles");
+    VKRT_TRY(c, c->meshAliasQ.assign(meshAliasQ, meshCount, c->stream), "upload alias");
+    VKRT_TRY(c, c->meshAliasIdx.assign(meshAliasIdx, meshCount, c->stream), "upload alias");
+    VKRT_TRY(c, c->triAliasQ.assign(triAliasQ, triangleCount, c->stream), "upload alias");
+    VKRT_TRY(c, c->triAliasIdx.assign(triAliasIdx, triangleCount, c->stream), "upload alias");
+    c->emissiveMeshCount = meshCount;
+    c->emissiveTriangleCount = triangleCount;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_upload_texture(VKRT_CudaContext* c, uint32_t index, const void* pixels, uint32_t w, uint32_t h,
+                                 uint32_t format, uint32_t colorSpace) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (index >= VKRT_CUDA_MAX_TEXTURES) return invalid(c, "texture index out of range");
+    if (!pixels || w == 0 || h == 0) return invalid(c, "empty texture");
+    if (format > VKRT_CUDA_TEXTURE_FORMAT_RGBA32_SFLOAT || colorSpace > VKRT_CUDA_COLOR_SPACE_LINEAR)
+        return invalid(c, "unknown texture format or colour space");
+    size_t n = size_t(w) * h;
+    // texels are stored linear RGBA32F: 8/16-bit UNORM sRGB data is decoded here, as the sampler would before
+    // filtering; alpha is always linear
+    std::vector<float4> texels(n);
+    for (size_t i = 0; i < n; ++i) {
+        float v[4];
+        for (int k = 0; k < 4; ++k) {
+            switch (format) {
+                case VKRT_CUDA_TEXTURE_FORMAT_RGBA8_UNORM:
+                    v[k] = float(static_cast<const uint8_t*>(pixels)[i * 4 + k]) / 255.0f;
+                    break;
+                case VKRT_CUDA_TEXTURE_FORMAT_RGBA16_UNORM:
+                    v[k] = float(static_cast<const uint16_t*>(pixels)[i * 4 + k]) / 65535.0f;
+                    break;
+                case VKRT_CUDA_TEXTURE_FORMAT_RGBA16_SFLOAT:
+                    halfToFloatBits(static_cast<const uint16_t*>(pixels)[i * 4 + k], v[k]);
+                    break;
+                default:
+                    v[k] = static_cast<const float*>(pixels)[i * 4 + k];
+            }
+            if (k < 3 && colorSpace == VKRT_CUDA_COLOR_SPACE_SRGB &&
+                (format == VKRT_CUDA_TEXTURE_FORMAT_RGBA8_UNORM || format == VKRT_CUDA_TEXTURE_FORMAT_RGBA16_UNORM))
+                v[k] = srgbToLinear(v[k]);
+        }
+        texels[i] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->textureData[index].assign(texels.data(), n, c->stream), "upload texture");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "upload texture");
+    c->textureDescs[index] = TextureDesc{c->textureData[index].ptr, w, h};
+    c->textureTableDirty = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_set_environment(VKRT_CudaContext* c, uint32_t textureIndex) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (textureIndex == VKRT_CUDA_INVALID_INDEX) {
+        c->envTexture = VKRT_CUDA_INVALID_INDEX;
+        c->envWidth = c->envHeight = 0;
+        return VKRT_CUDA_SUCCESS;
+    }
+    if (textureIndex >= VKRT_CUDA_MAX_TEXTURES || !c->textureDescs[textureIndex].texels)
+        return invalid(c, "environment texture slot is not bound");
+    const TextureDesc& t = c->textureDescs[textureIndex];
+    uint32_t W = t.width, H = t.height;
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->envMarginal.reserve(H + 1), "environment CDF");
+    VKRT_TRY(c, c->envConditional.reserve(size_t(H) * (W + 1)), "environment CDF");
+    VKRT_TRY(c, c->envTexelPdf.reserve(size_t(W) * H), "environment CDF");
+    VKRT_TRY(c, c->envScratch.reserve(size_t(W) * H + H + 2), "environment CDF");
+    VKRT_TRY(c, launchBuildEnvDistribution(t.texels, W, H, c->envMarginal.ptr, c->envConditional.ptr, c->envTexelPdf.ptr,
+                                           c->envScratch.ptr, c->stream),
+             "environment CDF");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "environment CDF");
+    c->envWidth = W;
+    c->envHeight = H;
+    c->envTexture = textureIndex;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_upload_rgb2spec(VKRT_CudaContext* c, const float* table, uint32_t floatCount,
+                                  const VKRT_CudaRGB2SpecTableInfo* info) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!table || !info || info->res < 2) return invalid(c, "rgb2spec table");
+    uint64_t need = std::max<uint64_t>(uint64_t(info->scaleOffset) + info->res,
+                                       uint64_t(info->dataOffset) + 9ull * info->res * info->res * info->res);
+    if (floatCount < need) return invalid(c, "rgb2spec table smaller than its layout");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->rgb2spec.assign(table, floatCount, c->stream), "upload rgb2spec");
+    c->rgb2specFloats = floatCount;
+    c->rgb2specInfo = *info;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_generate_rgb2spec(VKRT_CudaContext* c, uint32_t res, VKRT_CudaRGB2SpecTableInfo* outInfo) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (res < 3 || res > 256) return invalid(c, "rgb2spec resolution must be in [3, 256]");
+    uint32_t floats = res + 9u * res * res * res;
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->rgb2spec.reserve(floats), "rgb2spec");
+    VKRT_TRY(c, launchGenerateRgb2Spec(res, c->rgb2spec.ptr, c->stream), "rgb2spec fit");
+    c->rgb2specFloats = floats;
+    c->rgb2specInfo = VKRT_CudaRGB2SpecTableInfo{res, 0u, res};
+    if (outInfo) *outInfo = c->rgb2specInfo;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_download_rgb2spec(VKRT_CudaContext* c, float* table, uint32_t floatCount) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!table || floatCount < c->rgb2specFloats || !c->rgb2spec.ptr) return invalid(c, "rgb2spec download buffer");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, cudaMemcpyAsync(table, c->rgb2spec.ptr, sizeof(float) * c->rgb2specFloats, cudaMemcpyDeviceToHost, c->stream),
+             "download rgb2spec");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "download rgb2spec");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_resize(VKRT_CudaContext* c, uint32_t w, uint32_t h) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (w == 0 || h == 0 || uint64_t(w) * h > (1ull << 31)) return invalid(c, "film size");
+    cudaSetDevice(c->device);
+    size_t n = size_t(w) * h;
+    VKRT_TRY(c, c->accum[0].reserve(n), "film");
+    VKRT_TRY(c, c->accum[1].reserve(n), "film");
+    VKRT_TRY(c, c->output.reserve(n), "film");
+    c->width = w;
+    c->height = h;
+    c->readIndex = 0;
+    VKRT_TRY(c, launchClearFilm(c->accum[0].ptr, c->accum[1].ptr, c->output.ptr, n, c->stream), "film clear");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* c) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!c->width) return invalid(c, "no film");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, launchClearFilm(c->accum[0].ptr, c->accum[1].ptr, c->output.ptr, size_t(c->width) * c->height, c->stream),
+             "film clear");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!sd) return invalid(c, "null SceneData");
+    if (!c->width) return invalid(c, "no film: call vkrt_cuda_resize first");
+    if (uint64_t(sd->viewportRect[0]) + sd->viewportRect[2] > c->width ||
+        uint64_t(sd->viewportRect[1]) + sd->viewportRect[3] > c->height)
+        return invalid(c, "viewport outside the film");
+    if (sd->rrMaxDepth > 1024u) return invalid(c, "rrMaxDepth above 1024");
+    if (sd->emissiveMeshCount > c->emissiveMeshCount) return invalid(c, "SceneData.emissiveMeshCount exceeds the uploaded lights");
+    for (const VKRT_CudaMeshInfo& m : c->hostMeshes)
+        if (m.materialIndex >= c->materialCount) return invalid(c, "mesh material index out of range");
+    const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
+    if (spectral) {
+        const VKRT_CudaRGB2SpecTableInfo& ti = sd->rgb2specSRGB;
+        if (!c->rgb2spec.ptr || ti.res < 2 ||
+            uint64_t(ti.scaleOffset) + ti.res > c->rgb2specFloats ||
+            uint64_t(ti.dataOffset) + 9ull * ti.res * ti.res * ti.res > c->rgb2specFloats)
+            return invalid(c, "spectral mode needs an rgb2spec table matching SceneData.rgb2specSRGB");
+        if (VKRT_CUDA_SPECTRAL_MODE_OF(sd->packedRenderSettings) != VKRT_CUDA_SPECTRAL_HERO)
+            return invalid(c, "only hero-wavelength spectral sampling is implemented");
+    }
+    cudaSetDevice(c->device);
+    DeviceScene scene = makeDeviceScene(c);
+    RenderParams rp{};
+    rp.rngMode = c->cfg.rngMode;
+    rp.rngSeed = c->cfg.rngSeed;
+    rp.envNee = (c->cfg.environmentSampling == VKRT_CUDA_ENV_IMPORTANCE && c->envTexture != VKRT_CUDA_INVALID_INDEX &&
+                 sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u)
+                    ? 1u
+                    : 0u;
+    rp.width = c->width;
+    rp.height = c->height;
+    rp.countBytes = c->cfg.countRays;
+    FilmBuffers film{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
+    VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "render");
+    VKRT_TRY(c, launchRender(scene, *sd, rp, film, c->counters, c->cfg.threadsPerBlock, c->stream), "render launch");
+    c->readIndex ^= 1;  // VKRT_endFrame's ping-pong swap (frame.c:386-389)
+    c->countersPending = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_sync(VKRT_CudaContext* c, uint32_t timeoutMs) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (timeoutMs == 0) {
+        VKRT_TRY(c, cudaStreamSynchronize(c->stream), "sync");
+        return VKRT_CUDA_SUCCESS;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(c->stream);
+        if (e == cudaSuccess) return VKRT_CUDA_SUCCESS;
+        if (e != cudaErrorNotReady) return fail(c, e, "sync");
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeoutMs)) {
+            c->lastError = "sync: timed out";
+            return VKRT_CUDA_ERROR_OPERATION_FAILED;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+}
+
+int32_t vkrt_cuda_read_accumulation(VKRT_CudaContext* c, float* rgba, size_t bytes) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    size_t need = size_t(c->width) * c->height * sizeof(float4);
+    if (!rgba || bytes < need || !need) return invalid(c, "accumulation buffer too small");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, cudaMemcpyAsync(rgba, c->accum[c->readIndex].ptr, need, cudaMemcpyDeviceToHost, c->stream), "read accumulation");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read accumulation");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_read_output(VKRT_CudaContext* c, uint16_t* rgba, size_t bytes) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    size_t need = size_t(c->width) * c->height * sizeof(ushort4);
+    if (!rgba || bytes < need || !need) return invalid(c, "output buffer too small");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, cudaMemcpyAsync(rgba, c->output.ptr, need, cudaMemcpyDeviceToHost, c->stream), "read output");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read output");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_get_stats(VKRT_CudaContext* c, VKRT_CudaStats* st) {
+    if (!c || !st) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->countersPending) {
+        VKRT_TRY(c, cudaMemcpyAsync(&c->lastCounters, c->counters, sizeof(RenderCounters), cudaMemcpyDeviceToHost, c->stream),
+                 "stats");
+        VKRT_TRY(c, cudaStreamSynchronize(c->stream), "stats");
+        c->countersPending = false;
+    }
+    std::memset(st, 0, sizeof(*st));
+    st->primaryRays = c->lastCounters.primaryRays;
+    st->extensionRays = c->lastCounters.extensionRays;
+    st->shadowRays = c->lastCounters.shadowRays;
+    st->pathSamples = c->lastCounters.pathSamples;
+    st->nodeFetchBytes = c->lastCounters.nodeBytes;
+    st->triFetchBytes = c->lastCounters.triBytes;
+    st->errorFlags = c->lastCounters.errorFlags;
+    st->bvhNodeCount = c->bvh.nodeCount;
+    st->bvhTriangleCount = c->bvh.triCount;
+    st->bvhBytes = uint64_t(c->bvh.nodeCount) * sizeof(WideNode) + uint64_t(c->bvh.triCount) * sizeof(TriRecord);
+    st->bvhBuildMs = c->bvhStats.buildMs;
+    return VKRT_CUDA_SUCCESS;
+}
+
+void* vkrt_cuda_stream(VKRT_CudaContext* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
+
+int32_t vkrt_cuda_trace_rays_device(VKRT_CudaContext* c, const VKRT_CudaRay* rays, uint32_t count, uint32_t anyHit,
+                                    VKRT_CudaHit* hits) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (count && (!rays || !hits)) return invalid(c, "null ray or hit array");
+    if ((reinterpret_cast<uintptr_t>(rays) | reinterpret_cast<uintptr_t>(hits)) & 15u)
+        return invalid(c, "ray and hit arrays must be 16-byte aligned");
+    cudaSetDevice(c->device);
+    DeviceScene scene = makeDeviceScene(c);
+    VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "trace");
+    VKRT_TRY(c, launchTraceRays(scene, rays, count, anyHit, hits, c->counters, c->stream), "trace launch");
+    c->countersPending = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_trace_rays(VKRT_CudaContext* c, const VKRT_CudaRay* rays, uint32_t count, uint32_t anyHit,
+                             VKRT_CudaHit* hits) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (count && (!rays || !hits)) return invalid(c, "null ray or hit array");
+    if (count == 0) return VKRT_CUDA_SUCCESS;
+    cudaSetDevice(c->device);
+    VKRT_CudaRay* dRays = nullptr;
+    VKRT_CudaHit* dHits = nullptr;
+    cudaError_t e = cudaMalloc(&dRays, sizeof(VKRT_CudaRay) * count);
+    if (e == cudaSuccess) e = cudaMalloc(&dHits, sizeof(VKRT_CudaHit) * count);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dRays, rays, sizeof(VKRT_CudaRay) * count, cudaMemcpyHostToDevice, c->stream);
+    int32_t r = VKRT_CUDA_SUCCESS;
+    if (e == cudaSuccess) r = vkrt_cuda_trace_rays_device(c, dRays, count, anyHit, dHits);
+    if (e == cudaSuccess && r == VKRT_CUDA_SUCCESS)
+        e = cudaMemcpyAsync(hits, dHits, sizeof(VKRT_CudaHit) * count, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && r == VKRT_CUDA_SUCCESS) e = cudaStreamSynchronize(c->stream);
+    cudaFree(dRays);
+    cudaFree(dHits);
+    if (e != cudaSuccess) return fail(c, e, "trace rays");
+    return r;
+}
+
+const char* vkrt_cuda_last_error(VKRT_CudaContext* c) { return c ? c->lastError.c_str() : "null context"; }
+
+}  // extern "C"

@@ -1,0 +1,43 @@
+// render.h — host-side launchers of the render, trace, film, environment and rgb2spec kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "scene.cuh"
+
+namespace vkrt {
+
+struct RenderParams {
+    uint32_t rngMode;
+    uint64_t rngSeed;
+    uint32_t envNee;     // environment importance sampling active for this frame
+    uint32_t width;      // film size (the viewport rectangle lives in SceneData)
+    uint32_t height;
+    uint32_t countBytes; // accumulate node / triangle fetch bytes
+};
+
+struct FilmBuffers {
+    float4* accumRead;
+    float4* accumWrite;
+    ushort4* output;
+};
+
+// One frame of vkrt's ray-generation pass (entry/path/raygen_rgb.slang / raygen_spectral_hero.slang).
+cudaError_t launchRender(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const RenderParams& rp,
+                         const FilmBuffers& film, RenderCounters* counters, uint32_t threadsPerBlock,
+                         cudaStream_t stream);
+
+cudaError_t launchTraceRays(const DeviceScene& sc, const VKRT_CudaRay* rays, uint32_t count, uint32_t anyHit,
+                            VKRT_CudaHit* hits, RenderCounters* counters, cudaStream_t stream);
+
+cudaError_t launchClearFilm(float4* a, float4* b, ushort4* out, size_t pixels, cudaStream_t stream);
+
+// Environment importance distribution from an RGBA32F lat-long map; buffers sized by the caller:
+// marginal H+1, conditional H*(W+1), texelPdf W*H floats; scratch (W*H + H) doubles + 2 doubles.
+cudaError_t launchBuildEnvDistribution(const float4* texels, uint32_t width, uint32_t height, float* marginal,
+                                       float* conditional, float* texelPdf, double* scratch, cudaStream_t stream);
+
+// rgb2spec table fit on the device; `table` holds res + 3*res^3*3 floats.
+cudaError_t launchGenerateRgb2Spec(uint32_t res, float* table, cudaStream_t stream);
+
+}  // namespace vkrt

@@ -1,0 +1,260 @@
+"""Seeded synthetic scenes for the benchmark configurations (no dataset or asset is needed).
+
+* cornell(...)          — the Cornell box: unit cube open at the front (10 wall triangles), a 0.25 x 0.25 ceiling
+                          light (2 triangles, own mesh for alias-table NEE) and two boxes rotated +-18 degrees about
+                          Z (24 triangles, placed through MeshInfo position/rotation so the instance transform path
+                          is exercised). Lambertian materials (metallic 0, roughness 1, specular 0).
+* icosphere_field(...)  — N icospheres of 1,280 triangles (three subdivisions of the icosahedron), centres uniform
+                          in [-10, 10]^3, radii log-uniform in [0.1, 1], vertices flattened to world space, one mesh
+                          record per sphere so each keeps its own material; glTF metallic-roughness materials.
+* sky_environment(...)  — 1024 x 512 FP32 lat-long map: grey sky gradient 0.2-1.0 plus a 0.5-degree sun disc of
+                          radiance 5e3 at a seeded direction.
+All scenes are Z-up like vkrt's default camera (src/core/scene/uniform.c:133-138).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import abi
+from .context import Scene, build_light_tables
+
+
+def default_material(**overrides) -> np.ndarray:
+    m = np.zeros(1, dtype=abi.MATERIAL)
+    abi.load().vkrt_host_default_material(abi.ptr(m))
+    for k, v in overrides.items():
+        m[k] = v
+    return m
+
+
+def default_scene_data(width: int, height: int) -> np.ndarray:
+    sd = np.zeros(1, dtype=abi.SCENE_DATA)
+    abi.load().vkrt_host_default_scene_data(width, height, abi.ptr(sd))
+    return sd
+
+
+def set_camera(sd: np.ndarray, pos, target, up=(0.0, 0.0, 1.0), vfov: float = 40.0) -> None:
+    p = np.array(pos, dtype=np.float32)
+    t = np.array(target, dtype=np.float32)
+    u = np.array(up, dtype=np.float32)
+    w, h = int(sd["viewportRect"][0][2]), int(sd["viewportRect"][0][3])
+    abi.load().vkrt_host_camera_matrices(abi.ptr(p), abi.ptr(t), abi.ptr(u), vfov, 0.001, 10000.0, w, h, abi.ptr(sd))
+
+
+def _quad(p0, p1, p2, p3, normal):
+    """Two triangles (p0,p1,p2), (p0,p2,p3) with a flat normal and unit UVs."""
+    verts = np.zeros(4, dtype=abi.VERTEX)
+    pts = np.array([p0, p1, p2, p3], dtype=np.float32)
+    verts["position"][:, :3] = pts
+    verts["position"][:, 3] = 1.0
+    n = np.asarray(normal, dtype=np.float32)
+    verts["normal"][:, :3] = n
+    t = pts[1] - pts[0]
+    t = t / max(np.linalg.norm(t), 1e-12)
+    verts["tangent"][:, :3] = t
+    verts["tangent"][:, 3] = 1.0
+    verts["color"] = 1.0
+    verts["texcoord0"] = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], dtype=np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3], dtype=np.uint32)
+    return verts, idx
+
+
+def _box(sx, sy, sz):
+    """Axis-aligned box [-sx/2, sx/2] x [-sy/2, sy/2] x [0, sz], 6 faces, outward normals."""
+    x0, x1, y0, y1, z0, z1 = -sx / 2, sx / 2, -sy / 2, sy / 2, 0.0, sz
+    faces = [
+        ((x0, y0, z0), (x0, y1, z0), (x1, y1, z0), (x1, y0, z0), (0, 0, -1)),
+        ((x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1), (0, 0, 1)),
+        ((x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1), (0, -1, 0)),
+        ((x1, y1, z0), (x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (0, 1, 0)),
+        ((x0, y1, z0), (x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (-1, 0, 0)),
+        ((x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1), (1, 0, 0)),
+    ]
+    vs, ids = [], []
+    for f in faces:
+        v, i = _quad(*f)
+        ids.append(i + 4 * len(vs))
+        vs.append(v)
+    return np.concatenate(vs), np.concatenate(ids)
+
+
+def _assemble(parts, materials, scene_data, name) -> Scene:
+    """parts: list of (vertices, mesh-relative indices, material index, position, rotation, scale)."""
+    verts, idxs = [], []
+    meshes = np.zeros(len(parts), dtype=abi.MESH_INFO)
+    vb = ib = 0
+    for k, (v, i, mat, pos, rot, scl) in enumerate(parts):
+        meshes[k]["position"] = pos
+        meshes[k]["rotation"] = rot
+        meshes[k]["scale"] = scl
+        meshes[k]["vertexBase"] = vb
+        meshes[k]["vertexCount"] = len(v)
+        meshes[k]["indexBase"] = ib
+        meshes[k]["indexCount"] = len(i)
+        meshes[k]["materialIndex"] = mat
+        meshes[k]["opacity"] = 1.0
+        verts.append(v)
+        idxs.append(i.astype(np.uint32))
+        vb += len(v)
+        ib += len(i)
+    s = Scene(vertices=np.concatenate(verts), indices=np.concatenate(idxs), meshes=meshes,
+              materials=np.concatenate(materials), scene_data=scene_data, name=name)
+    build_light_tables(s)
+    return s
+
+
+def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 8) -> Scene:
+    lamb = dict(metallic=0.0, roughness=1.0, specular=0.0, diffuseRoughness=0.0)
+    mats = [default_material(baseColor=(0.73, 0.73, 0.73), **lamb),
+            default_material(baseColor=(0.65, 0.05, 0.05), **lamb),
+            default_material(baseColor=(0.12, 0.45, 0.15), **lamb),
+            default_material(baseColor=(0.0, 0.0, 0.0), emissionColor=(1.0, 1.0, 1.0), emissionLuminance=15.0, **lamb)]
+    WHITE, RED, GREEN, LIGHT = 0, 1, 2, 3
+    ident = ((0, 0, 0), (0, 0, 0), (1, 1, 1))
+    parts = []
+    # walls: x = left/right, y = depth (open at y = 0), z = up; normals point into the box
+    walls = [
+        (((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1)), WHITE),   # floor
+        (((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1), (0, 0, -1)), WHITE),  # ceiling
+        (((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1), (0, -1, 0)), WHITE),  # back
+        (((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (1, 0, 0)), RED),     # left
+        (((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0), (-1, 0, 0)), GREEN),  # right
+    ]
+    for (q, mat) in walls:
+        v, i = _quad(*q)
+        parts.append((v, i, mat) + ident)
+    h = 1.0 - 1e-3
+    v, i = _quad((0.375, 0.375, h), (0.375, 0.625, h), (0.625, 0.625, h), (0.625, 0.375, h), (0, 0, -1))
+    parts.append((v, i, LIGHT) + ident)
+    sv, si = _box(0.3, 0.3, 0.3)
+    parts.append((sv, si, WHITE, (0.68, 0.32, 0.0), (0.0, 0.0, -18.0), (1, 1, 1)))
+    tv, ti = _box(0.3, 0.3, 0.6)
+    parts.append((tv, ti, WHITE, (0.32, 0.65, 0.0), (0.0, 0.0, 18.0), (1, 1, 1)))
+    sd = default_scene_data(width, height)
+    set_camera(sd, (0.5, -1.35, 0.5), (0.5, 0.5, 0.5))
+    sd["samplesPerPixel"] = spp
+    sd["rrMaxDepth"] = max_depth
+    sd["environmentLight"] = (0.0, 0.0, 0.0, 0.0)
+    sd["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES, abi.RENDER_MODE_RGB, abi.SPECTRAL_HERO)
+    return _assemble(parts, mats, sd, "cornell")
+
+
+def unit_icosphere(subdivisions: int = 3) -> tuple[np.ndarray, np.ndarray]:
+    """Icosahedron refined `subdivisions` times (20 * 4^s triangles); vertices on the unit sphere."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(subdivisions):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts, dtype=np.float64), np.array(faces, dtype=np.uint32).reshape(-1)
+
+
+def sky_environment(width: int = 1024, height: int = 512, seed: int = 1, sun_radiance: float = 5e3,
+                    sun_diameter_deg: float = 0.5) -> tuple[np.ndarray, np.ndarray]:
+    """Returns (rgba float32 (H, W, 4), unit sun direction)."""
+    rng = np.random.default_rng(seed + 1000)
+    elev = math.radians(rng.uniform(20.0, 70.0))
+    azim = rng.uniform(0.0, 2.0 * math.pi)
+    sun = np.array([math.cos(elev) * math.cos(azim), math.cos(elev) * math.sin(azim), math.sin(elev)])
+    j = (np.arange(height) + 0.5) / height
+    theta = j * math.pi
+    grad = 0.2 + 0.8 * np.clip(np.cos(theta), 0.0, 1.0)
+    img = np.zeros((height, width, 4), dtype=np.float32)
+    img[..., :3] = grad[:, None, None].astype(np.float32)
+    img[..., 3] = 1.0
+    # sun disc with 8x8 supersampled coverage near the sun's texels (lookup: u = frac(phi/2pi + 0.5), v = theta/pi)
+    cos_r = math.cos(math.radians(sun_diameter_deg * 0.5))
+    sun_theta = math.acos(sun[2])
+    sun_phi = math.atan2(sun[1], sun[0])
+    jc = int(sun_theta / math.pi * height)
+    ic = int(((sun_phi / (2 * math.pi) + 0.5) % 1.0) * width)
+    ss = 8
+    offs = (np.arange(ss) + 0.5) / ss
+    for jj in range(max(0, jc - 4), min(height, jc + 5)):
+        for ii0 in range(ic - 4, ic + 5):
+            ii = ii0 % width
+            u = (ii + offs[None, :]) / width
+            v = (jj + offs[:, None]) / height
+            th = v * math.pi
+            ph = (u - 0.5) * 2 * math.pi
+            d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th) * np.ones_like(ph)], -1)
+            cover = float(((d @ sun) >= cos_r).mean())
+            if cover > 0:
+                img[jj, ii, :3] += np.float32(sun_radiance * cover)
+    return img, sun
+
+
+def icosphere_field(n_spheres: int = 800, width: int = 1920, height: int = 1080, spp: int = 16, max_depth: int = 12,
+                    seed: int = 1, spectral: bool = True, env_size=(1024, 512), subdivisions: int = 3,
+                    extent: float = 10.0) -> Scene:
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(-extent, extent, size=(n_spheres, 3))
+    radii = np.exp(rng.uniform(math.log(0.1), math.log(1.0), size=n_spheres))
+    base_color = rng.uniform(0.1, 0.9, size=(n_spheres, 3))
+    roughness = rng.uniform(0.05, 1.0, size=n_spheres)
+    metallic = (rng.uniform(0.0, 1.0, size=n_spheres) < 0.3).astype(np.float32)
+    uv, uf = unit_icosphere(subdivisions)
+    nv, nt = len(uv), len(uf) // 3
+    verts = np.zeros(n_spheres * nv, dtype=abi.VERTEX)
+    pos = (centers[:, None, :] + radii[:, None, None] * uv[None, :, :]).reshape(-1, 3)
+    nrm = np.broadcast_to(uv[None], (n_spheres, nv, 3)).reshape(-1, 3)
+    verts["position"][:, :3] = pos.astype(np.float32)
+    verts["position"][:, 3] = 1.0
+    verts["normal"][:, :3] = nrm.astype(np.float32)
+    up = np.where(np.abs(nrm[:, 2:3]) < 0.999, np.array([[0.0, 0.0, 1.0]]), np.array([[1.0, 0.0, 0.0]]))
+    tan = np.cross(up, nrm)
+    tan /= np.linalg.norm(tan, axis=1, keepdims=True)
+    verts["tangent"][:, :3] = tan.astype(np.float32)
+    verts["tangent"][:, 3] = 1.0
+    verts["color"] = 1.0
+    verts["texcoord0"][:, 0] = (np.arctan2(nrm[:, 1], nrm[:, 0]) / (2 * math.pi) + 0.5).astype(np.float32)
+    verts["texcoord0"][:, 1] = (np.arccos(np.clip(nrm[:, 2], -1, 1)) / math.pi).astype(np.float32)
+    indices = np.tile(uf, n_spheres).astype(np.uint32)
+    meshes = np.zeros(n_spheres, dtype=abi.MESH_INFO)
+    meshes["vertexBase"] = np.arange(n_spheres, dtype=np.uint32) * nv
+    meshes["vertexCount"] = nv
+    meshes["indexBase"] = np.arange(n_spheres, dtype=np.uint32) * (3 * nt)
+    meshes["indexCount"] = 3 * nt
+    meshes["materialIndex"] = np.arange(n_spheres, dtype=np.uint32)
+    meshes["scale"] = 1.0
+    meshes["opacity"] = 1.0
+    mats = np.concatenate([default_material() for _ in range(n_spheres)])
+    mats["baseColor"] = base_color.astype(np.float32)
+    mats["roughness"] = roughness.astype(np.float32)
+    mats["metallic"] = metallic
+    mats["specular"] = 0.5
+    mats["ior"] = 1.5
+    sd = default_scene_data(width, height)
+    set_camera(sd, (0.0, -30.0, 6.0), (0.0, 0.0, 0.0))
+    sd["samplesPerPixel"] = spp
+    sd["rrMaxDepth"] = max_depth
+    mode = abi.RENDER_MODE_SPECTRAL if spectral else abi.RENDER_MODE_RGB
+    sd["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES, mode, abi.SPECTRAL_HERO)
+    env, _sun = sky_environment(env_size[0], env_size[1], seed)
+    sd["environmentTextureIndex"] = 0
+    sd["environmentLight"] = (1.0, 1.0, 1.0, 1.0)
+    s = Scene(vertices=verts, indices=indices, meshes=meshes, materials=mats, scene_data=sd,
+              textures={0: env}, env_texture=0, name=f"icospheres{n_spheres}")
+    build_light_tables(s)
+    return s
