@@ -164,6 +164,17 @@ int32_t vkrt_cuda_trace_rays(VKRT_CudaContext* context, const VKRT_CudaRay* rays
 int32_t vkrt_cuda_trace_rays_device(VKRT_CudaContext* context, const VKRT_CudaRay* deviceRays, uint32_t count,
                                     uint32_t anyHit, VKRT_CudaHit* deviceHits);
 
+/* Same trace as vkrt_cuda_trace_rays, for callers that must not allocate device memory (a real-time frame thread
+ * that cannot absorb the device-wide synchronisation of cudaFree, or a host with a fixed device-memory budget).
+ * No counterpart in vkrt: it is an addition of this backend. Rays and hits are staged in two fixed file-scope
+ * device arrays instead of per-call cudaMalloc buffers, so the call performs no allocation. At most 65,536 rays per
+ * call (larger counts return VKRT_CUDA_ERROR_INVALID_ARGUMENT). The arrays (4 MiB) exist once per device and are
+ * shared by every call on that device: calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device resolves the arrays' addresses; make it before any stream capture. Host arrays;
+ * synchronous. */
+int32_t vkrt_cuda_trace_rays_noalloc(VKRT_CudaContext* context, const VKRT_CudaRay* rays, uint32_t count,
+                                     uint32_t anyHit, VKRT_CudaHit* hits);
+
 /* Last error message of this context (never NULL). */
 const char* vkrt_cuda_last_error(VKRT_CudaContext* context);
 

@@ -142,6 +142,7 @@ EXPORTS = {
     "vkrt_cuda_stream": (_V, [_V]),
     "vkrt_cuda_trace_rays": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_trace_rays_device": (_I32, [_V, _V, _U32, _U32, _V]),
+    "vkrt_cuda_trace_rays_noalloc": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_last_error": (C.c_char_p, [_V]),
     "vkrt_host_pack_shader_vertices": (None, [_V, _U32, _V]),
     "vkrt_host_mesh_transform": (None, [_V, _V, _V, _V]),

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "context_view.h"
 #include "render.h"
 #include "scene.cuh"
 #include "vkrt_cuda.h"
@@ -647,5 +648,33 @@ int32_t vkrt_cuda_trace_rays(VKRT_CudaContext* c, const VKRT_CudaRay* rays, uint
 }
 
 const char* vkrt_cuda_last_error(VKRT_CudaContext* c) { return c ? c->lastError.c_str() : "null context"; }
+
+}  // extern "C"
+
+// Read-only view of a context for entry points implemented in other translation units (context_view.h).
+namespace vkrt {
+ContextView contextView(VKRT_CudaContext* c) {
+    ContextView v{};
+    if (!c) return v;
+    v.device = c->device;
+    v.stream = c->stream;
+    v.counters = c->counters;
+    v.nodes = c->bvh.nodes;
+    v.tris = c->bvh.tris;
+    v.nodeCount = c->bvh.nodeCount;
+    v.triCount = c->bvh.triCount;
+    return v;
+}
+
+void contextSetError(VKRT_CudaContext* c, const char* message) {
+    if (c) c->lastError = message;
+}
+
+void contextMarkCountersPending(VKRT_CudaContext* c) {
+    if (c) c->countersPending = true;
+}
+}  // namespace vkrt
+
+extern "C" {
 
 }  // extern "C"
