@@ -35,6 +35,10 @@ extern "C" {
 #define VKRT_CUDA_ENV_BSDF_ONLY 0u   /* vkrt: environment only on BSDF-sampled misses (environment.slang:16-27) */
 #define VKRT_CUDA_ENV_IMPORTANCE 1u  /* equirect luminance*sin(theta) importance sampling + MIS with the BSDF */
 
+/* integrator selected by VKRT_CudaConfig.integrator */
+#define VKRT_CUDA_INTEGRATOR_MEGAKERNEL 0u /* one thread per pixel runs whole paths (vkrt's raygen structure) */
+#define VKRT_CUDA_INTEGRATOR_WAVEFRONT 1u  /* persistent stage kernels over compacted path queues, one graph launch */
+
 typedef struct VKRT_CudaContext VKRT_CudaContext;
 
 typedef struct VKRT_CudaConfig {
@@ -42,11 +46,24 @@ typedef struct VKRT_CudaConfig {
     uint32_t rngMode;             /* VKRT_CUDA_RNG_* */
     uint64_t rngSeed;             /* PCG32 seed (ignored by the reference stream) */
     uint32_t environmentSampling; /* VKRT_CUDA_ENV_* */
-    uint32_t countRays;           /* 1: keep per-frame ray counters (primary / extension / shadow) */
+    uint32_t countRays;           /* 1: also count BVH node / triangle fetch bytes per frame */
     uint32_t threadsPerBlock;     /* megakernel block size, 0 = default (128) */
-    uint32_t blocksPerSM;         /* persistent megakernel residency, 0 = default */
-    uint32_t reserved[8];
+    uint32_t blocksPerSM;         /* reserved for the megakernel, 0 = default */
+    uint32_t integrator;          /* VKRT_CUDA_INTEGRATOR_* */
+    uint32_t reserved[7];
 } VKRT_CudaConfig;
+
+/* Wavefront integrator parameters (autotuned by vkrt_cuda_autotune_batch). 64 bytes. */
+typedef struct VKRT_CudaWavefrontConfig {
+    uint32_t queueCapacity;        /* path slots; 0 = one per pixel of the batch, capped at 4M */
+    uint32_t tileWidth;            /* pixels are handed to path slots in tiles of tileWidth x tileHeight */
+    uint32_t tileHeight;
+    uint32_t sortByMaterial;       /* 1: shade queue counting-sorted by (scene, material) before shading */
+    uint32_t intersectBlocksPerSM; /* persistent grid of the traversal kernels, per SM */
+    uint32_t shadeBlocksPerSM;     /* persistent grid of the shading kernels, per SM */
+    uint32_t useGraph;             /* 1: the frame is one CUDA-graph launch (conditional while node) */
+    uint32_t reserved[9];
+} VKRT_CudaWavefrontConfig;
 
 typedef struct VKRT_CudaStats {
     uint64_t primaryRays;    /* camera rays traced by the last render call */
@@ -140,6 +157,27 @@ int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* context);
  * ping-pong accumulation images (VKRT_trace -> recordMainTracePass plus the swap in VKRT_endFrame,
  * src/core/api/frame.c:267-337,380-390). Asynchronous on the context stream; SceneData is copied at call time. */
 int32_t vkrt_cuda_render_frame(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData);
+
+void vkrt_cuda_default_wavefront_config(VKRT_CudaWavefrontConfig* config);
+int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* context, const VKRT_CudaWavefrontConfig* config);
+int32_t vkrt_cuda_get_wavefront_config(VKRT_CudaContext* context, VKRT_CudaWavefrontConfig* config);
+
+/* Renders one frame of every context in one batched wavefront pass: all contexts on one device and in one render
+ * mode (all RGB or all hero spectral), each with its own scene, BVH, camera (sceneDatas[i]) and film; scenes and
+ * resolutions may differ. The work runs on contexts[0]'s stream as a single CUDA-graph launch with contexts[0]'s
+ * wavefront configuration; every context's accumulation images are swapped as by vkrt_cuda_render_frame. Ray
+ * counters of the whole batch are reported by contexts[0]. This has no single counterpart in vkrt, which renders
+ * one scene per VKRT_draw; per scene it computes what vkrt_cuda_render_frame computes. */
+int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_CudaSceneData* sceneDatas,
+                               uint32_t count);
+
+/* Picks queue capacity, tile shape, material sorting and per-SM residency of the wavefront integrator for this
+ * batch by timing candidate configurations (coordinate descent, `framesPerTrial` frames each at two samples per
+ * pixel), stores the best in contexts[0] and returns it with its frame time. Clears the accumulation of every
+ * context in the batch. */
+int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_CudaSceneData* sceneDatas,
+                                 uint32_t count, uint32_t framesPerTrial, VKRT_CudaWavefrontConfig* best,
+                                 float* bestFrameMs);
 
 /* Waits for all work on the context stream, polling up to timeoutMs (0 = wait without limit). Returns
  * VKRT_CUDA_ERROR_OPERATION_FAILED on timeout, VKRT_CUDA_ERROR_DEVICE_LOST on a CUDA error. */

@@ -74,9 +74,14 @@ HIT = np.dtype({"names": ["instanceIndex", "primitiveIndex", "t", "u", "v", "res
                 "itemsize": 32})
 
 CONFIG = np.dtype({"names": ["deviceIndex", "rngMode", "rngSeed", "environmentSampling", "countRays",
-                             "threadsPerBlock", "blocksPerSM", "reserved"],
-                   "formats": ["<i4", "<u4", "<u8", "<u4", "<u4", "<u4", "<u4", ("<u4", 8)],
-                   "offsets": [0, 4, 8, 16, 20, 24, 28, 32], "itemsize": 64})
+                             "threadsPerBlock", "blocksPerSM", "integrator", "reserved"],
+                   "formats": ["<i4", "<u4", "<u8", "<u4", "<u4", "<u4", "<u4", "<u4", ("<u4", 7)],
+                   "offsets": [0, 4, 8, 16, 20, 24, 28, 32, 36], "itemsize": 64})
+
+WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
+                                       "intersectBlocksPerSM", "shadeBlocksPerSM", "useGraph", "reserved"],
+                             "formats": ["<u4"] * 7 + [("<u4", 9)], "offsets": [0, 4, 8, 12, 16, 20, 24, 28],
+                             "itemsize": 64})
 
 STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathSamples", "nodeFetchBytes",
                             "triFetchBytes", "bvhNodeCount", "bvhTriangleCount", "bvhBytes", "bvhBuildMs",
@@ -90,6 +95,7 @@ RENDER_MODE_RGB, RENDER_MODE_SPECTRAL = 0, 1
 SPECTRAL_SINGLE, SPECTRAL_HERO = 0, 1
 RNG_REFERENCE, RNG_PCG32 = 0, 1
 ENV_BSDF_ONLY, ENV_IMPORTANCE = 0, 1
+INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT = 0, 1
 TEXTURE_FORMAT_RGBA8_UNORM, TEXTURE_FORMAT_RGBA16_UNORM, TEXTURE_FORMAT_RGBA16_SFLOAT, TEXTURE_FORMAT_RGBA32_SFLOAT = 0, 1, 2, 3
 COLOR_SPACE_SRGB, COLOR_SPACE_LINEAR = 0, 1
 WRAP_REPEAT, WRAP_CLAMP, WRAP_MIRROR = 10497, 33071, 33648
@@ -144,6 +150,11 @@ EXPORTS = {
     "vkrt_cuda_trace_rays_device": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_trace_rays_noalloc": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_last_error": (C.c_char_p, [_V]),
+    "vkrt_cuda_default_wavefront_config": (None, [_V]),
+    "vkrt_cuda_set_wavefront_config": (_I32, [_V, _V]),
+    "vkrt_cuda_get_wavefront_config": (_I32, [_V, _V]),
+    "vkrt_cuda_render_batch": (_I32, [_V, _V, _U32]),
+    "vkrt_cuda_autotune_batch": (_I32, [_V, _V, _U32, _U32, _V, _V]),
     "vkrt_host_pack_shader_vertices": (None, [_V, _U32, _V]),
     "vkrt_host_mesh_transform": (None, [_V, _V, _V, _V]),
     "vkrt_host_camera_matrices": (None, [_V, _V, _V, _F, _F, _F, _U32, _U32, _V]),

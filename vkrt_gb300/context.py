@@ -91,7 +91,8 @@ class RenderContext:
     """A CUDA context of the backend: scene buffers, BVH, film and one stream."""
 
     def __init__(self, device: int = 0, rng_mode: int = abi.RNG_REFERENCE, rng_seed: int = 1,
-                 environment_sampling: int = abi.ENV_BSDF_ONLY, count_rays: bool = False):
+                 environment_sampling: int = abi.ENV_BSDF_ONLY, count_rays: bool = False,
+                 integrator: int = abi.INTEGRATOR_MEGAKERNEL):
         self.lib = abi.load()
         cfg = np.zeros(1, dtype=abi.CONFIG)
         self.lib.vkrt_cuda_default_config(abi.ptr(cfg))
@@ -100,6 +101,7 @@ class RenderContext:
         cfg["rngSeed"] = rng_seed
         cfg["environmentSampling"] = environment_sampling
         cfg["countRays"] = 1 if count_rays else 0
+        cfg["integrator"] = integrator
         handle = C.c_void_p()
         r = self.lib.vkrt_cuda_create(abi.ptr(cfg), C.byref(handle))
         if r != abi.SUCCESS:
@@ -184,6 +186,20 @@ class RenderContext:
         self._check(self.lib.vkrt_cuda_download_rgb2spec(self.handle, abi.ptr(table), len(table)), "download rgb2spec")
         return table, info
 
+    # -- wavefront integrator --------------------------------------------------------------------------------
+    def wavefront_config(self) -> np.ndarray:
+        w = np.zeros(1, dtype=abi.WAVEFRONT_CONFIG)
+        self._check(self.lib.vkrt_cuda_get_wavefront_config(self.handle, abi.ptr(w)), "get wavefront config")
+        return w
+
+    def set_wavefront_config(self, w: np.ndarray | None = None, **fields) -> None:
+        if w is None:
+            w = self.wavefront_config()
+        w = np.ascontiguousarray(w, dtype=abi.WAVEFRONT_CONFIG).copy()
+        for k, v in fields.items():
+            w[k] = v
+        self._check(self.lib.vkrt_cuda_set_wavefront_config(self.handle, abi.ptr(w)), "set wavefront config")
+
     # -- film / frames -----------------------------------------------------------------------------------------
     def resize(self, width: int, height: int) -> None:
         self._check(self.lib.vkrt_cuda_resize(self.handle, width, height), "resize")
@@ -226,3 +242,28 @@ class RenderContext:
         self._check(self.lib.vkrt_cuda_trace_rays_device(self.handle, C.c_void_p(rays_ptr), count,
                                                          1 if any_hit else 0, C.c_void_p(hits_ptr)),
                     "trace rays (device)")
+
+
+def _handles(contexts):
+    arr = (C.c_void_p * len(contexts))(*[c.handle.value for c in contexts])
+    return arr
+
+
+def render_batch(contexts: list, scene_datas: np.ndarray) -> None:
+    """One batched wavefront frame over several contexts (vkrt_cuda_render_batch)."""
+    sds = np.ascontiguousarray(scene_datas, dtype=abi.SCENE_DATA)
+    arr = _handles(contexts)
+    r = contexts[0].lib.vkrt_cuda_render_batch(C.cast(arr, C.c_void_p), abi.ptr(sds), len(contexts))
+    contexts[0]._check(r, "render batch")
+
+
+def autotune_batch(contexts: list, scene_datas: np.ndarray, frames_per_trial: int = 1):
+    """Autotunes the wavefront configuration of a batch; returns (config, frame ms)."""
+    sds = np.ascontiguousarray(scene_datas, dtype=abi.SCENE_DATA)
+    arr = _handles(contexts)
+    best = np.zeros(1, dtype=abi.WAVEFRONT_CONFIG)
+    ms = C.c_float(0.0)
+    r = contexts[0].lib.vkrt_cuda_autotune_batch(C.cast(arr, C.c_void_p), abi.ptr(sds), len(contexts),
+                                                 frames_per_trial, abi.ptr(best), C.byref(ms))
+    contexts[0]._check(r, "autotune batch")
+    return best, ms.value

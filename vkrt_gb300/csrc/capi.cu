@@ -5,7 +5,10 @@
 // invalid arguments -1, other failures -2, allocation failures -3, CUDA faults that poison the context -4.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
+#include <memory>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -15,6 +18,7 @@
 #include "bvh_build.h"
 #include "context_view.h"
 #include "render.h"
+#include "wavefront.h"
 #include "scene.cuh"
 #include "vkrt_cuda.h"
 #include "vkrt_cuda_host.h"
@@ -103,6 +107,11 @@ struct VKRT_CudaContext {
     RenderCounters* counters = nullptr;
     RenderCounters lastCounters{};
     bool countersPending = false;
+
+    // wavefront integrator (owned by the context that leads a batch)
+    VKRT_CudaWavefrontConfig wfCfg{};
+    std::unique_ptr<WavefrontEngine> wavefront;
+    cudaEvent_t order = nullptr;  // orders this context's stream against a batch leader's stream
 };
 
 namespace {
@@ -203,6 +212,34 @@ uint16_t halfToFloatBits(uint16_t h, float& out) {
 
 float srgbToLinear(float c) { return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f); }
 
+int32_t validateFrame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
+    if (!sd) return invalid(c, "null SceneData");
+    if (!c->width) return invalid(c, "no film: call vkrt_cuda_resize first");
+    if (uint64_t(sd->viewportRect[0]) + sd->viewportRect[2] > c->width ||
+        uint64_t(sd->viewportRect[1]) + sd->viewportRect[3] > c->height)
+        return invalid(c, "viewport outside the film");
+    if (sd->rrMaxDepth > 1024u) return invalid(c, "rrMaxDepth above 1024");
+    if (sd->emissiveMeshCount > c->emissiveMeshCount) return invalid(c, "SceneData.emissiveMeshCount exceeds the uploaded lights");
+    for (const VKRT_CudaMeshInfo& m : c->hostMeshes)
+        if (m.materialIndex >= c->materialCount) return invalid(c, "mesh material index out of range");
+    const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
+    if (spectral) {
+        const VKRT_CudaRGB2SpecTableInfo& ti = sd->rgb2specSRGB;
+        if (!c->rgb2spec.ptr || ti.res < 2 ||
+            uint64_t(ti.scaleOffset) + ti.res > c->rgb2specFloats ||
+            uint64_t(ti.dataOffset) + 9ull * ti.res * ti.res * ti.res > c->rgb2specFloats)
+            return invalid(c, "spectral mode needs an rgb2spec table matching SceneData.rgb2specSRGB");
+        if (VKRT_CUDA_SPECTRAL_MODE_OF(sd->packedRenderSettings) != VKRT_CUDA_SPECTRAL_HERO)
+            return invalid(c, "only hero-wavelength spectral sampling is implemented");
+    }
+    return VKRT_CUDA_SUCCESS;
+}
+
+bool envNeeActive(const VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
+    return c->cfg.environmentSampling == VKRT_CUDA_ENV_IMPORTANCE && c->envTexture != VKRT_CUDA_INVALID_INDEX &&
+           sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u;
+}
+
 }  // namespace
 
 extern "C" {
@@ -217,6 +254,7 @@ void vkrt_cuda_default_config(VKRT_CudaConfig* cfg) {
     cfg->countRays = 0u;
     cfg->threadsPerBlock = 0u;
     cfg->blocksPerSM = 0u;
+    cfg->integrator = VKRT_CUDA_INTEGRATOR_MEGAKERNEL;
 }
 
 int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** out) {
@@ -235,13 +273,20 @@ int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** out) 
     c->cfg = cfg;
     c->device = cfg.deviceIndex;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->order, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&c->counters, sizeof(RenderCounters)) != cudaSuccess) {
+        if (c->order) cudaEventDestroy(c->order);
         if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return VKRT_CUDA_ERROR_INITIALIZATION_FAILED;
     }
     cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream);
     c->textureData.resize(VKRT_CUDA_MAX_TEXTURES);
+    vkrt_cuda_default_wavefront_config(&c->wfCfg);
+    if (cfg.integrator > VKRT_CUDA_INTEGRATOR_WAVEFRONT) {
+        vkrt_cuda_destroy(c);
+        return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    }
     c->textureDescs.assign(VKRT_CUDA_MAX_TEXTURES, TextureDesc{nullptr, 0u, 0u});
     *out = c;
     return VKRT_CUDA_SUCCESS;
@@ -273,6 +318,8 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     c->accum[1].release();
     c->output.release();
     if (c->counters) cudaFree(c->counters);
+    c->wavefront.reset();
+    if (c->order) cudaEventDestroy(c->order);
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -506,34 +553,20 @@ int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* c) {
 
 int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
     if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
-    if (!sd) return invalid(c, "null SceneData");
-    if (!c->width) return invalid(c, "no film: call vkrt_cuda_resize first");
-    if (uint64_t(sd->viewportRect[0]) + sd->viewportRect[2] > c->width ||
-        uint64_t(sd->viewportRect[1]) + sd->viewportRect[3] > c->height)
-        return invalid(c, "viewport outside the film");
-    if (sd->rrMaxDepth > 1024u) return invalid(c, "rrMaxDepth above 1024");
-    if (sd->emissiveMeshCount > c->emissiveMeshCount) return invalid(c, "SceneData.emissiveMeshCount exceeds the uploaded lights");
-    for (const VKRT_CudaMeshInfo& m : c->hostMeshes)
-        if (m.materialIndex >= c->materialCount) return invalid(c, "mesh material index out of range");
-    const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
-    if (spectral) {
-        const VKRT_CudaRGB2SpecTableInfo& ti = sd->rgb2specSRGB;
-        if (!c->rgb2spec.ptr || ti.res < 2 ||
-            uint64_t(ti.scaleOffset) + ti.res > c->rgb2specFloats ||
-            uint64_t(ti.dataOffset) + 9ull * ti.res * ti.res * ti.res > c->rgb2specFloats)
-            return invalid(c, "spectral mode needs an rgb2spec table matching SceneData.rgb2specSRGB");
-        if (VKRT_CUDA_SPECTRAL_MODE_OF(sd->packedRenderSettings) != VKRT_CUDA_SPECTRAL_HERO)
-            return invalid(c, "only hero-wavelength spectral sampling is implemented");
-    }
+    int32_t v = validateFrame(c, sd);
+    if (v != VKRT_CUDA_SUCCESS) return v;
     cudaSetDevice(c->device);
+    if (c->cfg.integrator == VKRT_CUDA_INTEGRATOR_WAVEFRONT) {
+        VKRT_CudaContext* one[1] = {c};
+        return vkrt_cuda_render_batch(one, sd, 1);
+    }
+    const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
+    (void)spectral;
     DeviceScene scene = makeDeviceScene(c);
     RenderParams rp{};
     rp.rngMode = c->cfg.rngMode;
     rp.rngSeed = c->cfg.rngSeed;
-    rp.envNee = (c->cfg.environmentSampling == VKRT_CUDA_ENV_IMPORTANCE && c->envTexture != VKRT_CUDA_INVALID_INDEX &&
-                 sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u)
-                    ? 1u
-                    : 0u;
+    rp.envNee = envNeeActive(c, sd) ? 1u : 0u;
     rp.width = c->width;
     rp.height = c->height;
     rp.countBytes = c->cfg.countRays;
@@ -542,6 +575,202 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     VKRT_TRY(c, launchRender(scene, *sd, rp, film, c->counters, c->cfg.threadsPerBlock, c->stream), "render launch");
     c->readIndex ^= 1;  // VKRT_endFrame's ping-pong swap (frame.c:386-389)
     c->countersPending = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+void vkrt_cuda_default_wavefront_config(VKRT_CudaWavefrontConfig* w) {
+    if (!w) return;
+    std::memset(w, 0, sizeof(*w));
+    w->queueCapacity = 0u;
+    w->tileWidth = 16u;
+    w->tileHeight = 8u;
+    w->sortByMaterial = 0u;
+    w->intersectBlocksPerSM = 8u;
+    w->shadeBlocksPerSM = 4u;
+    w->useGraph = 1u;
+}
+
+int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* c, const VKRT_CudaWavefrontConfig* w) {
+    if (!c || !w) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (w->tileWidth == 0 || w->tileHeight == 0 || w->tileWidth * w->tileHeight > 4096u)
+        return invalid(c, "tile must be between 1 and 4096 pixels");
+    if (w->intersectBlocksPerSM == 0 || w->intersectBlocksPerSM > 16u || w->shadeBlocksPerSM == 0 ||
+        w->shadeBlocksPerSM > 16u)
+        return invalid(c, "blocks per SM must be in [1, 16]");
+    if (w->queueCapacity > (1u << 26)) return invalid(c, "queue capacity above 64M path slots");
+    c->wfCfg = *w;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_get_wavefront_config(VKRT_CudaContext* c, VKRT_CudaWavefrontConfig* w) {
+    if (!c || !w) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    *w = c->wfCfg;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_CudaSceneData* sds, uint32_t count) {
+    if (!contexts || !sds || count == 0) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    VKRT_CudaContext* c0 = contexts[0];
+    if (!c0) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    bool spectral = VKRT_CUDA_RENDER_MODE_OF(sds[0].packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
+    std::vector<WfScene> scenes(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        VKRT_CudaContext* c = contexts[i];
+        if (!c) return invalid(c0, "null context in batch");
+        if (c->device != c0->device) return invalid(c0, "all contexts of a batch must be on one device");
+        if ((VKRT_CUDA_RENDER_MODE_OF(sds[i].packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL) != spectral)
+            return invalid(c0, "all scenes of a batch must share the render mode");
+        if (c->cfg.rngMode != c0->cfg.rngMode || c->cfg.rngSeed != c0->cfg.rngSeed)
+            return invalid(c0, "all contexts of a batch must share the random stream configuration");
+        for (uint32_t j = 0; j < i; ++j)
+            if (contexts[j] == c) return invalid(c0, "a context appears twice in the batch");
+        int32_t v = validateFrame(c, &sds[i]);
+        if (v != VKRT_CUDA_SUCCESS) {
+            c0->lastError = c->lastError;
+            return v;
+        }
+    }
+    cudaSetDevice(c0->device);
+    for (uint32_t i = 0; i < count; ++i) {
+        VKRT_CudaContext* c = contexts[i];
+        const VKRT_CudaSceneData& sd = sds[i];
+        WfScene& S = scenes[i];
+        std::memset(&S, 0, sizeof(S));
+        S.sc = makeDeviceScene(c);
+        S.sd = sd;
+        S.film = FilmBuffers{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
+        S.filmWidth = c->width;
+        S.filmHeight = c->height;
+        S.vx0 = sd.viewportRect[0];
+        S.vy0 = sd.viewportRect[1];
+        S.vw = sd.viewportRect[2];
+        S.vh = sd.viewportRect[3];
+        S.spp = std::max(sd.samplesPerPixel, 1u);
+        S.spectral = spectral ? 1u : 0u;
+        S.neeEnabled = (sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u) ? 1u : 0u;
+        S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
+        // c0's stream reads this context's buffers: order it after the work already queued on its own stream
+        if (c != c0) {
+            VKRT_TRY(c0, cudaEventRecord(c->order, c->stream), "batch ordering");
+            VKRT_TRY(c0, cudaStreamWaitEvent(c0->stream, c->order, 0), "batch ordering");
+        }
+    }
+    if (!c0->wavefront) c0->wavefront.reset(new WavefrontEngine());
+    WavefrontConfig wc{c0->wfCfg.queueCapacity, c0->wfCfg.tileWidth,     c0->wfCfg.tileHeight,
+                       c0->wfCfg.sortByMaterial, c0->wfCfg.intersectBlocksPerSM, c0->wfCfg.shadeBlocksPerSM,
+                       c0->wfCfg.useGraph};
+    VKRT_TRY(c0, cudaMemsetAsync(c0->counters, 0, sizeof(RenderCounters), c0->stream), "batch render");
+    VKRT_TRY(c0, c0->wavefront->render(scenes, spectral, wc, c0->cfg.rngMode, c0->cfg.rngSeed, c0->counters, c0->stream),
+             "batch render");
+    for (uint32_t i = 0; i < count; ++i) {
+        VKRT_CudaContext* c = contexts[i];
+        c->readIndex ^= 1;
+        if (c != c0) {
+            // later work on this context's own stream (reads, next frames) waits for the batch
+            VKRT_TRY(c0, cudaEventRecord(c->order, c0->stream), "batch ordering");
+            VKRT_TRY(c0, cudaStreamWaitEvent(c->stream, c->order, 0), "batch ordering");
+        }
+    }
+    c0->countersPending = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_CudaSceneData* sds, uint32_t count,
+                                 uint32_t framesPerTrial, VKRT_CudaWavefrontConfig* best, float* bestFrameMs) {
+    if (!contexts || !sds || count == 0 || !contexts[0]) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    VKRT_CudaContext* c0 = contexts[0];
+    cudaSetDevice(c0->device);
+    framesPerTrial = std::max(1u, std::min(framesPerTrial, 8u));
+    std::vector<VKRT_CudaSceneData> trial(sds, sds + count);
+    uint64_t pixels = 0;
+    for (auto& sd : trial) {
+        sd.samplesPerPixel = 2u;
+        pixels += uint64_t(sd.viewportRect[2]) * sd.viewportRect[3];
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto timeConfig = [&](const VKRT_CudaWavefrontConfig& w, float& ms) -> int32_t {
+        int32_t r = vkrt_cuda_set_wavefront_config(c0, &w);
+        if (r != VKRT_CUDA_SUCCESS) return r;
+        r = vkrt_cuda_render_batch(contexts, trial.data(), count);  // warm-up (graph build)
+        if (r != VKRT_CUDA_SUCCESS) return r;
+        cudaEventRecord(e0, c0->stream);
+        for (uint32_t f = 0; f < framesPerTrial; ++f) {
+            r = vkrt_cuda_render_batch(contexts, trial.data(), count);
+            if (r != VKRT_CUDA_SUCCESS) return r;
+        }
+        cudaEventRecord(e1, c0->stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) return fail(c0, e, "autotune");
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= float(framesPerTrial);
+        return VKRT_CUDA_SUCCESS;
+    };
+    VKRT_CudaWavefrontConfig cur;
+    vkrt_cuda_default_wavefront_config(&cur);
+    cur.queueCapacity = uint32_t(std::min<uint64_t>(pixels, 1u << 21));
+    float curMs = 0.0f;
+    int32_t r = timeConfig(cur, curMs);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    // coordinate descent over the knobs, each axis scanned with the others fixed at the best so far
+    std::vector<uint32_t> qs;
+    for (uint64_t q = 1u << 18; q <= std::min<uint64_t>(pixels * 2, 1u << 23); q <<= 1) qs.push_back(uint32_t(q));
+    const uint32_t tiles[][2] = {{8, 8}, {16, 8}, {32, 4}, {16, 16}, {32, 8}};
+    for (int axis = 0; axis < 5; ++axis) {
+        std::vector<VKRT_CudaWavefrontConfig> cands;
+        if (axis == 0)
+            for (uint32_t q : qs) {
+                VKRT_CudaWavefrontConfig w = cur;
+                w.queueCapacity = q;
+                cands.push_back(w);
+            }
+        if (axis == 1)
+            for (auto& t : tiles) {
+                VKRT_CudaWavefrontConfig w = cur;
+                w.tileWidth = t[0];
+                w.tileHeight = t[1];
+                cands.push_back(w);
+            }
+        if (axis == 2)
+            for (uint32_t s = 0; s < 2; ++s) {
+                VKRT_CudaWavefrontConfig w = cur;
+                w.sortByMaterial = s;
+                cands.push_back(w);
+            }
+        if (axis == 3)
+            for (uint32_t b : {4u, 6u, 8u}) {
+                VKRT_CudaWavefrontConfig w = cur;
+                w.intersectBlocksPerSM = b;
+                cands.push_back(w);
+            }
+        if (axis == 4)
+            for (uint32_t b : {2u, 3u, 4u}) {
+                VKRT_CudaWavefrontConfig w = cur;
+                w.shadeBlocksPerSM = b;
+                cands.push_back(w);
+            }
+        for (const auto& w : cands) {
+            if (std::memcmp(&w, &cur, sizeof(w)) == 0) continue;
+            float ms = 0.0f;
+            r = timeConfig(w, ms);
+            if (r != VKRT_CUDA_SUCCESS) return r;
+            if (ms < curMs) {
+                curMs = ms;
+                cur = w;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    r = vkrt_cuda_set_wavefront_config(c0, &cur);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    for (uint32_t i = 0; i < count; ++i) {
+        r = vkrt_cuda_reset_accumulation(contexts[i]);
+        if (r != VKRT_CUDA_SUCCESS) return r;
+    }
+    if (best) *best = cur;
+    if (bestFrameMs) *bestFrameMs = curMs;
     return VKRT_CUDA_SUCCESS;
 }
 

@@ -10,223 +10,15 @@
 #include <cmath>
 #include <vector>
 
-#include "integrator.cuh"
+#include "path.cuh"
 #include "render.h"
 
 namespace vkrt {
 
 namespace {
 
-// RGB path sample (integrator/path/rgb/integrator.slang:15-113)
-template <bool kCountBytes>
-VKRT_DEV float3 traceRgbPath(const KernelCtx& k, const RenderParams& rp, int px, int py, uint32_t sampleIndex,
-                             bool neeEnabled, bool envNee, PathCounts& pc) {
-    const VKRT_CudaSceneData& sd = k.sd;
-    Rng rng = makeRng(rp.rngMode, rp.rngSeed, px, py, sd.frameNumber, sampleIndex);
-    pc.samples++;
-    float jx = rng.next() - 0.5f;
-    float jy = rng.next() - 0.5f;
-    float3 o;
-    float3 d = primaryRay(sd, px, py, jx, jy, o);
-    float3 radiance = f3(0.0f), thr = f3(1.0f);
-    float prevBsdfPdf = 0.0f;
-    bool prevNee = false;
-    const float rot = sd.environmentRotation;
-    for (uint32_t depth = 0; depth < sd.rrMaxDepth; ++depth) {
-        if (depth == 0) pc.primary++;
-        else pc.extension++;
-        TraceHit h = closest<kCountBytes>(k, o, d);
-        if (h.mesh == VKRT_CUDA_INVALID_INDEX) {
-            float3 L = envRadiance(k.sc, sd, d);
-            float w = 1.0f;
-            if (envNee && prevNee && depth > 0 && prevBsdfPdf > 0.0f) {
-                float pe = envPdf(k.sc.env, d, rot);
-                if (pe > 0.0f) w = powerHeuristic(prevBsdfPdf, pe);
-            }
-            radiance += thr * L * w;
-            break;
-        }
-        if (!anyPos(thr)) break;
-        Surface s = reconstructSurface(k.sc, h.mesh, h.prim, h.u, h.v, o, d, h.t);
-        ShadeMaterial mat;
-        Basis basis;
-        shadeVertex(k.sc, s, d, mat, basis);
-        Bsdf bsdf = makeBsdf(mat, toLocal(-d, basis), s.frontFace);
-        float3 contrib = f3(0.0f);
-        if (neeEnabled && bsdf.wo.z > 0.0f) {  // light/direct/rgb_lighting.slang:7-31
-            LightSample ls;
-            if (sampleEmissive(k.sc, s.hitPoint, rng, ls)) {
-                pc.shadow++;
-                if (visible<kCountBytes>(k, s.hitPoint, s.geometricNormal, ls.wi, ls.shadowDist)) {
-                    float3 wl = toLocal(ls.wi, basis);
-                    float pdf;
-                    float3 f = evalRgb(bsdf, wl, pdf);
-                    if (pdf > 0.0f) contrib += f * fabsf(wl.z) * ls.emission * (powerHeuristic(ls.pdfSA, pdf) / ls.pdfSA);
-                }
-            }
-        }
-        if (envNee && bsdf.wo.z > 0.0f) {  // environment importance sampling, MIS with the BSDF
-            float u1 = rng.next(), u2 = rng.next();
-            float3 wi;
-            float pe;
-            if (envSample(k.sc.env, u1, u2, rot, wi, pe)) {
-                pc.shadow++;
-                if (visible<kCountBytes>(k, s.hitPoint, s.geometricNormal, wi, kTMax)) {
-                    float3 wl = toLocal(wi, basis);
-                    float pdf;
-                    float3 f = evalRgb(bsdf, wl, pdf);
-                    if (pdf > 0.0f)
-                        contrib += f * fabsf(wl.z) * envRadiance(k.sc, sd, wi) * (powerHeuristic(pe, pdf) / pe);
-                }
-            }
-        }
-        if (anyPos(mat.emission)) {
-            float w = 1.0f;
-            if (neeEnabled && prevNee && depth > 0 && prevBsdfPdf > 0.0f) {
-                float lps = emitterLightPdfSA(k.sc, h.mesh, h.t, d, s.geometricNormal);
-                w = lps <= 0.0f ? 1.0f : powerHeuristic(prevBsdfPdf, lps);
-            }
-            contrib += mat.emission * w;
-        }
-        radiance += thr * contrib;
-        if (bsdf.wo.z <= 0.0f) break;
-        float3 wl;
-        if (!sampleDirection(bsdf, rng, wl)) break;
-        float pdf;
-        float3 f = evalRgb(bsdf, wl, pdf);
-        if (!(pdf > 0.0f)) break;
-        float3 weight = f * (fabsf(wl.z) / pdf);
-        if (!anyPos(weight)) break;
-        thr *= weight;
-        if (!anyPos(thr)) break;
-        prevBsdfPdf = pdf;
-        prevNee = true;
-        if (depth + 1u >= sd.rrMinDepth) {
-            float p = fminf(fmaxf(maxc(thr), kRRMin), kRRMax);
-            if (rng.next() > p) break;
-            thr = thr / p;
-        }
-        o = s.hitPoint + s.geometricNormal * kShadowOriginOffset;
-        d = toWorld(wl, basis);
-    }
-    return radiance;
-}
-
-// Hero-wavelength path sample (integrator/path/spectral_hero/integrator.slang:16-172); returns CIE XYZ.
-// In the reflection-only subset every lane shares one technique pdf per vertex, so the four technique path pdfs
-// stay equal and are tracked as one scalar (the hero balance weights reduce to 1/4 per lane).
-template <bool kCountBytes>
-VKRT_DEV float3 traceHeroPath(const KernelCtx& k, const RenderParams& rp, const SpecTable& tab, int px, int py,
-                              uint32_t sampleIndex, bool neeEnabled, bool envNee, PathCounts& pc) {
-    const VKRT_CudaSceneData& sd = k.sd;
-    Rng rng = makeRng(rp.rngMode, rp.rngSeed, px, py, sd.frameNumber, sampleIndex);
-    pc.samples++;
-    float jx = rng.next() - 0.5f;
-    float jy = rng.next() - 0.5f;
-    float3 o;
-    float3 d = primaryRay(sd, px, py, jx, jy, o);
-    // sampleHeroWavelengths4 (sampling/wavelength.slang:29-47)
-    float radInv = float(reverseBits32(sampleIndex)) * (1.0f / 4294967296.0f);
-    float unit = fracf(radInv + rng.next());
-    float4 lam = make_float4(kLambdaMin + fracf(unit) * kLambdaRange, kLambdaMin + fracf(unit + 0.25f) * kLambdaRange,
-                             kLambdaMin + fracf(unit + 0.5f) * kLambdaRange, kLambdaMin + fracf(unit + 0.75f) * kLambdaRange);
-    float4 thr = f4(1.0f), spec = f4(0.0f);
-    // technique path pdfs are equal across lanes here: keep the common value and the previous vertex's
-    float techPath = 1.0f, prevVertexTech = 0.0f, prevBsdfTech = 0.0f;
-    bool prevNee = false;
-    const float rot = sd.environmentRotation;
-    for (uint32_t depth = 0; depth < sd.rrMaxDepth; ++depth) {
-        if (depth == 0) pc.primary++;
-        else pc.extension++;
-        TraceHit h = closest<kCountBytes>(k, o, d);
-        if (h.mesh == VKRT_CUDA_INVALID_INDEX) {
-            float3 L = envRadiance(k.sc, sd, d);
-            float w = techPath > 0.0f ? 0.25f : 0.0f;  // heroWavelengthBalanceWeight of four equal lanes
-            if (envNee && prevNee && depth > 0) {
-                float pe = envPdf(k.sc.env, d, rot);
-                float bt = prevVertexTech * prevBsdfTech, lt = prevVertexTech * pe;
-                float den = 4.0f * bt + 4.0f * lt;
-                w = den > 0.0f ? bt / den : 0.0f;
-            }
-            spec += thr * spectral4(tab, L, lam) * w;
-            break;
-        }
-        if (!anyPos(thr)) break;
-        Surface s = reconstructSurface(k.sc, h.mesh, h.prim, h.u, h.v, o, d, h.t);
-        ShadeMaterial mat;
-        Basis basis;
-        shadeVertex(k.sc, s, d, mat, basis);
-        Bsdf bsdf = makeBsdf(mat, toLocal(-d, basis), s.frontFace);
-        float4 contrib = f4(0.0f);
-        if (neeEnabled && bsdf.wo.z > 0.0f) {  // light/direct/spectral_lighting.slang:34-64
-            LightSample ls;
-            if (sampleEmissive(k.sc, s.hitPoint, rng, ls)) {
-                pc.shadow++;
-                if (visible<kCountBytes>(k, s.hitPoint, s.geometricNormal, ls.wi, ls.shadowDist)) {
-                    float3 wl = toLocal(ls.wi, basis);
-                    float pdf;
-                    float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
-                    float lt = techPath * ls.pdfSA, bt = techPath * pdf;
-                    float den = 4.0f * lt + 4.0f * bt;
-                    float mis = den > 0.0f ? lt / den : 0.0f;
-                    if (mis > 0.0f) contrib += fcos * spectral4(tab, ls.emission, lam) * (mis / ls.pdfSA);
-                }
-            }
-        }
-        if (envNee && bsdf.wo.z > 0.0f) {
-            float u1 = rng.next(), u2 = rng.next();
-            float3 wi;
-            float pe;
-            if (envSample(k.sc.env, u1, u2, rot, wi, pe)) {
-                pc.shadow++;
-                if (visible<kCountBytes>(k, s.hitPoint, s.geometricNormal, wi, kTMax)) {
-                    float3 wl = toLocal(wi, basis);
-                    float pdf;
-                    float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
-                    float lt = techPath * pe, bt = techPath * pdf;
-                    float den = 4.0f * lt + 4.0f * bt;
-                    float mis = den > 0.0f ? lt / den : 0.0f;
-                    if (mis > 0.0f) contrib += fcos * spectral4(tab, envRadiance(k.sc, sd, wi), lam) * (mis / pe);
-                }
-            }
-        }
-        if (anyPos(mat.emission)) {
-            float w = techPath > 0.0f ? 0.25f : 0.0f;
-            if (neeEnabled && prevNee && depth > 0) {
-                float lps = emitterLightPdfSA(k.sc, h.mesh, h.t, d, s.geometricNormal);
-                float bt = prevVertexTech * prevBsdfTech, lt = prevVertexTech * lps;
-                float den = 4.0f * bt + 4.0f * lt;
-                w = den > 0.0f ? bt / den : 0.0f;
-            }
-            contrib += spectral4(tab, mat.emission, lam) * w;
-        }
-        spec += thr * contrib;
-        if (bsdf.wo.z <= 0.0f) break;
-        float3 wl;
-        if (!sampleDirection(bsdf, rng, wl)) break;
-        float pdf;
-        float4 val = evalSpectral(bsdf, tab, wl, lam, pdf);
-        if (!(pdf > 0.0f)) break;
-        float4 weight = val * (fabsf(wl.z) / pdf);
-        if (!anyPos(weight)) break;
-        prevVertexTech = techPath;
-        prevBsdfTech = pdf;
-        techPath *= pdf;
-        thr *= weight;
-        if (!anyPos(thr)) break;
-        prevNee = true;
-        if (depth + 1u >= sd.rrMinDepth) {
-            float p = fminf(fmaxf(max4(thr), kRRMin), kRRMax);
-            if (rng.next() > p) break;
-            techPath *= p;
-            thr = thr / p;
-        }
-        o = s.hitPoint + s.geometricNormal * kShadowOriginOffset;
-        d = toWorld(wl, basis);
-    }
-    return spectral4ToXYZ(spec, lam, kLambdaRange);
-}
-
+// One pixel: SceneData.samplesPerPixel paths, each traced to the end (shadow rays traced inline), blended into the
+// running mean (writeback.slang:72-114) and encoded for display.
 template <bool kSpectral, bool kCountBytes>
 __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, VKRT_CudaSceneData sd, RenderParams rp,
                                                                FilmBuffers film, RenderCounters* counters) {
@@ -247,13 +39,30 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
             const float4 prev = film.accumRead[pixel];
             const uint32_t prevN = uint32_t(prev.w + 0.5f);  // integrator/path/state.slang:72
             const uint32_t spp = max(sd.samplesPerPixel, 1u);
-            const bool neeEnabled = sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u;
-            const bool envNee = rp.envNee != 0u;
+            StepConfig cfg{kSpectral, sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u, rp.envNee != 0u, rp.rngMode,
+                           rp.rngSeed};
             SpecTable tab{sc.rgb2spec, sd.rgb2specSRGB.res, sd.rgb2specSRGB.scaleOffset, sd.rgb2specSRGB.dataOffset};
             float3 sum = f3(0.0f);
             for (uint32_t si = 0; si < spp; ++si) {
-                if (kSpectral) sum += traceHeroPath<kCountBytes>(k, rp, tab, px, py, prevN + si, neeEnabled, envNee, pc);
-                else sum += traceRgbPath<kCountBytes>(k, rp, px, py, prevN + si, neeEnabled, envNee, pc);
+                PathState p = beginPath<kSpectral>(cfg, sd, px, py, prevN + si);
+                pc.samples++;
+                for (;;) {
+                    if (p.depth == 0) pc.primary++;
+                    else pc.extension++;
+                    TraceHit h = closest<kCountBytes>(k, p.o, p.d);
+                    ShadowRequest sh[2];
+                    uint32_t ns;
+                    bool cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
+                    for (uint32_t i = 0; i < ns; ++i) {
+                        pc.shadow++;
+                        TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
+                        if (traceBvh<true, kCountBytes>(sc, r, k.stackColumn, k.stackStride, counters).mesh ==
+                            VKRT_CUDA_INVALID_INDEX)
+                            p.radiance += sh[i].contribution;
+                    }
+                    if (!cont) break;
+                }
+                sum += pathResult<kSpectral>(cfg, p);
             }
             float3 cur = sum / float(spp);
             float pw = float(prevN), tw = pw + float(spp);

@@ -1,0 +1,682 @@
+// wavefront.cu — batched wavefront path tracing on sm_103a.
+//
+// One call renders one frame of every scene of a batch (one or many contexts of uneven size) with the same per-vertex
+// arithmetic as the megakernel (path.cuh), restructured into persistent stage kernels over compacted queues:
+//
+//   setup, init                      reset counters; every path slot takes a pixel and starts sample 0
+//   while (paths remain)             one conditional-while CUDA graph node, two ping-pong iterations per body:
+//     begin                          reset the output queues (and the material histogram)
+//     intersect                      closest hit of every queued path; material key + histogram when sorting
+//     sort (optional)                counting sort of the queue by (scene, material)
+//     shade                          pending shadow results applied, vertex shaded, shadow requests queued,
+//                                    continuing paths queued, finished ones handed to finalize
+//     shadow                         any-hit rays; visible requests flagged on their slot
+//     finalize                       sample radiance added to the pixel sum; next sample of the pixel, or the
+//                                    pixel written (running-mean blend + display encode) and the next pixel taken
+//     condition                      cudaGraphSetConditional(more work && iteration < bound)
+//
+// A path slot owns one pixel at a time and runs that pixel's samples one after another, so every pixel's samples are
+// summed in a fixed order by one slot: the result is deterministic and needs no atomics on the film. Pixels are
+// handed out in tiles (tileWidth x tileHeight, row-major) from one cursor over all scenes of the batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "path.cuh"
+#include "wavefront.h"
+
+namespace vkrt {
+
+namespace {
+
+constexpr uint32_t kWfThreads = 128;
+constexpr uint32_t kCntActive0 = 0, kCntActive1 = 1, kCntShadow = 2, kCntFinished = 3, kCntCursor = 4,
+                   kCntIteration = 5, kCntSlotsBusy = 6;
+
+struct WfGlobals {
+    const WfScene* scenes;
+    uint32_t sceneCount;
+    uint32_t totalWork;
+    uint32_t Q;
+    uint32_t maxIter;
+    uint32_t sort;
+    uint32_t keyCount;
+    uint32_t rngMode;
+    uint64_t rngSeed;
+    // slot state (structure of arrays, Q entries)
+    uint4* rng;
+    float4* o;       // xyz origin, w = depth (bits)
+    float4* d;       // xyz direction, w = flags (bits)
+    float4* thr;
+    float4* rad;
+    float4* mis;     // lamUnit, techPath, prevVertexTech, prevBsdfTech
+    float* pdf;      // prevBsdfPdf
+    uint32_t* slotScene;
+    uint32_t* slotWork;    // work item (tile-ordered pixel) within the scene
+    uint32_t* slotSample;  // samples of the pixel finished so far
+    float4* pixelSum;
+    uint4* hitA;     // mesh, prim, t, u
+    float* hitV;
+    uint32_t* hitKey;
+    float4* pend0;
+    float4* pend1;
+    uint32_t* pendFlags;  // bit 0/1: request 0/1 pending, bit 2/3: request 0/1 visible
+    // queues
+    uint32_t* queue0;
+    uint32_t* queue1;
+    uint32_t* finished;
+    uint32_t* sorted;
+    float4* shadowA;  // origin, tmax
+    float4* shadowB;  // direction, slot | request << 31
+    uint32_t* keyHist;
+    uint32_t* counts;
+    RenderCounters* counters;
+    cudaGraphConditionalHandle cond;
+};
+
+VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
+    unsigned mask = __activemask();
+    unsigned ballot = __ballot_sync(mask, want);
+    if (!ballot) return 0xFFFFFFFFu;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    return want ? base + __popc(ballot & ((1u << lane) - 1u)) : 0xFFFFFFFFu;
+}
+
+// warp-aggregated counter increment; every stage loop keeps whole warps together, so the warp is reconverged first
+VKRT_DEV void warpCount(unsigned long long* counter, uint32_t v) {
+    __syncwarp();
+    uint32_t total = __reduce_add_sync(0xFFFFFFFFu, v);
+    if ((threadIdx.x & 31u) == 0u && total) atomicAdd(counter, (unsigned long long)total);
+}
+
+VKRT_DEV uint32_t sceneOfWork(const WfGlobals& g, uint32_t w) {
+    uint32_t lo = 0, hi = g.sceneCount;
+    while (hi - lo > 1u) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (g.scenes[mid].workBase <= w) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// tile-ordered work item -> viewport pixel; false for padding items outside the viewport
+VKRT_DEV bool workPixel(const WfScene& S, uint32_t local, int& px, int& py) {
+    uint32_t tileArea = S.tileW * S.tileH;
+    uint32_t t = local / tileArea, i = local % tileArea;
+    uint32_t tx = t % S.tilesX, ty = t / S.tilesX;
+    uint32_t x = tx * S.tileW + i % S.tileW, y = ty * S.tileH + i / S.tileW;
+    if (x >= S.vw || y >= S.vh) return false;
+    px = int(S.vx0 + x);
+    py = int(S.vy0 + y);
+    return true;
+}
+
+VKRT_DEV void storePath(const WfGlobals& g, uint32_t s, const PathState& p) {
+    g.rng[s] = make_uint4(uint32_t(p.rng.state), uint32_t(p.rng.state >> 32), uint32_t(p.rng.inc),
+                          uint32_t(p.rng.inc >> 32));
+    g.o[s] = make_float4(p.o.x, p.o.y, p.o.z, __uint_as_float(p.depth));
+    g.d[s] = make_float4(p.d.x, p.d.y, p.d.z, __uint_as_float(p.flags));
+    g.thr[s] = p.thr;
+    g.rad[s] = p.radiance;
+    g.mis[s] = make_float4(p.lamUnit, p.techPath, p.prevVertexTech, p.prevBsdfTech);
+    g.pdf[s] = p.prevBsdfPdf;
+}
+
+VKRT_DEV PathState loadPath(const WfGlobals& g, uint32_t s) {
+    PathState p;
+    uint4 r = g.rng[s];
+    p.rng.state = uint64_t(r.x) | (uint64_t(r.y) << 32);
+    p.rng.inc = uint64_t(r.z) | (uint64_t(r.w) << 32);
+    float4 o = g.o[s], d = g.d[s];
+    p.o = make_float3(o.x, o.y, o.z);
+    p.depth = __float_as_uint(o.w);
+    p.d = make_float3(d.x, d.y, d.z);
+    p.flags = __float_as_uint(d.w);
+    p.thr = g.thr[s];
+    p.radiance = g.rad[s];
+    float4 m = g.mis[s];
+    p.lamUnit = m.x;
+    p.techPath = m.y;
+    p.prevVertexTech = m.z;
+    p.prevBsdfTech = m.w;
+    p.prevBsdfPdf = g.pdf[s];
+    return p;
+}
+
+VKRT_DEV StepConfig stepConfig(const WfGlobals& g, const WfScene& S) {
+    return StepConfig{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed};
+}
+
+VKRT_DEV SpecTable specTable(const WfScene& S) {
+    return SpecTable{S.sc.rgb2spec, S.sd.rgb2specSRGB.res, S.sd.rgb2specSRGB.scaleOffset, S.sd.rgb2specSRGB.dataOffset};
+}
+
+// starts sample `sample` of the slot's pixel; returns false for a padding work item
+template <bool kSpectral>
+VKRT_DEV bool startSample(const WfGlobals& g, uint32_t slot, uint32_t sceneId, uint32_t work, uint32_t sample) {
+    const WfScene& S = g.scenes[sceneId];
+    int px, py;
+    if (!workPixel(S, work, px, py)) return false;
+    uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
+    uint32_t prevN = uint32_t(S.film.accumRead[pix].w + 0.5f);
+    StepConfig cfg = stepConfig(g, S);
+    PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, prevN + sample);
+    storePath(g, slot, p);
+    g.pendFlags[slot] = 0u;
+    return true;
+}
+
+// takes work items from the cursor until a real pixel is found; false when the batch is exhausted
+template <bool kSpectral>
+VKRT_DEV bool acquirePixel(const WfGlobals& g, uint32_t slot, uint32_t w) {
+    for (;;) {
+        if (w >= g.totalWork) return false;
+        uint32_t sceneId = sceneOfWork(g, w);
+        uint32_t local = w - g.scenes[sceneId].workBase;
+        if (startSample<kSpectral>(g, slot, sceneId, local, 0u)) {
+            g.slotScene[slot] = sceneId;
+            g.slotWork[slot] = local;
+            g.slotSample[slot] = 0u;
+            g.pixelSum[slot] = f4(0.0f);
+            return true;
+        }
+        w = atomicAdd(&g.counts[kCntCursor], 1u);
+    }
+}
+
+__global__ void kWfSetup(WfGlobals g) {
+    if (threadIdx.x < 8u) g.counts[threadIdx.x] = 0u;
+    if (threadIdx.x == 0u) g.counts[kCntCursor] = min(g.Q, g.totalWork);
+}
+
+template <bool kSpectral>
+__global__ void __launch_bounds__(kWfThreads) kWfInit(WfGlobals g) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < g.Q; s += gridDim.x * blockDim.x) {
+        bool ok = acquirePixel<kSpectral>(g, s, s < g.totalWork ? s : g.totalWork);
+        uint32_t pos = warpPush(&g.counts[kCntActive0], ok);
+        if (ok) g.queue0[pos] = s;
+    }
+}
+
+// screen-space clear of film pixels outside each scene's viewport (writeback of raygen for !insideViewport)
+__global__ void kWfClearOutside(WfGlobals g) {
+    for (uint32_t si = blockIdx.y; si < g.sceneCount; si += gridDim.y) {
+        const WfScene& S = g.scenes[si];
+        uint32_t n = S.filmWidth * S.filmHeight;
+        if (S.vx0 == 0u && S.vy0 == 0u && S.vw == S.filmWidth && S.vh == S.filmHeight) continue;
+        for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+            uint32_t x = p % S.filmWidth, y = p / S.filmWidth;
+            if (x >= S.vx0 && y >= S.vy0 && x < S.vx0 + S.vw && y < S.vy0 + S.vh) continue;
+            S.film.accumWrite[p] = f4(0.0f);
+            S.film.output[p] = make_ushort4(0, 0, 0, 0);
+        }
+    }
+}
+
+__global__ void kWfBegin(WfGlobals g, uint32_t outQueue) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        g.counts[outQueue] = 0u;
+        g.counts[kCntShadow] = 0u;
+        g.counts[kCntFinished] = 0u;
+    }
+    if (g.sort)
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < g.keyCount; k += gridDim.x * blockDim.x)
+            g.keyHist[k] = 0u;
+}
+
+__global__ void __launch_bounds__(kWfThreads) kWfIntersect(WfGlobals g, uint32_t inQueue) {
+    extern __shared__ uint2 smemStack[];
+    const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
+    const uint32_t n = g.counts[inQueue];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        uint32_t primary = 0, ext = 0;
+        if (valid) {
+            uint32_t slot = q[i];
+            const WfScene& S = g.scenes[g.slotScene[slot]];
+            float4 o = g.o[slot], d = g.d[slot];
+            TraceRay r{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
+            TraceHit h = traceBvh<false, false>(S.sc, r, smemStack + threadIdx.x, blockDim.x, g.counters);
+            g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
+            g.hitV[slot] = h.v;
+            if (__float_as_uint(o.w) == 0u) primary = 1;
+            else ext = 1;
+            if (g.sort) {
+                uint32_t key = h.mesh == VKRT_CUDA_INVALID_INDEX
+                                   ? 0u
+                                   : 1u + S.materialKeyBase + S.sc.meshes[h.mesh].materialIndex;
+                g.hitKey[i] = key;
+                atomicAdd(&g.keyHist[key], 1u);
+            }
+        }
+        warpCount(&g.counters->primaryRays, primary);
+        warpCount(&g.counters->extensionRays, ext);
+    }
+}
+
+__global__ void __launch_bounds__(1024) kWfSortScan(WfGlobals g) {
+    // exclusive scan of the key histogram in place (one block)
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0u;
+    __syncthreads();
+    for (uint32_t base = 0; base < g.keyCount; base += 1024u) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < g.keyCount ? g.keyHist[i] : 0u;
+        uint32_t x = v;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+            if ((threadIdx.x & 31u) >= uint32_t(off)) x += y;
+        }
+        if ((threadIdx.x & 31u) == 31u) warpSums[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32u) {
+            uint32_t s = warpSums[threadIdx.x];
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, off);
+                if (threadIdx.x >= uint32_t(off)) s += y;
+            }
+            warpSums[threadIdx.x] = s;
+        }
+        __syncthreads();
+        uint32_t incl = x + ((threadIdx.x >> 5) ? warpSums[(threadIdx.x >> 5) - 1u] : 0u);
+        if (i < g.keyCount) g.keyHist[i] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 1023u) carry += incl;
+        __syncthreads();
+    }
+}
+
+__global__ void kWfSortScatter(WfGlobals g, uint32_t inQueue) {
+    const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
+    const uint32_t n = g.counts[inQueue];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t pos = atomicAdd(&g.keyHist[g.hitKey[i]], 1u);
+        g.sorted[pos] = q[i];
+    }
+}
+
+VKRT_DEV void applyPending(const WfGlobals& g, uint32_t slot, float4& radiance) {
+    uint32_t f = g.pendFlags[slot];
+    if ((f & 1u) && (f & 4u)) radiance += g.pend0[slot];
+    if ((f & 2u) && (f & 8u)) radiance += g.pend1[slot];
+}
+
+template <bool kSpectral>
+__global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
+    const uint32_t* q = g.sort ? g.sorted : (inQueue == 0 ? g.queue0 : g.queue1);
+    uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
+    const uint32_t n = g.counts[inQueue];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        bool cont = false;
+        uint32_t slot = 0, ns = 0;
+        ShadowRequest sh[2];
+        if (valid) {
+            slot = q[i];
+            const WfScene& S = g.scenes[g.slotScene[slot]];
+            PathState p = loadPath(g, slot);
+            applyPending(g, slot, p.radiance);
+            g.pendFlags[slot] = 0u;
+            uint4 a = g.hitA[slot];
+            TraceHit h{a.x, a.y, 0u, __uint_as_float(a.z), __uint_as_float(a.w), g.hitV[slot]};
+            StepConfig cfg = stepConfig(g, S);
+            cont = shadePathVertex<kSpectral>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns);
+            storePath(g, slot, p);
+            uint32_t flags = 0u;
+            if (ns > 0) {
+                g.pend0[slot] = sh[0].contribution;
+                flags |= 1u;
+            }
+            if (ns > 1) {
+                g.pend1[slot] = sh[1].contribution;
+                flags |= 2u;
+            }
+            g.pendFlags[slot] = flags;
+        }
+        // continuing paths to the next queue, finished ones to finalize (one atomic per warp and queue)
+        __syncwarp();
+        uint32_t pos = warpPush(&g.counts[outQueue], valid && cont);
+        if (valid && cont) outQ[pos] = slot;
+        pos = warpPush(&g.counts[kCntFinished], valid && !cont);
+        if (valid && !cont) g.finished[pos] = slot;
+        for (uint32_t r = 0; r < 2; ++r) {
+            bool want = valid && r < ns;
+            pos = warpPush(&g.counts[kCntShadow], want);
+            if (want) {
+                g.shadowA[pos] = make_float4(sh[r].origin.x, sh[r].origin.y, sh[r].origin.z, sh[r].tmax);
+                g.shadowB[pos] = make_float4(sh[r].dir.x, sh[r].dir.y, sh[r].dir.z, __uint_as_float(slot | (r << 31)));
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kWfThreads) kWfShadow(WfGlobals g) {
+    extern __shared__ uint2 smemStack[];
+    const uint32_t n = g.counts[kCntShadow];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        if (valid) {
+            float4 a = g.shadowA[i], b = g.shadowB[i];
+            uint32_t tag = __float_as_uint(b.w);
+            uint32_t slot = tag & 0x7FFFFFFFu, req = tag >> 31;
+            const WfScene& S = g.scenes[g.slotScene[slot]];
+            TraceRay r{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
+            TraceHit h = traceBvh<true, false>(S.sc, r, smemStack + threadIdx.x, blockDim.x, g.counters);
+            if (h.mesh == VKRT_CUDA_INVALID_INDEX) atomicOr(&g.pendFlags[slot], 4u << req);
+        }
+        warpCount(&g.counters->shadowRays, valid ? 1u : 0u);
+    }
+}
+
+template <bool kSpectral>
+__global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t outQueue) {
+    uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
+    const uint32_t n = g.counts[kCntFinished];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        bool requeue = false;
+        uint32_t slot = 0, samples = 0;
+        if (valid) {
+            slot = g.finished[i];
+            uint32_t sceneId = g.slotScene[slot];
+            const WfScene& S = g.scenes[sceneId];
+            PathState p = loadPath(g, slot);
+            applyPending(g, slot, p.radiance);
+            g.pendFlags[slot] = 0u;
+            StepConfig cfg = stepConfig(g, S);
+            float3 res = pathResult<kSpectral>(cfg, p);
+            float4 sum = g.pixelSum[slot] + make_float4(res.x, res.y, res.z, 0.0f);
+            uint32_t sample = g.slotSample[slot] + 1u;
+            samples = 1;
+            if (sample < S.spp) {
+                g.pixelSum[slot] = sum;
+                g.slotSample[slot] = sample;
+                requeue = startSample<kSpectral>(g, slot, sceneId, g.slotWork[slot], sample);
+            } else {
+                // pixel done: running-mean blend (writeback.slang:72-114) and display encode
+                int px, py;
+                workPixel(S, g.slotWork[slot], px, py);
+                uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
+                float4 prev = S.film.accumRead[pix];
+                float pw = float(uint32_t(prev.w + 0.5f)), tw = pw + float(S.spp);
+                float3 cur = xyz(sum) / float(S.spp);
+                float3 acc = tw <= 0.0f ? f3(0.0f) : (xyz(prev) * pw + cur * float(S.spp)) / tw;
+                S.film.accumWrite[pix] = make_float4(acc.x, acc.y, acc.z, tw);
+                S.film.output[pix] = encodeOutput(S.sd, acc, kSpectral);
+                uint32_t w = atomicAdd(&g.counts[kCntCursor], 1u);
+                requeue = acquirePixel<kSpectral>(g, slot, w);
+            }
+        }
+        __syncwarp();
+        uint32_t pos = warpPush(&g.counts[outQueue], valid && requeue);
+        if (valid && requeue) outQ[pos] = slot;
+        warpCount(&g.counters->pathSamples, samples);
+    }
+}
+
+__global__ void kWfCondition(WfGlobals g, uint32_t useGraph) {
+    uint32_t it = g.counts[kCntIteration] + 1u;
+    g.counts[kCntIteration] = it;
+    bool more = g.counts[kCntActive0] > 0u;
+    if (more && it >= g.maxIter) {
+        g.counters->errorFlags |= 2u;  // iteration bound reached with work left (never expected)
+        more = false;
+    }
+    if (useGraph) cudaGraphSetConditional(g.cond, more ? 1u : 0u);
+}
+
+template <class T>
+cudaError_t grow(T*& p, size_t& cap, size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1));
+    if (e == cudaSuccess) cap = n;
+    return e;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------------------------------------------
+struct WavefrontEngine::Buffers {
+    WfGlobals g{};
+    size_t capQ = 0, capKeys = 0, capScenes = 0;
+    size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
+           c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
+           c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0;
+    WfScene* scenes = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graphSpectral = false;
+    WavefrontConfig graphCfg{};
+    uint32_t graphQ = 0, graphKeys = 0, graphScenesCap = 0, graphMaxIter = 0, graphTotal = 0, graphSceneCount = 0;
+    WfGlobals graphG{};  // kernel arguments baked into the graph (conditional handle zeroed)
+};
+
+WavefrontEngine::WavefrontEngine() : b_(new Buffers()) {}
+
+WavefrontEngine::~WavefrontEngine() {
+    release();
+    delete b_;
+}
+
+void WavefrontEngine::release() {
+    if (!b_) return;
+    if (b_->exec) cudaGraphExecDestroy(b_->exec);
+    if (b_->graph) cudaGraphDestroy(b_->graph);
+    b_->exec = nullptr;
+    b_->graph = nullptr;
+    WfGlobals& g = b_->g;
+    void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotWork, g.slotSample, g.pixelSum,
+                    g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
+                    g.sorted, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    Buffers* fresh = new Buffers();
+    std::swap(*b_, *fresh);
+    delete fresh;
+}
+
+cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool spectral, const WavefrontConfig& cfgIn,
+                                    uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters,
+                                    cudaStream_t stream) {
+    Buffers& B = *b_;
+    WavefrontConfig cfg = cfgIn;
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (sms <= 0) sms = 1;
+    std::vector<WfScene> scenes = scenesIn;
+    uint32_t total = 0, keys = 1, maxSpp = 1, maxDepth = 1;
+    for (WfScene& S : scenes) {
+        S.tileW = std::max(1u, cfg.tileWidth);
+        S.tileH = std::max(1u, cfg.tileHeight);
+        S.tilesX = (S.vw + S.tileW - 1) / S.tileW;
+        uint32_t tilesY = (S.vh + S.tileH - 1) / S.tileH;
+        S.workBase = total;
+        S.workCount = S.tilesX * tilesY * S.tileW * S.tileH;
+        total += S.workCount;
+        S.materialKeyBase = keys - 1u;
+        keys += S.sc.materialCount;
+        maxSpp = std::max(maxSpp, S.spp);
+        maxDepth = std::max(maxDepth, S.sd.rrMaxDepth);
+    }
+    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(total, 1u << 22);
+    Q = std::max(1u, std::min(Q, std::max(total, 1u)));
+    uint32_t waves = (total + Q - 1) / Q;
+    uint32_t maxIter = (2u * waves + 2u) * maxSpp * (maxDepth + 2u) + 64u;
+
+    cudaError_t e = cudaSuccess;
+    WfGlobals& g = B.g;
+#define WF_GROW(field, cap, n) \
+    if (e == cudaSuccess) e = grow(g.field, B.cap, (n))
+    WF_GROW(rng, c_rng, Q);
+    WF_GROW(o, c_o, Q);
+    WF_GROW(d, c_d, Q);
+    WF_GROW(thr, c_thr, Q);
+    WF_GROW(rad, c_rad, Q);
+    WF_GROW(mis, c_mis, Q);
+    WF_GROW(pdf, c_pdf, Q);
+    WF_GROW(slotScene, c_scene, Q);
+    WF_GROW(slotWork, c_work, Q);
+    WF_GROW(slotSample, c_sample, Q);
+    WF_GROW(pixelSum, c_sum, Q);
+    WF_GROW(hitA, c_hitA, Q);
+    WF_GROW(hitV, c_hitV, Q);
+    WF_GROW(hitKey, c_key, Q);
+    WF_GROW(pend0, c_p0, Q);
+    WF_GROW(pend1, c_p1, Q);
+    WF_GROW(pendFlags, c_pf, Q);
+    WF_GROW(queue0, c_q0, Q);
+    WF_GROW(queue1, c_q1, Q);
+    WF_GROW(finished, c_fin, Q);
+    WF_GROW(sorted, c_sorted, Q);
+    WF_GROW(shadowA, c_sA, 2 * size_t(Q));
+    WF_GROW(shadowB, c_sB, 2 * size_t(Q));
+    WF_GROW(keyHist, c_hist, keys);
+    WF_GROW(counts, c_counts, 16);
+#undef WF_GROW
+    if (e == cudaSuccess) e = grow(B.scenes, B.c_sc, scenes.size());
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(B.scenes, scenes.data(), sizeof(WfScene) * scenes.size(), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    g.scenes = B.scenes;
+    g.sceneCount = uint32_t(scenes.size());
+    g.totalWork = total;
+    g.Q = Q;
+    g.maxIter = maxIter;
+    g.sort = cfg.sortByMaterial ? 1u : 0u;
+    g.keyCount = keys;
+    g.rngMode = rngMode;
+    g.rngSeed = rngSeed;
+    g.counters = counters;
+
+    const uint32_t gridI = uint32_t(sms) * std::max(1u, cfg.intersectBlocksPerSM);
+    const uint32_t gridS = uint32_t(sms) * std::max(1u, cfg.shadeBlocksPerSM);
+    const size_t smem = size_t(kWfThreads) * VKRT_SMEM_STACK * sizeof(uint2);
+
+    auto body = [&](uint32_t in, uint32_t out, bool useGraph) {
+        kWfBegin<<<4, 1024, 0, stream>>>(g, out);
+        kWfIntersect<<<gridI, kWfThreads, smem, stream>>>(g, in);
+        if (g.sort) {
+            kWfSortScan<<<1, 1024, 0, stream>>>(g);
+            kWfSortScatter<<<gridS, 256, 0, stream>>>(g, in);
+        }
+        if (spectral) kWfShade<true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+        else kWfShade<false><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+        kWfShadow<<<gridI, kWfThreads, smem, stream>>>(g);
+        if (spectral) kWfFinalize<true><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        else kWfFinalize<false><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        (void)useGraph;
+    };
+    auto prologue = [&]() {
+        kWfSetup<<<1, 32, 0, stream>>>(g);
+        dim3 cg(std::max(1, sms), std::min<uint32_t>(g.sceneCount, 64u));
+        kWfClearOutside<<<cg, 256, 0, stream>>>(g);
+        if (spectral) kWfInit<true><<<gridS, kWfThreads, 0, stream>>>(g);
+        else kWfInit<false><<<gridS, kWfThreads, 0, stream>>>(g);
+    };
+
+    if (!cfg.useGraph) {
+        prologue();
+        uint32_t* hostCount = nullptr;
+        e = cudaMallocHost(&hostCount, sizeof(uint32_t));
+        if (e != cudaSuccess) return e;
+        for (uint32_t it = 0; it < maxIter; it += 2) {
+            body(0, 1, false);
+            body(1, 0, false);
+            kWfCondition<<<1, 1, 0, stream>>>(g, 0u);
+            if ((it & 7u) == 6u || it + 2 >= maxIter) {
+                e = cudaMemcpyAsync(hostCount, g.counts + kCntActive0, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                    stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess || *hostCount == 0u) break;
+            }
+        }
+        cudaFreeHost(hostCount);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        return e;
+    }
+
+    // one graph per engine shape: setup/init kernels then a conditional while node over the two-iteration body
+    bool rebuild = !B.exec || B.graphSpectral != spectral || std::memcmp(&B.graphCfg, &cfg, sizeof(cfg)) != 0 ||
+                   B.graphQ != Q || B.graphKeys != keys || B.graphMaxIter != maxIter || B.graphTotal != total ||
+                   B.graphSceneCount != g.sceneCount;
+    {
+        WfGlobals a = g, b = B.graphG;
+        a.cond = 0;
+        b.cond = 0;
+        if (std::memcmp(&a, &b, sizeof(a)) != 0) rebuild = true;
+    }
+    if (rebuild) {
+        if (B.exec) cudaGraphExecDestroy(B.exec);
+        if (B.graph) cudaGraphDestroy(B.graph);
+        B.exec = nullptr;
+        B.graph = nullptr;
+        e = cudaGraphCreate(&B.graph, 0);
+        if (e != cudaSuccess) return e;
+        e = cudaGraphConditionalHandleCreate(&g.cond, B.graph, 1u, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) return e;
+        // prologue captured into the top-level graph
+        e = cudaStreamBeginCaptureToGraph(stream, B.graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) return e;
+        prologue();
+        cudaGraph_t captured = nullptr;
+        e = cudaStreamEndCapture(stream, &captured);
+        if (e != cudaSuccess) return e;
+        // the conditional node depends on every node of the prologue
+        size_t numNodes = 0;
+        cudaGraphGetNodes(B.graph, nullptr, &numNodes);
+        std::vector<cudaGraphNode_t> nodes(numNodes);
+        if (numNodes) cudaGraphGetNodes(B.graph, nodes.data(), &numNodes);
+        // zero-filled storage: the parameter union has no usable default constructor
+        alignas(cudaGraphNodeParams) unsigned char cpStorage[sizeof(cudaGraphNodeParams)];
+        std::memset(cpStorage, 0, sizeof(cpStorage));
+        cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cpStorage);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = g.cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t condNode;
+        e = cudaGraphAddNode(&condNode, B.graph, nodes.data(), nullptr, numNodes, &cp);
+        if (e != cudaSuccess) return e;
+        cudaGraph_t bodyGraph = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(stream, bodyGraph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) return e;
+        body(0, 1, true);
+        body(1, 0, true);
+        kWfCondition<<<1, 1, 0, stream>>>(g, 1u);
+        e = cudaStreamEndCapture(stream, &bodyGraph);
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&B.exec, B.graph, 0);
+        if (e != cudaSuccess) return e;
+        B.graphSpectral = spectral;
+        B.graphCfg = cfg;
+        B.graphQ = Q;
+        B.graphKeys = keys;
+        B.graphMaxIter = maxIter;
+        B.graphTotal = total;
+        B.graphSceneCount = g.sceneCount;
+        B.graphG = g;
+        B.graphG.cond = 0;
+    }
+    e = cudaGraphLaunch(B.exec, stream);
+    return e;
+}
+
+}  // namespace vkrt

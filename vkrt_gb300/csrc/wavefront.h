@@ -1,0 +1,57 @@
+// wavefront.h — host interface of the batched wavefront integrator (wavefront.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "render.h"
+#include "scene.cuh"
+
+namespace vkrt {
+
+// one scene of a batch as the stage kernels read it
+struct WfScene {
+    DeviceScene sc;
+    VKRT_CudaSceneData sd;
+    FilmBuffers film;
+    uint32_t filmWidth, filmHeight;
+    uint32_t vx0, vy0, vw, vh;  // viewport rectangle
+    uint32_t spp;
+    uint32_t spectral;
+    uint32_t neeEnabled;
+    uint32_t envNee;
+    // filled by the engine
+    uint32_t tileW, tileH, tilesX;
+    uint32_t workBase, workCount;
+    uint32_t materialKeyBase;
+};
+
+struct WavefrontConfig {
+    uint32_t queueCapacity;  // path slots; 0 = one per work item, capped at 4M
+    uint32_t tileWidth;
+    uint32_t tileHeight;
+    uint32_t sortByMaterial;
+    uint32_t intersectBlocksPerSM;
+    uint32_t shadeBlocksPerSM;
+    uint32_t useGraph;
+};
+
+class WavefrontEngine {
+public:
+    WavefrontEngine();
+    ~WavefrontEngine();
+    WavefrontEngine(const WavefrontEngine&) = delete;
+    WavefrontEngine& operator=(const WavefrontEngine&) = delete;
+
+    // Renders one frame of every scene (all spectral or all RGB) on `stream`, asynchronously.
+    cudaError_t render(const std::vector<WfScene>& scenes, bool spectral, const WavefrontConfig& cfg,
+                       uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters, cudaStream_t stream);
+    void release();
+
+private:
+    struct Buffers;
+    Buffers* b_;
+};
+
+}  // namespace vkrt
