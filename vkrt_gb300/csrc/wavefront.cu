@@ -3,7 +3,7 @@
 // One call renders one frame of every scene of a batch (one or many contexts of uneven size) with the same per-vertex
 // arithmetic as the megakernel (path.cuh), restructured into persistent stage kernels over compacted queues:
 //
-//   setup, init                      reset counters; every path slot takes a pixel and starts sample 0
+//   setup, init                      reset counters; every path slot takes a (pixel, sample) item and starts it
 //   while (paths remain)             one conditional-while CUDA graph node, two ping-pong iterations per body:
 //     begin                          reset the output queues (and the material histogram)
 //     intersect                      closest hit of every queued path; material key + histogram when sorting
@@ -11,13 +11,15 @@
 //     shade                          pending shadow results applied, vertex shaded, shadow requests queued,
 //                                    continuing paths queued, finished ones handed to finalize
 //     shadow                         any-hit rays; visible requests flagged on their slot
-//     finalize                       sample radiance added to the pixel sum; next sample of the pixel, or the
-//                                    pixel written (running-mean blend + display encode) and the next pixel taken
+//     finalize                       the sample's result stored in its item's place; the slot takes the next item
 //     condition                      cudaGraphSetConditional(more work && iteration < bound)
+//   resolve                          per pixel, results summed in sample order, blended into the running mean,
+//                                    encoded for display
 //
-// A path slot owns one pixel at a time and runs that pixel's samples one after another, so every pixel's samples are
-// summed in a fixed order by one slot: the result is deterministic and needs no atomics on the film. Pixels are
-// handed out in tiles (tileWidth x tileHeight, row-major) from one cursor over all scenes of the batch.
+// Items are handed out from one cursor over all scenes of the batch; the items of a pixel are consecutive and pixels
+// follow a tile order (tileWidth x tileHeight, row-major). Every slot stays busy until the cursor runs out, and
+// because each pixel's samples are summed in sample order by one thread of the resolve kernel the image is
+// deterministic, needs no atomics on the film, and equals the megakernel's bit for bit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,13 +35,24 @@ namespace vkrt {
 namespace {
 
 constexpr uint32_t kWfThreads = 128;
-constexpr uint32_t kCntActive0 = 0, kCntActive1 = 1, kCntShadow = 2, kCntFinished = 3, kCntCursor = 4,
-                   kCntIteration = 5, kCntSlotsBusy = 6;
+// counts[]: queue lengths (queue0, queue1, shadow, finished), the item cursor, the iteration, the fetch cursors
+enum : uint32_t {
+    kCntActive0 = 0,
+    kCntActive1 = 1,
+    kCntShadow = 2,
+    kCntFinished = 3,
+    kCntCursor = 4,
+    kCntIteration = 5,
+    kCntFetchIntersect = 6,
+    kCntFetchShadow = 7,
+};
+constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
 
 struct WfGlobals {
     const WfScene* scenes;
     uint32_t sceneCount;
-    uint32_t totalWork;
+    uint32_t totalWork;   // padded pixels of all scenes
+    uint32_t totalItems;  // (pixel, sample) items of all scenes
     uint32_t Q;
     uint32_t maxIter;
     uint32_t sort;
@@ -55,9 +68,8 @@ struct WfGlobals {
     float4* mis;     // lamUnit, techPath, prevVertexTech, prevBsdfTech
     float* pdf;      // prevBsdfPdf
     uint32_t* slotScene;
-    uint32_t* slotWork;    // work item (tile-ordered pixel) within the scene
-    uint32_t* slotSample;  // samples of the pixel finished so far
-    float4* pixelSum;
+    uint32_t* slotItem;    // (pixel, sample) item within the scene
+    float4* sampleBuf;     // one result per item, summed per pixel in sample order by the resolve kernel
     uint4* hitA;     // mesh, prim, t, u
     float* hitV;
     uint32_t* hitKey;
@@ -173,18 +185,28 @@ VKRT_DEV bool startSample(const WfGlobals& g, uint32_t slot, uint32_t sceneId, u
     return true;
 }
 
-// takes work items from the cursor until a real pixel is found; false when the batch is exhausted
+VKRT_DEV uint32_t sceneOfItem(const WfGlobals& g, uint32_t w) {
+    uint32_t lo = 0, hi = g.sceneCount;
+    while (hi - lo > 1u) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (g.scenes[mid].itemBase <= w) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Takes (pixel, sample) items from the cursor, starting with `w`, until one lies inside a viewport; false when the
+// batch is exhausted. Items of one pixel are consecutive (item = pixel work index * spp + sample).
 template <bool kSpectral>
-VKRT_DEV bool acquirePixel(const WfGlobals& g, uint32_t slot, uint32_t w) {
+VKRT_DEV bool acquireItem(const WfGlobals& g, uint32_t slot, uint32_t w) {
     for (;;) {
-        if (w >= g.totalWork) return false;
-        uint32_t sceneId = sceneOfWork(g, w);
-        uint32_t local = w - g.scenes[sceneId].workBase;
-        if (startSample<kSpectral>(g, slot, sceneId, local, 0u)) {
+        if (w >= g.totalItems) return false;
+        uint32_t sceneId = sceneOfItem(g, w);
+        const WfScene& S = g.scenes[sceneId];
+        uint32_t local = w - S.itemBase;
+        if (startSample<kSpectral>(g, slot, sceneId, local / S.spp, local % S.spp)) {
             g.slotScene[slot] = sceneId;
-            g.slotWork[slot] = local;
-            g.slotSample[slot] = 0u;
-            g.pixelSum[slot] = f4(0.0f);
+            g.slotItem[slot] = local;
             return true;
         }
         w = atomicAdd(&g.counts[kCntCursor], 1u);
@@ -193,15 +215,37 @@ VKRT_DEV bool acquirePixel(const WfGlobals& g, uint32_t slot, uint32_t w) {
 
 __global__ void kWfSetup(WfGlobals g) {
     if (threadIdx.x < 8u) g.counts[threadIdx.x] = 0u;
-    if (threadIdx.x == 0u) g.counts[kCntCursor] = min(g.Q, g.totalWork);
+    if (threadIdx.x == 0u) g.counts[kCntCursor] = min(g.Q, g.totalItems);
 }
 
 template <bool kSpectral>
 __global__ void __launch_bounds__(kWfThreads) kWfInit(WfGlobals g) {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < g.Q; s += gridDim.x * blockDim.x) {
-        bool ok = acquirePixel<kSpectral>(g, s, s < g.totalWork ? s : g.totalWork);
+        bool ok = acquireItem<kSpectral>(g, s, s < g.totalItems ? s : g.totalItems);
         uint32_t pos = warpPush(&g.counts[kCntActive0], ok);
         if (ok) g.queue0[pos] = s;
+    }
+}
+
+// Per pixel: the samples' results summed in sample order (as one thread summing its pixel's samples would), blended
+// into the running mean (writeback.slang:72-114) and encoded for display.
+template <bool kSpectral>
+__global__ void kWfResolve(WfGlobals g) {
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < g.totalWork; w += gridDim.x * blockDim.x) {
+        const WfScene& S = g.scenes[sceneOfWork(g, w)];
+        uint32_t local = w - S.workBase;
+        int px, py;
+        if (!workPixel(S, local, px, py)) continue;
+        const float4* r = g.sampleBuf + size_t(S.itemBase) + size_t(local) * S.spp;
+        float3 sum = f3(0.0f);
+        for (uint32_t s = 0; s < S.spp; ++s) sum += xyz(r[s]);
+        uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
+        float4 prev = S.film.accumRead[pix];
+        float pw = float(uint32_t(prev.w + 0.5f)), tw = pw + float(S.spp);
+        float3 cur = sum / float(S.spp);
+        float3 acc = tw <= 0.0f ? f3(0.0f) : (xyz(prev) * pw + cur * float(S.spp)) / tw;
+        S.film.accumWrite[pix] = make_float4(acc.x, acc.y, acc.z, tw);
+        S.film.output[pix] = encodeOutput(S.sd, acc, kSpectral);
     }
 }
 
@@ -225,6 +269,8 @@ __global__ void kWfBegin(WfGlobals g, uint32_t outQueue) {
         g.counts[outQueue] = 0u;
         g.counts[kCntShadow] = 0u;
         g.counts[kCntFinished] = 0u;
+        g.counts[kCntFetchIntersect] = 0u;
+        g.counts[kCntFetchShadow] = 0u;
     }
     if (g.sort)
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < g.keyCount; k += gridDim.x * blockDim.x)
@@ -235,31 +281,35 @@ __global__ void __launch_bounds__(kWfThreads) kWfIntersect(WfGlobals g, uint32_t
     extern __shared__ uint2 smemStack[];
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        uint32_t i = base + threadIdx.x;
-        bool valid = i < n;
-        uint32_t primary = 0, ext = 0;
-        if (valid) {
+    uint32_t primary = 0, ext = 0;
+    persistentTrace<false, kRefillLanes>(
+        n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
+        [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             uint32_t slot = q[i];
-            const WfScene& S = g.scenes[g.slotScene[slot]];
+            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
             float4 o = g.o[slot], d = g.d[slot];
-            TraceRay r{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
-            TraceHit h = traceBvh<false, false>(S.sc, r, smemStack + threadIdx.x, blockDim.x, g.counters);
+            r = TraceRay{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
+            nodes = sc.nodes;
+            tris = sc.tris;
+            nodeCount = sc.nodeCount;
+            if (__float_as_uint(o.w) == 0u) ++primary;
+            else ++ext;
+        },
+        [&](uint32_t i, const TraceHit& h) {
+            uint32_t slot = q[i];
             g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
             g.hitV[slot] = h.v;
-            if (__float_as_uint(o.w) == 0u) primary = 1;
-            else ext = 1;
             if (g.sort) {
+                const WfScene& S = g.scenes[g.slotScene[slot]];
                 uint32_t key = h.mesh == VKRT_CUDA_INVALID_INDEX
                                    ? 0u
                                    : 1u + S.materialKeyBase + S.sc.meshes[h.mesh].materialIndex;
                 g.hitKey[i] = key;
                 atomicAdd(&g.keyHist[key], 1u);
             }
-        }
-        warpCount(&g.counters->primaryRays, primary);
-        warpCount(&g.counters->extensionRays, ext);
-    }
+        });
+    warpCount(&g.counters->primaryRays, primary);
+    warpCount(&g.counters->extensionRays, ext);
 }
 
 __global__ void __launch_bounds__(1024) kWfSortScan(WfGlobals g) {
@@ -363,20 +413,25 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQ
 __global__ void __launch_bounds__(kWfThreads) kWfShadow(WfGlobals g) {
     extern __shared__ uint2 smemStack[];
     const uint32_t n = g.counts[kCntShadow];
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        uint32_t i = base + threadIdx.x;
-        bool valid = i < n;
-        if (valid) {
+    uint32_t traced = 0;
+    persistentTrace<true, kRefillLanes>(
+        n, &g.counts[kCntFetchShadow], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
+        [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             float4 a = g.shadowA[i], b = g.shadowB[i];
-            uint32_t tag = __float_as_uint(b.w);
-            uint32_t slot = tag & 0x7FFFFFFFu, req = tag >> 31;
-            const WfScene& S = g.scenes[g.slotScene[slot]];
-            TraceRay r{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
-            TraceHit h = traceBvh<true, false>(S.sc, r, smemStack + threadIdx.x, blockDim.x, g.counters);
-            if (h.mesh == VKRT_CUDA_INVALID_INDEX) atomicOr(&g.pendFlags[slot], 4u << req);
-        }
-        warpCount(&g.counters->shadowRays, valid ? 1u : 0u);
-    }
+            uint32_t slot = __float_as_uint(b.w) & 0x7FFFFFFFu;
+            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            r = TraceRay{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
+            nodes = sc.nodes;
+            tris = sc.tris;
+            nodeCount = sc.nodeCount;
+            ++traced;
+        },
+        [&](uint32_t i, const TraceHit& h) {
+            if (h.mesh != VKRT_CUDA_INVALID_INDEX) return;
+            uint32_t tag = __float_as_uint(g.shadowB[i].w);
+            atomicOr(&g.pendFlags[tag & 0x7FFFFFFFu], 4u << (tag >> 31));
+        });
+    warpCount(&g.counters->shadowRays, traced);
 }
 
 template <bool kSpectral>
@@ -397,27 +452,10 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             g.pendFlags[slot] = 0u;
             StepConfig cfg = stepConfig(g, S);
             float3 res = pathResult<kSpectral>(cfg, p);
-            float4 sum = g.pixelSum[slot] + make_float4(res.x, res.y, res.z, 0.0f);
-            uint32_t sample = g.slotSample[slot] + 1u;
+            g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
             samples = 1;
-            if (sample < S.spp) {
-                g.pixelSum[slot] = sum;
-                g.slotSample[slot] = sample;
-                requeue = startSample<kSpectral>(g, slot, sceneId, g.slotWork[slot], sample);
-            } else {
-                // pixel done: running-mean blend (writeback.slang:72-114) and display encode
-                int px, py;
-                workPixel(S, g.slotWork[slot], px, py);
-                uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
-                float4 prev = S.film.accumRead[pix];
-                float pw = float(uint32_t(prev.w + 0.5f)), tw = pw + float(S.spp);
-                float3 cur = xyz(sum) / float(S.spp);
-                float3 acc = tw <= 0.0f ? f3(0.0f) : (xyz(prev) * pw + cur * float(S.spp)) / tw;
-                S.film.accumWrite[pix] = make_float4(acc.x, acc.y, acc.z, tw);
-                S.film.output[pix] = encodeOutput(S.sd, acc, kSpectral);
-                uint32_t w = atomicAdd(&g.counts[kCntCursor], 1u);
-                requeue = acquirePixel<kSpectral>(g, slot, w);
-            }
+            uint32_t w = atomicAdd(&g.counts[kCntCursor], 1u);
+            requeue = acquireItem<kSpectral>(g, slot, w);
         }
         __syncwarp();
         uint32_t pos = warpPush(&g.counts[outQueue], valid && requeue);
@@ -482,7 +520,7 @@ void WavefrontEngine::release() {
     b_->exec = nullptr;
     b_->graph = nullptr;
     WfGlobals& g = b_->g;
-    void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotWork, g.slotSample, g.pixelSum,
+    void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotItem, g.sampleBuf,
                     g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
                     g.sorted, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes};
     for (void* p : ptrs)
@@ -503,6 +541,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     if (sms <= 0) sms = 1;
     std::vector<WfScene> scenes = scenesIn;
     uint32_t total = 0, keys = 1, maxSpp = 1, maxDepth = 1;
+    uint64_t items = 0;
     for (WfScene& S : scenes) {
         S.tileW = std::max(1u, cfg.tileWidth);
         S.tileH = std::max(1u, cfg.tileHeight);
@@ -511,15 +550,21 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         S.workBase = total;
         S.workCount = S.tilesX * tilesY * S.tileW * S.tileH;
         total += S.workCount;
+        S.itemBase = uint32_t(items);
+        items += uint64_t(S.workCount) * S.spp;
         S.materialKeyBase = keys - 1u;
         keys += S.sc.materialCount;
         maxSpp = std::max(maxSpp, S.spp);
         maxDepth = std::max(maxDepth, S.sd.rrMaxDepth);
     }
-    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(total, 1u << 22);
-    Q = std::max(1u, std::min(Q, std::max(total, 1u)));
-    uint32_t waves = (total + Q - 1) / Q;
-    uint32_t maxIter = (2u * waves + 2u) * maxSpp * (maxDepth + 2u) + 64u;
+    if (items >= 0xFFFFFFF0ull) return cudaErrorInvalidValue;  // item indices are 32-bit
+    const uint32_t totalItems = uint32_t(items);
+    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, 1u << 21);
+    Q = std::max(1u, std::min(Q, std::max(totalItems, 1u)));
+    // until the item cursor runs out every slot is busy, so the bounces of all items bound the iteration count;
+    // the condition kernel counts two-iteration bodies
+    uint64_t bodies = (uint64_t(totalItems) * (maxDepth + 1u) + Q - 1) / Q / 2u + maxDepth + 64u;
+    uint32_t maxIter = uint32_t(std::min<uint64_t>(bodies, 0x7FFFFFFFull));
 
     cudaError_t e = cudaSuccess;
     WfGlobals& g = B.g;
@@ -533,9 +578,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(mis, c_mis, Q);
     WF_GROW(pdf, c_pdf, Q);
     WF_GROW(slotScene, c_scene, Q);
-    WF_GROW(slotWork, c_work, Q);
-    WF_GROW(slotSample, c_sample, Q);
-    WF_GROW(pixelSum, c_sum, Q);
+    WF_GROW(slotItem, c_work, Q);
+    WF_GROW(sampleBuf, c_sum, std::max<size_t>(totalItems, 1));
     WF_GROW(hitA, c_hitA, Q);
     WF_GROW(hitV, c_hitV, Q);
     WF_GROW(hitKey, c_key, Q);
@@ -558,6 +602,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.scenes = B.scenes;
     g.sceneCount = uint32_t(scenes.size());
     g.totalWork = total;
+    g.totalItems = totalItems;
     g.Q = Q;
     g.maxIter = maxIter;
     g.sort = cfg.sortByMaterial ? 1u : 0u;
@@ -584,6 +629,10 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         else kWfFinalize<false><<<gridS, kWfThreads, 0, stream>>>(g, out);
         (void)useGraph;
     };
+    auto resolve = [&]() {
+        if (spectral) kWfResolve<true><<<gridS, 256, 0, stream>>>(g);
+        else kWfResolve<false><<<gridS, 256, 0, stream>>>(g);
+    };
     auto prologue = [&]() {
         kWfSetup<<<1, 32, 0, stream>>>(g);
         dim3 cg(std::max(1, sms), std::min<uint32_t>(g.sceneCount, 64u));
@@ -597,17 +646,18 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         uint32_t* hostCount = nullptr;
         e = cudaMallocHost(&hostCount, sizeof(uint32_t));
         if (e != cudaSuccess) return e;
-        for (uint32_t it = 0; it < maxIter; it += 2) {
+        for (uint32_t bodyIndex = 0; bodyIndex < maxIter; ++bodyIndex) {
             body(0, 1, false);
             body(1, 0, false);
             kWfCondition<<<1, 1, 0, stream>>>(g, 0u);
-            if ((it & 7u) == 6u || it + 2 >= maxIter) {
+            if ((bodyIndex & 3u) == 3u || bodyIndex + 1 >= maxIter) {
                 e = cudaMemcpyAsync(hostCount, g.counts + kCntActive0, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                     stream);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
                 if (e != cudaSuccess || *hostCount == 0u) break;
             }
         }
+        resolve();
         cudaFreeHost(hostCount);
         if (e == cudaSuccess) e = cudaGetLastError();
         return e;
@@ -662,6 +712,12 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         body(1, 0, true);
         kWfCondition<<<1, 1, 0, stream>>>(g, 1u);
         e = cudaStreamEndCapture(stream, &bodyGraph);
+        if (e != cudaSuccess) return e;
+        // the resolve kernel runs once the loop has drained every item
+        e = cudaStreamBeginCaptureToGraph(stream, B.graph, &condNode, nullptr, 1, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) return e;
+        resolve();
+        e = cudaStreamEndCapture(stream, &captured);
         if (e != cudaSuccess) return e;
         e = cudaGraphInstantiate(&B.exec, B.graph, 0);
         if (e != cudaSuccess) return e;

@@ -23,7 +23,8 @@ struct WfScene {
     uint32_t envNee;
     // filled by the engine
     uint32_t tileW, tileH, tilesX;
-    uint32_t workBase, workCount;
+    uint32_t workBase, workCount;  // padded pixel work items (tile order)
+    uint32_t itemBase;             // first (pixel, sample) item of the scene; items of a pixel are consecutive
     uint32_t materialKeyBase;
 };
 
