@@ -213,6 +213,54 @@ int32_t vkrt_cuda_trace_rays_device(VKRT_CudaContext* context, const VKRT_CudaRa
 int32_t vkrt_cuda_trace_rays_noalloc(VKRT_CudaContext* context, const VKRT_CudaRay* rays, uint32_t count,
                                      uint32_t anyHit, VKRT_CudaHit* hits);
 
+/* ---------------------------------------------------------------------------------------------------------------
+ * Differentiable rendering (path-replay backpropagation). No counterpart in vkrt, whose renderer has no adjoint:
+ * these calls are an addition of this backend, built on the same RGB integrator as vkrt_cuda_render_frame.
+ * ------------------------------------------------------------------------------------------------------------- */
+#define VKRT_CUDA_GRADIENT_BASE_COLOR 1u /* Material.baseColor and baseColor-texture texels (RGB) */
+#define VKRT_CUDA_GRADIENT_ROUGHNESS 2u  /* Material.roughness and metallic-roughness-texture texels (G) */
+#define VKRT_CUDA_GRADIENT_EMISSION 4u   /* emission radiance (emissionColor x emissionLuminance) per material */
+
+typedef struct VKRT_CudaAdjointConfig {
+    uint32_t sampleBase; /* accumulated sample count before the differentiated frame (0 after a reset) */
+    uint32_t gradients;  /* VKRT_CUDA_GRADIENT_* mask; 0 = all */
+    uint32_t accumulate; /* nonzero: add to the gradient buffers; zero: clear them first */
+    uint32_t reserved[5];
+} VKRT_CudaAdjointConfig;
+
+/* Per-material gradient record, 32 bytes. */
+typedef struct VKRT_CudaMaterialGradient {
+    float baseColor[3];
+    float roughness;
+    float emission[3];
+    float reserved;
+} VKRT_CudaMaterialGradient;
+
+void vkrt_cuda_default_adjoint_config(VKRT_CudaAdjointConfig* config);
+
+/* Material of each emissive-mesh entry uploaded with vkrt_cuda_upload_lights (the mesh whose emission the entry
+ * copies), needed to route light-sampling terms to emission gradients. */
+int32_t vkrt_cuda_set_emissive_mesh_materials(VKRT_CudaContext* context, const uint32_t* materials, uint32_t count);
+
+/* Adds to the gradient buffers d(loss)/d(parameters) for the frame vkrt_cuda_render_frame renders from
+ * `sceneData` (same frame number, seeds and scene), given dImage = d(loss)/d(accumulation) as width*height RGBA32F
+ * values (alpha ignored). RGB render mode only; materials must have specularTint 0 (its F0 tint couples the colour
+ * channels and is not differentiated). Gradients are unbiased for the expected image; with Russian roulette off
+ * (rrMinDepth > rrMaxDepth) and sampling densities independent of the parameters they are the exact derivative of
+ * the fixed-seed estimator. Host dImage: synchronous upload, asynchronous kernel on the context stream. */
+int32_t vkrt_cuda_render_adjoint(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData, const float* dImage,
+                                 const VKRT_CudaAdjointConfig* config);
+/* Same with dImage in device memory (asynchronous on the context stream). */
+int32_t vkrt_cuda_render_adjoint_device(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData,
+                                        const float* deviceDImage, const VKRT_CudaAdjointConfig* config);
+
+/* Gradient of the texels of texture slot `textureIndex` (width*height RGBA32F, same layout as the upload; zeros
+ * for slots no material samples as baseColor or metallic-roughness). Synchronous. */
+int32_t vkrt_cuda_read_texture_gradient(VKRT_CudaContext* context, uint32_t textureIndex, float* rgba, size_t bytes);
+/* Per-material gradients, `count` <= material count. Synchronous. */
+int32_t vkrt_cuda_read_material_gradients(VKRT_CudaContext* context, VKRT_CudaMaterialGradient* gradients,
+                                          uint32_t count);
+
 /* Last error message of this context (never NULL). */
 const char* vkrt_cuda_last_error(VKRT_CudaContext* context);
 

@@ -52,12 +52,13 @@ def load():
         "oracle_trace_fp32": (_I32, [_V, _V, _U32, _U32, _V, _U32]),
         "oracle_trace_fp64_bruteforce": (_I32, [_V, _V, _U32, _V, _V, _D, _U32]),
         "oracle_render": (_I32, [_V, _V, _V, _V, _V, _V, _V]),
+        "oracle_render_f64": (_I32, [_V, _V, _V, _V, _V]),
         "oracle_hash": (_U32, [_U32]), "oracle_init_pixel_seed": (_U32, [C.c_int32, C.c_int32, _U32, _U32]),
         "oracle_rand": (_F, [_V]), "oracle_pcg32": (_U32, [_V, _U64]),
         "oracle_world_triangles": (_U32, [_V, _V, _U32]),
         "oracle_env_cdf": (_I32, [_V, _U32, _U32, _V, _V, _V]),
         "oracle_env_pdf": (_F, [_V, _V, _F]), "oracle_env_sample": (_I32, [_V, _F, _F, _F, _V, _V]),
-        "oracle_rgb2spec_generate": (_I32, [_V, _U32, _V, _U32, _U32]) if False else (_I32, [_U32, _V, _U32, _U32]),
+        "oracle_rgb2spec_generate": (_I32, [_U32, _V, _U32, _U32]),
         "oracle_rgb2spec_fetch": (None, [_V, _U32, _V, _V]), "oracle_rgb2spec_eval": (_F, [_V, _F]),
         "oracle_spectral_to_xyz": (None, [_F, _V]), "oracle_xyz_to_linear_srgb": (None, [_V, _V]),
         "oracle_bsdf_eval_rgb": (_I32, [_V, _V, _V, _U32, _V, _V]),
@@ -159,6 +160,20 @@ class OracleScene:
             raise RuntimeError(f"oracle_render failed ({r})")
         stats = {k: getattr(st, k) for k, _ in OracleRenderStats._fields_}
         return (acc_out, out, stats) if want_output else (acc_out, stats)
+
+    def render_f64(self, scene_data, rng_mode=0, rng_seed=1, precision=64, threads=0):
+        """One frame from a cleared film, the accumulation returned in float64 (H, W, 4)."""
+        from vkrt_gb300 import abi
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA)
+        w = int(sd["viewportRect"][0][0] + sd["viewportRect"][0][2])
+        h = int(sd["viewportRect"][0][1] + sd["viewportRect"][0][3])
+        acc_in = np.zeros((h, w, 4), np.float32)
+        acc_out = np.zeros((h, w, 4), np.float64)
+        p = OracleRenderParams(rng_mode, rng_seed, precision, threads, 0, 0, 0)
+        r = self.lib.oracle_render_f64(self.handle, _p(sd), C.byref(p), _p(acc_in), _p(acc_out))
+        if r != 0:
+            raise RuntimeError(f"oracle_render_f64 failed ({r})")
+        return acc_out
 
     def env_pdf(self, direction, rotation=0.0):
         d = np.ascontiguousarray(direction, np.float32)

@@ -1779,7 +1779,7 @@ void tonemapPixel(const VKRT_CudaSceneData& sd, V3<float> acc, bool spectral, ui
 template <class R>
 void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderParams& p, const float* accIn,
                 float* accOut, uint16_t* outImg, OracleRenderStats* statsOut,
-                const std::vector<std::array<double, 9>>* tri64) {
+                const std::vector<std::array<double, 9>>* tri64, double* accOut64 = nullptr) {
     uint32_t W = sd.viewportRect[0] + sd.viewportRect[2];
     uint32_t H = sd.viewportRect[1] + sd.viewportRect[3];
     uint32_t r0 = p.rowBegin, r1 = p.rowEnd ? std::min(p.rowEnd, H) : H;
@@ -1827,6 +1827,12 @@ void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderPa
             accOut[pi * 4 + 1] = float(acc.y);
             accOut[pi * 4 + 2] = float(acc.z);
             accOut[pi * 4 + 3] = float(tw);
+            if (accOut64) {
+                accOut64[pi * 4 + 0] = double(acc.x);
+                accOut64[pi * 4 + 1] = double(acc.y);
+                accOut64[pi * 4 + 2] = double(acc.z);
+                accOut64[pi * 4 + 3] = double(tw);
+            }
             if (outImg) tonemapPixel(sd, V3<float>(acc), spectral, &outImg[pi * 4]);
         }
         rowStats[ri] = c.stats;
@@ -2020,6 +2026,19 @@ int32_t oracle_render(void* p, const VKRT_CudaSceneData* sd, const OracleRenderP
         renderRows<double>(*sp, *sd, *params, accIn, accOut, out, stats, &h->tri64);
     else
         renderRows<float>(*sp, *sd, *params, accIn, accOut, out, stats, &h->tri64);
+    return 0;
+}
+
+int32_t oracle_render_f64(void* p, const VKRT_CudaSceneData* sd, const OracleRenderParams* params, const float* accIn,
+                          double* accOut64) {
+    SceneHandle* h = static_cast<SceneHandle*>(p);
+    if (!h || !sd || !params || !accIn || !accOut64) return -1;
+    size_t n = size_t(sd->viewportRect[0] + sd->viewportRect[2]) * (sd->viewportRect[1] + sd->viewportRect[3]) * 4;
+    std::vector<float> acc32(n);
+    if (params->precision == 64)
+        renderRows<double>(h->s, *sd, *params, accIn, acc32.data(), nullptr, nullptr, &h->tri64, accOut64);
+    else
+        renderRows<float>(h->s, *sd, *params, accIn, acc32.data(), nullptr, nullptr, &h->tri64, accOut64);
     return 0;
 }
 

@@ -80,6 +80,11 @@ int32_t oracle_trace_fp64_bruteforce(void* scene, const VKRT_CudaRay* rays, uint
 int32_t oracle_render(void* scene, const VKRT_CudaSceneData* sceneData, const OracleRenderParams* params,
                       const float* accumIn, float* accumOut, uint16_t* outputRGBA16, OracleRenderStats* stats);
 
+/* Same frame with the accumulation written in double precision (the image before its FP32 store), for
+ * finite-difference checks of gradients. */
+int32_t oracle_render_f64(void* scene, const VKRT_CudaSceneData* sceneData, const OracleRenderParams* params,
+                          const float* accumIn, double* accumOut);
+
 /* RNG known answers */
 uint32_t oracle_hash(uint32_t v);
 uint32_t oracle_init_pixel_seed(int32_t x, int32_t y, uint32_t frame, uint32_t sampleIndex);

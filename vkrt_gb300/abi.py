@@ -89,6 +89,15 @@ STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathS
                   "formats": ["<u8", "<u8", "<u8", "<u8", "<u8", "<u8", "<u4", "<u4", "<u8", "<f4", "<u4"],
                   "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 64, 68], "itemsize": 72})
 
+ADJOINT_CONFIG = np.dtype({"names": ["sampleBase", "gradients", "accumulate", "reserved"],
+                           "formats": ["<u4", "<u4", "<u4", ("<u4", 5)], "offsets": [0, 4, 8, 12], "itemsize": 32})
+
+MATERIAL_GRADIENT = np.dtype({"names": ["baseColor", "roughness", "emission", "reserved"],
+                              "formats": [("<f4", 3), "<f4", ("<f4", 3), "<f4"], "offsets": [0, 12, 16, 28],
+                              "itemsize": 32})
+
+GRADIENT_BASE_COLOR, GRADIENT_ROUGHNESS, GRADIENT_EMISSION = 1, 2, 4
+
 # constants (src/shared/constants.h)
 TONE_MAPPING_NONE, TONE_MAPPING_ACES = 0, 1
 RENDER_MODE_RGB, RENDER_MODE_SPECTRAL = 0, 1
@@ -155,6 +164,12 @@ EXPORTS = {
     "vkrt_cuda_get_wavefront_config": (_I32, [_V, _V]),
     "vkrt_cuda_render_batch": (_I32, [_V, _V, _U32]),
     "vkrt_cuda_autotune_batch": (_I32, [_V, _V, _U32, _U32, _V, _V]),
+    "vkrt_cuda_default_adjoint_config": (None, [_V]),
+    "vkrt_cuda_set_emissive_mesh_materials": (_I32, [_V, _V, _U32]),
+    "vkrt_cuda_render_adjoint": (_I32, [_V, _V, _V, _V]),
+    "vkrt_cuda_render_adjoint_device": (_I32, [_V, _V, _V, _V]),
+    "vkrt_cuda_read_texture_gradient": (_I32, [_V, _U32, _V, _SZ]),
+    "vkrt_cuda_read_material_gradients": (_I32, [_V, _V, _U32]),
     "vkrt_host_pack_shader_vertices": (None, [_V, _U32, _V]),
     "vkrt_host_mesh_transform": (None, [_V, _V, _V, _V]),
     "vkrt_host_camera_matrices": (None, [_V, _V, _V, _F, _F, _F, _U32, _U32, _V]),

@@ -37,6 +37,7 @@ class Scene:
     tri_alias_q: np.ndarray | None = None
     tri_alias_idx: np.ndarray | None = None
     rgb2spec: np.ndarray | None = None    # float32 table in vkrt's layout
+    emissive_mesh_materials: np.ndarray | None = None  # uint32, material of each emissive-mesh entry
     name: str = ""
 
     @property
@@ -83,6 +84,10 @@ def build_light_tables(scene: Scene) -> None:
     scene.emissive_triangles = et[: nt.value].copy()
     scene.mesh_alias_q, scene.mesh_alias_idx = mq[: nm.value].copy(), mi[: nm.value].copy()
     scene.tri_alias_q, scene.tri_alias_idx = tq[: nt.value].copy(), ti[: nt.value].copy()
+    # entries follow mesh order and every entry's mesh gets lightPdfArea > 0
+    lit = np.nonzero(scene.meshes["lightPdfArea"] > 0.0)[0]
+    scene.emissive_mesh_materials = np.ascontiguousarray(scene.meshes["materialIndex"][lit][: nm.value],
+                                                         dtype=np.uint32)
     scene.scene_data["emissiveMeshCount"] = nm.value
     scene.scene_data["emissiveTriangleCount"] = nt.value
 
@@ -147,12 +152,7 @@ class RenderContext:
                     "upload materials")
         self._check(self.lib.vkrt_cuda_upload_geometry(self.handle, abi.ptr(sv), len(sv), abi.ptr(idx), len(idx),
                                                        abi.ptr(scene.meshes), len(scene.meshes)), "upload geometry")
-        if scene.emissive_meshes is not None and len(scene.emissive_meshes):
-            self._check(self.lib.vkrt_cuda_upload_lights(
-                self.handle, abi.ptr(scene.emissive_meshes), len(scene.emissive_meshes),
-                abi.ptr(scene.emissive_triangles), len(scene.emissive_triangles), abi.ptr(scene.mesh_alias_q),
-                abi.ptr(scene.mesh_alias_idx), abi.ptr(scene.tri_alias_q), abi.ptr(scene.tri_alias_idx)),
-                "upload lights")
+        self._upload_lights(scene)
         for slot, tex in scene.textures.items():
             self.upload_texture(slot, tex)
         if scene.env_texture != abi.INVALID_INDEX:
@@ -168,6 +168,27 @@ class RenderContext:
             scene.scene_data["rgb2specSRGB"] = info
         self.resize(scene.width, scene.height)
         self.scene = scene
+
+    def _upload_lights(self, scene: Scene) -> None:
+        if scene.emissive_meshes is None or not len(scene.emissive_meshes):
+            return
+        self._check(self.lib.vkrt_cuda_upload_lights(
+            self.handle, abi.ptr(scene.emissive_meshes), len(scene.emissive_meshes),
+            abi.ptr(scene.emissive_triangles), len(scene.emissive_triangles), abi.ptr(scene.mesh_alias_q),
+            abi.ptr(scene.mesh_alias_idx), abi.ptr(scene.tri_alias_q), abi.ptr(scene.tri_alias_idx)),
+            "upload lights")
+        if scene.emissive_mesh_materials is not None:
+            m = np.ascontiguousarray(scene.emissive_mesh_materials, dtype=np.uint32)
+            self._check(self.lib.vkrt_cuda_set_emissive_mesh_materials(self.handle, abi.ptr(m), len(m)),
+                        "set emissive mesh materials")
+
+    def upload_scene_materials(self, scene: Scene) -> None:
+        """Re-uploads materials, mesh records (lightPdfArea) and light tables after material edits; call
+        build_light_tables(scene) first when emission changed."""
+        self._check(self.lib.vkrt_cuda_upload_materials(self.handle, abi.ptr(scene.materials), len(scene.materials)),
+                    "upload materials")
+        self.update_meshes(scene.meshes)
+        self._upload_lights(scene)
 
     def upload_texture(self, slot: int, rgba: np.ndarray, fmt: int = abi.TEXTURE_FORMAT_RGBA32_SFLOAT,
                        color_space: int = abi.COLOR_SPACE_LINEAR) -> None:
@@ -224,6 +245,44 @@ class RenderContext:
     def read_output(self) -> np.ndarray:
         out = np.empty((self.height, self.width, 4), dtype=np.uint16)
         self._check(self.lib.vkrt_cuda_read_output(self.handle, abi.ptr(out), out.nbytes), "read output")
+        return out
+
+    # ---- path-replay adjoint -----------------------------------------------------------------------------------
+    def render_adjoint(self, scene_data: np.ndarray, d_image: np.ndarray, sample_base: int = 0, gradients: int = 0,
+                       accumulate: bool = False) -> None:
+        """Adds d(loss)/d(parameters) for the frame `scene_data` renders, given d_image = d(loss)/d(accumulation)
+        as (height, width, 3 or 4) float32 (vkrt_cuda_render_adjoint)."""
+        d = np.zeros((self.height, self.width, 4), dtype=np.float32)
+        d[..., : d_image.shape[-1]] = d_image
+        cfg = np.zeros(1, dtype=abi.ADJOINT_CONFIG)
+        cfg["sampleBase"] = sample_base
+        cfg["gradients"] = gradients
+        cfg["accumulate"] = 1 if accumulate else 0
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA)
+        self._check(self.lib.vkrt_cuda_render_adjoint(self.handle, abi.ptr(sd), abi.ptr(d), abi.ptr(cfg)),
+                    "render adjoint")
+
+    def render_adjoint_device(self, scene_data: np.ndarray, d_image_ptr: int, sample_base: int = 0,
+                              gradients: int = 0, accumulate: bool = False) -> None:
+        """Same with d(loss)/d(accumulation) in device memory (height*width RGBA32F at d_image_ptr)."""
+        cfg = np.zeros(1, dtype=abi.ADJOINT_CONFIG)
+        cfg["sampleBase"] = sample_base
+        cfg["gradients"] = gradients
+        cfg["accumulate"] = 1 if accumulate else 0
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA)
+        self._check(self.lib.vkrt_cuda_render_adjoint_device(self.handle, abi.ptr(sd), C.c_void_p(d_image_ptr),
+                                                             abi.ptr(cfg)), "render adjoint")
+
+    def read_texture_gradient(self, slot: int, shape: tuple[int, int]) -> np.ndarray:
+        out = np.empty((shape[0], shape[1], 4), dtype=np.float32)
+        self._check(self.lib.vkrt_cuda_read_texture_gradient(self.handle, slot, abi.ptr(out), out.nbytes),
+                    "read texture gradient")
+        return out
+
+    def read_material_gradients(self, count: int) -> np.ndarray:
+        out = np.zeros(count, dtype=abi.MATERIAL_GRADIENT)
+        self._check(self.lib.vkrt_cuda_read_material_gradients(self.handle, abi.ptr(out), count),
+                    "read material gradients")
         return out
 
     def stats(self) -> dict:

@@ -15,6 +15,7 @@
 #include <thread>
 #include <vector>
 
+#include "adjoint.h"
 #include "bvh_build.h"
 #include "context_view.h"
 #include "render.h"
@@ -74,6 +75,7 @@ struct VKRT_CudaContext {
 
     // materials, lights
     DeviceArray<VKRT_CudaMaterial> materials;
+    std::vector<VKRT_CudaMaterial> hostMaterials;
     uint32_t materialCount = 0;
     DeviceArray<VKRT_CudaEmissiveMesh> emissiveMeshes;
     DeviceArray<VKRT_CudaEmissiveTriangle> emissiveTriangles;
@@ -112,6 +114,14 @@ struct VKRT_CudaContext {
     VKRT_CudaWavefrontConfig wfCfg{};
     std::unique_ptr<WavefrontEngine> wavefront;
     cudaEvent_t order = nullptr;  // orders this context's stream against a batch leader's stream
+
+    // path-replay adjoint: gradient buffers (per texture slot, per material) and its input
+    std::vector<DeviceArray<float4>> textureGrad;
+    DeviceArray<float4*> textureGradTable;
+    DeviceArray<MaterialGradient> materialGrad;
+    DeviceArray<uint32_t> emissiveMeshMaterial;
+    uint32_t emissiveMeshMaterialCount = 0;
+    DeviceArray<float4> dImage;
 };
 
 namespace {
@@ -317,6 +327,11 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     c->accum[0].release();
     c->accum[1].release();
     c->output.release();
+    for (auto& t : c->textureGrad) t.release();
+    c->textureGradTable.release();
+    c->materialGrad.release();
+    c->emissiveMeshMaterial.release();
+    c->dImage.release();
     if (c->counters) cudaFree(c->counters);
     c->wavefront.reset();
     if (c->order) cudaEventDestroy(c->order);
@@ -391,6 +406,7 @@ int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* c, const VKRT_CudaMaterial*
     if (count && !materials) return invalid(c, "null materials");
     cudaSetDevice(c->device);
     VKRT_TRY(c, c->materials.assign(materials, count, c->stream), "upload materials");
+    c->hostMaterials.assign(materials, materials + count);
     c->materialCount = count;
     return VKRT_CUDA_SUCCESS;
 }
@@ -418,6 +434,7 @@ int32_t vkrt_cuda_upload_lights(VKRT_CudaContext* c, const VKRT_CudaEmissiveMesh
     VKRT_TRY(c, c->meshAliasIdx.assign(meshAliasIdx, meshCount, c->stream), "upload alias");
     VKRT_TRY(c, c->triAliasQ.assign(triAliasQ, triangleCount, c->stream), "upload alias");
     VKRT_TRY(c, c->triAliasIdx.assign(triAliasIdx, triangleCount, c->stream), "upload alias");
+    if (meshCount != c->emissiveMeshCount) c->emissiveMeshMaterialCount = 0;  // the mapping no longer applies
     c->emissiveMeshCount = meshCount;
     c->emissiveTriangleCount = triangleCount;
     return VKRT_CUDA_SUCCESS;
@@ -801,6 +818,153 @@ int32_t vkrt_cuda_read_accumulation(VKRT_CudaContext* c, float* rgba, size_t byt
     cudaSetDevice(c->device);
     VKRT_TRY(c, cudaMemcpyAsync(rgba, c->accum[c->readIndex].ptr, need, cudaMemcpyDeviceToHost, c->stream), "read accumulation");
     VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read accumulation");
+    return VKRT_CUDA_SUCCESS;
+}
+
+void vkrt_cuda_default_adjoint_config(VKRT_CudaAdjointConfig* a) {
+    if (!a) return;
+    std::memset(a, 0, sizeof(*a));
+}
+
+int32_t vkrt_cuda_set_emissive_mesh_materials(VKRT_CudaContext* c, const uint32_t* materials, uint32_t count) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (count != c->emissiveMeshCount) return invalid(c, "one material per uploaded emissive mesh");
+    if (count && !materials) return invalid(c, "null material array");
+    for (uint32_t i = 0; i < count; ++i)
+        if (materials[i] >= c->materialCount) return invalid(c, "emissive mesh material out of range");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->emissiveMeshMaterial.assign(materials, count, c->stream), "emissive mesh materials");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "emissive mesh materials");
+    c->emissiveMeshMaterialCount = count;
+    return VKRT_CUDA_SUCCESS;
+}
+
+namespace {
+
+int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const float4* dImageDevice,
+                      const VKRT_CudaAdjointConfig* cfg) {
+    int32_t v = validateFrame(c, sd);
+    if (v != VKRT_CUDA_SUCCESS) return v;
+    if (VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL)
+        return invalid(c, "the adjoint differentiates the RGB render mode only");
+    for (const VKRT_CudaMaterial& m : c->hostMaterials)
+        if (m.specularTint != 0.0f) return invalid(c, "the adjoint needs specularTint 0 on every material");
+    VKRT_CudaAdjointConfig a{};
+    if (cfg) a = *cfg;
+    const uint32_t want = a.gradients ? a.gradients
+                                      : (VKRT_CUDA_GRADIENT_BASE_COLOR | VKRT_CUDA_GRADIENT_ROUGHNESS |
+                                         VKRT_CUDA_GRADIENT_EMISSION);
+    const bool neeActive = sd->misNeeEnabled != 0u && sd->emissiveMeshCount > 0u;
+    if ((want & VKRT_CUDA_GRADIENT_EMISSION) && neeActive && c->emissiveMeshMaterialCount != c->emissiveMeshCount)
+        return invalid(c, "emission gradients need vkrt_cuda_set_emissive_mesh_materials after uploading lights");
+    cudaSetDevice(c->device);
+    // gradient buffers: one per texture slot that a material samples as base colour or metallic-roughness
+    if (c->textureGrad.size() != c->textureDescs.size()) c->textureGrad.resize(c->textureDescs.size());
+    std::vector<float4*> table(c->textureDescs.size(), nullptr);
+    std::vector<uint8_t> used(c->textureDescs.size(), 0);
+    for (const VKRT_CudaMaterial& m : c->hostMaterials) {
+        if (m.baseColorTextureIndex < used.size()) used[m.baseColorTextureIndex] = 1;
+        if (m.metallicRoughnessTextureIndex < used.size()) used[m.metallicRoughnessTextureIndex] = 1;
+    }
+    for (size_t i = 0; i < used.size(); ++i) {
+        const TextureDesc& t = c->textureDescs[i];
+        if (!used[i] || !t.texels) continue;
+        size_t n = size_t(t.width) * t.height;
+        bool fresh = c->textureGrad[i].count != n;
+        if (fresh) c->textureGrad[i].release();
+        VKRT_TRY(c, c->textureGrad[i].reserve(n), "texture gradient");
+        if (fresh || !a.accumulate)
+            VKRT_TRY(c, cudaMemsetAsync(c->textureGrad[i].ptr, 0, n * sizeof(float4), c->stream), "texture gradient");
+        table[i] = c->textureGrad[i].ptr;
+    }
+    VKRT_TRY(c, c->textureGradTable.assign(table.data(), table.size(), c->stream), "texture gradient table");
+    bool freshMat = c->materialGrad.count != c->materialCount;
+    if (freshMat) c->materialGrad.release();
+    VKRT_TRY(c, c->materialGrad.reserve(std::max(c->materialCount, 1u)), "material gradient");
+    if (freshMat || !a.accumulate)
+        VKRT_TRY(c, cudaMemsetAsync(c->materialGrad.ptr, 0, sizeof(MaterialGradient) * std::max(c->materialCount, 1u),
+                                    c->stream),
+                 "material gradient");
+
+    DeviceScene scene = makeDeviceScene(c);
+    AdjointParams ap{};
+    ap.rngMode = c->cfg.rngMode;
+    ap.rngSeed = c->cfg.rngSeed;
+    ap.envNee = envNeeActive(c, sd) ? 1u : 0u;
+    ap.width = c->width;
+    ap.height = c->height;
+    ap.sampleBase = a.sampleBase;
+    ap.wantBase = (want & VKRT_CUDA_GRADIENT_BASE_COLOR) ? 1u : 0u;
+    ap.wantRoughness = (want & VKRT_CUDA_GRADIENT_ROUGHNESS) ? 1u : 0u;
+    ap.wantEmission = (want & VKRT_CUDA_GRADIENT_EMISSION) ? 1u : 0u;
+    ap.dImage = dImageDevice;
+    ap.textureGrad = c->textureGradTable.ptr;
+    ap.materialGrad = c->materialGrad.ptr;
+    ap.emissiveMeshMaterial = c->emissiveMeshMaterial.ptr;
+    VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "adjoint");
+    VKRT_TRY(c, launchAdjoint(scene, *sd, ap, c->counters, c->stream), "adjoint launch");
+    c->countersPending = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+}  // namespace
+
+int32_t vkrt_cuda_render_adjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const float* dImage,
+                                 const VKRT_CudaAdjointConfig* cfg) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!dImage) return invalid(c, "null dImage");
+    if (!c->width) return invalid(c, "no film: call vkrt_cuda_resize first");
+    size_t n = size_t(c->width) * c->height;
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->dImage.reserve(n), "adjoint input");
+    VKRT_TRY(c, cudaMemcpyAsync(c->dImage.ptr, dImage, n * sizeof(float4), cudaMemcpyHostToDevice, c->stream),
+             "adjoint input");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "adjoint input");
+    return renderAdjoint(c, sd, c->dImage.ptr, cfg);
+}
+
+int32_t vkrt_cuda_render_adjoint_device(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const float* dImage,
+                                        const VKRT_CudaAdjointConfig* cfg) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!dImage) return invalid(c, "null dImage");
+    if ((reinterpret_cast<uintptr_t>(dImage) & 15u) != 0u) return invalid(c, "dImage must be 16-byte aligned");
+    return renderAdjoint(c, sd, reinterpret_cast<const float4*>(dImage), cfg);
+}
+
+int32_t vkrt_cuda_read_texture_gradient(VKRT_CudaContext* c, uint32_t index, float* rgba, size_t bytes) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (index >= c->textureDescs.size() || !c->textureDescs[index].texels)
+        return invalid(c, "texture slot is not bound");
+    const TextureDesc& t = c->textureDescs[index];
+    size_t n = size_t(t.width) * t.height;
+    if (!rgba || bytes < n * sizeof(float4)) return invalid(c, "gradient buffer too small");
+    cudaSetDevice(c->device);
+    if (index < c->textureGrad.size() && c->textureGrad[index].count == n) {
+        VKRT_TRY(c, cudaMemcpyAsync(rgba, c->textureGrad[index].ptr, n * sizeof(float4), cudaMemcpyDeviceToHost,
+                                    c->stream),
+                 "read texture gradient");
+        VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read texture gradient");
+    } else {
+        std::memset(rgba, 0, n * sizeof(float4));
+    }
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_read_material_gradients(VKRT_CudaContext* c, VKRT_CudaMaterialGradient* out, uint32_t count) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (count > c->materialCount) return invalid(c, "more materials than uploaded");
+    if (count && !out) return invalid(c, "null gradient array");
+    if (!count) return VKRT_CUDA_SUCCESS;
+    cudaSetDevice(c->device);
+    if (c->materialGrad.count == c->materialCount) {
+        static_assert(sizeof(MaterialGradient) == sizeof(VKRT_CudaMaterialGradient), "material gradient layout");
+        VKRT_TRY(c, cudaMemcpyAsync(out, c->materialGrad.ptr, count * sizeof(VKRT_CudaMaterialGradient),
+                                    cudaMemcpyDeviceToHost, c->stream),
+                 "read material gradients");
+        VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read material gradients");
+    } else {
+        std::memset(out, 0, count * sizeof(VKRT_CudaMaterialGradient));
+    }
     return VKRT_CUDA_SUCCESS;
 }
 

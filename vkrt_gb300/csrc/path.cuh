@@ -86,12 +86,27 @@ VKRT_DEV float3 pathResult(const StepConfig& cfg, const PathState& p) {
 
 VKRT_DEV float3 thr3(const PathState& p) { return xyz(p.thr); }
 
+// Observer of the RGB vertex arithmetic, for the adjoint integrator. The forward integrators use NoVertexHook, whose
+// empty members compile away. Arguments are the factors of each radiance term the vertex adds:
+//   surface       the shaded surface, its material after texturing and the BSDF at the vertex
+//   emission      radiance added = thrW * emission (thrW = throughput x MIS weight)
+//   nee*          shadow request `req`: contribution = factor * f * Le, f = f(wl) the BSDF value toward the light,
+//                 factor = throughput x |cos| x MIS / pdf
+//   bsdfSample    the continuation: throughput *= f(wl) * |cos| / pdf
+struct NoVertexHook {
+    VKRT_DEV void surface(const Surface&, const ShadeMaterial&, const Bsdf&) {}
+    VKRT_DEV void emission(float3) {}
+    VKRT_DEV void neeEmissive(uint32_t, const Bsdf&, float3, float3, float3, float3, uint32_t) {}
+    VKRT_DEV void neeEnvironment(uint32_t, const Bsdf&, float3, float3, float3, float3) {}
+    VKRT_DEV void bsdfSample(const Bsdf&, float3, float3) {}
+};
+
 // Processes the hit of p's current ray. Returns true when the path continues with a new ray in p.o / p.d.
 // `shadows` receives up to two requests (count in `numShadows`).
-template <bool kSpectral>
+template <bool kSpectral, class Hook = NoVertexHook>
 VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const StepConfig& cfg,
                               const SpecTable& tab, PathState& p, const TraceHit& h, ShadowRequest* shadows,
-                              uint32_t& numShadows) {
+                              uint32_t& numShadows, Hook hook = Hook()) {
     numShadows = 0;
     const uint32_t depth = p.depth;
     const float rot = sd.environmentRotation;
@@ -125,6 +140,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
     shadeVertex(sc, s, p.d, mat, basis);
     Bsdf bsdf = makeBsdf(mat, toLocal(-p.d, basis), s.frontFace);
     const float4 lam = heroLambdas(p.lamUnit);
+    hook.surface(s, mat, bsdf);
 
     // emission at the vertex, MIS against emissive NEE at the previous vertex (loop.slang:62-80)
     if (anyPos(mat.emission)) {
@@ -145,6 +161,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             }
             float3 c = thr3(p) * mat.emission * w;
             p.radiance += make_float4(c.x, c.y, c.z, 0.0f);
+            hook.emission(thr3(p) * w);
         }
     }
 
@@ -166,6 +183,9 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
                 if (pdf > 0.0f) {
                     float3 v = thr3(p) * (f * fabsf(wl.z) * ls.emission * (powerHeuristic(ls.pdfSA, pdf) / ls.pdfSA));
                     c = make_float4(v.x, v.y, v.z, 0.0f);
+                    hook.neeEmissive(numShadows, bsdf, wl, f,
+                                     thr3(p) * (fabsf(wl.z) * (powerHeuristic(ls.pdfSA, pdf) / ls.pdfSA)), ls.emission,
+                                     ls.emissiveMesh);
                 }
             }
             float3 off = dot(ls.wi, s.geometricNormal) >= 0.0f ? s.geometricNormal : -s.geometricNormal;
@@ -190,8 +210,11 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             } else {
                 float3 f = evalRgb(bsdf, wl, pdf);
                 if (pdf > 0.0f) {
-                    float3 v = thr3(p) * (f * fabsf(wl.z) * envRadiance(sc, sd, wi) * (powerHeuristic(pe, pdf) / pe));
+                    float3 Le = envRadiance(sc, sd, wi);
+                    float3 v = thr3(p) * (f * fabsf(wl.z) * Le * (powerHeuristic(pe, pdf) / pe));
                     c = make_float4(v.x, v.y, v.z, 0.0f);
+                    hook.neeEnvironment(numShadows, bsdf, wl, f,
+                                        thr3(p) * (fabsf(wl.z) * (powerHeuristic(pe, pdf) / pe)), Le);
                 }
             }
             float3 off = dot(wi, s.geometricNormal) >= 0.0f ? s.geometricNormal : -s.geometricNormal;
@@ -220,6 +243,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
         if (!anyPos(weight)) return false;
         p.thr = make_float4(p.thr.x * weight.x, p.thr.y * weight.y, p.thr.z * weight.z, 0.0f);
         p.prevBsdfPdf = pdf;
+        hook.bsdfSample(bsdf, wl, f);
     }
     if (!anyPos(p.thr)) return false;
     p.flags |= kPathPrevNee;

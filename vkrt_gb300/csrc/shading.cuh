@@ -613,6 +613,7 @@ struct LightSample {
     float pdfSA;
     float shadowDist;
     float3 emission;
+    uint32_t emissiveMesh;  // entry of the emissive-mesh table that was sampled
 };
 
 VKRT_DEV uint32_t sampleAlias(float u, uint32_t count, uint32_t off, const float* q, const uint32_t* idx) {
@@ -649,6 +650,7 @@ VKRT_DEV bool sampleEmissive(const DeviceScene& sc, float3 p, Rng& rng, LightSam
     ls.shadowDist = d2 * invD - kShadowDistanceOffset;
     if (ls.shadowDist <= 0.0f) return false;
     ls.emission = make_float3(em.emission[0], em.emission[1], em.emission[2]);
+    ls.emissiveMesh = mi;
     return true;
 }
 

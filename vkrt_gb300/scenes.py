@@ -105,13 +105,30 @@ def _assemble(parts, materials, scene_data, name) -> Scene:
     return s
 
 
-def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 8) -> Scene:
+def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 8,
+            wall_textures: list | None = None) -> Scene:
+    """The Cornell box. With `wall_textures` (five (albedo, roughness) pairs of float32 (H, W) or (H, W, 3)
+    arrays, for floor, ceiling, back, left, right), each wall gets its own material whose base colour (1, 1, 1) is
+    multiplied by the albedo texture (slot 2k) and whose roughness 1 by the G channel of a metallic-roughness
+    texture (slot 2k + 1); walls stay Lambertian (specular 0), so roughness acts through the dielectric
+    directional-albedo attenuation of the Lambert lobe."""
     lamb = dict(metallic=0.0, roughness=1.0, specular=0.0, diffuseRoughness=0.0)
     mats = [default_material(baseColor=(0.73, 0.73, 0.73), **lamb),
             default_material(baseColor=(0.65, 0.05, 0.05), **lamb),
             default_material(baseColor=(0.12, 0.45, 0.15), **lamb),
             default_material(baseColor=(0.0, 0.0, 0.0), emissionColor=(1.0, 1.0, 1.0), emissionLuminance=15.0, **lamb)]
     WHITE, RED, GREEN, LIGHT = 0, 1, 2, 3
+    textures = {}
+    wall_mats = [WHITE, WHITE, WHITE, RED, GREEN]
+    if wall_textures is not None:
+        if len(wall_textures) != 5:
+            raise ValueError("five (albedo, roughness) texture pairs: floor, ceiling, back, left, right")
+        for k, (alb, rough) in enumerate(wall_textures):
+            textures[2 * k] = albedo_texture(alb)
+            textures[2 * k + 1] = roughness_texture(rough)
+            mats.append(default_material(baseColor=(1.0, 1.0, 1.0), baseColorTextureIndex=2 * k,
+                                         metallicRoughnessTextureIndex=2 * k + 1, **lamb))
+            wall_mats[k] = len(mats) - 1
     ident = ((0, 0, 0), (0, 0, 0), (1, 1, 1))
     parts = []
     # walls: x = left/right, y = depth (open at y = 0), z = up; normals point into the box
@@ -122,9 +139,9 @@ def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 
         (((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (1, 0, 0)), RED),     # left
         (((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0), (-1, 0, 0)), GREEN),  # right
     ]
-    for (q, mat) in walls:
+    for k, (q, _) in enumerate(walls):
         v, i = _quad(*q)
-        parts.append((v, i, mat) + ident)
+        parts.append((v, i, wall_mats[k]) + ident)
     h = 1.0 - 1e-3
     v, i = _quad((0.375, 0.375, h), (0.375, 0.625, h), (0.625, 0.625, h), (0.625, 0.375, h), (0, 0, -1))
     parts.append((v, i, LIGHT) + ident)
@@ -138,7 +155,50 @@ def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 
     sd["rrMaxDepth"] = max_depth
     sd["environmentLight"] = (0.0, 0.0, 0.0, 0.0)
     sd["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES, abi.RENDER_MODE_RGB, abi.SPECTRAL_HERO)
-    return _assemble(parts, mats, sd, "cornell")
+    scene = _assemble(parts, mats, sd, "cornell")
+    scene.textures = textures
+    return scene
+
+
+def albedo_texture(albedo: np.ndarray) -> np.ndarray:
+    """RGBA32F base-colour texture from (H, W) grey or (H, W, 3) RGB albedo."""
+    a = np.asarray(albedo, dtype=np.float32)
+    if a.ndim == 2:
+        a = np.repeat(a[..., None], 3, axis=2)
+    t = np.ones(a.shape[:2] + (4,), dtype=np.float32)
+    t[..., :3] = a
+    return t
+
+
+def roughness_texture(roughness: np.ndarray) -> np.ndarray:
+    """RGBA32F glTF metallic-roughness texture: roughness in G, metallic factor B = 1 (the material's metallic 0
+    keeps the surface dielectric)."""
+    r = np.asarray(roughness, dtype=np.float32)
+    t = np.ones(r.shape[:2] + (4,), dtype=np.float32)
+    t[..., 1] = r
+    return t
+
+
+def inverse_rendering_cornell(width: int = 128, height: int = 128, spp: int = 16, max_depth: int = 6,
+                              tex_size: int = 64, seed: int = 3, target: bool = False) -> Scene:
+    """Differentiable-rendering workload on the Cornell geometry: five 64 x 64 FP32 wall textures, albedo 0.5 and
+    roughness 0.5 (target=False), or seeded albedo uniform in [0.05, 0.95]^3 and roughness uniform in [0.1, 0.9]
+    (target=True). Russian roulette is off (rrMinDepth > rrMaxDepth) so the fixed-seed estimator is smooth in the
+    texture values."""
+    rng = np.random.default_rng(seed)
+    pairs = []
+    for _ in range(5):
+        if target:
+            alb = rng.uniform(0.05, 0.95, (tex_size, tex_size, 3)).astype(np.float32)
+            rough = rng.uniform(0.1, 0.9, (tex_size, tex_size)).astype(np.float32)
+        else:
+            alb = np.full((tex_size, tex_size, 3), 0.5, np.float32)
+            rough = np.full((tex_size, tex_size), 0.5, np.float32)
+        pairs.append((alb, rough))
+    s = cornell(width, height, spp=spp, max_depth=max_depth, wall_textures=pairs)
+    s.scene_data["rrMinDepth"] = max_depth + 1
+    s.name = "cornell-inverse"
+    return s
 
 
 def unit_icosphere(subdivisions: int = 3) -> tuple[np.ndarray, np.ndarray]:
