@@ -19,10 +19,10 @@ ROUGH_SLOTS = [1, 3, 5, 7, 9]
 LIGHT_MATERIAL = 3
 
 
-def _problem(width, height, spp, depth, tex):
+def _problem(width, height, spp, depth, tex, integrator):
     target = scenes.inverse_rendering_cornell(width, height, spp, depth, tex_size=tex, target=True)
     scene = scenes.inverse_rendering_cornell(width, height, spp, depth, tex_size=tex, target=False)
-    ctx = RenderContext(rng_mode=abi.RNG_PCG32, rng_seed=1)
+    ctx = RenderContext(rng_mode=abi.RNG_PCG32, rng_seed=1, integrator=integrator)
     ctx.upload_scene(target)
     ctx.render_frame(target.scene_data)
     t_img = ctx.read_accumulation()[..., :3].copy()
@@ -63,8 +63,8 @@ def _check(name, got, want, rel=1e-2):
     assert (err <= rel).all(), f"{name}: worst relative error {err.max():.3e}\nadjoint {got}\nfd      {want}"
 
 
-def _run_check(width, height, spp, depth, tex, n_albedo, n_rough, seed):
-    ctx, scene, renderer, t_img = _problem(width, height, spp, depth, tex)
+def _run_check(width, height, spp, depth, tex, n_albedo, n_rough, seed, integrator):
+    ctx, scene, renderer, t_img = _problem(width, height, spp, depth, tex, integrator)
     try:
         params = [p.clone().requires_grad_() for p in renderer.parameters()]
         img = render(renderer, *params)
@@ -112,13 +112,38 @@ def _run_check(width, height, spp, depth, tex, n_albedo, n_rough, seed):
     return alb, rough, em
 
 
-def test_adjoint_matches_central_differences_small(built):
-    _run_check(48, 48, spp=4, depth=4, tex=16, n_albedo=12, n_rough=8, seed=7)
+INTEGRATORS = [pytest.param(abi.INTEGRATOR_MEGAKERNEL, id="per-path"),
+               pytest.param(abi.INTEGRATOR_WAVEFRONT, id="wavefront")]
 
 
-def test_adjoint_matches_central_differences_inverse_rendering_workload(built):
+@pytest.mark.parametrize("integrator", INTEGRATORS)
+def test_adjoint_matches_central_differences_small(built, integrator):
+    _run_check(48, 48, spp=4, depth=4, tex=16, n_albedo=12, n_rough=8, seed=7, integrator=integrator)
+
+
+@pytest.mark.parametrize("integrator", INTEGRATORS)
+def test_adjoint_matches_central_differences_inverse_rendering_workload(built, integrator):
     # 128 x 128, 16 spp, depth 6, five 64 x 64 albedo + roughness textures; 32 random texels (20 albedo, 12 roughness)
-    _run_check(128, 128, spp=16, depth=6, tex=64, n_albedo=20, n_rough=12, seed=11)
+    _run_check(128, 128, spp=16, depth=6, tex=64, n_albedo=20, n_rough=12, seed=11, integrator=integrator)
+
+
+def test_wavefront_adjoint_equals_per_path_adjoint(built):
+    """Both adjoint implementations replay the same paths: their gradients agree to float summation order."""
+    s = scenes.inverse_rendering_cornell(64, 48, 4, 5, tex_size=16, target=False)
+    d = np.random.default_rng(1).normal(size=(48, 64, 3)).astype(np.float32)
+    out = []
+    for integ in (abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT):
+        with RenderContext(rng_mode=abi.RNG_PCG32, integrator=integ) as ctx:
+            ctx.upload_scene(s)
+            if integ == abi.INTEGRATOR_WAVEFRONT:
+                ctx.set_wavefront_config(queueCapacity=1000)  # slots reused across many items
+            ctx.render_adjoint(s.scene_data, d)
+            tex = np.stack([ctx.read_texture_gradient(k, (16, 16)) for k in range(10)])
+            mat = ctx.read_material_gradients(len(s.materials))
+            out.append((tex, np.concatenate([mat["baseColor"], mat["roughness"][:, None], mat["emission"]], 1)))
+    scale = np.abs(out[0][0]).max()
+    np.testing.assert_allclose(out[1][0], out[0][0], rtol=1e-3, atol=1e-5 * scale)
+    np.testing.assert_allclose(out[1][1], out[0][1], rtol=1e-3, atol=1e-5 * np.abs(out[0][1]).max())
 
 
 def test_adjoint_gradient_linear_in_dimage(built):

@@ -6,29 +6,22 @@
 //   roughness         Material.roughness and the G texels of the metallic-roughness texture
 //   emitter radiance  emissionColor x emissionLuminance of each material, through both emitter hits and NEE.
 //
-// One thread per (pixel, sample). Replay 1 runs the forward path (path.cuh, the same arithmetic as the megakernel)
-// and keeps its total radiance L; replay 2 runs it again with the same random numbers and, at each vertex,
-//   * emission term    d/dLe of thr * w * Le
-//   * NEE terms        d/dtheta of thr * f(wl) * |cos| * Le * mis / pdf, for visible requests
-//   * continuation     (L - radiance gathered so far) * (df/dtheta) / f, the path-replay identity for the
-//                      throughput factor f * |cos| / pdf with the sampling density held fixed
-// and scatters the vertex's gradient to the bilinear texel footprint of its hit with atomics. Sampling decisions,
-// MIS weights and Russian roulette are held fixed (detached), which is unbiased for the gradient of the expected
-// image; when no sampling density depends on the differentiated parameters and Russian roulette is off, the result
-// is the exact derivative of the fixed-seed estimator, so it matches central differences with common random numbers.
-// Replay 2 reuses replay 1's closest hits and shadow visibility for the first kReplayCache vertices and re-traces
-// beyond them.
-//
-// BSDF derivatives are analytic for the Principled subset this backend renders (bsdf/principled/eval_rgb.slang:4-121
-// restricted to metal + dielectric + Lambert): GGX D and Smith G through alpha = max(roughness^2, 1e-3)
-// (bsdf/lobes/ggx.slang:16-30), the dielectric directional-albedo attenuation of the Lambert lobe
-// (principled/attenuation.slang:30-51), Schlick F0 of non-conducting metals, and the Lambert base colour.
+// Two implementations share the per-vertex arithmetic of adjoint.cuh:
+//   * this file: one thread per (pixel, sample). Pass 0 runs the forward path (path.cuh, the megakernel's
+//     arithmetic) and keeps its total radiance L; pass 1 replays it with the same random numbers and scatters each
+//     vertex's gradient to the bilinear texel footprint of its hit with atomics, reusing pass 0's closest hits and
+//     shadow visibility for the first kReplayCache vertices.
+//   * wavefront.cu: a primal wavefront pass stores L per (pixel, sample) and an adjoint wavefront pass replays the
+//     paths through the stage kernels, finishing each vertex once its shadow rays have been traced.
+// Sampling decisions, MIS weights and Russian roulette are held fixed (detached), which is unbiased for the gradient
+// of the expected image; when no sampling density depends on the differentiated parameters and Russian roulette is
+// off, the result is the exact derivative of the fixed-seed estimator, so it matches central differences with common
+// random numbers.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
-#include "adjoint.h"
-#include "path.cuh"
+#include "adjoint.cuh"
 
 namespace vkrt {
 
@@ -38,365 +31,85 @@ constexpr uint32_t kAdjThreads = 128;
 constexpr uint32_t kReplayCache = 8;
 
 // ---------------------------------------------------------------------------------------------------------------
-// analytic BSDF derivatives
-// ---------------------------------------------------------------------------------------------------------------
-VKRT_DEV bool interior(float x) { return x > 0.0f && x < 1.0f; }  // d sat(x) / dx = 1
-
-// d(dielDirAtten)/d(roughness), same branches as dielDirAtten
-VKRT_DEV float3 dielDirAttenDRoughness(float roughness, float3 f0, float cosT) {
-    if (fabsf(cosT) <= 0.0f) return f3(0.0f);
-    float rr = sat(roughness), ct = sat(fabsf(cosT));
-    float drr = interior(roughness) ? 1.0f : 0.0f;
-    float r0 = rr * -1.0f + 1.0f, r1 = rr * -0.0275f + 0.0425f, r2 = rr * -0.572f + 1.04f, r3 = rr * 0.022f - 0.04f;
-    float e = exp2f(-9.28f * ct), r02 = r0 * r0;
-    float mn = fminf(r02, e);
-    float dmn = r02 < e ? -2.0f * r0 * drr : 0.0f;
-    float a004 = mn * r0 + r1;
-    float da = dmn * r0 - mn * drr - 0.0275f * drr;
-    float Araw = -1.04f * a004 + r2, Braw = 1.04f * a004 + r3;
-    float A = sat(Araw), B = sat(Braw);
-    float dA = interior(Araw) ? -1.04f * da - 0.572f * drr : 0.0f;
-    float dB = interior(Braw) ? 1.04f * da + 0.022f * drr : 0.0f;
-    float f[3] = {f0.x, f0.y, f0.z}, out[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        float inner = f[c] * A + B;
-        float dInner = interior(inner) ? f[c] * dA + dB : 0.0f;
-        out[c] = interior(1.0f - sat(inner)) ? -dInner : 0.0f;
-    }
-    return make_float3(out[0], out[1], out[2]);
-}
-
-VKRT_DEV float ggxLambdaD(float3 w, const Ggx& g, float dax, float day) {
-    float z2 = fmaxf(w.z * w.z, kGgxEps);
-    float slope2 = (g.ax * g.ax * w.x * w.x + g.ay * g.ay * w.y * w.y) / z2;
-    float dSlope2 = (2.0f * g.ax * dax * w.x * w.x + 2.0f * g.ay * day * w.y * w.y) / z2;
-    return 0.25f * dSlope2 / sqrtf(1.0f + slope2);
-}
-
-// df/d(baseColor) (diagonal) and df/d(roughness) of evalRgb at wi
-VKRT_DEV void evalRgbGrad(const Bsdf& s, float3 wi, float3& dBase, float3& dRough) {
-    dBase = f3(0.0f);
-    dRough = f3(0.0f);
-    if (wi.z <= 0.0f) return;
-    const ShadeMaterial& m = s.mat;
-    // alpha derivatives (makeGgx)
-    float r = fmaxf(m.roughness, kGgxMinAlpha);
-    float dr = m.roughness > kGgxMinAlpha ? 1.0f : 0.0f;
-    float aspect = sqrtf(fmaxf(1.0f - 0.9f * m.anisotropic, kGgxMinAlpha));
-    float a = r * r, da = 2.0f * r * dr;
-    float dax = a / aspect > kGgxMinAlpha ? da / aspect : 0.0f;
-    float day = a * aspect > kGgxMinAlpha ? da * aspect : 0.0f;
-
-    float3 h = s.wo + wi;
-    float h2 = dot(h, h);
-    float3 mh = h * rsqrtf(h2);
-    float wom = dot(s.wo, mh);
-    bool halfOk = h2 > kGgxEps && wom > 0.0f && s.wo.z > 0.0f;
-    float DG = 0.0f, dDG = 0.0f;
-    if (halfOk && (s.wMetal > 0.0f || s.wDiel > 0.0f)) {
-        const Ggx& g = s.ggx;
-        float lo = ggxLambda(s.wo, g), li = ggxLambda(wi, g);
-        float G = 1.0f / (1.0f + lo + li);
-        float dG = -G * G * (ggxLambdaD(s.wo, g, dax, day) + ggxLambdaD(wi, g, dax, day));
-        float D = ggxD(mh, g), dD = 0.0f;
-        if (mh.z > 0.0f) {
-            float c = (mh.x * mh.x) / (g.ax * g.ax) + (mh.y * mh.y) / (g.ay * g.ay) + mh.z * mh.z;
-            float dcx = -2.0f * mh.x * mh.x / (g.ax * g.ax * g.ax), dcy = -2.0f * mh.y * mh.y / (g.ay * g.ay * g.ay);
-            dD = (-D / g.ax - 2.0f * D / c * dcx) * dax + (-D / g.ay - 2.0f * D / c * dcy) * day;
-        }
-        float den = fmaxf(4.0f * s.wo.z * wi.z, kGgxEps);
-        DG = D * G / den;
-        dDG = (dD * G + D * dG) / den;
-    }
-    if (s.wMetal > 0.0f && halfOk) {
-        float3 F = metalFresnel(s, wom);
-        dRough += F * (dDG * m.metallic);
-        if (!m.conductor) dBase += f3((1.0f - pow5(1.0f - sat(wom))) * DG * m.metallic);
-    }
-    if (s.wDiel > 0.0f && halfOk && !dielIdentity(m)) dRough += schlick(wom, s.f0Diel) * (dDG * (1.0f - m.metallic));
-    if (s.wDiff > 0.0f) {
-        float k = (1.0f - m.metallic) * kInvPi;
-        float3 sub = m.baseColor * k;
-        dBase += s.viewAtten * (k * (1.0f - m.metallic));
-        dRough += dielDirAttenDRoughness(m.roughness, s.f0Diel, s.wo.z) * sub * (1.0f - m.metallic);
-    }
-}
-
-VKRT_DEV float3 ratio(float3 a, float3 b) {
-    return make_float3(b.x > 0.0f ? a.x / b.x : 0.0f, b.y > 0.0f ? a.y / b.y : 0.0f, b.z > 0.0f ? a.z / b.z : 0.0f);
-}
-
-// ---------------------------------------------------------------------------------------------------------------
-// per-vertex record filled by the hook during replay 2
-// ---------------------------------------------------------------------------------------------------------------
-struct AdjVertex {
-    uint32_t materialIndex;
-    TexCoords tex;
-    bool hasSurface, emitted, sampled;
-    bool reqValid[2];
-    float3 emitW;         // delta * thr * w
-    float3 reqBase[2];    // delta * factor * Le * df/dbase
-    float reqRough[2];    // sum delta * factor * Le * df/droughness
-    float3 reqEmit[2];    // delta * factor * f
-    uint32_t reqLight[2]; // emissive mesh, VKRT_CUDA_INVALID_INDEX for the environment
-    float3 ratioBase, ratioRough;
-};
-
-struct AdjointHook {
-    AdjVertex* v;
-    float3 delta;
-    VKRT_DEV void surface(const Surface& s, const ShadeMaterial&, const Bsdf&) {
-        v->hasSurface = true;
-        v->materialIndex = s.materialIndex;
-        v->tex = s.tex;
-    }
-    VKRT_DEV void emission(float3 thrW) {
-        v->emitted = true;
-        v->emitW = delta * thrW;
-    }
-    VKRT_DEV void nee(uint32_t r, const Bsdf& b, float3 wl, float3 f, float3 factor, float3 Le, uint32_t light) {
-        if (r > 1u) return;
-        float3 dB, dR;
-        evalRgbGrad(b, wl, dB, dR);
-        float3 dl = delta * factor;
-        v->reqValid[r] = true;
-        v->reqBase[r] = dl * Le * dB;
-        v->reqRough[r] = dot(dl * Le, dR);
-        v->reqEmit[r] = dl * f;
-        v->reqLight[r] = light;
-    }
-    VKRT_DEV void neeEmissive(uint32_t r, const Bsdf& b, float3 wl, float3 f, float3 factor, float3 Le, uint32_t mesh) {
-        nee(r, b, wl, f, factor, Le, mesh);
-    }
-    VKRT_DEV void neeEnvironment(uint32_t r, const Bsdf& b, float3 wl, float3 f, float3 factor, float3 Le) {
-        nee(r, b, wl, f, factor, Le, VKRT_CUDA_INVALID_INDEX);
-    }
-    VKRT_DEV void bsdfSample(const Bsdf& b, float3 wl, float3 f) {
-        float3 dB, dR;
-        evalRgbGrad(b, wl, dB, dR);
-        v->sampled = true;
-        v->ratioBase = ratio(dB, f);
-        v->ratioRough = ratio(dR, f);
-    }
-};
-
-// ---------------------------------------------------------------------------------------------------------------
-// scatter to texels and materials
-// ---------------------------------------------------------------------------------------------------------------
-struct TexFootprint {
-    const float4* texels;
-    uint32_t index[4];
-    float weight[4];
-};
-
-// Texels and weights sampleMaterialTexture blends for this lookup; false when the slot is unbound.
-VKRT_DEV bool materialTextureFootprint(const DeviceScene& sc, uint32_t idx, uint32_t wrap, const float* xf, float rot,
-                                       uint32_t set, const TexCoords& tc, TexFootprint& fp) {
-    if (idx >= VKRT_CUDA_MAX_TEXTURES) return false;
-    TextureDesc t = sc.textures[idx];
-    if (!t.texels) return false;
-    float2 uv = set == 1u ? tc.uv1 : tc.uv0;
-    float sx = uv.x * xf[0], sy = uv.y * xf[1];
-    float sn, cs;
-    sincosf(rot, &sn, &cs);
-    float u = cs * sx - sn * sy + xf[2], v = sn * sx + cs * sy + xf[3];
-    uint32_t wu = wrapMode(wrap & 0xffffu), wv = wrapMode((wrap >> 16) & 0xffffu);
-    float x = u * float(t.width) - 0.5f, y = v * float(t.height) - 0.5f;
-    float fx = floorf(x), fy = floorf(y);
-    int x0 = int(fx), y0 = int(fy);
-    float ax = x - fx, ay = y - fy;
-    int xa = wrapIndex(x0, int(t.width), wu), xb = wrapIndex(x0 + 1, int(t.width), wu);
-    int ya = wrapIndex(y0, int(t.height), wv), yb = wrapIndex(y0 + 1, int(t.height), wv);
-    fp.texels = t.texels;
-    fp.index[0] = uint32_t(ya) * t.width + uint32_t(xa);
-    fp.index[1] = uint32_t(ya) * t.width + uint32_t(xb);
-    fp.index[2] = uint32_t(yb) * t.width + uint32_t(xa);
-    fp.index[3] = uint32_t(yb) * t.width + uint32_t(xb);
-    fp.weight[0] = (1.0f - ax) * (1.0f - ay);
-    fp.weight[1] = ax * (1.0f - ay);
-    fp.weight[2] = (1.0f - ax) * ay;
-    fp.weight[3] = ax * ay;
-    return true;
-}
-
-VKRT_DEV float4 footprintValue(const TexFootprint& fp) {
-    float4 c = f4(0.0f);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) c += __ldg(fp.texels + fp.index[k]) * fp.weight[k];
-    return c;
-}
-
-VKRT_DEV void addEmissionGrad(const AdjointParams& ap, uint32_t material, float3 g) {
-    MaterialGradient* mg = ap.materialGrad + material;
-    atomicAdd(&mg->emission.x, g.x);
-    atomicAdd(&mg->emission.y, g.y);
-    atomicAdd(&mg->emission.z, g.z);
-}
-
-// dLoss/d(shaded baseColor) = gBase and dLoss/d(shaded roughness) = gRough at one vertex, pushed back through
-// shadeVertex's texturing to the material constants and the texels
-VKRT_DEV void scatterSurface(const DeviceScene& sc, const AdjointParams& ap, const AdjVertex& av, float3 gBase,
-                             float gRough) {
-    const VKRT_CudaMaterial& m = sc.materials[av.materialIndex];
-    MaterialGradient* mg = ap.materialGrad + av.materialIndex;
-    if (ap.wantBase && (gBase.x != 0.0f || gBase.y != 0.0f || gBase.z != 0.0f)) {
-        float3 vcol = xyz(av.tex.color);
-        TexFootprint fp;
-        bool tex = materialTextureFootprint(sc, m.baseColorTextureIndex, m.baseColorTextureWrap,
-                                            m.baseColorTextureTransform, m.textureRotations[0],
-                                            m.textureTexcoordSets & 0xffu, av.tex, fp);
-        float3 tv = tex ? xyz(footprintValue(fp)) : f3(1.0f);
-        float3 gm = gBase * tv * vcol;
-        atomicAdd(&mg->base.x, gm.x);
-        atomicAdd(&mg->base.y, gm.y);
-        atomicAdd(&mg->base.z, gm.z);
-        float4* tg = tex ? ap.textureGrad[m.baseColorTextureIndex] : nullptr;
-        if (tg) {
-            float3 gt = gBase * make_float3(m.baseColor[0], m.baseColor[1], m.baseColor[2]) * vcol;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                float w = fp.weight[k];
-                if (w == 0.0f) continue;
-                float4* d = tg + fp.index[k];
-                atomicAdd(&d->x, gt.x * w);
-                atomicAdd(&d->y, gt.y * w);
-                atomicAdd(&d->z, gt.z * w);
-            }
-        }
-    }
-    if (ap.wantRoughness && gRough != 0.0f) {
-        TexFootprint fp;
-        bool tex = m.metallicRoughnessTextureIndex != VKRT_CUDA_INVALID_INDEX &&
-                   materialTextureFootprint(sc, m.metallicRoughnessTextureIndex, m.metallicRoughnessTextureWrap,
-                                            m.metallicRoughnessTextureTransform, m.textureRotations[1],
-                                            (m.textureTexcoordSets >> 8) & 0xffu, av.tex, fp);
-        float mr = tex ? footprintValue(fp).y : 1.0f;
-        if (interior(m.roughness * mr)) {  // shaded roughness = sat(roughness * texel.g)
-            atomicAdd(&mg->base.w, gRough * mr);
-            float4* tg = tex ? ap.textureGrad[m.metallicRoughnessTextureIndex] : nullptr;
-            if (tg) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (fp.weight[k] != 0.0f) atomicAdd(&tg[fp.index[k]].y, gRough * m.roughness * fp.weight[k]);
-            }
-        }
-    }
-}
-
-VKRT_DEV void scatterHitEmission(const DeviceScene& sc, const AdjointParams& ap, const AdjVertex& av) {
-    const VKRT_CudaMaterial& m = sc.materials[av.materialIndex];
-    float3 g = av.emitW;
-    if (m.emissiveTextureIndex != VKRT_CUDA_INVALID_INDEX) {
-        float4 em = sampleMaterialTexture(sc, m.emissiveTextureIndex, m.emissiveTextureWrap, m.emissiveTextureTransform,
-                                          m.textureRotations[3], (m.textureTexcoordSets >> 24) & 0xffu, av.tex,
-                                          f4(1.0f));
-        g = g * xyz(em);
-    }
-    addEmissionGrad(ap, av.materialIndex, g);
-}
-
-// ---------------------------------------------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kAdjThreads) kAdjoint(DeviceScene sc, VKRT_CudaSceneData sd, AdjointParams ap,
                                                         RenderCounters* counters) {
     extern __shared__ uint2 smemStack[];
+    __shared__ MaterialGradient smemMatStorage[kSmemMaterials];
+    MaterialGradient* smemMat = sc.materialCount <= kSmemMaterials ? smemMatStorage : nullptr;
+    clearMaterialSmem(smemMat, sc.materialCount);
+    __syncthreads();
     const uint32_t vx0 = sd.viewportRect[0], vy0 = sd.viewportRect[1];
     const uint32_t vw = sd.viewportRect[2], vh = sd.viewportRect[3];
     const uint32_t spp = max(sd.samplesPerPixel, 1u);
     const uint32_t pixels = vw * vh;
-    const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t items = pixels * spp;
+    const float invTw = 1.0f / float(ap.sampleBase + spp);
+    KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
+    const StepConfig cfg{false, sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u, ap.envNee != 0u, ap.rngMode,
+                         ap.rngSeed};
+    const SpecTable tab{sc.rgb2spec, sd.rgb2specSRGB.res, sd.rgb2specSRGB.scaleOffset, sd.rgb2specSRGB.dataOffset};
     PathCounts pc{0u, 0u, 0u, 0u};
-    if (item < pixels * spp) {
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < items; item += gridDim.x * blockDim.x) {
         // sample-major order: a warp holds neighbouring pixels of one sample, so its texel atomics spread out
         const uint32_t sample = item / pixels, local = item % pixels;
         const int px = int(vx0 + local % vw), py = int(vy0 + local / vw);
         const uint32_t pix = uint32_t(py) * ap.width + uint32_t(px);
-        const float invTw = 1.0f / float(ap.sampleBase + spp);
         const float3 delta = xyz(ap.dImage[pix]) * invTw;
-        if (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f) {
-            KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
-            StepConfig cfg{false, sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u, ap.envNee != 0u, ap.rngMode,
-                           ap.rngSeed};
-            SpecTable tab{sc.rgb2spec, sd.rgb2specSRGB.res, sd.rgb2specSRGB.scaleOffset, sd.rgb2specSRGB.dataOffset};
-            TraceHit cache[kReplayCache];
-            uint32_t visBits = 0u;
-
-            // replay 1: the forward path and its radiance
+        if (delta.x == 0.0f && delta.y == 0.0f && delta.z == 0.0f) continue;
+        TraceHit cache[kReplayCache];
+        uint32_t visBits = 0u;
+        float3 total = f3(0.0f);
+        // pass 0 runs the forward path and keeps its radiance; pass 1 replays it with the same random numbers and
+        // accumulates gradients vertex by vertex. One loop body serves both passes, so the path step, the
+        // traversal and the gradient code each exist once in the kernel.
+        for (uint32_t pass = 0; pass < 2u; ++pass) {
+            const bool grad = pass == 1u;
             PathState p = beginPath<false>(cfg, sd, px, py, ap.sampleBase + sample);
             for (uint32_t v = 0;; ++v) {
-                TraceHit h = closest<false>(k, p.o, p.d);
-                if (v == 0u) pc.primary++;
-                else pc.extension++;
-                if (v < kReplayCache) cache[v] = h;
-                ShadowRequest sh[2];
-                uint32_t ns;
-                bool cont = shadePathVertex<false>(sc, sd, cfg, tab, p, h, sh, ns);
-                for (uint32_t i = 0; i < ns; ++i) {
-                    pc.shadow++;
-                    TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
-                    if (traceBvh<true, false>(sc, r, k.stackColumn, k.stackStride, counters).mesh ==
-                        VKRT_CUDA_INVALID_INDEX) {
-                        p.radiance += sh[i].contribution;
-                        if (v < kReplayCache) visBits |= 1u << (2u * v + i);
-                    }
-                }
-                if (!cont) break;
-            }
-            const float3 total = xyz(p.radiance);
-
-            // replay 2: same random numbers, gradients vertex by vertex
-            p = beginPath<false>(cfg, sd, px, py, ap.sampleBase + sample);
-            for (uint32_t v = 0;; ++v) {
+                const bool cached = grad && v < kReplayCache;
                 TraceHit h;
-                if (v < kReplayCache) {
+                if (cached) {
                     h = cache[v];
                 } else {
                     h = closest<false>(k, p.o, p.d);
-                    pc.extension++;
+                    if (v == 0u) pc.primary++;
+                    else pc.extension++;
+                    if (v < kReplayCache) cache[v] = h;
                 }
                 AdjVertex av;
                 av.hasSurface = av.emitted = av.sampled = false;
                 av.reqValid[0] = av.reqValid[1] = false;
                 ShadowRequest sh[2];
                 uint32_t ns;
-                bool cont = shadePathVertex<false, AdjointHook>(sc, sd, cfg, tab, p, h, sh, ns, AdjointHook{&av, delta});
+                bool cont = shadePathVertex<false, AdjointHook>(sc, sd, cfg, tab, p, h, sh, ns,
+                                                                AdjointHook{grad ? &av : nullptr, delta});
                 bool vis[2] = {false, false};
                 for (uint32_t i = 0; i < ns; ++i) {
-                    if (v < kReplayCache) {
+                    if (cached) {
                         vis[i] = ((visBits >> (2u * v + i)) & 1u) != 0u;
                     } else {
                         pc.shadow++;
                         TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
                         vis[i] = traceBvh<true, false>(sc, r, k.stackColumn, k.stackStride, counters).mesh ==
                                  VKRT_CUDA_INVALID_INDEX;
+                        if (vis[i] && v < kReplayCache) visBits |= 1u << (2u * v + i);
                     }
                     if (vis[i]) p.radiance += sh[i].contribution;
                 }
-                if (av.hasSurface) {
-                    float3 gBase = f3(0.0f);
-                    float gRough = 0.0f;
-                    for (uint32_t i = 0; i < ns && i < 2u; ++i) {
-                        if (!vis[i] || !av.reqValid[i]) continue;
-                        gBase += av.reqBase[i];
-                        gRough += av.reqRough[i];
-                        if (ap.wantEmission && av.reqLight[i] != VKRT_CUDA_INVALID_INDEX)
-                            addEmissionGrad(ap, ap.emissiveMeshMaterial[av.reqLight[i]], av.reqEmit[i]);
-                    }
-                    if (cont && av.sampled) {
-                        float3 dl = delta * (total - xyz(p.radiance));  // radiance the continuation carries
-                        gBase += dl * av.ratioBase;
-                        gRough += dot(dl, av.ratioRough);
-                    }
-                    if (ap.wantEmission && av.emitted) scatterHitEmission(sc, ap, av);
-                    scatterSurface(sc, ap, av, gBase, gRough);
+                if (grad && av.hasSurface) {
+                    if (ap.wantEmission && av.emitted) scatterHitEmission(sc, ap, smemMat, av);
+                    finishVertex(sc, ap, smemMat, av, vis, cont, delta, total, xyz(p.radiance));
                 }
                 if (!cont) break;
             }
-            pc.samples++;
+            if (!grad) total = xyz(p.radiance);
         }
+        pc.samples++;
     }
+    __syncthreads();
+    flushMaterialSmem(ap, smemMat, sc.materialCount);
     for (int off = 16; off > 0; off >>= 1) {
         pc.primary += __shfl_xor_sync(0xFFFFFFFFu, pc.primary, off);
         pc.extension += __shfl_xor_sync(0xFFFFFFFFu, pc.extension, off);
@@ -418,8 +131,14 @@ cudaError_t launchAdjoint(const DeviceScene& sc, const VKRT_CudaSceneData& sd, c
     const uint64_t items = uint64_t(sd.viewportRect[2]) * sd.viewportRect[3] * std::max(sd.samplesPerPixel, 1u);
     if (items == 0) return cudaSuccess;
     if (items > 0x7FFFFFFFull) return cudaErrorInvalidValue;
-    const uint32_t blocks = uint32_t((items + kAdjThreads - 1) / kAdjThreads);
+    int device = 0, sms = 0, perSM = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const size_t smem = size_t(kAdjThreads) * VKRT_SMEM_STACK * sizeof(uint2);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kAdjoint, kAdjThreads, smem);
+    // a resident grid that loops over the items: blocks flush their material gradients once, at the end
+    const uint64_t needed = (items + kAdjThreads - 1) / kAdjThreads;
+    const uint32_t blocks = uint32_t(std::min<uint64_t>(needed, uint64_t(std::max(sms, 1)) * std::max(perSM, 1)));
     kAdjoint<<<blocks, kAdjThreads, smem, stream>>>(sc, sd, ap, counters);
     return cudaGetLastError();
 }

@@ -250,6 +250,31 @@ bool envNeeActive(const VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
            sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u;
 }
 
+WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spectral) {
+    WfScene S;
+    std::memset(&S, 0, sizeof(S));
+    S.sc = makeDeviceScene(c);
+    S.sd = sd;
+    S.film = FilmBuffers{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
+    S.filmWidth = c->width;
+    S.filmHeight = c->height;
+    S.vx0 = sd.viewportRect[0];
+    S.vy0 = sd.viewportRect[1];
+    S.vw = sd.viewportRect[2];
+    S.vh = sd.viewportRect[3];
+    S.spp = std::max(sd.samplesPerPixel, 1u);
+    S.spectral = spectral ? 1u : 0u;
+    S.neeEnabled = (sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u) ? 1u : 0u;
+    S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
+    return S;
+}
+
+WavefrontConfig engineConfig(const VKRT_CudaContext* c) {
+    return WavefrontConfig{c->wfCfg.queueCapacity,  c->wfCfg.tileWidth,           c->wfCfg.tileHeight,
+                           c->wfCfg.sortByMaterial, c->wfCfg.intersectBlocksPerSM, c->wfCfg.shadeBlocksPerSM,
+                           c->wfCfg.useGraph};
+}
+
 }  // namespace
 
 extern "C" {
@@ -650,22 +675,7 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     cudaSetDevice(c0->device);
     for (uint32_t i = 0; i < count; ++i) {
         VKRT_CudaContext* c = contexts[i];
-        const VKRT_CudaSceneData& sd = sds[i];
-        WfScene& S = scenes[i];
-        std::memset(&S, 0, sizeof(S));
-        S.sc = makeDeviceScene(c);
-        S.sd = sd;
-        S.film = FilmBuffers{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
-        S.filmWidth = c->width;
-        S.filmHeight = c->height;
-        S.vx0 = sd.viewportRect[0];
-        S.vy0 = sd.viewportRect[1];
-        S.vw = sd.viewportRect[2];
-        S.vh = sd.viewportRect[3];
-        S.spp = std::max(sd.samplesPerPixel, 1u);
-        S.spectral = spectral ? 1u : 0u;
-        S.neeEnabled = (sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u) ? 1u : 0u;
-        S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
+        scenes[i] = makeWfScene(c, sds[i], spectral);
         // c0's stream reads this context's buffers: order it after the work already queued on its own stream
         if (c != c0) {
             VKRT_TRY(c0, cudaEventRecord(c->order, c->stream), "batch ordering");
@@ -673,9 +683,7 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
         }
     }
     if (!c0->wavefront) c0->wavefront.reset(new WavefrontEngine());
-    WavefrontConfig wc{c0->wfCfg.queueCapacity, c0->wfCfg.tileWidth,     c0->wfCfg.tileHeight,
-                       c0->wfCfg.sortByMaterial, c0->wfCfg.intersectBlocksPerSM, c0->wfCfg.shadeBlocksPerSM,
-                       c0->wfCfg.useGraph};
+    WavefrontConfig wc = engineConfig(c0);
     VKRT_TRY(c0, cudaMemsetAsync(c0->counters, 0, sizeof(RenderCounters), c0->stream), "batch render");
     VKRT_TRY(c0, c0->wavefront->render(scenes, spectral, wc, c0->cfg.rngMode, c0->cfg.rngSeed, c0->counters, c0->stream),
              "batch render");
@@ -902,7 +910,20 @@ int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const f
     ap.materialGrad = c->materialGrad.ptr;
     ap.emissiveMeshMaterial = c->emissiveMeshMaterial.ptr;
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "adjoint");
-    VKRT_TRY(c, launchAdjoint(scene, *sd, ap, c->counters, c->stream), "adjoint launch");
+    if (c->cfg.integrator == VKRT_CUDA_INTEGRATOR_WAVEFRONT) {
+        // a primal wavefront pass keeps each (pixel, sample) radiance, the adjoint pass replays those paths
+        std::vector<WfScene> scenes(1, makeWfScene(c, *sd, false));
+        if (!c->wavefront) c->wavefront.reset(new WavefrontEngine());
+        WavefrontConfig wc = engineConfig(c);
+        VKRT_TRY(c, c->wavefront->render(scenes, false, wc, c->cfg.rngMode, c->cfg.rngSeed, c->counters, c->stream,
+                                         kWavefrontPrimal, &ap),
+                 "adjoint primal pass");
+        VKRT_TRY(c, c->wavefront->render(scenes, false, wc, c->cfg.rngMode, c->cfg.rngSeed, c->counters, c->stream,
+                                         kWavefrontAdjoint, &ap),
+                 "adjoint pass");
+    } else {
+        VKRT_TRY(c, launchAdjoint(scene, *sd, ap, c->counters, c->stream), "adjoint launch");
+    }
     c->countersPending = true;
     return VKRT_CUDA_SUCCESS;
 }

@@ -27,7 +27,7 @@
 #include <cstring>
 #include <vector>
 
-#include "path.cuh"
+#include "adjoint.cuh"
 #include "wavefront.h"
 
 namespace vkrt {
@@ -49,6 +49,7 @@ enum : uint32_t {
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
 
 struct WfGlobals {
+    uint32_t mode;  // WavefrontMode
     const WfScene* scenes;
     uint32_t sceneCount;
     uint32_t totalWork;   // padded pixels of all scenes
@@ -87,6 +88,18 @@ struct WfGlobals {
     uint32_t* counts;
     RenderCounters* counters;
     cudaGraphConditionalHandle cond;
+    // adjoint pass (one scene): parameters and, per slot, the pending vertex's gradient factors
+    AdjointParams adj;
+    float4* adjDelta;   // d(loss)/d(sample radiance) of the slot's item
+    float4* adjTotal;   // the item's radiance from the primal pass
+    float4* adjUv;      // uv0.xy, uv1.xy of the pending vertex
+    float4* adjColor;   // its vertex colour
+    float4* adjReq0;    // request 0: delta * factor * Le * df/dbase (xyz), roughness term (w)
+    float4* adjReq1;
+    float4* adjEm0;     // request 0: delta * factor * f (xyz), emissive mesh (w bits)
+    float4* adjEm1;
+    float4* adjRatioB;  // (df/dbase) / f (xyz), material index (w bits)
+    float4* adjRatioR;  // (df/droughness) / f (xyz), kAdjFlag* bits (w)
 };
 
 VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
@@ -177,11 +190,17 @@ VKRT_DEV bool startSample(const WfGlobals& g, uint32_t slot, uint32_t sceneId, u
     int px, py;
     if (!workPixel(S, work, px, py)) return false;
     uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
-    uint32_t prevN = uint32_t(S.film.accumRead[pix].w + 0.5f);
+    // a frame continues the film's sample count; the primal and adjoint passes replay the samples from sampleBase
+    uint32_t first = g.mode == kWavefrontForward ? uint32_t(S.film.accumRead[pix].w + 0.5f) : g.adj.sampleBase;
     StepConfig cfg = stepConfig(g, S);
-    PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, prevN + sample);
+    PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, first + sample);
     storePath(g, slot, p);
     g.pendFlags[slot] = 0u;
+    if (g.mode == kWavefrontAdjoint) {
+        float inv = 1.0f / float(g.adj.sampleBase + S.spp);
+        g.adjDelta[slot] = g.adj.dImage[pix] * inv;
+        g.adjRatioR[slot] = f4(0.0f);  // no pending vertex
+    }
     return true;
 }
 
@@ -207,6 +226,7 @@ VKRT_DEV bool acquireItem(const WfGlobals& g, uint32_t slot, uint32_t w) {
         if (startSample<kSpectral>(g, slot, sceneId, local / S.spp, local % S.spp)) {
             g.slotScene[slot] = sceneId;
             g.slotItem[slot] = local;
+            if (g.mode == kWavefrontAdjoint) g.adjTotal[slot] = g.sampleBuf[size_t(S.itemBase) + local];
             return true;
         }
         w = atomicAdd(&g.counts[kCntCursor], 1u);
@@ -360,8 +380,77 @@ VKRT_DEV void applyPending(const WfGlobals& g, uint32_t slot, float4& radiance) 
     if ((f & 2u) && (f & 8u)) radiance += g.pend1[slot];
 }
 
-template <bool kSpectral>
+// the vertex gradient factors recorded by the hook, kept per slot until the vertex's shadow rays are traced
+VKRT_DEV void adjStoreVertex(const WfGlobals& g, uint32_t slot, const AdjVertex& av, bool cont) {
+    if (!av.hasSurface) {
+        g.adjRatioR[slot] = f4(0.0f);
+        return;
+    }
+    uint32_t flags = kAdjFlagSurface | (cont && av.sampled ? kAdjFlagContinued : 0u) |
+                     (av.reqValid[0] ? kAdjFlagReq0 : 0u) | (av.reqValid[1] ? kAdjFlagReq1 : 0u);
+    g.adjUv[slot] = make_float4(av.tex.uv0.x, av.tex.uv0.y, av.tex.uv1.x, av.tex.uv1.y);
+    g.adjColor[slot] = av.tex.color;
+    if (av.reqValid[0]) {
+        g.adjReq0[slot] = make_float4(av.reqBase[0].x, av.reqBase[0].y, av.reqBase[0].z, av.reqRough[0]);
+        g.adjEm0[slot] = make_float4(av.reqEmit[0].x, av.reqEmit[0].y, av.reqEmit[0].z, __uint_as_float(av.reqLight[0]));
+    }
+    if (av.reqValid[1]) {
+        g.adjReq1[slot] = make_float4(av.reqBase[1].x, av.reqBase[1].y, av.reqBase[1].z, av.reqRough[1]);
+        g.adjEm1[slot] = make_float4(av.reqEmit[1].x, av.reqEmit[1].y, av.reqEmit[1].z, __uint_as_float(av.reqLight[1]));
+    }
+    g.adjRatioB[slot] = make_float4(av.ratioBase.x, av.ratioBase.y, av.ratioBase.z, __uint_as_float(av.materialIndex));
+    g.adjRatioR[slot] = make_float4(av.ratioRough.x, av.ratioRough.y, av.ratioRough.z, __uint_as_float(flags));
+}
+
+// Finishes the slot's pending vertex: pendFlags carries its requests' visibility, radiance the path radiance with
+// them applied.
+VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t slot, uint32_t pendFlags,
+                               float4 radiance, MaterialGradient* smemMat) {
+    float4 rr = g.adjRatioR[slot];
+    uint32_t flags = __float_as_uint(rr.w);
+    if (!(flags & kAdjFlagSurface)) return;
+    AdjVertex av;
+    float4 rb = g.adjRatioB[slot], uv = g.adjUv[slot];
+    av.materialIndex = __float_as_uint(rb.w);
+    av.tex.uv0 = make_float2(uv.x, uv.y);
+    av.tex.uv1 = make_float2(uv.z, uv.w);
+    av.tex.color = g.adjColor[slot];
+    av.hasSurface = true;
+    av.emitted = false;
+    av.sampled = true;
+    av.ratioBase = xyz(rb);
+    av.ratioRough = xyz(rr);
+    av.reqValid[0] = (flags & kAdjFlagReq0) != 0u;
+    av.reqValid[1] = (flags & kAdjFlagReq1) != 0u;
+    if (av.reqValid[0]) {
+        float4 a = g.adjReq0[slot], e = g.adjEm0[slot];
+        av.reqBase[0] = xyz(a);
+        av.reqRough[0] = a.w;
+        av.reqEmit[0] = xyz(e);
+        av.reqLight[0] = __float_as_uint(e.w);
+    }
+    if (av.reqValid[1]) {
+        float4 a = g.adjReq1[slot], e = g.adjEm1[slot];
+        av.reqBase[1] = xyz(a);
+        av.reqRough[1] = a.w;
+        av.reqEmit[1] = xyz(e);
+        av.reqLight[1] = __float_as_uint(e.w);
+    }
+    bool vis[2] = {(pendFlags & 1u) && (pendFlags & 4u), (pendFlags & 2u) && (pendFlags & 8u)};
+    finishVertex(S.sc, g.adj, smemMat, av, vis, (flags & kAdjFlagContinued) != 0u, xyz(g.adjDelta[slot]),
+                 xyz(g.adjTotal[slot]), xyz(radiance));
+}
+
+template <bool kSpectral, bool kAdjoint>
 __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
+    MaterialGradient* smemMat = nullptr;
+    if constexpr (kAdjoint) {
+        __shared__ MaterialGradient smemMatStorage[kSmemMaterials];
+        const uint32_t mc = g.scenes[0].sc.materialCount;
+        smemMat = mc <= kSmemMaterials ? smemMatStorage : nullptr;
+        clearMaterialSmem(smemMat, mc);
+        __syncthreads();
+    }
     const uint32_t* q = g.sort ? g.sorted : (inQueue == 0 ? g.queue0 : g.queue1);
     uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
@@ -375,12 +464,24 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQ
             slot = q[i];
             const WfScene& S = g.scenes[g.slotScene[slot]];
             PathState p = loadPath(g, slot);
+            const uint32_t pf = g.pendFlags[slot];
             applyPending(g, slot, p.radiance);
+            if constexpr (kAdjoint) adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
             g.pendFlags[slot] = 0u;
             uint4 a = g.hitA[slot];
             TraceHit h{a.x, a.y, 0u, __uint_as_float(a.z), __uint_as_float(a.w), g.hitV[slot]};
             StepConfig cfg = stepConfig(g, S);
-            cont = shadePathVertex<kSpectral>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns);
+            if constexpr (kAdjoint) {
+                AdjVertex av;
+                av.hasSurface = av.emitted = av.sampled = false;
+                av.reqValid[0] = av.reqValid[1] = false;
+                cont = shadePathVertex<kSpectral, AdjointHook>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
+                                                               AdjointHook{&av, xyz(g.adjDelta[slot])});
+                if (g.adj.wantEmission && av.emitted) scatterHitEmission(S.sc, g.adj, smemMat, av);
+                adjStoreVertex(g, slot, av, cont);
+            } else {
+                cont = shadePathVertex<kSpectral>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns);
+            }
             storePath(g, slot, p);
             uint32_t flags = 0u;
             if (ns > 0) {
@@ -408,6 +509,10 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQ
             }
         }
     }
+    if constexpr (kAdjoint) {
+        __syncthreads();
+        flushMaterialSmem(g.adj, smemMat, g.scenes[0].sc.materialCount);
+    }
 }
 
 __global__ void __launch_bounds__(kWfThreads) kWfShadow(WfGlobals g) {
@@ -434,8 +539,16 @@ __global__ void __launch_bounds__(kWfThreads) kWfShadow(WfGlobals g) {
     warpCount(&g.counters->shadowRays, traced);
 }
 
-template <bool kSpectral>
+template <bool kSpectral, bool kAdjoint>
 __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t outQueue) {
+    MaterialGradient* smemMat = nullptr;
+    if constexpr (kAdjoint) {
+        __shared__ MaterialGradient smemMatStorage[kSmemMaterials];
+        const uint32_t mc = g.scenes[0].sc.materialCount;
+        smemMat = mc <= kSmemMaterials ? smemMatStorage : nullptr;
+        clearMaterialSmem(smemMat, mc);
+        __syncthreads();
+    }
     uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[kCntFinished];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -448,11 +561,16 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             uint32_t sceneId = g.slotScene[slot];
             const WfScene& S = g.scenes[sceneId];
             PathState p = loadPath(g, slot);
+            const uint32_t pf = g.pendFlags[slot];
             applyPending(g, slot, p.radiance);
             g.pendFlags[slot] = 0u;
-            StepConfig cfg = stepConfig(g, S);
-            float3 res = pathResult<kSpectral>(cfg, p);
-            g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
+            if constexpr (kAdjoint) {
+                adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
+            } else {
+                StepConfig cfg = stepConfig(g, S);
+                float3 res = pathResult<kSpectral>(cfg, p);
+                g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
+            }
             samples = 1;
             uint32_t w = atomicAdd(&g.counts[kCntCursor], 1u);
             requeue = acquireItem<kSpectral>(g, slot, w);
@@ -461,6 +579,10 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
         uint32_t pos = warpPush(&g.counts[outQueue], valid && requeue);
         if (valid && requeue) outQ[pos] = slot;
         warpCount(&g.counters->pathSamples, samples);
+    }
+    if constexpr (kAdjoint) {
+        __syncthreads();
+        flushMaterialSmem(g.adj, smemMat, g.scenes[0].sc.materialCount);
     }
 }
 
@@ -491,19 +613,25 @@ cudaError_t grow(T*& p, size_t& cap, size_t n) {
 // ---------------------------------------------------------------------------------------------------------------
 // engine
 // ---------------------------------------------------------------------------------------------------------------
+// one instantiated graph per mode, rebuilt when the launch shape or the kernel arguments change
+struct WfGraphCache {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool spectral = false;
+    WavefrontConfig cfg{};
+    uint32_t Q = 0, keys = 0, maxIter = 0, total = 0, sceneCount = 0;
+    WfGlobals g{};  // kernel arguments baked into the graph (conditional handle zeroed)
+};
+
 struct WavefrontEngine::Buffers {
     WfGlobals g{};
     size_t capQ = 0, capKeys = 0, capScenes = 0;
     size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
            c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
            c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0;
+    size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
     WfScene* scenes = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    bool graphSpectral = false;
-    WavefrontConfig graphCfg{};
-    uint32_t graphQ = 0, graphKeys = 0, graphScenesCap = 0, graphMaxIter = 0, graphTotal = 0, graphSceneCount = 0;
-    WfGlobals graphG{};  // kernel arguments baked into the graph (conditional handle zeroed)
+    WfGraphCache graphs[3];
 };
 
 WavefrontEngine::WavefrontEngine() : b_(new Buffers()) {}
@@ -515,14 +643,17 @@ WavefrontEngine::~WavefrontEngine() {
 
 void WavefrontEngine::release() {
     if (!b_) return;
-    if (b_->exec) cudaGraphExecDestroy(b_->exec);
-    if (b_->graph) cudaGraphDestroy(b_->graph);
-    b_->exec = nullptr;
-    b_->graph = nullptr;
+    for (WfGraphCache& gc : b_->graphs) {
+        if (gc.exec) cudaGraphExecDestroy(gc.exec);
+        if (gc.graph) cudaGraphDestroy(gc.graph);
+        gc.exec = nullptr;
+        gc.graph = nullptr;
+    }
     WfGlobals& g = b_->g;
     void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotItem, g.sampleBuf,
                     g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
-                    g.sorted, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes};
+                    g.sorted, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, g.adjDelta, g.adjTotal,
+                    g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     Buffers* fresh = new Buffers();
@@ -532,8 +663,10 @@ void WavefrontEngine::release() {
 
 cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool spectral, const WavefrontConfig& cfgIn,
                                     uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters,
-                                    cudaStream_t stream) {
+                                    cudaStream_t stream, WavefrontMode mode, const AdjointParams* adjoint) {
     Buffers& B = *b_;
+    const bool adjMode = mode == kWavefrontAdjoint;
+    if (adjMode && (!adjoint || spectral || scenesIn.size() != 1)) return cudaErrorInvalidValue;
     WavefrontConfig cfg = cfgIn;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
@@ -594,11 +727,25 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(shadowB, c_sB, 2 * size_t(Q));
     WF_GROW(keyHist, c_hist, keys);
     WF_GROW(counts, c_counts, 16);
+    if (adjMode) {
+        WF_GROW(adjDelta, c_aD, Q);
+        WF_GROW(adjTotal, c_aT, Q);
+        WF_GROW(adjUv, c_aU, Q);
+        WF_GROW(adjColor, c_aC, Q);
+        WF_GROW(adjReq0, c_aR0, Q);
+        WF_GROW(adjReq1, c_aR1, Q);
+        WF_GROW(adjEm0, c_aE0, Q);
+        WF_GROW(adjEm1, c_aE1, Q);
+        WF_GROW(adjRatioB, c_aRB, Q);
+        WF_GROW(adjRatioR, c_aRR, Q);
+    }
 #undef WF_GROW
     if (e == cudaSuccess) e = grow(B.scenes, B.c_sc, scenes.size());
     if (e != cudaSuccess) return e;
     e = cudaMemcpyAsync(B.scenes, scenes.data(), sizeof(WfScene) * scenes.size(), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
+    g.mode = uint32_t(mode);
+    g.adj = adjoint ? *adjoint : AdjointParams{};
     g.scenes = B.scenes;
     g.sceneCount = uint32_t(scenes.size());
     g.totalWork = total;
@@ -622,21 +769,24 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             kWfSortScan<<<1, 1024, 0, stream>>>(g);
             kWfSortScatter<<<gridS, 256, 0, stream>>>(g, in);
         }
-        if (spectral) kWfShade<true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-        else kWfShade<false><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+        if (adjMode) kWfShade<false, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+        else if (spectral) kWfShade<true, false><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+        else kWfShade<false, false><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
         kWfShadow<<<gridI, kWfThreads, smem, stream>>>(g);
-        if (spectral) kWfFinalize<true><<<gridS, kWfThreads, 0, stream>>>(g, out);
-        else kWfFinalize<false><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        if (adjMode) kWfFinalize<false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        else if (spectral) kWfFinalize<true, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        else kWfFinalize<false, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
         (void)useGraph;
     };
-    auto resolve = [&]() {
+    auto resolve = [&]() {  // the film is written by forward frames only
+        if (mode != kWavefrontForward) return;
         if (spectral) kWfResolve<true><<<gridS, 256, 0, stream>>>(g);
         else kWfResolve<false><<<gridS, 256, 0, stream>>>(g);
     };
     auto prologue = [&]() {
         kWfSetup<<<1, 32, 0, stream>>>(g);
         dim3 cg(std::max(1, sms), std::min<uint32_t>(g.sceneCount, 64u));
-        kWfClearOutside<<<cg, 256, 0, stream>>>(g);
+        if (mode == kWavefrontForward) kWfClearOutside<<<cg, 256, 0, stream>>>(g);
         if (spectral) kWfInit<true><<<gridS, kWfThreads, 0, stream>>>(g);
         else kWfInit<false><<<gridS, kWfThreads, 0, stream>>>(g);
     };
@@ -663,27 +813,29 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         return e;
     }
 
-    // one graph per engine shape: setup/init kernels then a conditional while node over the two-iteration body
-    bool rebuild = !B.exec || B.graphSpectral != spectral || std::memcmp(&B.graphCfg, &cfg, sizeof(cfg)) != 0 ||
-                   B.graphQ != Q || B.graphKeys != keys || B.graphMaxIter != maxIter || B.graphTotal != total ||
-                   B.graphSceneCount != g.sceneCount;
+    // one graph per engine shape and mode: setup/init kernels then a conditional while node over the two-iteration
+    // body
+    WfGraphCache& GC = B.graphs[uint32_t(mode)];
+    bool rebuild = !GC.exec || GC.spectral != spectral || std::memcmp(&GC.cfg, &cfg, sizeof(cfg)) != 0 ||
+                   GC.Q != Q || GC.keys != keys || GC.maxIter != maxIter || GC.total != total ||
+                   GC.sceneCount != g.sceneCount;
     {
-        WfGlobals a = g, b = B.graphG;
+        WfGlobals a = g, b = GC.g;
         a.cond = 0;
         b.cond = 0;
         if (std::memcmp(&a, &b, sizeof(a)) != 0) rebuild = true;
     }
     if (rebuild) {
-        if (B.exec) cudaGraphExecDestroy(B.exec);
-        if (B.graph) cudaGraphDestroy(B.graph);
-        B.exec = nullptr;
-        B.graph = nullptr;
-        e = cudaGraphCreate(&B.graph, 0);
+        if (GC.exec) cudaGraphExecDestroy(GC.exec);
+        if (GC.graph) cudaGraphDestroy(GC.graph);
+        GC.exec = nullptr;
+        GC.graph = nullptr;
+        e = cudaGraphCreate(&GC.graph, 0);
         if (e != cudaSuccess) return e;
-        e = cudaGraphConditionalHandleCreate(&g.cond, B.graph, 1u, cudaGraphCondAssignDefault);
+        e = cudaGraphConditionalHandleCreate(&g.cond, GC.graph, 1u, cudaGraphCondAssignDefault);
         if (e != cudaSuccess) return e;
         // prologue captured into the top-level graph
-        e = cudaStreamBeginCaptureToGraph(stream, B.graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        e = cudaStreamBeginCaptureToGraph(stream, GC.graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) return e;
         prologue();
         cudaGraph_t captured = nullptr;
@@ -691,9 +843,9 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         if (e != cudaSuccess) return e;
         // the conditional node depends on every node of the prologue
         size_t numNodes = 0;
-        cudaGraphGetNodes(B.graph, nullptr, &numNodes);
+        cudaGraphGetNodes(GC.graph, nullptr, &numNodes);
         std::vector<cudaGraphNode_t> nodes(numNodes);
-        if (numNodes) cudaGraphGetNodes(B.graph, nodes.data(), &numNodes);
+        if (numNodes) cudaGraphGetNodes(GC.graph, nodes.data(), &numNodes);
         // zero-filled storage: the parameter union has no usable default constructor
         alignas(cudaGraphNodeParams) unsigned char cpStorage[sizeof(cudaGraphNodeParams)];
         std::memset(cpStorage, 0, sizeof(cpStorage));
@@ -703,7 +855,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         cp.conditional.type = cudaGraphCondTypeWhile;
         cp.conditional.size = 1;
         cudaGraphNode_t condNode;
-        e = cudaGraphAddNode(&condNode, B.graph, nodes.data(), nullptr, numNodes, &cp);
+        e = cudaGraphAddNode(&condNode, GC.graph, nodes.data(), nullptr, numNodes, &cp);
         if (e != cudaSuccess) return e;
         cudaGraph_t bodyGraph = cp.conditional.phGraph_out[0];
         e = cudaStreamBeginCaptureToGraph(stream, bodyGraph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
@@ -714,24 +866,24 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         e = cudaStreamEndCapture(stream, &bodyGraph);
         if (e != cudaSuccess) return e;
         // the resolve kernel runs once the loop has drained every item
-        e = cudaStreamBeginCaptureToGraph(stream, B.graph, &condNode, nullptr, 1, cudaStreamCaptureModeRelaxed);
+        e = cudaStreamBeginCaptureToGraph(stream, GC.graph, &condNode, nullptr, 1, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) return e;
         resolve();
         e = cudaStreamEndCapture(stream, &captured);
         if (e != cudaSuccess) return e;
-        e = cudaGraphInstantiate(&B.exec, B.graph, 0);
+        e = cudaGraphInstantiate(&GC.exec, GC.graph, 0);
         if (e != cudaSuccess) return e;
-        B.graphSpectral = spectral;
-        B.graphCfg = cfg;
-        B.graphQ = Q;
-        B.graphKeys = keys;
-        B.graphMaxIter = maxIter;
-        B.graphTotal = total;
-        B.graphSceneCount = g.sceneCount;
-        B.graphG = g;
-        B.graphG.cond = 0;
+        GC.spectral = spectral;
+        GC.cfg = cfg;
+        GC.Q = Q;
+        GC.keys = keys;
+        GC.maxIter = maxIter;
+        GC.total = total;
+        GC.sceneCount = g.sceneCount;
+        GC.g = g;
+        GC.g.cond = 0;
     }
-    e = cudaGraphLaunch(B.exec, stream);
+    e = cudaGraphLaunch(GC.exec, stream);
     return e;
 }
 

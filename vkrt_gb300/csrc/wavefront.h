@@ -5,6 +5,7 @@
 
 #include <vector>
 
+#include "adjoint.h"
 #include "render.h"
 #include "scene.cuh"
 
@@ -28,6 +29,10 @@ struct WfScene {
     uint32_t materialKeyBase;
 };
 
+// forward: a frame blended into each scene's film; primal: the same paths, each (pixel, sample) radiance kept in the
+// engine's sample buffer and the film untouched; adjoint: the primal paths replayed with gradients (one scene)
+enum WavefrontMode : uint32_t { kWavefrontForward = 0, kWavefrontPrimal = 1, kWavefrontAdjoint = 2 };
+
 struct WavefrontConfig {
     uint32_t queueCapacity;  // path slots; 0 = one per work item, capped at 4M
     uint32_t tileWidth;
@@ -46,8 +51,11 @@ public:
     WavefrontEngine& operator=(const WavefrontEngine&) = delete;
 
     // Renders one frame of every scene (all spectral or all RGB) on `stream`, asynchronously.
+    // `adjoint` is read in adjoint mode, which must follow a primal pass over the same scene, configuration and
+    // sampleBase.
     cudaError_t render(const std::vector<WfScene>& scenes, bool spectral, const WavefrontConfig& cfg,
-                       uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters, cudaStream_t stream);
+                       uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters, cudaStream_t stream,
+                       WavefrontMode mode = kWavefrontForward, const AdjointParams* adjoint = nullptr);
     void release();
 
 private:
