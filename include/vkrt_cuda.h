@@ -55,14 +55,17 @@ typedef struct VKRT_CudaConfig {
 
 /* Wavefront integrator parameters (autotuned by vkrt_cuda_autotune_batch). 64 bytes. */
 typedef struct VKRT_CudaWavefrontConfig {
-    uint32_t queueCapacity;        /* path slots; 0 = one per pixel of the batch, capped at 4M */
+    uint32_t queueCapacity;        /* path slots; 0 = one per (pixel, sample) item of the batch, capped at 4M */
     uint32_t tileWidth;            /* pixels are handed to path slots in tiles of tileWidth x tileHeight */
     uint32_t tileHeight;
-    uint32_t sortByMaterial;       /* 1: shade queue counting-sorted by (scene, material) before shading */
+    uint32_t sortByMaterial;       /* shade-queue order: 0 as traced; 1 counting-sorted by (scene, material);
+                                      2 partitioned into misses, dielectric and metal hits by the intersect kernel */
     uint32_t intersectBlocksPerSM; /* persistent grid of the traversal kernels, per SM */
     uint32_t shadeBlocksPerSM;     /* persistent grid of the shading kernels, per SM */
     uint32_t useGraph;             /* 1: the frame is one CUDA-graph launch (conditional while node) */
-    uint32_t reserved[9];
+    uint32_t profileStages;        /* 1: stage-by-stage launches with device timers and fetch-byte counting (slower;
+                                      for profiling), reported in VKRT_CudaStats.stageMs / *FetchBytes */
+    uint32_t reserved[8];
 } VKRT_CudaWavefrontConfig;
 
 typedef struct VKRT_CudaStats {
@@ -70,13 +73,20 @@ typedef struct VKRT_CudaStats {
     uint64_t extensionRays;  /* closest-hit rays after the first bounce */
     uint64_t shadowRays;     /* any-hit (occlusion) rays */
     uint64_t pathSamples;    /* pixel samples started */
-    uint64_t nodeFetchBytes; /* BVH node bytes fetched (only with countRays) */
-    uint64_t triFetchBytes;  /* triangle bytes fetched (only with countRays) */
+    uint64_t nodeFetchBytes; /* closest-hit BVH node bytes fetched (countRays, or wavefront profileStages) */
+    uint64_t triFetchBytes;  /* closest-hit triangle bytes fetched (same) */
     uint32_t bvhNodeCount;   /* 8-wide nodes */
     uint32_t bvhTriangleCount;
     uint64_t bvhBytes;       /* nodes + triangle records resident in HBM */
     float bvhBuildMs;        /* device time of the last BVH build */
     uint32_t errorFlags;     /* device-side error word (bit 0: traversal stack overflow guard hit) */
+    uint32_t wavefrontBodies;      /* wavefront loop bodies (two bounces each) of the last call */
+    uint32_t reserved0;
+    uint64_t shadowNodeFetchBytes; /* any-hit traversal node / triangle bytes (same conditions as nodeFetchBytes) */
+    uint64_t shadowTriFetchBytes;
+    uint64_t kernelLaunches;       /* this backend's kernel launches made by the last call */
+    float stageMs[8];              /* wavefront profileStages device ms: prologue, begin, intersect, sort, shade,
+                                      shadow, finalize, resolve */
 } VKRT_CudaStats;
 
 /* ray record for the trace entry points: origin/tMin, direction/tMax (32 bytes, 16-byte aligned) */

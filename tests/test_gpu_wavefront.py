@@ -50,7 +50,8 @@ def test_wavefront_schedule_independence(built):
                                    env_size=(64, 32))
     kw = dict(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE)
     base, _ = _render(scene, abi.INTEGRATOR_WAVEFRONT, wf={"queueCapacity": 0}, **kw)
-    for wf in ({"sortByMaterial": 1}, {"useGraph": 0}, {"tileWidth": 4, "tileHeight": 4, "queueCapacity": 300},
+    for wf in ({"sortByMaterial": 1}, {"sortByMaterial": 2}, {"useGraph": 0},
+               {"tileWidth": 4, "tileHeight": 4, "queueCapacity": 300, "sortByMaterial": 2},
                {"queueCapacity": 97, "sortByMaterial": 1, "intersectBlocksPerSM": 2, "shadeBlocksPerSM": 1}):
         got, _ = _render(scene, abi.INTEGRATOR_WAVEFRONT, wf=wf, **kw)
         np.testing.assert_array_equal(got, base, err_msg=str(wf))

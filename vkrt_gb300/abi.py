@@ -79,15 +79,20 @@ CONFIG = np.dtype({"names": ["deviceIndex", "rngMode", "rngSeed", "environmentSa
                    "offsets": [0, 4, 8, 16, 20, 24, 28, 32, 36], "itemsize": 64})
 
 WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
-                                       "intersectBlocksPerSM", "shadeBlocksPerSM", "useGraph", "reserved"],
-                             "formats": ["<u4"] * 7 + [("<u4", 9)], "offsets": [0, 4, 8, 12, 16, 20, 24, 28],
+                                       "intersectBlocksPerSM", "shadeBlocksPerSM", "useGraph", "profileStages",
+                                       "reserved"],
+                             "formats": ["<u4"] * 8 + [("<u4", 8)], "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32],
                              "itemsize": 64})
 
 STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathSamples", "nodeFetchBytes",
                             "triFetchBytes", "bvhNodeCount", "bvhTriangleCount", "bvhBytes", "bvhBuildMs",
-                            "errorFlags"],
-                  "formats": ["<u8", "<u8", "<u8", "<u8", "<u8", "<u8", "<u4", "<u4", "<u8", "<f4", "<u4"],
-                  "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 64, 68], "itemsize": 72})
+                            "errorFlags", "wavefrontBodies", "reserved0", "shadowNodeFetchBytes",
+                            "shadowTriFetchBytes", "kernelLaunches", "stageMs"],
+                  "formats": ["<u8", "<u8", "<u8", "<u8", "<u8", "<u8", "<u4", "<u4", "<u8", "<f4", "<u4", "<u4",
+                              "<u4", "<u8", "<u8", "<u8", ("<f4", 8)],
+                  "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 64, 68, 72, 76, 80, 88, 96, 104], "itemsize": 136})
+
+WAVEFRONT_STAGES = ("prologue", "begin", "intersect", "sort", "shade", "shadow", "finalize", "resolve")
 
 ADJOINT_CONFIG = np.dtype({"names": ["sampleBase", "gradients", "accumulate", "reserved"],
                            "formats": ["<u4", "<u4", "<u4", ("<u4", 5)], "offsets": [0, 4, 8, 12], "itemsize": 32})

@@ -288,7 +288,7 @@ class RenderContext:
     def stats(self) -> dict:
         st = np.zeros(1, dtype=abi.STATS)
         self._check(self.lib.vkrt_cuda_get_stats(self.handle, abi.ptr(st)), "stats")
-        return {k: st[k][0].item() for k in abi.STATS.names}
+        return {k: st[k][0].tolist() for k in abi.STATS.names}
 
     def trace_rays(self, rays: np.ndarray, any_hit: bool = False) -> np.ndarray:
         r = np.ascontiguousarray(rays, dtype=abi.RAY)

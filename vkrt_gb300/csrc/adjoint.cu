@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kAdjThreads) kAdjoint(DeviceScene sc, VKRT_Cud
     KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
     const StepConfig cfg{false, sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u, ap.envNee != 0u, ap.rngMode,
                          ap.rngSeed};
-    const SpecTable tab{sc.rgb2spec, sd.rgb2specSRGB.res, sd.rgb2specSRGB.scaleOffset, sd.rgb2specSRGB.dataOffset};
+    const SpecTable tab = makeSpecTable(sc, sd);
     PathCounts pc{0u, 0u, 0u, 0u};
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < items; item += gridDim.x * blockDim.x) {
         // sample-major order: a warp holds neighbouring pixels of one sample, so its texel atomics spread out
@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(kAdjThreads) kAdjoint(DeviceScene sc, VKRT_Cud
     }
     __syncthreads();
     flushMaterialSmem(ap, smemMat, sc.materialCount);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && counters) atomicAdd(&counters->kernelLaunches, 1ull);
     for (int off = 16; off > 0; off >>= 1) {
         pc.primary += __shfl_xor_sync(0xFFFFFFFFu, pc.primary, off);
         pc.extension += __shfl_xor_sync(0xFFFFFFFFu, pc.extension, off);

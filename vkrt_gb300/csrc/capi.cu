@@ -93,9 +93,11 @@ struct VKRT_CudaContext {
     DeviceArray<float> rgb2spec;
     uint32_t rgb2specFloats = 0;
     VKRT_CudaRGB2SpecTableInfo rgb2specInfo{};
+    DeviceArray<float4> rgb2specCells;  // the table of rgb2specInfo repacked one float4 per cell
 
     // environment distribution
     DeviceArray<float> envMarginal, envConditional, envTexelPdf;
+    DeviceArray<uint32_t> envMarginalGuide, envConditionalGuide;
     DeviceArray<double> envScratch;
     uint32_t envWidth = 0, envHeight = 0, envTexture = VKRT_CUDA_INVALID_INDEX;
 
@@ -201,9 +203,13 @@ DeviceScene makeDeviceScene(VKRT_CudaContext* c) {
     s.textures = c->textureTable.ptr;
     s.rgb2spec = c->rgb2spec.ptr;
     s.rgb2specFloatCount = c->rgb2specFloats;
+    s.rgb2specCells = c->rgb2specCells.ptr;
+    s.rgb2specCellsInfo = c->rgb2specInfo;
     s.env.marginal = c->envMarginal.ptr;
     s.env.conditional = c->envConditional.ptr;
     s.env.texelPdf = c->envTexelPdf.ptr;
+    s.env.marginalGuide = c->envMarginalGuide.ptr;
+    s.env.conditionalGuide = c->envConditionalGuide.ptr;
     s.env.width = c->envWidth;
     s.env.height = c->envHeight;
     s.env.textureIndex = c->envTexture;
@@ -272,7 +278,7 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
 WavefrontConfig engineConfig(const VKRT_CudaContext* c) {
     return WavefrontConfig{c->wfCfg.queueCapacity,  c->wfCfg.tileWidth,           c->wfCfg.tileHeight,
                            c->wfCfg.sortByMaterial, c->wfCfg.intersectBlocksPerSM, c->wfCfg.shadeBlocksPerSM,
-                           c->wfCfg.useGraph};
+                           c->wfCfg.useGraph,       c->wfCfg.profileStages};
 }
 
 }  // namespace
@@ -345,6 +351,9 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     for (auto& t : c->textureData) t.release();
     c->textureTable.release();
     c->rgb2spec.release();
+    c->rgb2specCells.release();
+    c->envMarginalGuide.release();
+    c->envConditionalGuide.release();
     c->envMarginal.release();
     c->envConditional.release();
     c->envTexelPdf.release();
@@ -525,6 +534,11 @@ int32_t vkrt_cuda_set_environment(VKRT_CudaContext* c, uint32_t textureIndex) {
     VKRT_TRY(c, launchBuildEnvDistribution(t.texels, W, H, c->envMarginal.ptr, c->envConditional.ptr, c->envTexelPdf.ptr,
                                            c->envScratch.ptr, c->stream),
              "environment CDF");
+    VKRT_TRY(c, c->envMarginalGuide.reserve(kEnvGuide + 1u), "environment guide");
+    VKRT_TRY(c, c->envConditionalGuide.reserve(size_t(H) * (kEnvGuide + 1u)), "environment guide");
+    VKRT_TRY(c, launchBuildEnvGuides(c->envMarginal.ptr, c->envConditional.ptr, W, H, c->envMarginalGuide.ptr,
+                                     c->envConditionalGuide.ptr, c->stream),
+             "environment guide");
     VKRT_TRY(c, cudaStreamSynchronize(c->stream), "environment CDF");
     c->envWidth = W;
     c->envHeight = H;
@@ -543,6 +557,9 @@ int32_t vkrt_cuda_upload_rgb2spec(VKRT_CudaContext* c, const float* table, uint3
     VKRT_TRY(c, c->rgb2spec.assign(table, floatCount, c->stream), "upload rgb2spec");
     c->rgb2specFloats = floatCount;
     c->rgb2specInfo = *info;
+    VKRT_TRY(c, c->rgb2specCells.reserve(size_t(3) * info->res * info->res * info->res), "rgb2spec cells");
+    VKRT_TRY(c, launchRepackRgb2Spec(c->rgb2spec.ptr, info->res, info->dataOffset, c->rgb2specCells.ptr, c->stream),
+             "rgb2spec cells");
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -555,6 +572,8 @@ int32_t vkrt_cuda_generate_rgb2spec(VKRT_CudaContext* c, uint32_t res, VKRT_Cuda
     VKRT_TRY(c, launchGenerateRgb2Spec(res, c->rgb2spec.ptr, c->stream), "rgb2spec fit");
     c->rgb2specFloats = floats;
     c->rgb2specInfo = VKRT_CudaRGB2SpecTableInfo{res, 0u, res};
+    VKRT_TRY(c, c->rgb2specCells.reserve(size_t(3) * res * res * res), "rgb2spec cells");
+    VKRT_TRY(c, launchRepackRgb2Spec(c->rgb2spec.ptr, res, res, c->rgb2specCells.ptr, c->stream), "rgb2spec cells");
     if (outInfo) *outInfo = c->rgb2specInfo;
     return VKRT_CUDA_SUCCESS;
 }
@@ -626,7 +645,7 @@ void vkrt_cuda_default_wavefront_config(VKRT_CudaWavefrontConfig* w) {
     w->queueCapacity = 0u;
     w->tileWidth = 16u;
     w->tileHeight = 8u;
-    w->sortByMaterial = 0u;
+    w->sortByMaterial = 2u;
     w->intersectBlocksPerSM = 8u;
     w->shadeBlocksPerSM = 4u;
     w->useGraph = 1u;
@@ -640,6 +659,8 @@ int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* c, const VKRT_CudaWavef
         w->shadeBlocksPerSM > 16u)
         return invalid(c, "blocks per SM must be in [1, 16]");
     if (w->queueCapacity > (1u << 26)) return invalid(c, "queue capacity above 64M path slots");
+    if (w->profileStages > 1u) return invalid(c, "profileStages is 0 or 1");
+    if (w->sortByMaterial > 2u) return invalid(c, "sortByMaterial is 0, 1 or 2");
     c->wfCfg = *w;
     return VKRT_CUDA_SUCCESS;
 }
@@ -758,7 +779,7 @@ int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_C
                 cands.push_back(w);
             }
         if (axis == 2)
-            for (uint32_t s = 0; s < 2; ++s) {
+            for (uint32_t s = 0; s < 3; ++s) {
                 VKRT_CudaWavefrontConfig w = cur;
                 w.sortByMaterial = s;
                 cands.push_back(w);
@@ -770,7 +791,7 @@ int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_C
                 cands.push_back(w);
             }
         if (axis == 4)
-            for (uint32_t b : {2u, 3u, 4u}) {
+            for (uint32_t b : {3u, 4u, 6u, 8u}) {  // 6 and 8 select the 80- and 64-register shading kernels
                 VKRT_CudaWavefrontConfig w = cur;
                 w.shadeBlocksPerSM = b;
                 cands.push_back(w);
@@ -999,6 +1020,9 @@ int32_t vkrt_cuda_read_output(VKRT_CudaContext* c, uint16_t* rgba, size_t bytes)
     return VKRT_CUDA_SUCCESS;
 }
 
+static_assert(sizeof(VKRT_CudaStats) == 136, "VKRT_CudaStats layout");
+static_assert(sizeof(VKRT_CudaWavefrontConfig) == 64, "VKRT_CudaWavefrontConfig layout");
+
 int32_t vkrt_cuda_get_stats(VKRT_CudaContext* c, VKRT_CudaStats* st) {
     if (!c || !st) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     cudaSetDevice(c->device);
@@ -1016,6 +1040,14 @@ int32_t vkrt_cuda_get_stats(VKRT_CudaContext* c, VKRT_CudaStats* st) {
     st->nodeFetchBytes = c->lastCounters.nodeBytes;
     st->triFetchBytes = c->lastCounters.triBytes;
     st->errorFlags = c->lastCounters.errorFlags;
+    st->wavefrontBodies = c->lastCounters.wfBodies;
+    st->shadowNodeFetchBytes = c->lastCounters.shadowNodeBytes;
+    st->shadowTriFetchBytes = c->lastCounters.shadowTriBytes;
+    st->kernelLaunches = c->lastCounters.kernelLaunches;
+    if (c->wavefront) {
+        const float* ms = c->wavefront->lastStageMs();
+        for (int i = 0; i < 8; ++i) st->stageMs[i] = ms[i];
+    }
     st->bvhNodeCount = c->bvh.nodeCount;
     st->bvhTriangleCount = c->bvh.triCount;
     st->bvhBytes = uint64_t(c->bvh.nodeCount) * sizeof(WideNode) + uint64_t(c->bvh.triCount) * sizeof(TriRecord);

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
             const uint32_t spp = max(sd.samplesPerPixel, 1u);
             StepConfig cfg{kSpectral, sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u, rp.envNee != 0u, rp.rngMode,
                            rp.rngSeed};
-            SpecTable tab{sc.rgb2spec, sd.rgb2specSRGB.res, sd.rgb2specSRGB.scaleOffset, sd.rgb2specSRGB.dataOffset};
+            SpecTable tab = makeSpecTable(sc, sd);
             float3 sum = f3(0.0f);
             for (uint32_t si = 0; si < spp; ++si) {
                 PathState p = beginPath<kSpectral>(cfg, sd, px, py, prevN + si);
@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
             film.output[pixel] = encodeOutput(sd, acc, kSpectral);
         }
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && counters) atomicAdd(&counters->kernelLaunches, 1ull);
     // warp-aggregated ray counters
     for (int off = 16; off > 0; off >>= 1) {
         pc.primary += __shfl_xor_sync(0xFFFFFFFFu, pc.primary, off);
@@ -207,6 +208,28 @@ __global__ void kEnvMarginal(const double* rowSum, uint32_t H, float* marginal, 
     }
     marginal[H] = 1.0f;
     totalOut[0] = total;
+}
+
+// guide entry k of each CDF = search result for u = k / kEnvGuide (row H = the marginal)
+__global__ void kEnvGuides(const float* marginal, const float* conditional, uint32_t W, uint32_t H,
+                           uint32_t* marginalGuide, uint32_t* conditionalGuide) {
+    const uint32_t G1 = kEnvGuide + 1u;
+    const uint32_t total = (H + 1u) * G1;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        uint32_t row = t / G1, k = t % G1;
+        float u = float(k) / float(kEnvGuide);
+        if (row == H) marginalGuide[k] = cdfFind(marginal, H, u);
+        else conditionalGuide[size_t(row) * G1 + k] = cdfFind(conditional + size_t(row) * (W + 1u), W, u);
+    }
+}
+
+// the selected rgb2spec table repacked one float4 per cell
+__global__ void kRepackRgb2Spec(const float* table, uint32_t res, uint32_t dataOffset, float4* cells) {
+    const uint32_t n = 3u * res * res * res;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* c = table + dataOffset + size_t(i) * 3u;
+        cells[i] = make_float4(c[0], c[1], c[2], 0.0f);
+    }
 }
 
 __global__ void kEnvTexelPdf(const double* f, uint32_t W, uint32_t H, const double* total, float* pdf) {
@@ -370,6 +393,21 @@ cudaError_t launchBuildEnvDistribution(const float4* texels, uint32_t W, uint32_
     kEnvRows<<<H, 1024, 0, stream>>>(f, W, conditional, rowSum);
     kEnvMarginal<<<1, 32, 0, stream>>>(rowSum, H, marginal, total);
     kEnvTexelPdf<<<uint32_t((n + 255) / 256), 256, 0, stream>>>(f, W, H, total, texelPdf);
+    return cudaGetLastError();
+}
+
+cudaError_t launchBuildEnvGuides(const float* marginal, const float* conditional, uint32_t W, uint32_t H,
+                                 uint32_t* marginalGuide, uint32_t* conditionalGuide, cudaStream_t stream) {
+    const uint32_t total = (H + 1u) * (kEnvGuide + 1u);
+    kEnvGuides<<<(total + 255u) / 256u, 256, 0, stream>>>(marginal, conditional, W, H, marginalGuide,
+                                                          conditionalGuide);
+    return cudaGetLastError();
+}
+
+cudaError_t launchRepackRgb2Spec(const float* table, uint32_t res, uint32_t dataOffset, float4* cells,
+                                 cudaStream_t stream) {
+    const uint32_t n = 3u * res * res * res;
+    kRepackRgb2Spec<<<(n + 255u) / 256u, 256, 0, stream>>>(table, res, dataOffset, cells);
     return cudaGetLastError();
 }
 

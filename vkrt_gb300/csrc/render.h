@@ -37,6 +37,14 @@ cudaError_t launchClearFilm(float4* a, float4* b, ushort4* out, size_t pixels, c
 cudaError_t launchBuildEnvDistribution(const float4* texels, uint32_t width, uint32_t height, float* marginal,
                                        float* conditional, float* texelPdf, double* scratch, cudaStream_t stream);
 
+// Guide tables of the environment CDFs (kEnvGuide + 1 entries per CDF; marginal guide, then one per row).
+cudaError_t launchBuildEnvGuides(const float* marginal, const float* conditional, uint32_t width, uint32_t height,
+                                 uint32_t* marginalGuide, uint32_t* conditionalGuide, cudaStream_t stream);
+
+// rgb2spec coefficients starting at dataOffset repacked to 3*res^3 float4 cells.
+cudaError_t launchRepackRgb2Spec(const float* table, uint32_t res, uint32_t dataOffset, float4* cells,
+                                 cudaStream_t stream);
+
 // rgb2spec table fit on the device; `table` holds res + 3*res^3*3 floats.
 cudaError_t launchGenerateRgb2Spec(uint32_t res, float* table, cudaStream_t stream);
 

@@ -40,6 +40,10 @@ struct EnvDistribution {
     const float* marginal;     // H + 1
     const float* conditional;  // H * (W + 1)
     const float* texelPdf;     // W * H, pdf over the unit square
+    // guide tables (cutpoint method): entry k of a CDF's guide is the search result for u = k / kEnvGuide, so a
+    // search for u in [k, k + 1) / kEnvGuide only scans between two neighbouring entries
+    const uint32_t* marginalGuide;     // kEnvGuide + 1
+    const uint32_t* conditionalGuide;  // H * (kEnvGuide + 1)
     uint32_t width, height;
     uint32_t textureIndex;     // texture the distribution was built from (VKRT_CUDA_INVALID_INDEX = none)
 };
@@ -67,6 +71,9 @@ struct DeviceScene {
     const TextureDesc* textures;  // VKRT_CUDA_MAX_TEXTURES entries
     const float* rgb2spec;
     uint32_t rgb2specFloatCount;
+    // the table selected by rgb2specCellsInfo repacked one float4 (3 coefficients) per cell: [3][res][res][res]
+    const float4* rgb2specCells;
+    VKRT_CudaRGB2SpecTableInfo rgb2specCellsInfo;
     EnvDistribution env;
 };
 
@@ -75,12 +82,17 @@ struct RenderCounters {
     unsigned long long extensionRays;
     unsigned long long shadowRays;
     unsigned long long pathSamples;
-    unsigned long long nodeBytes;
+    unsigned long long nodeBytes;        // closest-hit traversal: node / triangle bytes fetched (counting kernels)
     unsigned long long triBytes;
+    unsigned long long shadowNodeBytes;  // any-hit traversal
+    unsigned long long shadowTriBytes;
+    unsigned long long kernelLaunches;   // launches of this backend's kernels since the counters were cleared
+    unsigned int wfBodies;               // wavefront loop bodies executed (two iterations each)
     unsigned int errorFlags;
     unsigned int workCursor;  // persistent-kernel pixel cursor
 };
 
 constexpr uint32_t kErrorStackOverflow = 1u;
+constexpr uint32_t kEnvGuide = 256u;
 
 }  // namespace vkrt

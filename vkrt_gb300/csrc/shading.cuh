@@ -188,8 +188,18 @@ VKRT_DEV float4 sampleMaterialTexture(const DeviceScene& sc, uint32_t idx, uint3
 struct SpecTable {
     const float* t;
     uint32_t res, scaleOffset, dataOffset;
+    const float4* cells;  // the same coefficients one float4 per cell, or null
 };
 
+// the frame's table (SceneData.rgb2specSRGB) with its repacked cells when the context holds them for that layout
+VKRT_DEV SpecTable makeSpecTable(const DeviceScene& sc, const VKRT_CudaSceneData& sd) {
+    const VKRT_CudaRGB2SpecTableInfo& i = sd.rgb2specSRGB;
+    bool packed = sc.rgb2specCells && sc.rgb2specCellsInfo.res == i.res &&
+                  sc.rgb2specCellsInfo.scaleOffset == i.scaleOffset && sc.rgb2specCellsInfo.dataOffset == i.dataOffset;
+    return SpecTable{sc.rgb2spec, i.res, i.scaleOffset, i.dataOffset, packed ? sc.rgb2specCells : nullptr};
+}
+
+// Largest i in [0, res - 2] with scale[i] <= x (utility/rgb2spec.slang:14-32).
 VKRT_DEV uint32_t rgb2specInterval(const SpecTable& tab, float x) {
     int left = 0, size = int(tab.res) - 2;
     while (size > 0) {
@@ -221,6 +231,20 @@ VKRT_DEV float3 rgb2specFetch(const SpecTable& tab, float3 rgb) {
     float x1 = x - float(xi), y1 = y - float(yi), x0 = 1.0f - x1, y0 = 1.0f - y1;
     float s0 = __ldg(tab.t + tab.scaleOffset + zi), s1 = __ldg(tab.t + tab.scaleOffset + zi + 1u);
     float z1 = (z - s0) / fmaxf(s1 - s0, 1e-8f), z0 = 1.0f - z1;
+    if (tab.cells) {  // eight 16-byte cell loads, the same arithmetic as the scalar path below
+        const float4* d = tab.cells + (((dom * tab.res + zi) * tab.res + yi) * tab.res + xi);
+        const uint32_t ry = tab.res, rz = tab.res * tab.res;
+        float4 c000 = __ldg(d), c100 = __ldg(d + 1), c010 = __ldg(d + ry), c110 = __ldg(d + ry + 1);
+        float4 c001 = __ldg(d + rz), c101 = __ldg(d + rz + 1), c011 = __ldg(d + rz + ry), c111 = __ldg(d + rz + ry + 1);
+        float a[3] = {c000.x, c000.y, c000.z}, b[3] = {c100.x, c100.y, c100.z}, c[3] = {c010.x, c010.y, c010.z},
+              e[3] = {c110.x, c110.y, c110.z}, f[3] = {c001.x, c001.y, c001.z}, g[3] = {c101.x, c101.y, c101.z},
+              h[3] = {c011.x, c011.y, c011.z}, k[3] = {c111.x, c111.y, c111.z}, o[3];
+#pragma unroll
+        for (uint32_t j = 0; j < 3; ++j)
+            o[j] = ((a[j] * x0 + b[j] * x1) * y0 + (c[j] * x0 + e[j] * x1) * y1) * z0 +
+                   ((f[j] * x0 + g[j] * x1) * y0 + (h[j] * x0 + k[j] * x1) * y1) * z1;
+        return make_float3(o[0], o[1], o[2]);
+    }
     float out[3];
 #pragma unroll
     for (uint32_t j = 0; j < 3; ++j) {
@@ -685,8 +709,8 @@ VKRT_DEV float envPdf(const EnvDistribution& e, float3 d, float rotDeg) {
     return __ldg(e.texelPdf + size_t(j) * e.width + i) / (2.0f * kPi * kPi * st);
 }
 
-VKRT_DEV uint32_t cdfFind(const float* cdf, uint32_t n, float u) {
-    uint32_t lo = 0, hi = n;
+// Largest index in [0, n) whose CDF entry is <= u (0 when none), searched within [lo, hi)
+VKRT_DEV uint32_t cdfFindRange(const float* cdf, uint32_t lo, uint32_t hi, float u) {
     while (hi - lo > 1u) {
         uint32_t mid = (lo + hi) >> 1;
         if (__ldg(cdf + mid) <= u) lo = mid;
@@ -695,12 +719,22 @@ VKRT_DEV uint32_t cdfFind(const float* cdf, uint32_t n, float u) {
     return lo;
 }
 
+VKRT_DEV uint32_t cdfFind(const float* cdf, uint32_t n, float u) { return cdfFindRange(cdf, 0u, n, u); }
+
+// Same answer through a guide table: the result for u lies between the guide entries of u's bucket
+VKRT_DEV uint32_t cdfFindGuided(const float* cdf, uint32_t n, const uint32_t* guide, float u) {
+    if (!guide || !(u >= 0.0f) || !(u < 1.0f)) return cdfFind(cdf, n, u);
+    uint32_t k = min(uint32_t(u * float(kEnvGuide)), kEnvGuide - 1u);
+    return cdfFindRange(cdf, __ldg(guide + k), min(__ldg(guide + k + 1u) + 1u, n), u);
+}
+
 VKRT_DEV bool envSample(const EnvDistribution& e, float u1, float u2, float rotDeg, float3& dir, float& pdf) {
-    uint32_t j = cdfFind(e.marginal, e.height, u1);
+    uint32_t j = cdfFindGuided(e.marginal, e.height, e.marginalGuide, u1);
     float m0 = __ldg(e.marginal + j), m1 = __ldg(e.marginal + j + 1);
     float dv = (u1 - m0) / fmaxf(m1 - m0, 1e-20f);
     const float* c = e.conditional + size_t(j) * (e.width + 1);
-    uint32_t i = cdfFind(c, e.width, u2);
+    uint32_t i = cdfFindGuided(c, e.width,
+                               e.conditionalGuide ? e.conditionalGuide + size_t(j) * (kEnvGuide + 1u) : nullptr, u2);
     float c0 = __ldg(c + i), c1 = __ldg(c + i + 1);
     float du = (u2 - c0) / fmaxf(c1 - c0, 1e-20f);
     float u = (float(i) + sat(du)) / float(e.width);

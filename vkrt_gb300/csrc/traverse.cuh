@@ -298,8 +298,8 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
         }
     }
     if (kCount && counters) {
-        atomicAdd(&counters->nodeBytes, (unsigned long long)nodeBytes);
-        atomicAdd(&counters->triBytes, (unsigned long long)triBytes);
+        atomicAdd(kAnyHit ? &counters->shadowNodeBytes : &counters->nodeBytes, (unsigned long long)nodeBytes);
+        atomicAdd(kAnyHit ? &counters->shadowTriBytes : &counters->triBytes, (unsigned long long)triBytes);
     }
     if (overflow) {
         best.mesh = VKRT_CUDA_INVALID_INDEX;
@@ -323,6 +323,7 @@ struct TravState {
     uint2 nodeGroup, triGroup;
     TraceHit best;
     bool overflow;
+    uint32_t nodeVisits, triTests;  // counted when the caller asks (persistentTrace<..., kCount = true>)
 };
 
 VKRT_DEV void travBegin(TravState& s, const WideNode* nodes, const TriRecord* tris, uint32_t nodeCount,
@@ -342,6 +343,7 @@ VKRT_DEV void travBegin(TravState& s, const WideNode* nodes, const TriRecord* tr
     s.best.gid = 0xFFFFFFFFu;
     s.best.t = s.best.u = s.best.v = 0.0f;
     s.overflow = false;
+    s.nodeVisits = s.triTests = 0u;
     s.triGroup = make_uint2(0u, 0u);
     s.nodeGroup = nodeCount ? make_uint2(0u, 0x80000000u | (1u << (7u ^ s.octInv))) : make_uint2(0u, 0u);
     stack.sp = 0;
@@ -349,7 +351,7 @@ VKRT_DEV void travBegin(TravState& s, const WideNode* nodes, const TriRecord* tr
 
 // One traversal step: a node visit with the triangle tests it exposes, or a popped triangle group. Returns true when
 // the ray is finished; its answer is then in s.best (a miss after a stack overflow, flagged in errorFlags).
-template <bool kAnyHit>
+template <bool kAnyHit, bool kCount = false>
 VKRT_DEV bool travStep(TravState& s, TraversalStack& stack, unsigned int* errorFlags) {
     if (s.nodeGroup.y > 0x00FFFFFFu) {
         uint32_t hits = s.nodeGroup.y;
@@ -366,6 +368,7 @@ VKRT_DEV bool travStep(TravState& s, TraversalStack& stack, unsigned int* errorF
         }
         uint32_t cbase, tbase, imask;
         uint32_t hm = intersectWideNode(s.nodes, child, s.org, s.idir, s.octInv4, s.tmin, s.tmax, cbase, tbase, imask);
+        if (kCount) s.nodeVisits++;
         s.nodeGroup.x = cbase;
         s.nodeGroup.y = (hm & 0xFF000000u) | imask;
         s.triGroup.x = tbase;
@@ -380,6 +383,7 @@ VKRT_DEV bool travStep(TravState& s, TraversalStack& stack, unsigned int* errorF
         s.triGroup.y &= ~(1u << tbit);
         const float4* tp = reinterpret_cast<const float4*>(s.tris + s.triGroup.x + tbit);
         float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (kCount) s.triTests++;
         float t, b1, b2;
         if (watertightHit(s.wr, s.org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
                           make_float3(c.x, c.y, c.z), s.tmin, s.tmax, t, b1, b2)) {
@@ -406,10 +410,12 @@ VKRT_DEV bool travStep(TravState& s, TraversalStack& stack, unsigned int* errorF
 // Persistent traversal of rays 0..n-1 by whole warps (Aila & Laine 2009, "while-while" with dynamic fetch): idle lanes
 // take the next rays from `fetch` (one atomic per warp), and the warp steps its rays in lock-step until fewer than
 // kRefill lanes remain busy, then refills. Every lane of the warp must call this with the same n and fetch.
-// load(i, ray, nodes, tris, nodeCount) describes ray i; store(i, hit) receives its answer.
-template <bool kAnyHit, int kRefill, class Load, class Store>
+// load(i, ray, nodes, tris, nodeCount) describes ray i; store(i, hit) receives its answer. With kCount the node
+// visits and triangle tests of this lane's rays are added to nodeVisits / triTests.
+template <bool kAnyHit, int kRefill, bool kCount, class Load, class Store>
 VKRT_DEV void persistentTrace(uint32_t n, uint32_t* fetch, uint2* smemColumn, uint32_t smemStride,
-                              unsigned int* errorFlags, Load load, Store store) {
+                              unsigned int* errorFlags, Load load, Store store, uint32_t& nodeVisits,
+                              uint32_t& triTests) {
     TraversalStack stack;
     stack.smem = smemColumn;
     stack.stride = smemStride;
@@ -449,12 +455,146 @@ VKRT_DEV void persistentTrace(uint32_t n, uint32_t* fetch, uint2* smemColumn, ui
         }
         const int minBusy = exhausted ? 1 : kRefill;
         for (;;) {
-            if (busy && travStep<kAnyHit>(s, stack, errorFlags)) {
+            if (busy && travStep<kAnyHit, kCount>(s, stack, errorFlags)) {
                 store(mine, s.best);
+                if (kCount) {
+                    nodeVisits += s.nodeVisits;
+                    triTests += s.triTests;
+                }
                 busy = false;
             }
             if (__popc(__ballot_sync(0xFFFFFFFFu, busy)) < minBusy) break;
         }
+    }
+}
+
+// Node visit of the vote-scheduled traversal: takes the nearest remaining child of the lane's node group, pushes the
+// rest, intersects the child's eight boxes; a new triangle group replaces the pending one, which is pushed.
+template <bool kCount>
+VKRT_DEV void voteNodeVisit(TravState& s, TraversalStack& stack, unsigned int* errorFlags) {
+    uint32_t hits = s.nodeGroup.y;
+    uint32_t bit = 31u - __clz(hits);
+    uint32_t slot = (bit - 24u) ^ s.octInv;
+    uint32_t rel = __popc((hits & 0xFFu) & ((1u << slot) - 1u));
+    uint32_t child = s.nodeGroup.x + rel;
+    s.nodeGroup.y &= ~(1u << bit);
+    if (s.nodeGroup.y > 0x00FFFFFFu) stack.push(s.nodeGroup, errorFlags, s.overflow);
+    uint32_t cbase, tbase, imask;
+    uint32_t hm = intersectWideNode(s.nodes, child, s.org, s.idir, s.octInv4, s.tmin, s.tmax, cbase, tbase, imask);
+    if (kCount) s.nodeVisits++;
+    s.nodeGroup = make_uint2(cbase, (hm & 0xFF000000u) | imask);
+    uint32_t tri = hm & 0x00FFFFFFu;
+    if (tri) {
+        if (s.triGroup.y) stack.push(s.triGroup, errorFlags, s.overflow);
+        s.triGroup = make_uint2(tbase, tri);
+    }
+}
+
+// One triangle of the lane's pending group; true when an any-hit query is answered.
+template <bool kAnyHit, bool kCount>
+VKRT_DEV bool voteTriangleTest(TravState& s) {
+    uint32_t tbit = 31u - __clz(s.triGroup.y);
+    s.triGroup.y &= ~(1u << tbit);
+    const float4* tp = reinterpret_cast<const float4*>(s.tris + s.triGroup.x + tbit);
+    float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    if (kCount) s.triTests++;
+    float t, b1, b2;
+    if (watertightHit(s.wr, s.org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z),
+                      s.tmin, s.tmax, t, b1, b2)) {
+        uint32_t gid = __float_as_uint(a.w);
+        if (t < s.tmax || gid < s.best.gid) {
+            s.tmax = t;
+            s.best.t = t;
+            s.best.u = b1;
+            s.best.v = b2;
+            s.best.gid = gid;
+            s.best.mesh = __float_as_uint(b.w);
+            s.best.prim = __float_as_uint(c.w);
+            if (kAnyHit) return true;
+        }
+    }
+    return false;
+}
+
+// Persistent traversal with dynamic fetch and a warp vote per step: every step the warp runs one kind of work only,
+// a node visit on the lanes that hold a node group or one triangle test on the lanes that hold triangles, whichever
+// more lanes want (triangles on ties), so node and triangle code never diverge within a step. Lanes with neither
+// pop their stack or finish; the warp refills once fewer than kRefill lanes are busy. Same tests and tie rule as
+// traceBvh: closest hits are identical.
+template <bool kAnyHit, int kRefill, bool kCount, class Load, class Store>
+VKRT_DEV void persistentTraceVote(uint32_t n, uint32_t* fetch, uint2* smemColumn, uint32_t smemStride,
+                                  unsigned int* errorFlags, Load load, Store store, uint32_t& nodeVisits,
+                                  uint32_t& triTests) {
+    TraversalStack stack;
+    stack.smem = smemColumn;
+    stack.stride = smemStride;
+    stack.sp = 0;
+    TravState s;
+    bool busy = false;
+    bool exhausted = false;  // warp-uniform
+    uint32_t mine = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    auto finish = [&](bool miss) {
+        if (miss) {
+            s.best.mesh = VKRT_CUDA_INVALID_INDEX;
+            s.best.prim = VKRT_CUDA_INVALID_INDEX;
+        }
+        store(mine, s.best);
+        if (kCount) {
+            nodeVisits += s.nodeVisits;
+            triTests += s.triTests;
+        }
+        busy = false;
+    };
+    for (;;) {
+        if (!exhausted) {
+            unsigned idle = __ballot_sync(0xFFFFFFFFu, !busy);
+            if (idle) {
+                uint32_t base = 0;
+                if (lane == 0u) base = atomicAdd(fetch, uint32_t(__popc(idle)));
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (base + uint32_t(__popc(idle)) >= n) exhausted = true;
+                if (!busy) {
+                    uint32_t i = base + uint32_t(__popc(idle & ((1u << lane) - 1u)));
+                    if (i < n) {
+                        TraceRay r;
+                        const WideNode* nodes;
+                        const TriRecord* tris;
+                        uint32_t nodeCount;
+                        load(i, r, nodes, tris, nodeCount);
+                        travBegin(s, nodes, tris, nodeCount, r, stack);
+                        mine = i;
+                        busy = true;
+                    }
+                }
+            }
+        }
+        const int minBusy = exhausted ? 1 : kRefill;
+        for (;;) {
+            // lanes without pending work take the next stack entry or finish their ray
+            if (busy && s.nodeGroup.y <= 0x00FFFFFFu && s.triGroup.y == 0u) {
+                if (stack.sp > 0) {
+                    uint2 e = stack.pop();
+                    if (e.y > 0x00FFFFFFu) s.nodeGroup = e;
+                    else s.triGroup = e;
+                } else {
+                    finish(false);
+                }
+            }
+            const unsigned busyMask = __ballot_sync(0xFFFFFFFFu, busy);
+            if (__popc(busyMask) < minBusy) break;
+            const bool wantNode = busy && s.nodeGroup.y > 0x00FFFFFFu;
+            const bool wantTri = busy && s.triGroup.y != 0u;
+            const int nNode = __popc(__ballot_sync(0xFFFFFFFFu, wantNode));
+            const int nTri = __popc(__ballot_sync(0xFFFFFFFFu, wantTri));
+            if (nTri >= nNode) {
+                if (wantTri && voteTriangleTest<kAnyHit, kCount>(s)) finish(false);
+            } else if (wantNode) {
+                voteNodeVisit<kCount>(s, stack, errorFlags);
+                if (s.overflow) finish(true);
+            }
+        }
+        if (exhausted && !__any_sync(0xFFFFFFFFu, busy)) break;
     }
 }
 

@@ -7,7 +7,8 @@
 //   while (paths remain)             one conditional-while CUDA graph node, two ping-pong iterations per body:
 //     begin                          reset the output queues (and the material histogram)
 //     intersect                      closest hit of every queued path; material key + histogram when sorting
-//     sort (optional)                counting sort of the queue by (scene, material)
+//     sort (optional)                counting sort of the queue by (scene, material); or, in class mode, the
+//                                    intersect kernel itself files each path under miss / dielectric / metal
 //     shade                          pending shadow results applied, vertex shaded, shadow requests queued,
 //                                    continuing paths queued, finished ones handed to finalize
 //     shadow                         any-hit rays; visible requests flagged on their slot
@@ -45,8 +46,13 @@ enum : uint32_t {
     kCntIteration = 5,
     kCntFetchIntersect = 6,
     kCntFetchShadow = 7,
+    kCntClass0 = 8,  // class-partitioned shade queue: misses, dielectric hits, metal hits
 };
+constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
+#ifndef VKRT_PERSISTENT_TRACE
+#define VKRT_PERSISTENT_TRACE persistentTraceVote
+#endif
 
 struct WfGlobals {
     uint32_t mode;  // WavefrontMode
@@ -82,11 +88,14 @@ struct WfGlobals {
     uint32_t* queue1;
     uint32_t* finished;
     uint32_t* sorted;
+    uint32_t* classQueue;  // 3 * Q: the shade queue partitioned by class (kSortClass)
     float4* shadowA;  // origin, tmax
     float4* shadowB;  // direction, slot | request << 31
     uint32_t* keyHist;
     uint32_t* counts;
     RenderCounters* counters;
+    uint32_t launchesOutsideLoop;  // setup/clear/init/resolve kernels of one render call
+    uint32_t launchesPerBody;      // stage kernels of two iterations plus the condition kernel
     cudaGraphConditionalHandle cond;
     // adjoint pass (one scene): parameters and, per slot, the pending vertex's gradient factors
     AdjointParams adj;
@@ -180,7 +189,7 @@ VKRT_DEV StepConfig stepConfig(const WfGlobals& g, const WfScene& S) {
 }
 
 VKRT_DEV SpecTable specTable(const WfScene& S) {
-    return SpecTable{S.sc.rgb2spec, S.sd.rgb2specSRGB.res, S.sd.rgb2specSRGB.scaleOffset, S.sd.rgb2specSRGB.dataOffset};
+    return makeSpecTable(S.sc, S.sd);
 }
 
 // starts sample `sample` of the slot's pixel; returns false for a padding work item
@@ -234,8 +243,11 @@ VKRT_DEV bool acquireItem(const WfGlobals& g, uint32_t slot, uint32_t w) {
 }
 
 __global__ void kWfSetup(WfGlobals g) {
-    if (threadIdx.x < 8u) g.counts[threadIdx.x] = 0u;
-    if (threadIdx.x == 0u) g.counts[kCntCursor] = min(g.Q, g.totalItems);
+    if (threadIdx.x < 16u) g.counts[threadIdx.x] = 0u;
+    if (threadIdx.x == 0u) {
+        g.counts[kCntCursor] = min(g.Q, g.totalItems);
+        atomicAdd(&g.counters->kernelLaunches, (unsigned long long)g.launchesOutsideLoop);
+    }
 }
 
 template <bool kSpectral>
@@ -291,18 +303,32 @@ __global__ void kWfBegin(WfGlobals g, uint32_t outQueue) {
         g.counts[kCntFinished] = 0u;
         g.counts[kCntFetchIntersect] = 0u;
         g.counts[kCntFetchShadow] = 0u;
+        g.counts[kCntClass0] = g.counts[kCntClass0 + 1] = g.counts[kCntClass0 + 2] = 0u;
     }
-    if (g.sort)
+    if (g.sort == kSortMaterial)
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < g.keyCount; k += gridDim.x * blockDim.x)
             g.keyHist[k] = 0u;
 }
 
-__global__ void __launch_bounds__(kWfThreads) kWfIntersect(WfGlobals g, uint32_t inQueue) {
+// node (80 B) and triangle (48 B) fetch bytes of a warp's traversals, for the profiling frames
+VKRT_DEV void warpCountBytes(unsigned long long* nodeBytes, unsigned long long* triBytes, uint32_t nodes,
+                             uint32_t tris) {
+    __syncwarp();
+    uint32_t n = __reduce_add_sync(0xFFFFFFFFu, nodes), t = __reduce_add_sync(0xFFFFFFFFu, tris);
+    if ((threadIdx.x & 31u) == 0u) {
+        if (n) atomicAdd(nodeBytes, 80ull * n);
+        if (t) atomicAdd(triBytes, 48ull * t);
+    }
+}
+
+// kMinBlocks: resident blocks per SM the register allocation must allow (the launch grid's blocks per SM)
+template <bool kCount, int kMinBlocks>
+__global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals g, uint32_t inQueue) {
     extern __shared__ uint2 smemStack[];
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
-    uint32_t primary = 0, ext = 0;
-    persistentTrace<false, kRefillLanes>(
+    uint32_t primary = 0, ext = 0, nodeVisits = 0, triTests = 0;
+    VKRT_PERSISTENT_TRACE<false, kRefillLanes, kCount>(
         n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             uint32_t slot = q[i];
@@ -319,17 +345,34 @@ __global__ void __launch_bounds__(kWfThreads) kWfIntersect(WfGlobals g, uint32_t
             uint32_t slot = q[i];
             g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
             g.hitV[slot] = h.v;
-            if (g.sort) {
+            if (g.sort == kSortMaterial) {
                 const WfScene& S = g.scenes[g.slotScene[slot]];
                 uint32_t key = h.mesh == VKRT_CUDA_INVALID_INDEX
                                    ? 0u
                                    : 1u + S.materialKeyBase + S.sc.meshes[h.mesh].materialIndex;
                 g.hitKey[i] = key;
                 atomicAdd(&g.keyHist[key], 1u);
+            } else if (g.sort == kSortClass) {
+                // miss / dielectric / metal, filed with one atomic per class and group of converged lanes
+                uint32_t c = 0u;
+                if (h.mesh != VKRT_CUDA_INVALID_INDEX) {
+                    const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+                    c = sc.materials[sc.meshes[h.mesh].materialIndex].metallic >= 0.5f ? 2u : 1u;
+                }
+                const unsigned active = __activemask();
+                const unsigned same = __match_any_sync(active, c);
+                const uint32_t lane = threadIdx.x & 31u;
+                const int leader = __ffs(same) - 1;
+                uint32_t base = 0u;
+                if (lane == uint32_t(leader)) base = atomicAdd(&g.counts[kCntClass0 + c], uint32_t(__popc(same)));
+                base = __shfl_sync(same, base, leader);
+                g.classQueue[size_t(c) * g.Q + base + __popc(same & ((1u << lane) - 1u))] = slot;
             }
-        });
+        },
+        nodeVisits, triTests);
     warpCount(&g.counters->primaryRays, primary);
     warpCount(&g.counters->extensionRays, ext);
+    if (kCount) warpCountBytes(&g.counters->nodeBytes, &g.counters->triBytes, nodeVisits, triTests);
 }
 
 __global__ void __launch_bounds__(1024) kWfSortScan(WfGlobals g) {
@@ -441,8 +484,8 @@ VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t sl
                  xyz(g.adjTotal[slot]), xyz(radiance));
 }
 
-template <bool kSpectral, bool kAdjoint>
-__global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
+template <bool kSpectral, bool kAdjoint, int kMinBlocks>
+__global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
     MaterialGradient* smemMat = nullptr;
     if constexpr (kAdjoint) {
         __shared__ MaterialGradient smemMatStorage[kSmemMaterials];
@@ -451,9 +494,10 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQ
         clearMaterialSmem(smemMat, mc);
         __syncthreads();
     }
-    const uint32_t* q = g.sort ? g.sorted : (inQueue == 0 ? g.queue0 : g.queue1);
+    const uint32_t* q = g.sort == kSortMaterial ? g.sorted : (inQueue == 0 ? g.queue0 : g.queue1);
     uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
+    const uint32_t nMiss = g.counts[kCntClass0], nDiel = g.counts[kCntClass0 + 1];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t i = base + threadIdx.x;
         bool valid = i < n;
@@ -461,7 +505,12 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQ
         uint32_t slot = 0, ns = 0;
         ShadowRequest sh[2];
         if (valid) {
-            slot = q[i];
+            if (g.sort == kSortClass)  // the three class queues read as one
+                slot = i < nMiss ? g.classQueue[i]
+                                 : (i < nMiss + nDiel ? g.classQueue[g.Q + (i - nMiss)]
+                                                      : g.classQueue[2u * size_t(g.Q) + (i - nMiss - nDiel)]);
+            else
+                slot = q[i];
             const WfScene& S = g.scenes[g.slotScene[slot]];
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
@@ -515,11 +564,12 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(WfGlobals g, uint32_t inQ
     }
 }
 
-__global__ void __launch_bounds__(kWfThreads) kWfShadow(WfGlobals g) {
+template <bool kCount, int kMinBlocks>
+__global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g) {
     extern __shared__ uint2 smemStack[];
     const uint32_t n = g.counts[kCntShadow];
-    uint32_t traced = 0;
-    persistentTrace<true, kRefillLanes>(
+    uint32_t traced = 0, nodeVisits = 0, triTests = 0;
+    VKRT_PERSISTENT_TRACE<true, kRefillLanes, kCount>(
         n, &g.counts[kCntFetchShadow], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             float4 a = g.shadowA[i], b = g.shadowB[i];
@@ -535,8 +585,10 @@ __global__ void __launch_bounds__(kWfThreads) kWfShadow(WfGlobals g) {
             if (h.mesh != VKRT_CUDA_INVALID_INDEX) return;
             uint32_t tag = __float_as_uint(g.shadowB[i].w);
             atomicOr(&g.pendFlags[tag & 0x7FFFFFFFu], 4u << (tag >> 31));
-        });
+        },
+        nodeVisits, triTests);
     warpCount(&g.counters->shadowRays, traced);
+    if (kCount) warpCountBytes(&g.counters->shadowNodeBytes, &g.counters->shadowTriBytes, nodeVisits, triTests);
 }
 
 template <bool kSpectral, bool kAdjoint>
@@ -589,6 +641,8 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
 __global__ void kWfCondition(WfGlobals g, uint32_t useGraph) {
     uint32_t it = g.counts[kCntIteration] + 1u;
     g.counts[kCntIteration] = it;
+    g.counters->wfBodies = it;
+    g.counters->kernelLaunches += g.launchesPerBody;
     bool more = g.counts[kCntActive0] > 0u;
     if (more && it >= g.maxIter) {
         g.counters->errorFlags |= 2u;  // iteration bound reached with work left (never expected)
@@ -628,11 +682,15 @@ struct WavefrontEngine::Buffers {
     size_t capQ = 0, capKeys = 0, capScenes = 0;
     size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
            c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
-           c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0;
+           c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0;
     size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
     WfScene* scenes = nullptr;
     WfGraphCache graphs[3];
+    float stageMs[kStageCount] = {};
+    uint32_t* hostCount = nullptr;  // pinned word the stage-by-stage loop polls
 };
+
+const float* WavefrontEngine::lastStageMs() const { return b_->stageMs; }
 
 WavefrontEngine::WavefrontEngine() : b_(new Buffers()) {}
 
@@ -652,10 +710,12 @@ void WavefrontEngine::release() {
     WfGlobals& g = b_->g;
     void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotItem, g.sampleBuf,
                     g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
-                    g.sorted, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, g.adjDelta, g.adjTotal,
+                    g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, g.adjDelta,
+                    g.adjTotal,
                     g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (b_->hostCount) cudaFreeHost(b_->hostCount);
     Buffers* fresh = new Buffers();
     std::swap(*b_, *fresh);
     delete fresh;
@@ -692,7 +752,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     }
     if (items >= 0xFFFFFFF0ull) return cudaErrorInvalidValue;  // item indices are 32-bit
     const uint32_t totalItems = uint32_t(items);
-    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, 1u << 21);
+    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, 1u << 22);
     Q = std::max(1u, std::min(Q, std::max(totalItems, 1u)));
     // until the item cursor runs out every slot is busy, so the bounces of all items bound the iteration count;
     // the condition kernel counts two-iteration bodies
@@ -723,6 +783,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(queue1, c_q1, Q);
     WF_GROW(finished, c_fin, Q);
     WF_GROW(sorted, c_sorted, Q);
+    if (cfg.sortByMaterial == kSortClass) WF_GROW(classQueue, c_class, 3 * size_t(Q));
     WF_GROW(shadowA, c_sA, 2 * size_t(Q));
     WF_GROW(shadowB, c_sB, 2 * size_t(Q));
     WF_GROW(keyHist, c_hist, keys);
@@ -752,50 +813,92 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.totalItems = totalItems;
     g.Q = Q;
     g.maxIter = maxIter;
-    g.sort = cfg.sortByMaterial ? 1u : 0u;
+    g.sort = cfg.sortByMaterial <= kSortClass ? cfg.sortByMaterial : kSortMaterial;
     g.keyCount = keys;
     g.rngMode = rngMode;
     g.rngSeed = rngSeed;
     g.counters = counters;
+    g.launchesOutsideLoop = 2u + (mode == kWavefrontForward ? 2u : 0u);
+    g.launchesPerBody = 2u * (5u + (g.sort == kSortMaterial ? 2u : 0u)) + 1u;
+    const bool profile = cfg.profileStages != 0u;
+    if (profile) cfg.useGraph = 0u;
+    for (float& t : B.stageMs) t = 0.0f;
+    // profiling: an event pair around every stage launch, summed per stage after the frame
+    std::vector<std::pair<uint32_t, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    auto stage = [&](uint32_t st, auto&& launch) {
+        if (!profile) {
+            launch();
+            return;
+        }
+        cudaEvent_t a = nullptr, b = nullptr;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, stream);
+        launch();
+        cudaEventRecord(b, stream);
+        marks.push_back({st, {a, b}});
+    };
 
     const uint32_t gridI = uint32_t(sms) * std::max(1u, cfg.intersectBlocksPerSM);
     const uint32_t gridS = uint32_t(sms) * std::max(1u, cfg.shadeBlocksPerSM);
+    const uint32_t shadeMin = cfg.shadeBlocksPerSM;
     const size_t smem = size_t(kWfThreads) * VKRT_SMEM_STACK * sizeof(uint2);
 
     auto body = [&](uint32_t in, uint32_t out, bool useGraph) {
-        kWfBegin<<<4, 1024, 0, stream>>>(g, out);
-        kWfIntersect<<<gridI, kWfThreads, smem, stream>>>(g, in);
-        if (g.sort) {
-            kWfSortScan<<<1, 1024, 0, stream>>>(g);
-            kWfSortScatter<<<gridS, 256, 0, stream>>>(g, in);
+        stage(kStageBegin, [&] { kWfBegin<<<4, 1024, 0, stream>>>(g, out); });
+        stage(kStageIntersect, [&] {
+            if (profile) kWfIntersect<true, 8><<<gridI, kWfThreads, smem, stream>>>(g, in);
+            else kWfIntersect<false, 8><<<gridI, kWfThreads, smem, stream>>>(g, in);
+        });
+        if (g.sort == kSortMaterial) {
+            stage(kStageSort, [&] {
+                kWfSortScan<<<1, 1024, 0, stream>>>(g);
+                kWfSortScatter<<<gridS, 256, 0, stream>>>(g, in);
+            });
         }
-        if (adjMode) kWfShade<false, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-        else if (spectral) kWfShade<true, false><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-        else kWfShade<false, false><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-        kWfShadow<<<gridI, kWfThreads, smem, stream>>>(g);
-        if (adjMode) kWfFinalize<false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
-        else if (spectral) kWfFinalize<true, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
-        else kWfFinalize<false, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        stage(kStageShade, [&] {
+            // register budget follows the requested residency: 128 (4 blocks/SM), 80 (6) or 64 (8) registers
+            if (adjMode) kWfShade<false, true, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (spectral && shadeMin >= 8) kWfShade<true, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (spectral && shadeMin >= 6) kWfShade<true, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (spectral) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (shadeMin >= 8) kWfShade<false, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (shadeMin >= 6) kWfShade<false, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else kWfShade<false, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+        });
+        stage(kStageShadow, [&] {
+            if (profile) kWfShadow<true, 8><<<gridI, kWfThreads, smem, stream>>>(g);
+            else kWfShadow<false, 8><<<gridI, kWfThreads, smem, stream>>>(g);
+        });
+        stage(kStageFinalize, [&] {
+            if (adjMode) kWfFinalize<false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
+            else if (spectral) kWfFinalize<true, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
+            else kWfFinalize<false, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
+        });
         (void)useGraph;
     };
     auto resolve = [&]() {  // the film is written by forward frames only
         if (mode != kWavefrontForward) return;
-        if (spectral) kWfResolve<true><<<gridS, 256, 0, stream>>>(g);
-        else kWfResolve<false><<<gridS, 256, 0, stream>>>(g);
+        stage(kStageResolve, [&] {
+            if (spectral) kWfResolve<true><<<gridS, 256, 0, stream>>>(g);
+            else kWfResolve<false><<<gridS, 256, 0, stream>>>(g);
+        });
     };
     auto prologue = [&]() {
-        kWfSetup<<<1, 32, 0, stream>>>(g);
-        dim3 cg(std::max(1, sms), std::min<uint32_t>(g.sceneCount, 64u));
-        if (mode == kWavefrontForward) kWfClearOutside<<<cg, 256, 0, stream>>>(g);
-        if (spectral) kWfInit<true><<<gridS, kWfThreads, 0, stream>>>(g);
-        else kWfInit<false><<<gridS, kWfThreads, 0, stream>>>(g);
+        stage(kStagePrologue, [&] {
+            kWfSetup<<<1, 32, 0, stream>>>(g);
+            dim3 cg(std::max(1, sms), std::min<uint32_t>(g.sceneCount, 64u));
+            if (mode == kWavefrontForward) kWfClearOutside<<<cg, 256, 0, stream>>>(g);
+            if (spectral) kWfInit<true><<<gridS, kWfThreads, 0, stream>>>(g);
+            else kWfInit<false><<<gridS, kWfThreads, 0, stream>>>(g);
+        });
     };
 
     if (!cfg.useGraph) {
         prologue();
-        uint32_t* hostCount = nullptr;
-        e = cudaMallocHost(&hostCount, sizeof(uint32_t));
+        if (!B.hostCount) e = cudaMallocHost(&B.hostCount, sizeof(uint32_t));
         if (e != cudaSuccess) return e;
+        uint32_t* hostCount = B.hostCount;
         for (uint32_t bodyIndex = 0; bodyIndex < maxIter; ++bodyIndex) {
             body(0, 1, false);
             body(1, 0, false);
@@ -808,8 +911,17 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             }
         }
         resolve();
-        cudaFreeHost(hostCount);
         if (e == cudaSuccess) e = cudaGetLastError();
+        if (profile) {
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            for (auto& m : marks) {
+                float ms = 0.0f;
+                if (e == cudaSuccess && cudaEventElapsedTime(&ms, m.second.first, m.second.second) == cudaSuccess)
+                    B.stageMs[m.first] += ms;
+                cudaEventDestroy(m.second.first);
+                cudaEventDestroy(m.second.second);
+            }
+        }
         return e;
     }
 

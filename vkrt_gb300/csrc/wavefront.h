@@ -34,13 +34,20 @@ struct WfScene {
 enum WavefrontMode : uint32_t { kWavefrontForward = 0, kWavefrontPrimal = 1, kWavefrontAdjoint = 2 };
 
 struct WavefrontConfig {
-    uint32_t queueCapacity;  // path slots; 0 = one per work item, capped at 4M
+    uint32_t queueCapacity;  // path slots; 0 = one per (pixel, sample) item, capped at 4M
     uint32_t tileWidth;
     uint32_t tileHeight;
     uint32_t sortByMaterial;
     uint32_t intersectBlocksPerSM;
     uint32_t shadeBlocksPerSM;
     uint32_t useGraph;
+    uint32_t profileStages;  // 1: no graph; traversal kernels count fetch bytes; per-stage device times recorded
+};
+
+// stages of the per-stage device times
+enum WavefrontStage : uint32_t {
+    kStagePrologue = 0, kStageBegin, kStageIntersect, kStageSort, kStageShade, kStageShadow, kStageFinalize,
+    kStageResolve, kStageCount
 };
 
 class WavefrontEngine {
@@ -57,6 +64,8 @@ public:
                        uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters, cudaStream_t stream,
                        WavefrontMode mode = kWavefrontForward, const AdjointParams* adjoint = nullptr);
     void release();
+    // per-stage device milliseconds of the last render call made with profileStages (zeros otherwise)
+    const float* lastStageMs() const;
 
 private:
     struct Buffers;
