@@ -309,9 +309,9 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
 }
 
 // ---------------------------------------------------------------------------------------------------------------
-// Resumable traversal for persistent kernels with dynamic ray fetch (Aila & Laine 2009): a lane advances its ray one
-// step at a time, and lanes whose ray finished fetch a new one while the others keep traversing, so the warp stays
-// full on incoherent rays. Same node/triangle tests and tie rule as traceBvh, so closest hits are identical.
+// Resumable traversal state for persistent kernels with dynamic ray fetch (Aila & Laine 2009): a lane advances its
+// ray one step at a time, and lanes whose ray finished fetch a new one while the others keep traversing, so the warp
+// stays full on incoherent rays.
 // ---------------------------------------------------------------------------------------------------------------
 struct TravState {
     const WideNode* nodes;
@@ -323,7 +323,7 @@ struct TravState {
     uint2 nodeGroup, triGroup;
     TraceHit best;
     bool overflow;
-    uint32_t nodeVisits, triTests;  // counted when the caller asks (persistentTrace<..., kCount = true>)
+    uint32_t nodeVisits, triTests;  // counted when the caller asks (persistentTraceVote<..., kCount = true>)
 };
 
 VKRT_DEV void travBegin(TravState& s, const WideNode* nodes, const TriRecord* tris, uint32_t nodeCount,
@@ -347,125 +347,6 @@ VKRT_DEV void travBegin(TravState& s, const WideNode* nodes, const TriRecord* tr
     s.triGroup = make_uint2(0u, 0u);
     s.nodeGroup = nodeCount ? make_uint2(0u, 0x80000000u | (1u << (7u ^ s.octInv))) : make_uint2(0u, 0u);
     stack.sp = 0;
-}
-
-// One traversal step: a node visit with the triangle tests it exposes, or a popped triangle group. Returns true when
-// the ray is finished; its answer is then in s.best (a miss after a stack overflow, flagged in errorFlags).
-template <bool kAnyHit, bool kCount = false>
-VKRT_DEV bool travStep(TravState& s, TraversalStack& stack, unsigned int* errorFlags) {
-    if (s.nodeGroup.y > 0x00FFFFFFu) {
-        uint32_t hits = s.nodeGroup.y;
-        uint32_t bit = 31u - __clz(hits);
-        uint32_t slot = (bit - 24u) ^ s.octInv;
-        uint32_t rel = __popc((hits & 0xFFu) & ((1u << slot) - 1u));
-        uint32_t child = s.nodeGroup.x + rel;
-        s.nodeGroup.y &= ~(1u << bit);
-        if (s.nodeGroup.y > 0x00FFFFFFu) stack.push(s.nodeGroup, errorFlags, s.overflow);
-        if (s.overflow) {
-            s.best.mesh = VKRT_CUDA_INVALID_INDEX;
-            s.best.prim = VKRT_CUDA_INVALID_INDEX;
-            return true;
-        }
-        uint32_t cbase, tbase, imask;
-        uint32_t hm = intersectWideNode(s.nodes, child, s.org, s.idir, s.octInv4, s.tmin, s.tmax, cbase, tbase, imask);
-        if (kCount) s.nodeVisits++;
-        s.nodeGroup.x = cbase;
-        s.nodeGroup.y = (hm & 0xFF000000u) | imask;
-        s.triGroup.x = tbase;
-        s.triGroup.y = hm & 0x00FFFFFFu;
-    } else {
-        s.triGroup = s.nodeGroup;
-        s.triGroup.y &= 0x00FFFFFFu;
-        s.nodeGroup = make_uint2(0u, 0u);
-    }
-    while (s.triGroup.y != 0u) {
-        uint32_t tbit = 31u - __clz(s.triGroup.y);
-        s.triGroup.y &= ~(1u << tbit);
-        const float4* tp = reinterpret_cast<const float4*>(s.tris + s.triGroup.x + tbit);
-        float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
-        if (kCount) s.triTests++;
-        float t, b1, b2;
-        if (watertightHit(s.wr, s.org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
-                          make_float3(c.x, c.y, c.z), s.tmin, s.tmax, t, b1, b2)) {
-            uint32_t gid = __float_as_uint(a.w);
-            if (t < s.tmax || gid < s.best.gid) {
-                s.tmax = t;
-                s.best.t = t;
-                s.best.u = b1;
-                s.best.v = b2;
-                s.best.gid = gid;
-                s.best.mesh = __float_as_uint(b.w);
-                s.best.prim = __float_as_uint(c.w);
-                if (kAnyHit) return true;
-            }
-        }
-    }
-    if (s.nodeGroup.y <= 0x00FFFFFFu) {
-        if (stack.sp == 0) return true;
-        s.nodeGroup = stack.pop();
-    }
-    return false;
-}
-
-// Persistent traversal of rays 0..n-1 by whole warps (Aila & Laine 2009, "while-while" with dynamic fetch): idle lanes
-// take the next rays from `fetch` (one atomic per warp), and the warp steps its rays in lock-step until fewer than
-// kRefill lanes remain busy, then refills. Every lane of the warp must call this with the same n and fetch.
-// load(i, ray, nodes, tris, nodeCount) describes ray i; store(i, hit) receives its answer. With kCount the node
-// visits and triangle tests of this lane's rays are added to nodeVisits / triTests.
-template <bool kAnyHit, int kRefill, bool kCount, class Load, class Store>
-VKRT_DEV void persistentTrace(uint32_t n, uint32_t* fetch, uint2* smemColumn, uint32_t smemStride,
-                              unsigned int* errorFlags, Load load, Store store, uint32_t& nodeVisits,
-                              uint32_t& triTests) {
-    TraversalStack stack;
-    stack.smem = smemColumn;
-    stack.stride = smemStride;
-    stack.sp = 0;
-    TravState s;
-    bool busy = false;
-    bool exhausted = false;  // warp-uniform
-    uint32_t mine = 0;
-    const uint32_t lane = threadIdx.x & 31u;
-    for (;;) {
-        if (!exhausted) {
-            unsigned idle = __ballot_sync(0xFFFFFFFFu, !busy);
-            if (idle) {
-                uint32_t base = 0;
-                if (lane == 0u) base = atomicAdd(fetch, uint32_t(__popc(idle)));
-                base = __shfl_sync(0xFFFFFFFFu, base, 0);
-                if (base + uint32_t(__popc(idle)) >= n) exhausted = true;
-                if (!busy) {
-                    uint32_t i = base + uint32_t(__popc(idle & ((1u << lane) - 1u)));
-                    if (i < n) {
-                        TraceRay r;
-                        const WideNode* nodes;
-                        const TriRecord* tris;
-                        uint32_t nodeCount;
-                        load(i, r, nodes, tris, nodeCount);
-                        travBegin(s, nodes, tris, nodeCount, r, stack);
-                        mine = i;
-                        busy = true;
-                    }
-                }
-            }
-        }
-        unsigned busyMask = __ballot_sync(0xFFFFFFFFu, busy);
-        if (!busyMask) {
-            if (exhausted) break;
-            continue;
-        }
-        const int minBusy = exhausted ? 1 : kRefill;
-        for (;;) {
-            if (busy && travStep<kAnyHit, kCount>(s, stack, errorFlags)) {
-                store(mine, s.best);
-                if (kCount) {
-                    nodeVisits += s.nodeVisits;
-                    triTests += s.triTests;
-                }
-                busy = false;
-            }
-            if (__popc(__ballot_sync(0xFFFFFFFFu, busy)) < minBusy) break;
-        }
-    }
 }
 
 // Node visit of the vote-scheduled traversal: takes the nearest remaining child of the lane's node group, pushes the

@@ -50,9 +50,7 @@ enum : uint32_t {
 };
 constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
-#ifndef VKRT_PERSISTENT_TRACE
-#define VKRT_PERSISTENT_TRACE persistentTraceVote
-#endif
+
 
 struct WfGlobals {
     uint32_t mode;  // WavefrontMode
@@ -328,7 +326,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
     uint32_t primary = 0, ext = 0, nodeVisits = 0, triTests = 0;
-    VKRT_PERSISTENT_TRACE<false, kRefillLanes, kCount>(
+    persistentTraceVote<false, kRefillLanes, kCount>(
         n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             uint32_t slot = q[i];
@@ -569,7 +567,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g)
     extern __shared__ uint2 smemStack[];
     const uint32_t n = g.counts[kCntShadow];
     uint32_t traced = 0, nodeVisits = 0, triTests = 0;
-    VKRT_PERSISTENT_TRACE<true, kRefillLanes, kCount>(
+    persistentTraceVote<true, kRefillLanes, kCount>(
         n, &g.counts[kCntFetchShadow], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             float4 a = g.shadowA[i], b = g.shadowB[i];
