@@ -16,6 +16,8 @@ roofline : the closest-hit traversal kernel (kWfIntersect) of one profiling fram
 megakernel : the same frame by the one-thread-per-pixel megakernel (vkrt's raygen structure), for comparison.
 adjoint : the path-replay adjoint of the inverse-rendering Cornell box (128 x 128, 16 spp, depth 6, five 64 x 64
         albedo + roughness textures): device time of the adjoint call / device time of the forward frame.
+batch : 64 uneven icosphere fields (10k-500k triangles, 256^2-1024^2, 8 spp, depth 10, RGB) in one autotuned graph
+        launch vs 64 sequential megakernel (and wavefront) frames.
 --impl reference : the CPU restatement of vkrt's integrator (the oracle, a port: vkrt's own renderer needs Vulkan
         and is unavailable here) on all host cores, on a bounded block of rows of the same frame per step.
 """
@@ -200,6 +202,73 @@ def adjoint_ratio(local: int) -> dict:
             "gradients": "albedo texels, roughness texels, emission radiance; FP64 central-difference tests"}
 
 
+def batch_measure(local: int) -> dict:
+    """Uneven batch: 64 seeded icosphere fields (10k-500k triangles, 256^2-1024^2, 8 spp, depth 10, RGB) rendered
+    as one autotuned graph launch, against 64 sequential megakernel frames and 64 sequential wavefront frames."""
+    import torch
+    from vkrt_gb300 import RenderContext, abi, scenes
+    from vkrt_gb300.context import autotune_batch, render_batch
+
+    ss = scenes.batch_workload(64, seed=2)
+    ctxs = []
+    for sc in ss:
+        c = RenderContext(device=local, rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE,
+                          integrator=abi.INTEGRATOR_WAVEFRONT)
+        c.upload_scene(sc)
+        ctxs.append(c)
+    sds = np.concatenate([sc.scene_data for sc in ss])
+    torch.cuda.synchronize()
+
+    def sequential(integrator):
+        ms = rays = 0.0
+        for c, sc in zip(ctxs, ss):
+            c.set_integrator(integrator)
+            st = torch.cuda.ExternalStream(c.stream, device=torch.device("cuda", local))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            c.render_frame(sc.scene_data)
+            b.record(st)
+            b.synchronize()
+            ms += a.elapsed_time(b)
+            rays += _rays(c.stats())
+        for c in ctxs:
+            c.set_integrator(abi.INTEGRATOR_WAVEFRONT)
+        return ms, rays
+
+    sequential(abi.INTEGRATOR_WAVEFRONT)  # warm-up: graphs, buffers
+    t0 = time.perf_counter()
+    best, tuned_ms = autotune_batch(ctxs, sds, frames_per_trial=1)
+    tune_s = time.perf_counter() - t0
+    stream0 = torch.cuda.ExternalStream(ctxs[0].stream, device=torch.device("cuda", local))
+    render_batch(ctxs, sds)  # warm-up of the tuned shape
+    torch.cuda.synchronize()
+    bms = []
+    for _ in range(2):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream0)
+        render_batch(ctxs, sds)
+        b.record(stream0)
+        b.synchronize()
+        bms.append(a.elapsed_time(b))
+    brays = _rays(ctxs[0].stats())
+    mega_ms, mega_rays = sequential(abi.INTEGRATOR_MEGAKERNEL)
+    wave_ms, wave_rays = sequential(abi.INTEGRATOR_WAVEFRONT)
+    for c in ctxs:
+        c.close()
+    batched = float(min(bms))
+    return {"workload": "64 icosphere fields, 10k-500k triangles (log-uniform), 256^2-1024^2, 8 spp, depth 10, RGB",
+            "triangles": int(sum(sc.triangle_count for sc in ss)), "pixels": int(sum(sc.width * sc.height for sc in ss)),
+            "batched_ms": round(batched, 2), "batched_Mrays_s": round(brays / (batched * 1e-3) / 1e6, 1),
+            "sequential_megakernel_ms": round(mega_ms, 2),
+            "sequential_megakernel_Mrays_s": round(mega_rays / (mega_ms * 1e-3) / 1e6, 1),
+            "sequential_wavefront_ms": round(wave_ms, 2),
+            "speedup_vs_sequential_megakernel": round(mega_ms / batched, 2),
+            "speedup_vs_sequential_wavefront": round(wave_ms / batched, 2),
+            "autotune_s": round(tune_s, 1),
+            "autotuned": {k: int(best[k][0]) for k in ("queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
+                                                       "intersectBlocksPerSM", "shadeBlocksPerSM")}}
+
+
 def run_ours(args) -> dict | None:
     import torch
     from vkrt_gb300 import RenderContext, abi
@@ -328,6 +397,8 @@ def run_ours(args) -> dict | None:
     }
     if rank == 0 and world == 1 and not args.no_adjoint:
         result["adjoint"] = adjoint_ratio(local)
+    if rank == 0 and world == 1 and not args.no_batch:
+        result["batch"] = batch_measure(local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(scene, budget_s=args.cpu_seconds)
     ctx.close()
@@ -396,6 +467,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--stage-launches", action="store_true",
                     help="launch the wavefront stages one by one instead of as one CUDA graph (ncu cannot profile "
                          "kernel nodes of graphs with conditional nodes)")

@@ -168,6 +168,9 @@ int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* context);
  * src/core/api/frame.c:267-337,380-390). Asynchronous on the context stream; SceneData is copied at call time. */
 int32_t vkrt_cuda_render_frame(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData);
 
+/* Selects the integrator of later render calls (VKRT_CUDA_INTEGRATOR_*); images are the same either way. */
+int32_t vkrt_cuda_set_integrator(VKRT_CudaContext* context, uint32_t integrator);
+
 void vkrt_cuda_default_wavefront_config(VKRT_CudaWavefrontConfig* config);
 int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* context, const VKRT_CudaWavefrontConfig* config);
 int32_t vkrt_cuda_get_wavefront_config(VKRT_CudaContext* context, VKRT_CudaWavefrontConfig* config);

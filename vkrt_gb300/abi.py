@@ -164,6 +164,7 @@ EXPORTS = {
     "vkrt_cuda_trace_rays_device": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_trace_rays_noalloc": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_last_error": (C.c_char_p, [_V]),
+    "vkrt_cuda_set_integrator": (_I32, [_V, _U32]),
     "vkrt_cuda_default_wavefront_config": (None, [_V]),
     "vkrt_cuda_set_wavefront_config": (_I32, [_V, _V]),
     "vkrt_cuda_get_wavefront_config": (_I32, [_V, _V]),

@@ -208,6 +208,9 @@ class RenderContext:
         return table, info
 
     # -- wavefront integrator --------------------------------------------------------------------------------
+    def set_integrator(self, integrator: int) -> None:
+        self._check(self.lib.vkrt_cuda_set_integrator(self.handle, integrator), "set integrator")
+
     def wavefront_config(self) -> np.ndarray:
         w = np.zeros(1, dtype=abi.WAVEFRONT_CONFIG)
         self._check(self.lib.vkrt_cuda_get_wavefront_config(self.handle, abi.ptr(w)), "get wavefront config")

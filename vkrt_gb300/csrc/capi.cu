@@ -639,6 +639,13 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     return VKRT_CUDA_SUCCESS;
 }
 
+int32_t vkrt_cuda_set_integrator(VKRT_CudaContext* c, uint32_t integrator) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (integrator > VKRT_CUDA_INTEGRATOR_WAVEFRONT) return invalid(c, "unknown integrator");
+    c->cfg.integrator = integrator;
+    return VKRT_CUDA_SUCCESS;
+}
+
 void vkrt_cuda_default_wavefront_config(VKRT_CudaWavefrontConfig* w) {
     if (!w) return;
     std::memset(w, 0, sizeof(*w));

@@ -7,8 +7,9 @@
 //   while (paths remain)             one conditional-while CUDA graph node, two ping-pong iterations per body:
 //     begin                          reset the output queues (and the material histogram)
 //     intersect                      closest hit of every queued path; material key + histogram when sorting
-//     sort (optional)                counting sort of the queue by (scene, material); or, in class mode, the
-//                                    intersect kernel itself files each path under miss / dielectric / metal
+//     sort (optional)                counting sort of the queue by (scene, class) with class = miss /
+//                                    dielectric / metal; or, in class mode, the intersect kernel itself files
+//                                    each path under its class (no scene grouping, no extra kernels)
 //     shade                          pending shadow results applied, vertex shaded, shadow requests queued,
 //                                    continuing paths queued, finished ones handed to finalize
 //     shadow                         any-hit rays; visible requests flagged on their slot
@@ -48,13 +49,15 @@ enum : uint32_t {
     kCntFetchShadow = 7,
     kCntClass0 = 8,  // class-partitioned shade queue: misses, dielectric hits, metal hits
 };
-constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;
+constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;  // kSortMaterial sorts by (scene, class)
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
 
 
 struct WfGlobals {
     uint32_t mode;  // WavefrontMode
     const WfScene* scenes;
+    const uint32_t* itemBases;  // scenes[i].itemBase, contiguous for the item -> scene search
+    const uint32_t* workBases;  // scenes[i].workBase
     uint32_t sceneCount;
     uint32_t totalWork;   // padded pixels of all scenes
     uint32_t totalItems;  // (pixel, sample) items of all scenes
@@ -132,10 +135,29 @@ VKRT_DEV uint32_t sceneOfWork(const WfGlobals& g, uint32_t w) {
     uint32_t lo = 0, hi = g.sceneCount;
     while (hi - lo > 1u) {
         uint32_t mid = (lo + hi) >> 1;
-        if (g.scenes[mid].workBase <= w) lo = mid;
+        if (__ldg(g.workBases + mid) <= w) lo = mid;
         else hi = mid;
     }
     return lo;
+}
+
+// Position among the converged lanes that hold the same key, with one atomic per distinct key: counters[key] is
+// advanced by the number of such lanes.
+VKRT_DEV uint32_t warpAggregatedSlot(uint32_t* counters, uint32_t key) {
+    const unsigned active = __activemask();
+    const unsigned same = __match_any_sync(active, key);
+    const uint32_t lane = threadIdx.x & 31u;
+    const int leader = __ffs(same) - 1;
+    uint32_t base = 0u;
+    if (lane == uint32_t(leader)) base = atomicAdd(counters + key, uint32_t(__popc(same)));
+    base = __shfl_sync(same, base, leader);
+    return base + __popc(same & ((1u << lane) - 1u));
+}
+
+// miss / dielectric / metal
+VKRT_DEV uint32_t hitClass(const DeviceScene& sc, const TraceHit& h) {
+    if (h.mesh == VKRT_CUDA_INVALID_INDEX) return 0u;
+    return sc.materials[sc.meshes[h.mesh].materialIndex].metallic >= 0.5f ? 2u : 1u;
 }
 
 // tile-ordered work item -> viewport pixel; false for padding items outside the viewport
@@ -192,8 +214,9 @@ VKRT_DEV SpecTable specTable(const WfScene& S) {
 
 // starts sample `sample` of the slot's pixel; returns false for a padding work item
 template <bool kSpectral>
-VKRT_DEV bool startSample(const WfGlobals& g, uint32_t slot, uint32_t sceneId, uint32_t work, uint32_t sample) {
-    const WfScene& S = g.scenes[sceneId];
+VKRT_DEV bool startSample(const WfGlobals& g, const WfScene* scenes, uint32_t slot, uint32_t sceneId, uint32_t work,
+                          uint32_t sample) {
+    const WfScene& S = scenes[sceneId];
     int px, py;
     if (!workPixel(S, work, px, py)) return false;
     uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
@@ -215,7 +238,7 @@ VKRT_DEV uint32_t sceneOfItem(const WfGlobals& g, uint32_t w) {
     uint32_t lo = 0, hi = g.sceneCount;
     while (hi - lo > 1u) {
         uint32_t mid = (lo + hi) >> 1;
-        if (g.scenes[mid].itemBase <= w) lo = mid;
+        if (__ldg(g.itemBases + mid) <= w) lo = mid;
         else hi = mid;
     }
     return lo;
@@ -224,13 +247,13 @@ VKRT_DEV uint32_t sceneOfItem(const WfGlobals& g, uint32_t w) {
 // Takes (pixel, sample) items from the cursor, starting with `w`, until one lies inside a viewport; false when the
 // batch is exhausted. Items of one pixel are consecutive (item = pixel work index * spp + sample).
 template <bool kSpectral>
-VKRT_DEV bool acquireItem(const WfGlobals& g, uint32_t slot, uint32_t w) {
+VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t slot, uint32_t w) {
     for (;;) {
         if (w >= g.totalItems) return false;
         uint32_t sceneId = sceneOfItem(g, w);
-        const WfScene& S = g.scenes[sceneId];
+        const WfScene& S = scenes[sceneId];
         uint32_t local = w - S.itemBase;
-        if (startSample<kSpectral>(g, slot, sceneId, local / S.spp, local % S.spp)) {
+        if (startSample<kSpectral>(g, scenes, slot, sceneId, local / S.spp, local % S.spp)) {
             g.slotScene[slot] = sceneId;
             g.slotItem[slot] = local;
             if (g.mode == kWavefrontAdjoint) g.adjTotal[slot] = g.sampleBuf[size_t(S.itemBase) + local];
@@ -250,8 +273,9 @@ __global__ void kWfSetup(WfGlobals g) {
 
 template <bool kSpectral>
 __global__ void __launch_bounds__(kWfThreads) kWfInit(WfGlobals g) {
+    const WfScene* scenes = g.scenes;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < g.Q; s += gridDim.x * blockDim.x) {
-        bool ok = acquireItem<kSpectral>(g, s, s < g.totalItems ? s : g.totalItems);
+        bool ok = acquireItem<kSpectral>(g, scenes, s, s < g.totalItems ? s : g.totalItems);
         uint32_t pos = warpPush(&g.counts[kCntActive0], ok);
         if (ok) g.queue0[pos] = s;
     }
@@ -261,8 +285,9 @@ __global__ void __launch_bounds__(kWfThreads) kWfInit(WfGlobals g) {
 // into the running mean (writeback.slang:72-114) and encoded for display.
 template <bool kSpectral>
 __global__ void kWfResolve(WfGlobals g) {
+    const WfScene* scenes = g.scenes;
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < g.totalWork; w += gridDim.x * blockDim.x) {
-        const WfScene& S = g.scenes[sceneOfWork(g, w)];
+        const WfScene& S = scenes[sceneOfWork(g, w)];
         uint32_t local = w - S.workBase;
         int px, py;
         if (!workPixel(S, local, px, py)) continue;
@@ -343,28 +368,15 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
             uint32_t slot = q[i];
             g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
             g.hitV[slot] = h.v;
-            if (g.sort == kSortMaterial) {
-                const WfScene& S = g.scenes[g.slotScene[slot]];
-                uint32_t key = h.mesh == VKRT_CUDA_INVALID_INDEX
-                                   ? 0u
-                                   : 1u + S.materialKeyBase + S.sc.meshes[h.mesh].materialIndex;
+            if (g.sort == kSortMaterial) {  // histogram of (scene, class) keys for the counting sort
+                const uint32_t sceneId = g.slotScene[slot];
+                const uint32_t key = 3u * sceneId + hitClass(g.scenes[sceneId].sc, h);
                 g.hitKey[i] = key;
-                atomicAdd(&g.keyHist[key], 1u);
-            } else if (g.sort == kSortClass) {
-                // miss / dielectric / metal, filed with one atomic per class and group of converged lanes
-                uint32_t c = 0u;
-                if (h.mesh != VKRT_CUDA_INVALID_INDEX) {
-                    const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
-                    c = sc.materials[sc.meshes[h.mesh].materialIndex].metallic >= 0.5f ? 2u : 1u;
-                }
-                const unsigned active = __activemask();
-                const unsigned same = __match_any_sync(active, c);
-                const uint32_t lane = threadIdx.x & 31u;
-                const int leader = __ffs(same) - 1;
-                uint32_t base = 0u;
-                if (lane == uint32_t(leader)) base = atomicAdd(&g.counts[kCntClass0 + c], uint32_t(__popc(same)));
-                base = __shfl_sync(same, base, leader);
-                g.classQueue[size_t(c) * g.Q + base + __popc(same & ((1u << lane) - 1u))] = slot;
+                warpAggregatedSlot(g.keyHist, key);
+            } else if (g.sort == kSortClass) {  // filed straight into the class queues
+                const uint32_t c = hitClass(g.scenes[g.slotScene[slot]].sc, h);
+                const uint32_t pos = warpAggregatedSlot(&g.counts[kCntClass0], c);
+                g.classQueue[size_t(c) * g.Q + pos] = slot;
             }
         },
         nodeVisits, triTests);
@@ -410,7 +422,7 @@ __global__ void kWfSortScatter(WfGlobals g, uint32_t inQueue) {
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t pos = atomicAdd(&g.keyHist[g.hitKey[i]], 1u);
+        uint32_t pos = warpAggregatedSlot(g.keyHist, g.hitKey[i]);
         g.sorted[pos] = q[i];
     }
 }
@@ -484,10 +496,11 @@ VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t sl
 
 template <bool kSpectral, bool kAdjoint, int kMinBlocks>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
+    const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
     if constexpr (kAdjoint) {
         __shared__ MaterialGradient smemMatStorage[kSmemMaterials];
-        const uint32_t mc = g.scenes[0].sc.materialCount;
+        const uint32_t mc = scenes[0].sc.materialCount;
         smemMat = mc <= kSmemMaterials ? smemMatStorage : nullptr;
         clearMaterialSmem(smemMat, mc);
         __syncthreads();
@@ -509,7 +522,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                                                       : g.classQueue[2u * size_t(g.Q) + (i - nMiss - nDiel)]);
             else
                 slot = q[i];
-            const WfScene& S = g.scenes[g.slotScene[slot]];
+            const WfScene& S = scenes[g.slotScene[slot]];
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
             applyPending(g, slot, p.radiance);
@@ -558,7 +571,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
     }
     if constexpr (kAdjoint) {
         __syncthreads();
-        flushMaterialSmem(g.adj, smemMat, g.scenes[0].sc.materialCount);
+        flushMaterialSmem(g.adj, smemMat, scenes[0].sc.materialCount);
     }
 }
 
@@ -591,10 +604,11 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g)
 
 template <bool kSpectral, bool kAdjoint>
 __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t outQueue) {
+    const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
     if constexpr (kAdjoint) {
         __shared__ MaterialGradient smemMatStorage[kSmemMaterials];
-        const uint32_t mc = g.scenes[0].sc.materialCount;
+        const uint32_t mc = scenes[0].sc.materialCount;
         smemMat = mc <= kSmemMaterials ? smemMatStorage : nullptr;
         clearMaterialSmem(smemMat, mc);
         __syncthreads();
@@ -609,7 +623,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
         if (valid) {
             slot = g.finished[i];
             uint32_t sceneId = g.slotScene[slot];
-            const WfScene& S = g.scenes[sceneId];
+            const WfScene& S = scenes[sceneId];
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
             applyPending(g, slot, p.radiance);
@@ -623,7 +637,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             }
             samples = 1;
             uint32_t w = atomicAdd(&g.counts[kCntCursor], 1u);
-            requeue = acquireItem<kSpectral>(g, slot, w);
+            requeue = acquireItem<kSpectral>(g, scenes, slot, w);
         }
         __syncwarp();
         uint32_t pos = warpPush(&g.counts[outQueue], valid && requeue);
@@ -632,7 +646,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
     }
     if constexpr (kAdjoint) {
         __syncthreads();
-        flushMaterialSmem(g.adj, smemMat, g.scenes[0].sc.materialCount);
+        flushMaterialSmem(g.adj, smemMat, scenes[0].sc.materialCount);
     }
 }
 
@@ -683,6 +697,8 @@ struct WavefrontEngine::Buffers {
            c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0;
     size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
     WfScene* scenes = nullptr;
+    uint32_t* bases = nullptr;  // itemBase of every scene, then workBase
+    size_t c_bases = 0;
     WfGraphCache graphs[3];
     float stageMs[kStageCount] = {};
     uint32_t* hostCount = nullptr;  // pinned word the stage-by-stage loop polls
@@ -708,7 +724,8 @@ void WavefrontEngine::release() {
     WfGlobals& g = b_->g;
     void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotItem, g.sampleBuf,
                     g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
-                    g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, g.adjDelta,
+                    g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, b_->bases,
+                    g.adjDelta,
                     g.adjTotal,
                     g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR};
     for (void* p : ptrs)
@@ -731,7 +748,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (sms <= 0) sms = 1;
     std::vector<WfScene> scenes = scenesIn;
-    uint32_t total = 0, keys = 1, maxSpp = 1, maxDepth = 1;
+    uint32_t total = 0, maxSpp = 1, maxDepth = 1;
+    const uint32_t keys = 3u * uint32_t(scenesIn.size());  // (scene, class) sort keys
     uint64_t items = 0;
     for (WfScene& S : scenes) {
         S.tileW = std::max(1u, cfg.tileWidth);
@@ -743,8 +761,6 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         total += S.workCount;
         S.itemBase = uint32_t(items);
         items += uint64_t(S.workCount) * S.spp;
-        S.materialKeyBase = keys - 1u;
-        keys += S.sc.materialCount;
         maxSpp = std::max(maxSpp, S.spp);
         maxDepth = std::max(maxDepth, S.sd.rrMaxDepth);
     }
@@ -800,12 +816,25 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     }
 #undef WF_GROW
     if (e == cudaSuccess) e = grow(B.scenes, B.c_sc, scenes.size());
+    if (e == cudaSuccess) e = grow(B.bases, B.c_bases, 2 * scenes.size());
     if (e != cudaSuccess) return e;
     e = cudaMemcpyAsync(B.scenes, scenes.data(), sizeof(WfScene) * scenes.size(), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
+    {
+        std::vector<uint32_t> bases(2 * scenes.size());
+        for (size_t i = 0; i < scenes.size(); ++i) {
+            bases[i] = scenes[i].itemBase;
+            bases[scenes.size() + i] = scenes[i].workBase;
+        }
+        // pageable source: the call returns once the bytes are staged, so the vector may go out of scope
+        e = cudaMemcpyAsync(B.bases, bases.data(), sizeof(uint32_t) * bases.size(), cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess) return e;
+    }
     g.mode = uint32_t(mode);
     g.adj = adjoint ? *adjoint : AdjointParams{};
     g.scenes = B.scenes;
+    g.itemBases = B.bases;
+    g.workBases = B.bases + scenes.size();
     g.sceneCount = uint32_t(scenes.size());
     g.totalWork = total;
     g.totalItems = totalItems;

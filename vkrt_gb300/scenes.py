@@ -201,6 +201,20 @@ def inverse_rendering_cornell(width: int = 128, height: int = 128, spp: int = 16
     return s
 
 
+def batch_workload(count: int = 64, seed: int = 2, spp: int = 8, max_depth: int = 10,
+                   tri_range=(10_000, 500_000), resolutions=(256, 512, 768, 1024)) -> list[Scene]:
+    """Uneven batch: `count` icosphere fields built as icosphere_field with triangle counts log-uniform over
+    tri_range (1,280 triangles per sphere), square resolutions drawn uniformly from `resolutions`, RGB transport."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        tris = math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))
+        res = int(rng.choice(resolutions))
+        out.append(icosphere_field(n_spheres=max(1, int(round(tris / 1280))), width=res, height=res, spp=spp,
+                                   max_depth=max_depth, seed=int(seed * 1000 + k), spectral=False))
+    return out
+
+
 def unit_icosphere(subdivisions: int = 3) -> tuple[np.ndarray, np.ndarray]:
     """Icosahedron refined `subdivisions` times (20 * 4^s triangles); vertices on the unit sphere."""
     t = (1.0 + 5 ** 0.5) / 2.0
