@@ -274,6 +274,47 @@ int32_t vkrt_cuda_read_texture_gradient(VKRT_CudaContext* context, uint32_t text
 int32_t vkrt_cuda_read_material_gradients(VKRT_CudaContext* context, VKRT_CudaMaterialGradient* gradients,
                                           uint32_t count);
 
+/* ---------------------------------------------------------------------------------------------------------------
+ * Neural radiance cache. No counterpart in vkrt: an addition of this backend (wavefront integrator). A multiresolution
+ * hash grid (16 levels x 2 FP16 features, 2^19 entries per level, base resolution 16, growth 1.5) and an MLP of five
+ * hidden ReLU layers of width 64 (FP16 weights, FP32 accumulation on the tensor cores) predict the radiance a surface
+ * vertex scatters toward the previous vertex. With the cache enabled, every wavefront frame first traces
+ * `trainingPaths` full-length paths from random pixels, trains the cache on their per-vertex radiance (relative L2
+ * loss, Adam), then renders with paths that stop at bounce `terminationDepth` and add the cache's prediction.
+ * ------------------------------------------------------------------------------------------------------------- */
+typedef struct VKRT_CudaNrcConfig {
+    uint32_t enabled;          /* 1: cache-terminated render paths and per-frame training (wavefront frames) */
+    uint32_t terminationDepth; /* bounce at which render paths query the cache and stop (default 2) */
+    uint32_t trainingPaths;    /* training paths traced per frame (default 65536) */
+    uint32_t trainingSteps;    /* optimiser steps per frame over the frame's training records (default 4) */
+    float learningRate;        /* Adam step size (default 1e-2; beta1 0.9, beta2 0.99, epsilon 1e-8) */
+    uint32_t seed;             /* parameter initialisation and training-pixel selection */
+    uint32_t reserved[10];
+} VKRT_CudaNrcConfig;
+
+/* cache input record: 16 floats (position xyz + roughness, outgoing direction xyz + metallic, shading normal xyz + 0,
+ * base colour rgb + 0); outputs are 4 floats per input (linear sRGB radiance, unused) */
+#define VKRT_CUDA_NRC_INPUT_FLOATS 16u
+#define VKRT_CUDA_NRC_WEIGHTS 21504u           /* FP16 weights: 5 x (64 x 64) then 16 x 64, [out][in] row-major */
+#define VKRT_CUDA_NRC_TABLE_HALVES 16777216u   /* FP16 hash table: 16 levels x 2^19 entries x 2 features */
+
+void vkrt_cuda_default_nrc_config(VKRT_CudaNrcConfig* config);
+/* (Re)initialises the cache over the bounds of the uploaded geometry and stores the configuration. */
+int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* context, const VKRT_CudaNrcConfig* config);
+/* Predictions for n host input records. Synchronous. */
+int32_t vkrt_cuda_nrc_infer(VKRT_CudaContext* context, const float* inputs, uint32_t n, float* outputs);
+/* One optimiser step on n host records (targets: 4 floats each, rgb used); apply = 0 computes the gradients only.
+ * *loss (may be NULL) receives the step's loss. Synchronous. */
+int32_t vkrt_cuda_nrc_train(VKRT_CudaContext* context, const float* inputs, const float* targets, uint32_t n,
+                            uint32_t apply, float* loss);
+/* Reads (write = 0) or writes (write = 1) the FP16 parameters; table may be NULL. */
+int32_t vkrt_cuda_nrc_parameters(VKRT_CudaContext* context, uint16_t* weights, uint16_t* table, uint32_t write);
+/* FP32 gradients of the last training step (weights: VKRT_CUDA_NRC_WEIGHTS floats; table: NULL or
+ * VKRT_CUDA_NRC_TABLE_HALVES floats). */
+int32_t vkrt_cuda_nrc_gradients(VKRT_CudaContext* context, float* weights, float* table);
+/* Hash-grid placement: scene bounds (3 + 3 floats), per-level resolution and dense flag (16 each). */
+int32_t vkrt_cuda_nrc_grid(VKRT_CudaContext* context, float* lo, float* hi, uint32_t* resolution, uint32_t* dense);
+
 /* Last error message of this context (never NULL). */
 const char* vkrt_cuda_last_error(VKRT_CudaContext* context);
 

@@ -1,0 +1,117 @@
+"""Neural radiance cache kernels (nrc.cu) against the FP64 oracle (oracle/nrc.py): predictions, loss and the gradients
+of the FP16 tensor-core forward/backward with respect to the MLP weights and the hash table, on the same FP16
+parameters. FP16 activations limit agreement to about a percent, which the tolerances state."""
+import numpy as np
+import pytest
+
+from oracle.nrc import Cache
+from vkrt_gb300 import RenderContext, abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _records(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 16), np.float32)
+    x[:, 0:3] = rng.uniform(lo, hi, size=(n, 3))
+    x[:, 3] = rng.uniform(0.05, 1.0, n)
+    d = rng.normal(size=(n, 3))
+    x[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    x[:, 7] = (rng.uniform(size=n) < 0.3).astype(np.float32)
+    nn = rng.normal(size=(n, 3))
+    x[:, 8:11] = nn / np.linalg.norm(nn, axis=1, keepdims=True)
+    x[:, 12:15] = rng.uniform(0.1, 0.9, size=(n, 3))
+    t = rng.uniform(0.0, 2.0, size=(n, 3)).astype(np.float32)
+    return x, t
+
+
+@pytest.fixture(scope="module")
+def cache_ctx(built):
+    s = scenes.icosphere_field(n_spheres=40, width=64, height=64, spp=1, max_depth=4, seed=3, spectral=False,
+                               env_size=(64, 32))
+    ctx = RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT)
+    ctx.upload_scene(s)
+    ctx.nrc_configure(seed=7, learningRate=1e-2)
+    yield ctx
+    ctx.close()
+
+
+def _oracle(ctx):
+    w, tb = ctx.nrc_parameters(read_table=True)
+    lo, hi, res, dense = ctx.nrc_grid()
+    return Cache(w, tb, lo, hi, res, dense), lo, hi
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_cache_inference_matches_fp64(cache_ctx):
+    # perturb the table so hash features are not negligible next to the other inputs
+    w, tb = cache_ctx.nrc_parameters(read_table=True)
+    rng = np.random.default_rng(1)
+    tbf = rng.uniform(-0.5, 0.5, tb.size).astype(np.float16).view(np.uint16)
+    cache_ctx.nrc_parameters(weights=w, table=tbf)
+    oc, lo, hi = _oracle(cache_ctx)
+    x, _ = _records(4099, lo, hi, seed=2)  # not a multiple of the 16-row tiles
+    got = cache_ctx.nrc_infer(x)[:, :3]
+    want, _, _ = oc.forward(x)
+    assert _rel(got, want[:, :3]) < 2e-2
+
+
+def test_cache_gradients_match_fp64(cache_ctx):
+    oc, lo, hi = _oracle(cache_ctx)
+    x, t = _records(3000, lo, hi, seed=3)
+    loss = cache_ctx.nrc_train(x, t, apply=False)
+    gw, gt = cache_ctx.nrc_gradients(table=True)
+    want_loss, _, want_gw, want_gt = oc.loss_and_grads(x, t)
+    assert abs(loss - want_loss) <= 1e-2 * want_loss
+    assert _rel(gw, want_gw) < 3e-2
+    assert float(gw @ want_gw) / (np.linalg.norm(gw) * np.linalg.norm(want_gw)) > 0.999
+    nz = np.abs(want_gt) > 0
+    assert nz.sum() > 1000
+    assert _rel(gt[nz], want_gt[nz]) < 3e-2
+    # entries the oracle leaves untouched only receive zero-weight corners of cells chosen differently in FP32
+    assert np.linalg.norm(gt[~nz]) < 1e-4 * np.linalg.norm(want_gt)
+
+
+def test_cache_training_reduces_loss(cache_ctx):
+    """Adam steps on a fixed smooth target field lower the relative L2 loss."""
+    cache_ctx.nrc_configure(seed=11, learningRate=1e-2)
+    _, lo, hi = _oracle(cache_ctx)
+    x, _ = _records(16384, lo, hi, seed=5)
+    p = (x[:, 0:3] - lo) / (hi - lo)
+    t = np.stack([1.0 + np.sin(3 * p[:, 0]), 0.5 + p[:, 1] ** 2, 0.2 + p[:, 2] * x[:, 4] ** 2], 1).astype(np.float32)
+    first = cache_ctx.nrc_train(x, t)
+    for _ in range(200):
+        last = cache_ctx.nrc_train(x, t)
+    assert last < 0.05 * first
+
+
+def test_cache_lowers_error_at_equal_samples(built):
+    """Cornell box, 1 spp frames: with the trained cache ending render paths at bounce 2, the running image is closer
+    to a 4096-spp reference than the plain tracer's after the same number of samples, and stays unbiased to 1%."""
+    s = scenes.cornell(128, 128, spp=1, max_depth=8)
+    with RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT) as ctx:
+        ctx.upload_scene(s)
+        sd = s.scene_data.copy()
+        sd["samplesPerPixel"] = 64
+        for f in range(64):
+            sd["frameNumber"] = 100000 + f
+            ctx.render_frame(sd)
+        ref = ctx.read_accumulation()[..., :3].copy()
+        sd["samplesPerPixel"] = 1
+
+        def run(**cache):
+            ctx.nrc_configure(**cache)
+            ctx.reset_accumulation()
+            for f in range(64):
+                sd["frameNumber"] = f
+                ctx.render_frame(sd)
+            img = ctx.read_accumulation()[..., :3]
+            return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2))), float(img.mean() / ref.mean())
+
+        plain, _ = run(enabled=0)
+        cached, ratio = run(enabled=1, terminationDepth=2, trainingPaths=65536, trainingSteps=4, seed=3)
+    assert cached < 0.9 * plain
+    assert abs(ratio - 1.0) < 0.01

@@ -103,6 +103,12 @@ MATERIAL_GRADIENT = np.dtype({"names": ["baseColor", "roughness", "emission", "r
 
 GRADIENT_BASE_COLOR, GRADIENT_ROUGHNESS, GRADIENT_EMISSION = 1, 2, 4
 
+NRC_CONFIG = np.dtype({"names": ["enabled", "terminationDepth", "trainingPaths", "trainingSteps", "learningRate", "seed",
+                                 "reserved"],
+                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", ("<u4", 10)],
+                       "offsets": [0, 4, 8, 12, 16, 20, 24], "itemsize": 64})
+NRC_INPUT_FLOATS, NRC_WEIGHTS, NRC_TABLE_HALVES = 16, 21504, 16777216
+
 # constants (src/shared/constants.h)
 TONE_MAPPING_NONE, TONE_MAPPING_ACES = 0, 1
 RENDER_MODE_RGB, RENDER_MODE_SPECTRAL = 0, 1
@@ -176,6 +182,13 @@ EXPORTS = {
     "vkrt_cuda_render_adjoint_device": (_I32, [_V, _V, _V, _V]),
     "vkrt_cuda_read_texture_gradient": (_I32, [_V, _U32, _V, _SZ]),
     "vkrt_cuda_read_material_gradients": (_I32, [_V, _V, _U32]),
+    "vkrt_cuda_default_nrc_config": (None, [_V]),
+    "vkrt_cuda_nrc_configure": (_I32, [_V, _V]),
+    "vkrt_cuda_nrc_infer": (_I32, [_V, _V, _U32, _V]),
+    "vkrt_cuda_nrc_train": (_I32, [_V, _V, _V, _U32, _U32, _V]),
+    "vkrt_cuda_nrc_parameters": (_I32, [_V, _V, _V, _U32]),
+    "vkrt_cuda_nrc_gradients": (_I32, [_V, _V, _V]),
+    "vkrt_cuda_nrc_grid": (_I32, [_V, _V, _V, _V, _V]),
     "vkrt_host_pack_shader_vertices": (None, [_V, _U32, _V]),
     "vkrt_host_mesh_transform": (None, [_V, _V, _V, _V]),
     "vkrt_host_camera_matrices": (None, [_V, _V, _V, _F, _F, _F, _U32, _U32, _V]),

@@ -288,6 +288,55 @@ class RenderContext:
                     "read material gradients")
         return out
 
+    # ---- neural radiance cache ---------------------------------------------------------------------------------
+    def nrc_configure(self, **fields) -> None:
+        cfg = np.zeros(1, dtype=abi.NRC_CONFIG)
+        self.lib.vkrt_cuda_default_nrc_config(abi.ptr(cfg))
+        for k, v in fields.items():
+            cfg[k] = v
+        self._check(self.lib.vkrt_cuda_nrc_configure(self.handle, abi.ptr(cfg)), "configure radiance cache")
+
+    def nrc_infer(self, inputs: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(inputs, dtype=np.float32).reshape(-1, abi.NRC_INPUT_FLOATS)
+        out = np.zeros((len(x), 4), np.float32)
+        self._check(self.lib.vkrt_cuda_nrc_infer(self.handle, abi.ptr(x), len(x), abi.ptr(out)), "cache inference")
+        return out
+
+    def nrc_train(self, inputs: np.ndarray, targets: np.ndarray, apply: bool = True) -> float:
+        x = np.ascontiguousarray(inputs, dtype=np.float32).reshape(-1, abi.NRC_INPUT_FLOATS)
+        t = np.zeros((len(x), 4), np.float32)
+        t[:, : targets.shape[1]] = targets
+        loss = np.zeros(1, np.float32)
+        self._check(self.lib.vkrt_cuda_nrc_train(self.handle, abi.ptr(x), abi.ptr(t), len(x), 1 if apply else 0,
+                                                 abi.ptr(loss)), "cache training")
+        return float(loss[0])
+
+    def nrc_parameters(self, weights: np.ndarray | None = None, table: np.ndarray | None = None,
+                       read_table: bool = False):
+        """Writes the given FP16 parameters (uint16 views), or reads them when none are given."""
+        if weights is None and table is None:
+            w = np.zeros(abi.NRC_WEIGHTS, np.uint16)
+            tb = np.zeros(abi.NRC_TABLE_HALVES, np.uint16) if read_table else None
+            self._check(self.lib.vkrt_cuda_nrc_parameters(self.handle, abi.ptr(w), abi.ptr(tb), 0), "cache parameters")
+            return w, tb
+        w = None if weights is None else np.ascontiguousarray(weights, np.uint16)
+        tb = None if table is None else np.ascontiguousarray(table, np.uint16)
+        self._check(self.lib.vkrt_cuda_nrc_parameters(self.handle, abi.ptr(w), abi.ptr(tb), 1), "cache parameters")
+        return None
+
+    def nrc_gradients(self, table: bool = False):
+        w = np.zeros(abi.NRC_WEIGHTS, np.float32)
+        tb = np.zeros(abi.NRC_TABLE_HALVES, np.float32) if table else None
+        self._check(self.lib.vkrt_cuda_nrc_gradients(self.handle, abi.ptr(w), abi.ptr(tb)), "cache gradients")
+        return w, tb
+
+    def nrc_grid(self):
+        lo, hi = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        res, dense = np.zeros(16, np.uint32), np.zeros(16, np.uint32)
+        self._check(self.lib.vkrt_cuda_nrc_grid(self.handle, abi.ptr(lo), abi.ptr(hi), abi.ptr(res), abi.ptr(dense)),
+                    "cache grid")
+        return lo, hi, res, dense
+
     def stats(self) -> dict:
         st = np.zeros(1, dtype=abi.STATS)
         self._check(self.lib.vkrt_cuda_get_stats(self.handle, abi.ptr(st)), "stats")

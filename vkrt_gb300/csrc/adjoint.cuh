@@ -157,6 +157,7 @@ struct AdjointHook {
     VKRT_DEV void neeEnvironment(uint32_t r, const Bsdf& b, float3 wl, float3 f, float3 factor, float3 Le) {
         nee(r, b, wl, f, factor, Le, VKRT_CUDA_INVALID_INDEX);
     }
+    VKRT_DEV void cacheQuery(const Surface&, const ShadeMaterial&) {}
     VKRT_DEV void bsdfSample(const Bsdf& b, float3 wl, float3 f) {
         if (!v) return;
         float3 dB, dR;

@@ -17,6 +17,7 @@
 
 #include "adjoint.h"
 #include "bvh_build.h"
+#include "nrc.h"
 #include "context_view.h"
 #include "render.h"
 #include "wavefront.h"
@@ -124,6 +125,15 @@ struct VKRT_CudaContext {
     DeviceArray<uint32_t> emissiveMeshMaterial;
     uint32_t emissiveMeshMaterialCount = 0;
     DeviceArray<float4> dImage;
+
+    // scene bounds of the uploaded geometry (world space)
+    float3 boundsLo = make_float3(0.0f, 0.0f, 0.0f), boundsHi = make_float3(0.0f, 0.0f, 0.0f);
+    // neural radiance cache
+    VKRT_CudaNrcConfig nrcCfg{};
+    std::unique_ptr<NrcEngine> nrc;
+    DeviceArray<NrcInput> nrcIn;
+    DeviceArray<float4> nrcTarget, nrcOut;
+    DeviceArray<float> nrcLoss;
 };
 
 namespace {
@@ -400,6 +410,24 @@ int32_t vkrt_cuda_upload_geometry(VKRT_CudaContext* c, const VKRT_CudaShaderVert
     c->vertexCount = vertexCount;
     c->indexCount = indexCount;
     c->triCount = uint32_t(tris);
+    // world-space bounds (the radiance cache's hash grid spans them)
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < meshCount; ++i) {
+        const VKRT_CudaMeshInfo& m = meshes[i];
+        float w[16];
+        vkrt_host_mesh_transform(m.position, m.rotation, m.scale, w);
+        for (uint32_t v = 0; v < m.vertexCount; ++v) {
+            const float* p = vertices[m.vertexBase + v].position;
+            for (int r = 0; r < 3; ++r) {
+                float q = w[0 * 4 + r] * p[0] + w[1 * 4 + r] * p[1] + w[2 * 4 + r] * p[2] + w[3 * 4 + r];
+                lo[r] = std::min(lo[r], q);
+                hi[r] = std::max(hi[r], q);
+            }
+        }
+    }
+    if (!(lo[0] <= hi[0])) lo[0] = lo[1] = lo[2] = hi[0] = hi[1] = hi[2] = 0.0f;
+    c->boundsLo = make_float3(lo[0], lo[1], lo[2]);
+    c->boundsHi = make_float3(hi[0], hi[1], hi[2]);
     VKRT_TRY(c, rebuildBvh(c), "BVH build");
     return VKRT_CUDA_SUCCESS;
 }
@@ -713,7 +741,14 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     if (!c0->wavefront) c0->wavefront.reset(new WavefrontEngine());
     WavefrontConfig wc = engineConfig(c0);
     VKRT_TRY(c0, cudaMemsetAsync(c0->counters, 0, sizeof(RenderCounters), c0->stream), "batch render");
-    VKRT_TRY(c0, c0->wavefront->render(scenes, spectral, wc, c0->cfg.rngMode, c0->cfg.rngSeed, c0->counters, c0->stream),
+    // a single context with an enabled radiance cache trains it and renders cache-terminated paths
+    WfCacheFrame cache{};
+    const bool useCache = count == 1 && c0->nrc && c0->nrc->ready() && c0->nrcCfg.enabled;
+    if (useCache)
+        cache = WfCacheFrame{c0->nrc.get(), c0->nrcCfg.terminationDepth, c0->nrcCfg.trainingPaths,
+                             c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber};
+    VKRT_TRY(c0, c0->wavefront->render(scenes, spectral, wc, c0->cfg.rngMode, c0->cfg.rngSeed, c0->counters, c0->stream,
+                                       kWavefrontForward, nullptr, useCache ? &cache : nullptr),
              "batch render");
     for (uint32_t i = 0; i < count; ++i) {
         VKRT_CudaContext* c = contexts[i];
@@ -854,6 +889,136 @@ int32_t vkrt_cuda_read_accumulation(VKRT_CudaContext* c, float* rgba, size_t byt
     cudaSetDevice(c->device);
     VKRT_TRY(c, cudaMemcpyAsync(rgba, c->accum[c->readIndex].ptr, need, cudaMemcpyDeviceToHost, c->stream), "read accumulation");
     VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read accumulation");
+    return VKRT_CUDA_SUCCESS;
+}
+
+void vkrt_cuda_default_nrc_config(VKRT_CudaNrcConfig* n) {
+    if (!n) return;
+    std::memset(n, 0, sizeof(*n));
+    n->enabled = 1u;
+    n->terminationDepth = 2u;
+    n->trainingPaths = 65536u;
+    n->trainingSteps = 4u;
+    n->learningRate = 1e-2f;
+    n->seed = 1u;
+}
+
+int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* c, const VKRT_CudaNrcConfig* n) {
+    if (!c || !n) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!(n->learningRate >= 0.0f) || n->trainingPaths > (1u << 22) || n->trainingSteps > 64u)
+        return invalid(c, "radiance cache configuration out of range");
+    cudaSetDevice(c->device);
+    if (!c->nrc) c->nrc.reset(new NrcEngine());
+    NrcSettings s{n->learningRate, 0.9f, 0.99f, 1e-8f, n->seed};
+    // pad the bounds a little so surface points never sit on the grid's outer faces
+    float3 ext = make_float3(c->boundsHi.x - c->boundsLo.x, c->boundsHi.y - c->boundsLo.y, c->boundsHi.z - c->boundsLo.z);
+    float pad = 1e-3f * std::max(std::max(ext.x, ext.y), std::max(ext.z, 1e-3f));
+    float3 lo = make_float3(c->boundsLo.x - pad, c->boundsLo.y - pad, c->boundsLo.z - pad);
+    float3 hi = make_float3(c->boundsHi.x + pad, c->boundsHi.y + pad, c->boundsHi.z + pad);
+    VKRT_TRY(c, c->nrc->reset(s, lo, hi, c->stream), "radiance cache init");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "radiance cache init");
+    c->nrcCfg = *n;
+    return VKRT_CUDA_SUCCESS;
+}
+
+namespace {
+int32_t nrcReady(VKRT_CudaContext* c) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!c->nrc || !c->nrc->ready()) return invalid(c, "radiance cache not configured");
+    return VKRT_CUDA_SUCCESS;
+}
+}  // namespace
+
+int32_t vkrt_cuda_nrc_infer(VKRT_CudaContext* c, const float* inputs, uint32_t n, float* outputs) {
+    int32_t r = nrcReady(c);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    if (n && (!inputs || !outputs)) return invalid(c, "null cache input or output");
+    if (!n) return VKRT_CUDA_SUCCESS;
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->nrcIn.assign(reinterpret_cast<const NrcInput*>(inputs), n, c->stream), "cache inputs");
+    VKRT_TRY(c, c->nrcOut.reserve(n), "cache outputs");
+    VKRT_TRY(c, c->nrc->infer(c->nrcIn.ptr, n, c->nrcOut.ptr, c->stream), "cache inference");
+    VKRT_TRY(c, cudaMemcpyAsync(outputs, c->nrcOut.ptr, sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream),
+             "cache outputs");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "cache inference");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_nrc_train(VKRT_CudaContext* c, const float* inputs, const float* targets, uint32_t n, uint32_t apply,
+                            float* loss) {
+    int32_t r = nrcReady(c);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    if (n && (!inputs || !targets)) return invalid(c, "null training records");
+    if (!n) return VKRT_CUDA_SUCCESS;
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->nrcIn.assign(reinterpret_cast<const NrcInput*>(inputs), n, c->stream), "training inputs");
+    VKRT_TRY(c, c->nrcTarget.assign(reinterpret_cast<const float4*>(targets), n, c->stream), "training targets");
+    VKRT_TRY(c, c->nrcLoss.reserve(1), "training loss");
+    VKRT_TRY(c, cudaMemsetAsync(c->nrcLoss.ptr, 0, sizeof(float), c->stream), "training loss");
+    VKRT_TRY(c, c->nrc->train(c->nrcIn.ptr, c->nrcTarget.ptr, n, c->nrcLoss.ptr, apply != 0u, c->stream),
+             "cache training");
+    float l = 0.0f;
+    VKRT_TRY(c, cudaMemcpyAsync(&l, c->nrcLoss.ptr, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "training loss");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "cache training");
+    if (loss) *loss = l;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_nrc_parameters(VKRT_CudaContext* c, uint16_t* weights, uint16_t* table, uint32_t write) {
+    int32_t r = nrcReady(c);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    cudaSetDevice(c->device);
+    const cudaMemcpyKind kind = write ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    if (weights) {
+        void* dst = write ? static_cast<void*>(c->nrc->weights()) : static_cast<void*>(weights);
+        const void* src = write ? static_cast<const void*>(weights) : static_cast<const void*>(c->nrc->weights());
+        VKRT_TRY(c, cudaMemcpyAsync(dst, src, sizeof(uint16_t) * kNrcWeightCount, kind, c->stream), "cache weights");
+    }
+    if (table) {
+        void* dst = write ? static_cast<void*>(c->nrc->table()) : static_cast<void*>(table);
+        const void* src = write ? static_cast<const void*>(table) : static_cast<const void*>(c->nrc->table());
+        VKRT_TRY(c, cudaMemcpyAsync(dst, src, sizeof(uint16_t) * size_t(kNrcTableParams), kind, c->stream),
+                 "cache table");
+    }
+    if (write) VKRT_TRY(c, c->nrc->syncMasters(c->stream), "cache parameters");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "cache parameters");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_nrc_gradients(VKRT_CudaContext* c, float* weights, float* table) {
+    int32_t r = nrcReady(c);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    cudaSetDevice(c->device);
+    if (weights)
+        VKRT_TRY(c, cudaMemcpyAsync(weights, c->nrc->weightGrad(), sizeof(float) * kNrcWeightCount,
+                                    cudaMemcpyDeviceToHost, c->stream),
+                 "cache gradients");
+    if (table)
+        VKRT_TRY(c, cudaMemcpyAsync(table, c->nrc->tableGrad(), sizeof(float) * size_t(kNrcTableParams),
+                                    cudaMemcpyDeviceToHost, c->stream),
+                 "cache gradients");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "cache gradients");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_nrc_grid(VKRT_CudaContext* c, float* lo, float* hi, uint32_t* res, uint32_t* dense) {
+    int32_t r = nrcReady(c);
+    if (r != VKRT_CUDA_SUCCESS) return r;
+    const NrcGridInfo& g = c->nrc->grid();
+    if (lo) {
+        lo[0] = g.lo.x;
+        lo[1] = g.lo.y;
+        lo[2] = g.lo.z;
+    }
+    if (hi) {
+        hi[0] = g.lo.x + 1.0f / g.invExtent.x;
+        hi[1] = g.lo.y + 1.0f / g.invExtent.y;
+        hi[2] = g.lo.z + 1.0f / g.invExtent.z;
+    }
+    for (int l = 0; l < kNrcLevels; ++l) {
+        if (res) res[l] = g.res[l];
+        if (dense) dense[l] = g.dense[l];
+    }
     return VKRT_CUDA_SUCCESS;
 }
 

@@ -1,0 +1,70 @@
+// nrc.h — host interface of the neural radiance cache (nrc.cu).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "nrc.cuh"
+
+namespace vkrt {
+
+struct NrcSettings {
+    float learningRate;
+    float beta1, beta2, epsilon;
+    uint32_t seed;
+};
+
+// Parameters, optimiser state and scratch of one cache. All device memory; methods run asynchronously on `stream`.
+class NrcEngine {
+public:
+    NrcEngine();
+    ~NrcEngine();
+    NrcEngine(const NrcEngine&) = delete;
+    NrcEngine& operator=(const NrcEngine&) = delete;
+
+    // (Re)initialises the parameters (seeded) and the optimiser; `lo`/`hi` bound the scene for the hash grid.
+    cudaError_t reset(const NrcSettings& s, float3 lo, float3 hi, cudaStream_t stream);
+    bool ready() const { return table_ != nullptr; }
+    const NrcGridInfo& grid() const { return grid_; }
+
+    // Radiance predictions (float4 per input, xyz used) for n inputs in device memory.
+    cudaError_t infer(const NrcInput* inputs, uint32_t n, float4* out, cudaStream_t stream);
+    // Device-side count: infers *count inputs (at most capacity), for graph-captured frames.
+    cudaError_t inferCounted(const NrcInput* inputs, const uint32_t* count, uint32_t capacity, float4* out,
+                             cudaStream_t stream);
+    // One optimiser step on n records (inputs and float4 targets, xyz used) with the relative L2 loss; adds the
+    // step's mean loss to *lossOut (device float) when given. applyUpdate = false keeps the parameters (gradients only).
+    cudaError_t train(const NrcInput* inputs, const float4* targets, uint32_t n, float* lossOut, bool applyUpdate,
+                      cudaStream_t stream);
+
+    // parameter and gradient access for tests: FP16 weights (kNrcWeightCount) and table (kNrcTableParams halves);
+    // FP32 gradients of the last step with respect to the same parameters (already divided by the batch size)
+    __half* weights() { return wHalf_; }
+    __half* table() { return reinterpret_cast<__half*>(table_); }
+    float* weightGrad() { return wGrad_; }
+    float* tableGrad() { return tGrad_; }
+    // refresh the FP32 master copies from the FP16 parameters (after a test wrote them)
+    cudaError_t syncMasters(cudaStream_t stream);
+    // allocates the inference scratch for `capacity` rows ahead of a graph capture (no allocation while capturing)
+    cudaError_t reserveInference(uint32_t capacity);
+
+private:
+    cudaError_t ensureScratch(uint32_t n);
+    NrcSettings s_{};
+    NrcGridInfo grid_{};
+    uint32_t step_ = 0;
+    // parameters: FP16 working copies, FP32 masters, Adam moments, gradients
+    __half* wHalf_ = nullptr;
+    float *wMaster_ = nullptr, *wM_ = nullptr, *wV_ = nullptr, *wGrad_ = nullptr;
+    __half2* table_ = nullptr;
+    float *tMaster_ = nullptr, *tM_ = nullptr, *tV_ = nullptr, *tGrad_ = nullptr;
+    // scratch for n rows
+    uint32_t cap_ = 0;
+    __half *x0_ = nullptr, *acts_ = nullptr, *dz_ = nullptr, *dy_ = nullptr;
+    __half* x0Infer_ = nullptr;
+    uint32_t capInfer_ = 0;
+    float* dx0_ = nullptr;
+    float4* out_ = nullptr;
+};
+
+}  // namespace vkrt

@@ -45,6 +45,7 @@ struct StepConfig {
     bool envNee;      // environment importance sampling active
     uint32_t rngMode;
     uint64_t rngSeed;
+    uint32_t cacheDepth = 0xFFFFFFFFu;  // surface vertex depth at which the path queries the radiance cache and ends
 };
 
 VKRT_DEV float4 heroLambdas(float unit) {
@@ -93,12 +94,15 @@ VKRT_DEV float3 thr3(const PathState& p) { return xyz(p.thr); }
 //   nee*          shadow request `req`: contribution = factor * f * Le, f = f(wl) the BSDF value toward the light,
 //                 factor = throughput x |cos| x MIS / pdf
 //   bsdfSample    the continuation: throughput *= f(wl) * |cos| / pdf
+//   cacheQuery    the path ends at this vertex (depth == cacheDepth): the radiance cache's prediction for the
+//                 vertex, times the throughput, completes it
 struct NoVertexHook {
     VKRT_DEV void surface(const Surface&, const ShadeMaterial&, const Bsdf&) {}
     VKRT_DEV void emission(float3) {}
     VKRT_DEV void neeEmissive(uint32_t, const Bsdf&, float3, float3, float3, float3, uint32_t) {}
     VKRT_DEV void neeEnvironment(uint32_t, const Bsdf&, float3, float3, float3, float3) {}
     VKRT_DEV void bsdfSample(const Bsdf&, float3, float3) {}
+    VKRT_DEV void cacheQuery(const Surface&, const ShadeMaterial&) {}
 };
 
 // Processes the hit of p's current ray. Returns true when the path continues with a new ray in p.o / p.d.
@@ -163,6 +167,12 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             p.radiance += make_float4(c.x, c.y, c.z, 0.0f);
             hook.emission(thr3(p) * w);
         }
+    }
+
+    // radiance-cache termination: the cache stands for everything the vertex scatters (NEE and continuation)
+    if (depth == cfg.cacheDepth) {
+        hook.cacheQuery(s, mat);
+        return false;
     }
 
     // emissive-triangle NEE (light/direct/light_sampling.slang, rgb_lighting.slang / spectral_lighting.slang)

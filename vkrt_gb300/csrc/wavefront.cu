@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "adjoint.cuh"
+#include "nrc.h"
 #include "wavefront.h"
 
 namespace vkrt {
@@ -48,7 +49,9 @@ enum : uint32_t {
     kCntFetchIntersect = 6,
     kCntFetchShadow = 7,
     kCntClass0 = 8,  // class-partitioned shade queue: misses, dielectric hits, metal hits
+    kCntQueries = 11,  // radiance-cache queries of the iteration
 };
+constexpr uint32_t kPendCache = 16u;  // pendFlags: the path ended at a radiance-cache query
 constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;  // kSortMaterial sorts by (scene, class)
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
 
@@ -110,6 +113,11 @@ struct WfGlobals {
     float4* adjEm1;
     float4* adjRatioB;  // (df/dbase) / f (xyz), material index (w bits)
     float4* adjRatioR;  // (df/droughness) / f (xyz), kAdjFlag* bits (w)
+    // radiance cache: paths end at surface depth cacheDepth (0xFFFFFFFF = off) with a query
+    uint32_t cacheDepth;
+    NrcInput* nrcQueries;  // Q inputs of the iteration's queries
+    uint32_t* slotQuery;   // query position of a slot whose path ended at the cache
+    float4* nrcPred;       // predictions, by query position
 };
 
 VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
@@ -205,7 +213,7 @@ VKRT_DEV PathState loadPath(const WfGlobals& g, uint32_t s) {
 }
 
 VKRT_DEV StepConfig stepConfig(const WfGlobals& g, const WfScene& S) {
-    return StepConfig{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed};
+    return StepConfig{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed, g.cacheDepth};
 }
 
 VKRT_DEV SpecTable specTable(const WfScene& S) {
@@ -327,6 +335,7 @@ __global__ void kWfBegin(WfGlobals g, uint32_t outQueue) {
         g.counts[kCntFetchIntersect] = 0u;
         g.counts[kCntFetchShadow] = 0u;
         g.counts[kCntClass0] = g.counts[kCntClass0 + 1] = g.counts[kCntClass0 + 2] = 0u;
+        g.counts[kCntQueries] = 0u;
     }
     if (g.sort == kSortMaterial)
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < g.keyCount; k += gridDim.x * blockDim.x)
@@ -433,6 +442,114 @@ VKRT_DEV void applyPending(const WfGlobals& g, uint32_t slot, float4& radiance) 
     if ((f & 2u) && (f & 8u)) radiance += g.pend1[slot];
 }
 
+// radiance-cache inputs of a vertex: world position, outgoing direction (toward the previous vertex), shading normal,
+// roughness, base colour, metallic
+VKRT_DEV NrcInput nrcInputOf(const Surface& s, const ShadeMaterial& m, float3 rayDir) {
+    NrcInput in;
+    in.posRough = make_float4(s.hitPoint.x, s.hitPoint.y, s.hitPoint.z, m.roughness);
+    in.dirMetal = make_float4(-rayDir.x, -rayDir.y, -rayDir.z, m.metallic);
+    in.normal = make_float4(s.shadingNormal.x, s.shadingNormal.y, s.shadingNormal.z, 0.0f);
+    in.albedo = make_float4(m.baseColor.x, m.baseColor.y, m.baseColor.z, 0.0f);
+    return in;
+}
+
+// forward-pass hook: records the radiance-cache query of a path that ends at the cache
+struct CacheHook : NoVertexHook {
+    NrcInput* in;
+    bool* queried;
+    float3 rayDir;
+    VKRT_DEV void cacheQuery(const Surface& s, const ShadeMaterial& m) {
+        *in = nrcInputOf(s, m, rayDir);
+        *queried = true;
+    }
+};
+
+// training-path hook: records the cache inputs of every surface vertex
+struct TrainHook : NoVertexHook {
+    NrcInput* in;
+    bool* has;
+    float3 rayDir;
+    VKRT_DEV void surface(const Surface& s, const ShadeMaterial& m, const Bsdf&) {
+        *in = nrcInputOf(s, m, rayDir);
+        *has = true;
+    }
+};
+
+constexpr uint32_t kNrcTrainVerts = 16;  // vertices of a training path that become records
+
+// Radiance-cache training paths: full-length paths from random pixels of scene 0 (their own random streams, sample
+// indices from 2^30), traced and shaded like render paths. Each surface vertex j becomes a record whose target is
+// the radiance the path gathered after the vertex's own emission, divided by the throughput that reached it: an
+// unbiased estimate of what the vertex scatters toward the previous one (linear sRGB; hero paths convert the four
+// wavelengths as a sample result is converted).
+template <bool kSpectral>
+__global__ void __launch_bounds__(kWfThreads) kNrcTrainPaths(const WfScene* __restrict__ scenes, uint32_t paths,
+                                                             uint32_t frame, uint32_t seed, uint32_t rngMode,
+                                                             uint64_t rngSeed, uint32_t maxRecords,
+                                                             NrcInput* __restrict__ recIn,
+                                                             float4* __restrict__ recTarget, uint32_t* recCount,
+                                                             RenderCounters* counters) {
+    extern __shared__ uint2 smemStack[];
+    const WfScene& S = scenes[0];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t primary = 0, ext = 0, shadow = 0;
+    if (i < paths && S.vw > 0u && S.vh > 0u) {
+        const uint32_t h0 = wellonsHash(seed ^ (frame * 0x9e3779b9u) ^ (i * 0x85ebca6bu));
+        const int px = int(S.vx0 + h0 % S.vw), py = int(S.vy0 + wellonsHash(h0) % S.vh);
+        const StepConfig cfg{kSpectral, S.neeEnabled != 0u, S.envNee != 0u, rngMode, rngSeed};
+        KernelCtx k{S.sc, S.sd, smemStack + threadIdx.x, blockDim.x, counters};
+        const SpecTable tab = makeSpecTable(S.sc, S.sd);
+        PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, 0x40000000u + i);
+        NrcInput vin[kNrcTrainVerts];
+        float4 vthr[kNrcTrainVerts], vrad[kNrcTrainVerts];
+        uint32_t nv = 0;
+        for (;;) {
+            TraceHit hit = closest<false>(k, p.o, p.d);
+            if (p.depth == 0u) ++primary;
+            else ++ext;
+            NrcInput in;
+            bool has = false;
+            const float4 thrBefore = p.thr;
+            ShadowRequest sh[2];
+            uint32_t ns;
+            bool cont = shadePathVertex<kSpectral, TrainHook>(S.sc, S.sd, cfg, tab, p, hit, sh, ns,
+                                                              TrainHook{{}, &in, &has, p.d});
+            if (has && nv < kNrcTrainVerts) {
+                vin[nv] = in;
+                vthr[nv] = thrBefore;
+                vrad[nv] = p.radiance;  // emission of the vertex included, its light samples not yet
+                ++nv;
+            }
+            for (uint32_t r = 0; r < ns; ++r) {
+                ++shadow;
+                TraceRay ray{sh[r].origin, sh[r].dir, kTMin, sh[r].tmax};
+                if (traceBvh<true, false>(S.sc, ray, k.stackColumn, k.stackStride, counters).mesh ==
+                    VKRT_CUDA_INVALID_INDEX)
+                    p.radiance += sh[r].contribution;
+            }
+            if (!cont) break;
+        }
+        const float4 total = p.radiance;
+        for (uint32_t j = 0; j < nv; ++j) {
+            float4 suf;
+            suf.x = vthr[j].x > 0.0f ? (total.x - vrad[j].x) / vthr[j].x : 0.0f;
+            suf.y = vthr[j].y > 0.0f ? (total.y - vrad[j].y) / vthr[j].y : 0.0f;
+            suf.z = vthr[j].z > 0.0f ? (total.z - vrad[j].z) / vthr[j].z : 0.0f;
+            suf.w = vthr[j].w > 0.0f ? (total.w - vrad[j].w) / vthr[j].w : 0.0f;
+            const float3 rgb = kSpectral ? xyzToLinearSrgb(spectral4ToXYZ(suf, heroLambdas(p.lamUnit), kLambdaRange))
+                                         : xyz(suf);
+            const uint32_t pos = atomicAdd(recCount, 1u);
+            if (pos < maxRecords) {
+                recIn[pos] = vin[j];
+                recTarget[pos] = make_float4(rgb.x, rgb.y, rgb.z, 0.0f);
+            }
+        }
+    }
+    warpCount(&counters->primaryRays, primary);
+    warpCount(&counters->extensionRays, ext);
+    warpCount(&counters->shadowRays, shadow);
+}
+
 // the vertex gradient factors recorded by the hook, kept per slot until the vertex's shadow rays are traced
 VKRT_DEV void adjStoreVertex(const WfGlobals& g, uint32_t slot, const AdjVertex& av, bool cont) {
     if (!av.hasSurface) {
@@ -515,6 +632,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         bool cont = false;
         uint32_t slot = 0, ns = 0;
         ShadowRequest sh[2];
+        NrcInput query;
+        bool queried = false;
         if (valid) {
             if (g.sort == kSortClass)  // the three class queues read as one
                 slot = i < nMiss ? g.classQueue[i]
@@ -540,10 +659,11 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                 if (g.adj.wantEmission && av.emitted) scatterHitEmission(S.sc, g.adj, smemMat, av);
                 adjStoreVertex(g, slot, av, cont);
             } else {
-                cont = shadePathVertex<kSpectral>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns);
+                cont = shadePathVertex<kSpectral, CacheHook>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
+                                                             CacheHook{{}, &query, &queried, p.d});
             }
             storePath(g, slot, p);
-            uint32_t flags = 0u;
+            uint32_t flags = queried ? kPendCache : 0u;
             if (ns > 0) {
                 g.pend0[slot] = sh[0].contribution;
                 flags |= 1u;
@@ -560,6 +680,13 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         if (valid && cont) outQ[pos] = slot;
         pos = warpPush(&g.counts[kCntFinished], valid && !cont);
         if (valid && !cont) g.finished[pos] = slot;
+        if (g.cacheDepth != 0xFFFFFFFFu) {
+            pos = warpPush(&g.counts[kCntQueries], valid && queried);
+            if (valid && queried) {
+                g.nrcQueries[pos] = query;
+                g.slotQuery[slot] = pos;
+            }
+        }
         for (uint32_t r = 0; r < 2; ++r) {
             bool want = valid && r < ns;
             pos = warpPush(&g.counts[kCntShadow], want);
@@ -631,6 +758,14 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             if constexpr (kAdjoint) {
                 adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
             } else {
+                if (pf & kPendCache) {  // the cache's radiance times the path throughput completes the path
+                    const float3 pred = fmax3(xyz(g.nrcPred[g.slotQuery[slot]]), f3(0.0f));
+                    // hero lanes carry the balance weight of four equal techniques, as every other term does
+                    if (kSpectral)
+                        p.radiance += p.thr * spectral4(specTable(S), pred, heroLambdas(p.lamUnit)) *
+                                      (p.techPath > 0.0f ? 0.25f : 0.0f);
+                    else p.radiance += make_float4(p.thr.x * pred.x, p.thr.y * pred.y, p.thr.z * pred.z, 0.0f);
+                }
                 StepConfig cfg = stepConfig(g, S);
                 float3 res = pathResult<kSpectral>(cfg, p);
                 g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
@@ -702,7 +837,15 @@ struct WavefrontEngine::Buffers {
     WfGraphCache graphs[3];
     float stageMs[kStageCount] = {};
     uint32_t* hostCount = nullptr;  // pinned word the stage-by-stage loop polls
+    // radiance cache: queries, predictions, training records
+    size_t c_nq = 0, c_sq = 0, c_np = 0, c_ri = 0, c_rt = 0, c_rc = 0;
+    NrcInput* recIn = nullptr;
+    float4* recTarget = nullptr;
+    uint32_t* recCount = nullptr;
+    uint32_t lastRecords = 0;
 };
+
+uint32_t WavefrontEngine::lastCacheRecords() const { return b_->lastRecords; }
 
 const float* WavefrontEngine::lastStageMs() const { return b_->stageMs; }
 
@@ -725,7 +868,7 @@ void WavefrontEngine::release() {
     void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotItem, g.sampleBuf,
                     g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
                     g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, b_->bases,
-                    g.adjDelta,
+                    g.nrcQueries, g.slotQuery, g.nrcPred, b_->recIn, b_->recTarget, b_->recCount, g.adjDelta,
                     g.adjTotal,
                     g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR};
     for (void* p : ptrs)
@@ -738,10 +881,13 @@ void WavefrontEngine::release() {
 
 cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool spectral, const WavefrontConfig& cfgIn,
                                     uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters,
-                                    cudaStream_t stream, WavefrontMode mode, const AdjointParams* adjoint) {
+                                    cudaStream_t stream, WavefrontMode mode, const AdjointParams* adjoint,
+                                    const WfCacheFrame* cache) {
     Buffers& B = *b_;
     const bool adjMode = mode == kWavefrontAdjoint;
     if (adjMode && (!adjoint || spectral || scenesIn.size() != 1)) return cudaErrorInvalidValue;
+    const bool useCache = cache && cache->engine && cache->engine->ready() && mode == kWavefrontForward;
+    if (useCache && scenesIn.size() != 1) return cudaErrorInvalidValue;
     WavefrontConfig cfg = cfgIn;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
@@ -802,6 +948,16 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(shadowB, c_sB, 2 * size_t(Q));
     WF_GROW(keyHist, c_hist, keys);
     WF_GROW(counts, c_counts, 16);
+    if (useCache) {
+        WF_GROW(nrcQueries, c_nq, Q);
+        WF_GROW(slotQuery, c_sq, Q);
+        WF_GROW(nrcPred, c_np, Q);
+        const size_t maxRecords = size_t(cache->trainingPaths) * kNrcTrainVerts;
+        if (e == cudaSuccess) e = grow(B.recIn, B.c_ri, maxRecords);
+        if (e == cudaSuccess) e = grow(B.recTarget, B.c_rt, maxRecords);
+        if (e == cudaSuccess) e = grow(B.recCount, B.c_rc, 1);
+        if (e == cudaSuccess) e = cache->engine->reserveInference(Q);
+    }
     if (adjMode) {
         WF_GROW(adjDelta, c_aD, Q);
         WF_GROW(adjTotal, c_aT, Q);
@@ -832,6 +988,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     }
     g.mode = uint32_t(mode);
     g.adj = adjoint ? *adjoint : AdjointParams{};
+    g.cacheDepth = useCache ? cache->cacheDepth : 0xFFFFFFFFu;
     g.scenes = B.scenes;
     g.itemBases = B.bases;
     g.workBases = B.bases + scenes.size();
@@ -846,7 +1003,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.rngSeed = rngSeed;
     g.counters = counters;
     g.launchesOutsideLoop = 2u + (mode == kWavefrontForward ? 2u : 0u);
-    g.launchesPerBody = 2u * (5u + (g.sort == kSortMaterial ? 2u : 0u)) + 1u;
+    g.launchesPerBody = 2u * (5u + (g.sort == kSortMaterial ? 2u : 0u) + (useCache ? 2u : 0u)) + 1u;
     const bool profile = cfg.profileStages != 0u;
     if (profile) cfg.useGraph = 0u;
     for (float& t : B.stageMs) t = 0.0f;
@@ -897,6 +1054,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             if (profile) kWfShadow<true, 8><<<gridI, kWfThreads, smem, stream>>>(g);
             else kWfShadow<false, 8><<<gridI, kWfThreads, smem, stream>>>(g);
         });
+        if (useCache)  // predictions for the paths that ended at the cache in this iteration
+            stage(kStageShade, [&] { cache->engine->inferCounted(g.nrcQueries, g.counts + kCntQueries, Q, g.nrcPred, stream); });
         stage(kStageFinalize, [&] {
             if (adjMode) kWfFinalize<false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
             else if (spectral) kWfFinalize<true, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
@@ -920,6 +1079,37 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             else kWfInit<false><<<gridS, kWfThreads, 0, stream>>>(g);
         });
     };
+
+    if (useCache) {
+        // train the cache on this frame's training paths before rendering with it
+        e = cudaMemsetAsync(B.recCount, 0, sizeof(uint32_t), stream);
+        if (e != cudaSuccess) return e;
+        const uint32_t maxRecords = cache->trainingPaths * kNrcTrainVerts;
+        const uint32_t tb = (cache->trainingPaths + kWfThreads - 1u) / kWfThreads;
+        if (cache->trainingPaths) {
+            if (spectral)
+                kNrcTrainPaths<true><<<tb, kWfThreads, smem, stream>>>(B.scenes, cache->trainingPaths, cache->frame,
+                                                                       cache->seed, rngMode, rngSeed, maxRecords, B.recIn,
+                                                                       B.recTarget, B.recCount, counters);
+            else
+                kNrcTrainPaths<false><<<tb, kWfThreads, smem, stream>>>(B.scenes, cache->trainingPaths, cache->frame,
+                                                                        cache->seed, rngMode, rngSeed, maxRecords,
+                                                                        B.recIn, B.recTarget, B.recCount, counters);
+        }
+        if (!B.hostCount) e = cudaMallocHost(&B.hostCount, sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.hostCount, B.recCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return e;
+        const uint32_t records = std::min(*B.hostCount, maxRecords);
+        B.lastRecords = records;
+        const uint32_t batch = std::min<uint32_t>(records, 1u << 16);
+        for (uint32_t k = 0; batch && k < cache->trainingSteps; ++k) {
+            const uint32_t off = uint32_t((uint64_t(k) * batch) % records);
+            const uint32_t n = std::min(batch, records - off);
+            e = cache->engine->train(B.recIn + off, B.recTarget + off, n, nullptr, true, stream);
+            if (e != cudaSuccess) return e;
+        }
+    }
 
     if (!cfg.useGraph) {
         prologue();

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "adjoint.h"
+#include "nrc.h"
 #include "render.h"
 #include "scene.cuh"
 
@@ -49,6 +50,17 @@ enum WavefrontStage : uint32_t {
     kStageResolve, kStageCount
 };
 
+// Radiance cache of a forward frame (one scene): trained on `trainingPaths` paths first, then queried by render paths
+// at surface depth `cacheDepth`.
+struct WfCacheFrame {
+    NrcEngine* engine;
+    uint32_t cacheDepth;
+    uint32_t trainingPaths;
+    uint32_t trainingSteps;
+    uint32_t seed;
+    uint32_t frame;
+};
+
 class WavefrontEngine {
 public:
     WavefrontEngine();
@@ -61,7 +73,10 @@ public:
     // sampleBase.
     cudaError_t render(const std::vector<WfScene>& scenes, bool spectral, const WavefrontConfig& cfg,
                        uint32_t rngMode, uint64_t rngSeed, RenderCounters* counters, cudaStream_t stream,
-                       WavefrontMode mode = kWavefrontForward, const AdjointParams* adjoint = nullptr);
+                       WavefrontMode mode = kWavefrontForward, const AdjointParams* adjoint = nullptr,
+                       const WfCacheFrame* cache = nullptr);
+    // records and steps of the last cache training
+    uint32_t lastCacheRecords() const;
     void release();
     // per-stage device milliseconds of the last render call made with profileStages (zeros otherwise)
     const float* lastStageMs() const;
