@@ -18,6 +18,7 @@ adjoint : the path-replay adjoint of the inverse-rendering Cornell box (128 x 12
         albedo + roughness textures): device time of the adjoint call / device time of the forward frame.
 batch : 64 uneven icosphere fields (10k-500k triangles, 256^2-1024^2, 8 spp, depth 10, RGB) in one autotuned graph
         launch vs 64 sequential megakernel (and wavefront) frames.
+convergence : time to relMSE <= 1e-3 against a 2048-spp reference, plain wavefront vs radiance-cache frames.
 --impl reference : the CPU restatement of vkrt's integrator (the oracle, a port: vkrt's own renderer needs Vulkan
         and is unavailable here) on all host cores, on a bounded block of rows of the same frame per step.
 """
@@ -200,6 +201,56 @@ def adjoint_ratio(local: int) -> dict:
             "forward_ms": round(fwd, 3), "adjoint_ms": round(adj, 3), "ratio": round(adj / fwd, 2),
             "integrator": "wavefront (primal + adjoint passes)",
             "gradients": "albedo texels, roughness texels, emission radiance; FP64 central-difference tests"}
+
+
+def convergence_measure(local: int, scene, mega_ms: float, max_frames: int = 96, ref_frames: int = 128) -> dict:
+    """Time to relMSE <= 1e-3 on the benchmark frame (16 spp per frame) for the plain wavefront tracer and for the
+    radiance-cache tracer, against a 2048-spp reference of the same scene rendered by the GPU tracer (which matches
+    the FP64 oracle per sample in the tests). relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2)."""
+    import torch
+    from vkrt_gb300 import RenderContext, abi
+
+    ctx = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE,
+                        integrator=abi.INTEGRATOR_WAVEFRONT)
+    ctx.upload_scene(scene)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    sd = scene.scene_data.copy()
+    ctx.reset_accumulation()
+    for f in range(ref_frames):
+        sd["frameNumber"] = 1_000_000 + f
+        ctx.render_frame(sd)
+    ref = ctx.read_accumulation()[..., :3].astype(np.float64)
+    den = ref ** 2 + 1e-2
+
+    def curve(**cache):
+        ctx.nrc_configure(**cache)
+        ctx.reset_accumulation()
+        total, pts, reached = 0.0, [], None
+        for f in range(max_frames):
+            sd["frameNumber"] = f
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.render_frame(sd)
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b)
+            err = float(np.mean((ctx.read_accumulation()[..., :3] - ref) ** 2 / den))
+            pts.append([f + 1, round(total, 1), round(err, 6)])
+            if err <= 1e-3:
+                reached = {"frames": f + 1, "spp": 16 * (f + 1), "ms": round(total, 1)}
+                break
+        return {"reached": reached, "curve": pts[:: max(1, len(pts) // 12)] + ([pts[-1]] if pts else [])}
+
+    plain = curve(enabled=0)
+    cached = curve(enabled=1, terminationDepth=2, trainingPaths=65536, trainingSteps=4, learningRate=1e-2, seed=3)
+    ctx.close()
+    out = {"threshold": 1e-3, "reference": f"{16 * ref_frames} spp, GPU wavefront tracer, independent seeds",
+           "plain_wavefront": plain, "radiance_cache": cached}
+    if plain["reached"]:
+        # the megakernel renders the same samples (tests: identical images), so it needs the same frames
+        out["megakernel_ms"] = round(plain["reached"]["frames"] * mega_ms, 1)
+        out["wavefront_over_megakernel"] = round(plain["reached"]["ms"] / out["megakernel_ms"], 4)
+    return out
 
 
 def batch_measure(local: int) -> dict:
@@ -399,6 +450,8 @@ def run_ours(args) -> dict | None:
         result["adjoint"] = adjoint_ratio(local)
     if rank == 0 and world == 1 and not args.no_batch:
         result["batch"] = batch_measure(local)
+    if rank == 0 and world == 1 and not args.no_convergence:
+        result["convergence"] = convergence_measure(local, scene, mega_ms)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(scene, budget_s=args.cpu_seconds)
     ctx.close()
@@ -468,6 +521,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-convergence", action="store_true")
     ap.add_argument("--stage-launches", action="store_true",
                     help="launch the wavefront stages one by one instead of as one CUDA graph (ncu cannot profile "
                          "kernel nodes of graphs with conditional nodes)")
