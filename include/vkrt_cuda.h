@@ -87,6 +87,8 @@ typedef struct VKRT_CudaStats {
     uint64_t kernelLaunches;       /* this backend's kernel launches made by the last call */
     float stageMs[8];              /* wavefront profileStages device ms: prologue, begin, intersect, sort, shade,
                                       shadow, finalize, resolve */
+    float bvhSahLbvh;              /* SAH cost / root area of the binary tree before treelet restructuring */
+    float bvhSahTreelets;          /* the same after */
 } VKRT_CudaStats;
 
 /* ray record for the trace entry points: origin/tMin, direction/tMax (32 bytes, 16-byte aligned) */

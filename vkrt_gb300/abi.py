@@ -87,10 +87,11 @@ WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight
 STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathSamples", "nodeFetchBytes",
                             "triFetchBytes", "bvhNodeCount", "bvhTriangleCount", "bvhBytes", "bvhBuildMs",
                             "errorFlags", "wavefrontBodies", "reserved0", "shadowNodeFetchBytes",
-                            "shadowTriFetchBytes", "kernelLaunches", "stageMs"],
+                            "shadowTriFetchBytes", "kernelLaunches", "stageMs", "bvhSahLbvh", "bvhSahTreelets"],
                   "formats": ["<u8", "<u8", "<u8", "<u8", "<u8", "<u8", "<u4", "<u4", "<u8", "<f4", "<u4", "<u4",
-                              "<u4", "<u8", "<u8", "<u8", ("<f4", 8)],
-                  "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 64, 68, 72, 76, 80, 88, 96, 104], "itemsize": 136})
+                              "<u4", "<u8", "<u8", "<u8", ("<f4", 8), "<f4", "<f4"],
+                  "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 64, 68, 72, 76, 80, 88, 96, 104, 136, 140],
+                  "itemsize": 144})
 
 WAVEFRONT_STAGES = ("prologue", "begin", "intersect", "sort", "shade", "shadow", "finalize", "resolve")
 

@@ -328,6 +328,144 @@ __global__ void kRefit(uint32_t n, const uint32_t* __restrict__ left, const uint
     }
 }
 
+// ---- 7. treelet restructuring (Karras & Aila 2013) --------------------------------------------------------------
+constexpr int kTreeletLeaves = 7;
+
+// Optimal binary topology of a treelet rooted at `root`: the root's subtree is expanded into up to 7 treelet
+// leaves (repeatedly opening the internal leaf of largest area); a dynamic program over the 127 leaf subsets finds
+// the SAH-optimal partition tree (every partition of a subset is tried, the lowest leaf fixed on one side); the
+// treelet's internal nodes are rewired to it and refit. The original topology is among the candidates, so the
+// SAH cost never rises.
+__device__ void restructureTreelet(uint32_t n, uint32_t root, uint32_t* left, uint32_t* right, uint32_t* parent,
+                                   float4* nodeLo, float4* nodeHi, uint32_t* leafCount, float* cost) {
+    uint32_t leaves[kTreeletLeaves], internals[kTreeletLeaves - 1];
+    int nl = 2, ni = 1;
+    internals[0] = root;
+    leaves[0] = __ldcg(&left[root]);
+    leaves[1] = __ldcg(&right[root]);
+    while (nl < kTreeletLeaves) {
+        int best = -1;
+        float bestA = -1.0f;
+        for (int i = 0; i < nl; ++i) {
+            uint32_t l = leaves[i];
+            if (l >= n - 1) continue;  // a triangle
+            float a = halfArea(__ldcg(&nodeLo[l]), __ldcg(&nodeHi[l]));
+            if (a > bestA) {
+                bestA = a;
+                best = i;
+            }
+        }
+        if (best < 0) break;
+        uint32_t x = leaves[best];
+        internals[ni++] = x;
+        leaves[best] = __ldcg(&left[x]);
+        leaves[nl++] = __ldcg(&right[x]);
+    }
+    if (nl < 3) return;
+    float4 llo[kTreeletLeaves], lhi[kTreeletLeaves];
+    uint32_t lcnt[kTreeletLeaves];
+    float area[1 << kTreeletLeaves], copt[1 << kTreeletLeaves];
+    uint8_t part[1 << kTreeletLeaves];
+    for (int i = 0; i < nl; ++i) {
+        llo[i] = __ldcg(&nodeLo[leaves[i]]);
+        lhi[i] = __ldcg(&nodeHi[leaves[i]]);
+        lcnt[i] = __ldcg(&leafCount[leaves[i]]);
+    }
+    const uint32_t full = (1u << nl) - 1u;
+    for (uint32_t s = 1; s <= full; ++s) {
+        float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        for (int i = 0; i < nl; ++i)
+            if (s & (1u << i)) {
+                lo = make_float4(fminf(lo.x, llo[i].x), fminf(lo.y, llo[i].y), fminf(lo.z, llo[i].z), 0.0f);
+                hi = make_float4(fmaxf(hi.x, lhi[i].x), fmaxf(hi.y, lhi[i].y), fmaxf(hi.z, lhi[i].z), 0.0f);
+            }
+        area[s] = halfArea(lo, hi);
+        if (__popc(s) == 1) {
+            copt[s] = __ldcg(&cost[leaves[__ffs(s) - 1]]);
+            continue;
+        }
+        const uint32_t low = s & (0u - s);
+        float best = INFINITY;
+        uint32_t bestP = low;
+        for (uint32_t p = (s - 1u) & s; p > 0u; p = (p - 1u) & s) {
+            if (!(p & low)) continue;
+            float c = copt[p] + copt[s ^ p];
+            if (c < best) {
+                best = c;
+                bestP = p;
+            }
+        }
+        copt[s] = kCostNode * area[s] + best;
+        part[s] = uint8_t(bestP);
+    }
+    // rewire: internal nodes in depth-first order of the optimal partition tree (parents before children)
+    uint32_t order[kTreeletLeaves - 1], subset[kTreeletLeaves - 1];
+    uint32_t stackNode[kTreeletLeaves], stackSet[kTreeletLeaves];
+    int sp = 0, used = 1, no = 0;
+    stackNode[sp] = internals[0];
+    stackSet[sp++] = full;
+    while (sp > 0) {
+        --sp;
+        const uint32_t node = stackNode[sp], s = stackSet[sp];
+        order[no] = node;
+        subset[no++] = s;
+        const uint32_t p = part[s], sides[2] = {p, s ^ p};
+        uint32_t child[2];
+        for (int k = 0; k < 2; ++k) {
+            if (__popc(sides[k]) == 1) {
+                child[k] = leaves[__ffs(sides[k]) - 1];
+            } else {
+                child[k] = internals[used++];
+                stackNode[sp] = child[k];
+                stackSet[sp++] = sides[k];
+            }
+            parent[child[k]] = node;
+        }
+        left[node] = child[0];
+        right[node] = child[1];
+    }
+    // refit children before parents
+    for (int k = no - 1; k >= 0; --k) {
+        const uint32_t node = order[k], s = subset[k];
+        float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        uint32_t cnt = 0;
+        for (int i = 0; i < nl; ++i)
+            if (s & (1u << i)) {
+                lo = make_float4(fminf(lo.x, llo[i].x), fminf(lo.y, llo[i].y), fminf(lo.z, llo[i].z), 0.0f);
+                hi = make_float4(fmaxf(hi.x, lhi[i].x), fmaxf(hi.y, lhi[i].y), fmaxf(hi.z, lhi[i].z), 0.0f);
+                cnt += lcnt[i];
+            }
+        nodeLo[node] = lo;
+        nodeHi[node] = hi;
+        leafCount[node] = cnt;
+        const float a = halfArea(lo, hi);
+        const uint32_t l = left[node], r = right[node];
+        cost[node] = fminf(kCostNode * a + __ldcg(&cost[l]) + __ldcg(&cost[r]), kCostTri * a * float(cnt));
+    }
+}
+
+// Bottom-up pass like the refit: a node is restructured once both of its subtrees are final.
+__global__ void kTreelets(uint32_t n, uint32_t minLeaves, uint32_t* left, uint32_t* right, uint32_t* parent,
+                          float4* nodeLo, float4* nodeHi, uint32_t* leafCount, float* cost, uint32_t* flags) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t node = __ldcg(&parent[n - 1 + k]);
+    while (node != kInvalid) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0u) return;
+        __threadfence();
+        if (__ldcg(&leafCount[node]) >= minLeaves)
+            restructureTreelet(n, node, left, right, parent, nodeLo, nodeHi, leafCount, cost);
+        __threadfence();
+        node = __ldcg(&parent[node]);
+    }
+}
+
+__global__ void kRootSah(const float4* nodeLo, const float4* nodeHi, const float* cost, float* out) {
+    float a = halfArea(nodeLo[0], nodeHi[0]);
+    *out = a > 0.0f ? cost[0] / a : 0.0f;
+}
+
 // ---- 8. collapse to 8-wide compressed nodes -------------------------------------------------------------------
 struct CollapseItem {
     uint32_t binary;  // binary node index
@@ -560,6 +698,7 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
     uint32_t* dLeafCount = dalloc<uint32_t>(2 * n, err);
     float* dCost = dalloc<float>(2 * n, err);
     uint32_t* dFlags = dalloc<uint32_t>(n, err);
+    float* dSah = dalloc<float>(2, err);
     // wide nodes: at most one per internal binary node
     uint32_t maxWide = n;  // internal binary nodes = n - 1, plus the root of a one-triangle scene
     out.nodes = dalloc<WideNode>(maxWide, err);
@@ -600,6 +739,13 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
         }
         kInitLeaves<<<(n + b - 1) / b, b, 0, stream>>>(dVals[0], dTriLo, dTriHi, n, dLo, dHi, dLeafCount, dCost, dFlags);
         if (n > 1) kRefit<<<(n + b - 1) / b, b, 0, stream>>>(n, dLeft, dRight, dParent, dLo, dHi, dLeafCount, dCost, dFlags);
+        if (n > 2) {
+            kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah);
+            cudaMemsetAsync(dFlags, 0, sizeof(uint32_t) * n, stream);
+            kTreelets<<<(n + b - 1) / b, b, 0, stream>>>(n, kTreeletLeaves, dLeft, dRight, dParent, dLo, dHi, dLeafCount,
+                                                         dCost, dFlags);
+            kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah + 1);
+        }
     }
     {
         // level-by-level collapse; the root wide node is slot 0
@@ -637,6 +783,11 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
         stats->buildMs = ms;
         stats->nodeCount = out.nodeCount;
         stats->triCount = out.triCount;
+        float sah[2] = {0.0f, 0.0f};
+        if (n > 2 && cudaMemcpy(sah, dSah, sizeof(sah), cudaMemcpyDeviceToHost) == cudaSuccess) {
+            stats->sahLbvh = sah[0];
+            stats->sahTreelets = sah[1];
+        }
     }
     if (err == cudaSuccess && out.triCount != n) err = cudaErrorUnknown;
 
@@ -660,6 +811,7 @@ done:
     cudaFree(dLeafCount);
     cudaFree(dCost);
     cudaFree(dFlags);
+    cudaFree(dSah);
     cudaFree(dQueue[0]);
     cudaFree(dQueue[1]);
     cudaFree(dCounters);

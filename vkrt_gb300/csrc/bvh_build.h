@@ -31,6 +31,8 @@ struct BvhBuildStats {
     float buildMs;
     uint32_t nodeCount;
     uint32_t triCount;
+    float sahLbvh;      // SAH cost of the binary tree / root area, before treelet restructuring
+    float sahTreelets;  // after
 };
 
 // Builds the 8-wide BVH on `stream` (synchronises it). Scratch buffers are allocated and freed inside.

@@ -1192,7 +1192,7 @@ int32_t vkrt_cuda_read_output(VKRT_CudaContext* c, uint16_t* rgba, size_t bytes)
     return VKRT_CUDA_SUCCESS;
 }
 
-static_assert(sizeof(VKRT_CudaStats) == 136, "VKRT_CudaStats layout");
+static_assert(sizeof(VKRT_CudaStats) == 144, "VKRT_CudaStats layout");
 static_assert(sizeof(VKRT_CudaWavefrontConfig) == 64, "VKRT_CudaWavefrontConfig layout");
 
 int32_t vkrt_cuda_get_stats(VKRT_CudaContext* c, VKRT_CudaStats* st) {
@@ -1224,6 +1224,8 @@ int32_t vkrt_cuda_get_stats(VKRT_CudaContext* c, VKRT_CudaStats* st) {
     st->bvhTriangleCount = c->bvh.triCount;
     st->bvhBytes = uint64_t(c->bvh.nodeCount) * sizeof(WideNode) + uint64_t(c->bvh.triCount) * sizeof(TriRecord);
     st->bvhBuildMs = c->bvhStats.buildMs;
+    st->bvhSahLbvh = c->bvhStats.sahLbvh;
+    st->bvhSahTreelets = c->bvhStats.sahTreelets;
     return VKRT_CUDA_SUCCESS;
 }
 
