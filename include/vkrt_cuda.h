@@ -81,7 +81,7 @@ typedef struct VKRT_CudaStats {
     float bvhBuildMs;        /* device time of the last BVH build */
     uint32_t errorFlags;     /* device-side error word (bit 0: traversal stack overflow guard hit) */
     uint32_t wavefrontBodies;      /* wavefront loop bodies (two bounces each) of the last call */
-    uint32_t reserved0;
+    uint32_t cacheTrainingRecords; /* radiance-cache training records gathered by the last call (cache enabled) */
     uint64_t shadowNodeFetchBytes; /* any-hit traversal node / triangle bytes (same conditions as nodeFetchBytes) */
     uint64_t shadowTriFetchBytes;
     uint64_t kernelLaunches;       /* this backend's kernel launches made by the last call */

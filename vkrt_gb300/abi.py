@@ -86,7 +86,7 @@ WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight
 
 STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathSamples", "nodeFetchBytes",
                             "triFetchBytes", "bvhNodeCount", "bvhTriangleCount", "bvhBytes", "bvhBuildMs",
-                            "errorFlags", "wavefrontBodies", "reserved0", "shadowNodeFetchBytes",
+                            "errorFlags", "wavefrontBodies", "cacheTrainingRecords", "shadowNodeFetchBytes",
                             "shadowTriFetchBytes", "kernelLaunches", "stageMs", "bvhSahLbvh", "bvhSahTreelets"],
                   "formats": ["<u8", "<u8", "<u8", "<u8", "<u8", "<u8", "<u4", "<u4", "<u8", "<f4", "<u4", "<u4",
                               "<u4", "<u8", "<u8", "<u8", ("<f4", 8), "<f4", "<f4"],

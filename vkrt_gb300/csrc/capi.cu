@@ -1219,6 +1219,7 @@ int32_t vkrt_cuda_get_stats(VKRT_CudaContext* c, VKRT_CudaStats* st) {
     if (c->wavefront) {
         const float* ms = c->wavefront->lastStageMs();
         for (int i = 0; i < 8; ++i) st->stageMs[i] = ms[i];
+        st->cacheTrainingRecords = c->wavefront->lastCacheRecords();
     }
     st->bvhNodeCount = c->bvh.nodeCount;
     st->bvhTriangleCount = c->bvh.triCount;

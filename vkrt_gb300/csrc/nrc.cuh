@@ -93,41 +93,46 @@ VKRT_DEV void nrcSH16(float3 d, float* o) {
     o[15] = 0.59004358992664352f * x * (-xx + 3.0f * yy);
 }
 
-// The 64 network inputs of one vertex (FP16), hash features read from `table` (levels x entries x 2 halves).
-VKRT_DEV void nrcEncode(const NrcGridInfo& gi, const __half2* __restrict__ table, const NrcInput& in, __half* out) {
-    const float3 u = nrcUnit(gi, xyz(in.posRough));
-#pragma unroll 4
-    for (int l = 0; l < kNrcLevels; ++l) {
-        uint32_t c[3];
-        float f[3];
-        nrcCell(gi, l, u, c, f);
-        float a0 = 0.0f, a1 = 0.0f;
+// The two interpolated hash features of one level (network inputs 2l, 2l+1), read from `table` (levels x entries x
+// 2 halves), as an FP16 pair.
+VKRT_DEV __half2 nrcEncodeLevel(const NrcGridInfo& gi, const __half2* __restrict__ table, float3 u, int l) {
+    uint32_t c[3];
+    float f[3];
+    nrcCell(gi, l, u, c, f);
+    float a0 = 0.0f, a1 = 0.0f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t dx = k & 1u, dy = (k >> 1) & 1u, dz = (k >> 2) & 1u;
-            const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-            const float2 v = __half22float2(table[size_t(l) * kNrcTable + nrcIndex(gi, l, c[0] + dx, c[1] + dy, c[2] + dz)]);
-            a0 += w * v.x;
-            a1 += w * v.y;
-        }
-        out[2 * l] = __float2half_rn(a0);
-        out[2 * l + 1] = __float2half_rn(a1);
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t dx = k & 1u, dy = (k >> 1) & 1u, dz = (k >> 2) & 1u;
+        const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+        const float2 v = __half22float2(table[size_t(l) * kNrcTable + nrcIndex(gi, l, c[0] + dx, c[1] + dy, c[2] + dz)]);
+        a0 += w * v.x;
+        a1 += w * v.y;
     }
-    float sh[16];
-    nrcSH16(xyz(in.dirMetal), sh);
+    return __floats2half2_rn(a0, a1);
+}
+
+// Network inputs 32 + 2q and 33 + 2q (q = 0..15) of one vertex: spherical harmonics, then the material inputs.
+VKRT_DEV __half2 nrcEncodeTail(const NrcInput& in, int q) {
+    if (q < 8) {
+        float sh[16];
+        nrcSH16(xyz(in.dirMetal), sh);
+        float lo = sh[0], hi = sh[1];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) out[32 + i] = __float2half_rn(sh[i]);
-    out[48] = __float2half_rn(in.normal.x);
-    out[49] = __float2half_rn(in.normal.y);
-    out[50] = __float2half_rn(in.normal.z);
-    out[51] = __float2half_rn(in.posRough.w);
-    out[52] = __float2half_rn(in.albedo.x);
-    out[53] = __float2half_rn(in.albedo.y);
-    out[54] = __float2half_rn(in.albedo.z);
-    out[55] = __float2half_rn(in.dirMetal.w);
-    out[56] = __float2half_rn(1.0f);
-#pragma unroll
-    for (int i = 57; i < 64; ++i) out[i] = __float2half_rn(0.0f);
+        for (int i = 1; i < 8; ++i)
+            if (q == i) {
+                lo = sh[2 * i];
+                hi = sh[2 * i + 1];
+            }
+        return __floats2half2_rn(lo, hi);
+    }
+    switch (q) {
+        case 8: return __floats2half2_rn(in.normal.x, in.normal.y);
+        case 9: return __floats2half2_rn(in.normal.z, in.posRough.w);
+        case 10: return __floats2half2_rn(in.albedo.x, in.albedo.y);
+        case 11: return __floats2half2_rn(in.albedo.z, in.dirMetal.w);
+        case 12: return __floats2half2_rn(1.0f, 0.0f);
+        default: return __floats2half2_rn(0.0f, 0.0f);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -135,6 +140,8 @@ VKRT_DEV void nrcEncode(const NrcGridInfo& gi, const __half2* __restrict__ table
 // Lane (g = lane / 4, t = lane % 4) holds A rows g and g+8, columns 2t..2t+1 and 2t+8..2t+9; B column g, rows
 // 2t..2t+1 and 2t+8..2t+9; C rows g and g+8, columns 2t..2t+1. The C fragments of two adjacent 8-column tiles are
 // the A fragment of the next layer's 16-column slice, so activations stay in registers from layer to layer.
+// Weight matrices sit in shared memory as rows of 64 halves at a stride of 72 halves (144 bytes): the eight row
+// addresses of an ldmatrix phase then fall on eight distinct groups of four banks.
 // ---------------------------------------------------------------------------------------------------------------
 VKRT_DEV void mma16816(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
     asm volatile(
@@ -142,6 +149,23 @@ VKRT_DEV void mma16816(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ldmatrix.x4: four 8x8 FP16 matrices from shared memory; lane L gives the address of row L % 8 of matrix L / 8
+// (16 bytes, 16-byte aligned). Lane (g, t) receives of matrix q, in r[q], row g columns 2t..2t+1 (plain) or column g
+// rows 2t..2t+1 (transposed).
+VKRT_DEV void ldsm4(uint32_t* r, const __half* p) {
+    const uint32_t a = uint32_t(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+VKRT_DEV void ldsm4t(uint32_t* r, const __half* p) {
+    const uint32_t a = uint32_t(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
 }
 
 VKRT_DEV uint32_t packHalf2(float lo, float hi) {

@@ -38,7 +38,8 @@ public:
                       cudaStream_t stream);
 
     // parameter and gradient access for tests: FP16 weights (kNrcWeightCount) and table (kNrcTableParams halves);
-    // FP32 gradients of the last step with respect to the same parameters (already divided by the batch size)
+    // FP32 gradients of the last step with respect to the same parameters (already divided by the batch size); the
+    // table gradient is consumed (cleared) by a step that applies the update
     __half* weights() { return wHalf_; }
     __half* table() { return reinterpret_cast<__half*>(table_); }
     float* weightGrad() { return wGrad_; }
@@ -58,12 +59,14 @@ private:
     float *wMaster_ = nullptr, *wM_ = nullptr, *wV_ = nullptr, *wGrad_ = nullptr;
     __half2* table_ = nullptr;
     float *tMaster_ = nullptr, *tM_ = nullptr, *tV_ = nullptr, *tGrad_ = nullptr;
+    bool tGradClear_ = false;  // the table gradient is all zeros (the sparse Adam step clears what it consumes)
     // scratch for n rows
     uint32_t cap_ = 0;
     __half *x0_ = nullptr, *acts_ = nullptr, *dz_ = nullptr, *dy_ = nullptr;
     __half* x0Infer_ = nullptr;
     uint32_t capInfer_ = 0;
     float* dx0_ = nullptr;
+    uint32_t* masks_ = nullptr;  // ReLU masks of the forward pass, 5 x tiles x 32 words
     float4* out_ = nullptr;
 };
 

@@ -1080,6 +1080,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         });
     };
 
+    B.lastRecords = 0;
     if (useCache) {
         // train the cache on this frame's training paths before rendering with it
         e = cudaMemsetAsync(B.recCount, 0, sizeof(uint32_t), stream);

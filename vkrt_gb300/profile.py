@@ -5,6 +5,8 @@
 prints one JSON line: rays by kind, node/triangle fetch bytes (with --stage-launches, which launches the wavefront
 stages one by one and times them), per-stage device milliseconds and the frame's device time. Under ncu, the kernels of
 every rendered frame (warm-up included) are captured; --warmup 0 --frames 1 keeps the capture to one frame.
+--cache renders with the radiance cache (default settings: 2^16 training paths and 4 training steps per frame, render
+paths ending at bounce 2), so its training and inference kernels run in every frame.
 """
 from __future__ import annotations
 
@@ -28,6 +30,7 @@ def main(argv=None) -> dict:
     ap.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
     ap.add_argument("--stage-launches", action="store_true")
     ap.add_argument("--rgb", action="store_true", help="RGB transport instead of hero spectral")
+    ap.add_argument("--cache", action="store_true", help="render with the radiance cache (wavefront only)")
     a = ap.parse_args(argv)
     import torch
 
@@ -41,6 +44,8 @@ def main(argv=None) -> dict:
     ctx.upload_scene(scene)
     if a.stage_launches:
         ctx.set_wavefront_config(profileStages=1)
+    if a.cache:
+        ctx.nrc_configure(enabled=1)
     stream = torch.cuda.ExternalStream(ctx.stream)
     sd = scene.scene_data.copy()
     out = {}
@@ -54,7 +59,8 @@ def main(argv=None) -> dict:
         st = ctx.stats()
         if f >= a.warmup:
             for k in ("primaryRays", "extensionRays", "shadowRays", "nodeFetchBytes", "triFetchBytes",
-                      "shadowNodeFetchBytes", "shadowTriFetchBytes", "kernelLaunches", "wavefrontBodies"):
+                      "shadowNodeFetchBytes", "shadowTriFetchBytes", "kernelLaunches", "wavefrontBodies",
+                      "cacheTrainingRecords"):
                 out[k] = out.get(k, 0) + int(st[k])
             ms = dict(zip(abi.WAVEFRONT_STAGES, st["stageMs"]))
             for k, v in ms.items():
@@ -62,7 +68,7 @@ def main(argv=None) -> dict:
             out["frame_ms"] = round(out.get("frame_ms", 0.0) + ev[0].elapsed_time(ev[1]), 3)
     out["workload"] = {"width": a.width, "height": a.height, "spp": a.spp, "depth": a.depth, "spheres": a.spheres,
                        "triangles": scene.triangle_count, "frames": a.frames, "integrator": a.integrator,
-                       "mode": "rgb" if a.rgb else "hero-spectral"}
+                       "mode": "rgb" if a.rgb else "hero-spectral", "cache": a.cache}
     ctx.close()
     print(json.dumps(out))
     return out
