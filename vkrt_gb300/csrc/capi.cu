@@ -797,13 +797,14 @@ int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_C
     };
     VKRT_CudaWavefrontConfig cur;
     vkrt_cuda_default_wavefront_config(&cur);
-    cur.queueCapacity = uint32_t(std::min<uint64_t>(pixels, 1u << 21));
+    cur.queueCapacity = 0u;  // one slot per item, up to 64M
     float curMs = 0.0f;
     int32_t r = timeConfig(cur, curMs);
     if (r != VKRT_CUDA_SUCCESS) return r;
     // coordinate descent over the knobs, each axis scanned with the others fixed at the best so far
-    std::vector<uint32_t> qs;
-    for (uint64_t q = 1u << 18; q <= std::min<uint64_t>(pixels * 2, 1u << 23); q <<= 1) qs.push_back(uint32_t(q));
+    // slot counts: 0 (one per item of the trial, up to 64M) and 2M, 8M, 32M below that
+    std::vector<uint32_t> qs{0u};
+    for (uint64_t q = 1u << 21; q < std::min<uint64_t>(pixels * 2u, 1u << 26); q <<= 2) qs.push_back(uint32_t(q));
     const uint32_t tiles[][2] = {{8, 8}, {16, 8}, {32, 4}, {16, 16}, {32, 8}};
     for (int axis = 0; axis < 5; ++axis) {
         std::vector<VKRT_CudaWavefrontConfig> cands;

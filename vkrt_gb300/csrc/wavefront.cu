@@ -912,7 +912,10 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     }
     if (items >= 0xFFFFFFF0ull) return cudaErrorInvalidValue;  // item indices are 32-bit
     const uint32_t totalItems = uint32_t(items);
-    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, 1u << 22);
+    // default: one slot per item up to 64M slots (about 18 GB of slot state and queues). A slot that is refilled with
+    // a new item sits wherever the finished path left it, so refills scatter the slot-indexed state accesses of the
+    // next bounces; with a slot per item there are no refills.
+    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, 1u << 26);
     Q = std::max(1u, std::min(Q, std::max(totalItems, 1u)));
     // until the item cursor runs out every slot is busy, so the bounces of all items bound the iteration count;
     // the condition kernel counts two-iteration bodies

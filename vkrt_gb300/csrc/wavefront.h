@@ -34,7 +34,7 @@ struct WfScene {
 enum WavefrontMode : uint32_t { kWavefrontForward = 0, kWavefrontPrimal = 1, kWavefrontAdjoint = 2 };
 
 struct WavefrontConfig {
-    uint32_t queueCapacity;  // path slots; 0 = one per (pixel, sample) item, capped at 4M
+    uint32_t queueCapacity;  // path slots; 0 = one per (pixel, sample) item, capped at 64M
     uint32_t tileWidth;
     uint32_t tileHeight;
     uint32_t sortByMaterial;
