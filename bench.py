@@ -320,6 +320,25 @@ def batch_measure(local: int) -> dict:
                                                        "intersectBlocksPerSM", "shadeBlocksPerSM")}}
 
 
+def selection_overlay_measure(ctx, sd, stream, torch) -> dict:
+    """Selection mask (a pixel-centre ray per pixel against the picked mesh) plus outline on the benchmark frame:
+    the mesh under the film centre is selected; device ms per overlay call (CUDA events, mean of 5 after 1)."""
+    from vkrt_gb300 import abi
+    mesh = ctx.pick_mesh(sd, ctx.width // 2, ctx.height // 2)
+    osd = sd.copy()
+    osd["selectionEnabled"] = 1 if mesh != abi.INVALID_INDEX else 0
+    osd["selectedMeshIndex"] = mesh
+    ctx.render_selection_overlay(osd)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(5):
+        ctx.render_selection_overlay(osd)
+    b.record(stream)
+    b.synchronize()
+    return {"workload": f"{ctx.width}x{ctx.height}, mesh {mesh} (under the film centre) selected",
+            "ms": round(a.elapsed_time(b) / 5, 3), "mask_pixels": int(ctx.read_selection_mask().sum())}
+
+
 def run_ours(args) -> dict | None:
     import torch
     from vkrt_gb300 import RenderContext, abi
@@ -418,6 +437,8 @@ def run_ours(args) -> dict | None:
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_rays / e2e_s / 1e6
 
+    overlay = selection_overlay_measure(ctx, sd, stream, torch)
+
     result = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True,
@@ -445,6 +466,7 @@ def run_ours(args) -> dict | None:
                        "unit": "Mrays/s", "speedup_of_wavefront": round(mega_ms / mean_ms, 2)},
         "clocks": clk,
         "gpu_launches": int(launches),
+        "selection_overlay": overlay,
     }
     if rank == 0 and world == 1 and not args.no_adjoint:
         result["adjoint"] = adjoint_ratio(local)

@@ -317,6 +317,23 @@ int32_t vkrt_cuda_nrc_gradients(VKRT_CudaContext* context, float* weights, float
 /* Hash-grid placement: scene bounds (3 + 3 floats), per-level resolution and dense flag (16 each). */
 int32_t vkrt_cuda_nrc_grid(VKRT_CudaContext* context, float* lo, float* hi, uint32_t* resolution, uint32_t* dense);
 
+/* Selection overlay, replacing vkrt's selection trace and outline post-pass (entry/select/raygen.slang:5-14,
+ * entry/post/outline.slang:19-60, recorded by runtime/command/record.c when selection is enabled): when
+ * sceneData->selectionEnabled is set, traces the selection mask of sceneData->selectedMeshIndex (a pixel-centre
+ * camera ray per pixel, first hit on that mesh only) and draws its outline (colour (1, 0.55, 0.1), radius
+ * clamp(round(min(W, H) * 2 / 1080), 1, 5)) into the current output image; otherwise the mask is cleared.
+ * Call after the frame's render. Asynchronous on the context stream. */
+int32_t vkrt_cuda_render_selection_overlay(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData);
+/* Copies the last selection mask (width*height uint32, 1 = selected mesh) to host memory. Synchronous. */
+int32_t vkrt_cuda_read_selection_mask(VKRT_CudaContext* context, uint32_t* mask, size_t bytes);
+/* Pick query (VKRT_requestSelectionAtPixel, api/settings.c:236-245, answered in integrator/path/debug.slang:21-29):
+ * mesh index of the closest hit of pixel (x, y)'s centre ray, VKRT_CUDA_INVALID_INDEX on a miss. Synchronous. */
+int32_t vkrt_cuda_pick_mesh(VKRT_CudaContext* context, const VKRT_CudaSceneData* sceneData, uint32_t x, uint32_t y,
+                            uint32_t* meshIndex);
+/* Device milliseconds of the last vkrt_cuda_render_frame call (CUDA events on the context stream); waits for that
+ * frame to finish. The render time vkrt's auto-SPP controller reads (scene/timing.c:54-59). */
+int32_t vkrt_cuda_last_frame_ms(VKRT_CudaContext* context, float* milliseconds);
+
 /* Last error message of this context (never NULL). */
 const char* vkrt_cuda_last_error(VKRT_CudaContext* context);
 

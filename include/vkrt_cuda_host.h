@@ -58,6 +58,21 @@ void vkrt_host_build_alias_table(const float* pmf, uint32_t count, float* outQ, 
 /* vkrt's default Material (src/core/api/vkrt_types.h:79-121). */
 void vkrt_host_default_material(VKRT_CudaMaterial* material);
 
+/* Auto-SPP controller state (VKRT renderControl.autoSPP, src/core/scene/timing.c). */
+typedef struct VKRT_CudaAutoSpp {
+    float targetFrameMs; /* frame budget: 1000 / target FPS */
+    float controlMs;     /* smoothed milliseconds per sample per pixel; 0 = no measurement yet */
+} VKRT_CudaAutoSpp;
+
+/* VKRT_setAutoSPPTargetFPS (src/core/api/settings.c:68-79): 0 selects 60 (no display refresh here), then clamps to
+ * [30, 360]; resets the smoothed measurement. */
+void vkrt_host_auto_spp_init(VKRT_CudaAutoSpp* state, uint32_t targetFPS);
+
+/* updateAutoSPP (src/core/scene/timing.c:121-178): given the last frame's render milliseconds at *samplesPerPixel,
+ * updates the smoothed cost per sample and moves *samplesPerPixel toward 90% of the budget, within deadbands and
+ * step limits, in [1, 2048]. Returns 1 when *samplesPerPixel changed, 0 when not, -1 on invalid arguments. */
+int32_t vkrt_host_auto_spp_update(VKRT_CudaAutoSpp* state, float renderMs, uint32_t* samplesPerPixel);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,6 @@ script, the ctypes view of the ABI (abi.py), a thin Python host mirror (context.
 (scenes.py). Nothing here renders on the CPU.
 """
 from . import abi
-from .context import RenderContext, Scene, VkrtError, build_light_tables, pack_vertices
+from .context import AutoSpp, RenderContext, Scene, VkrtError, build_light_tables, pack_vertices
 
 __all__ = ["abi", "RenderContext", "Scene", "VkrtError", "build_light_tables", "pack_vertices"]

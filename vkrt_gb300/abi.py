@@ -133,6 +133,11 @@ def pack_render_settings(tone: int, mode: int, spectral: int) -> int:
     return (tone & 0xFFFF) | ((mode & 0xFF) << 16) | ((spectral & 0xFF) << 24)
 
 
+def unpack_render_settings(packed: int) -> tuple[int, int, int]:
+    """(tone mapping mode, render mode, spectral sampling mode)"""
+    return packed & 0xFFFF, (packed >> 16) & 0xFF, (packed >> 24) & 0xFF
+
+
 def ptr(a: np.ndarray | None) -> C.c_void_p:
     if a is None:
         return C.c_void_p(None)
@@ -190,6 +195,10 @@ EXPORTS = {
     "vkrt_cuda_nrc_parameters": (_I32, [_V, _V, _V, _U32]),
     "vkrt_cuda_nrc_gradients": (_I32, [_V, _V, _V]),
     "vkrt_cuda_nrc_grid": (_I32, [_V, _V, _V, _V, _V]),
+    "vkrt_cuda_render_selection_overlay": (_I32, [_V, _V]),
+    "vkrt_cuda_read_selection_mask": (_I32, [_V, _V, _SZ]),
+    "vkrt_cuda_pick_mesh": (_I32, [_V, _V, _U32, _U32, _V]),
+    "vkrt_cuda_last_frame_ms": (_I32, [_V, _V]),
     "vkrt_host_pack_shader_vertices": (None, [_V, _U32, _V]),
     "vkrt_host_mesh_transform": (None, [_V, _V, _V, _V]),
     "vkrt_host_camera_matrices": (None, [_V, _V, _V, _F, _F, _F, _U32, _U32, _V]),
@@ -197,7 +206,12 @@ EXPORTS = {
     "vkrt_host_build_light_tables": (_I32, [_V, _U32, _V, _U32, _V, _V, _V, _U32, _V, _U32, _V, _V, _V, _V, _V, _V]),
     "vkrt_host_build_alias_table": (None, [_V, _U32, _V, _V]),
     "vkrt_host_default_material": (None, [_V]),
+    "vkrt_host_auto_spp_init": (None, [_V, _U32]),
+    "vkrt_host_auto_spp_update": (_I32, [_V, _F, _V]),
 }
+
+# VKRT_CudaAutoSpp
+AUTO_SPP = np.dtype([("targetFrameMs", "<f4"), ("controlMs", "<f4")])
 
 _lib: C.CDLL | None = None
 

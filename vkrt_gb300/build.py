@@ -21,7 +21,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "libvkrt_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["bvh_build.cu", "render.cu", "wavefront.cu", "adjoint.cu", "nrc.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["bvh_build.cu", "render.cu", "wavefront.cu", "adjoint.cu", "nrc.cu", "overlay.cu", "capi.cu",
+              "noalloc.cu"]
 C_SOURCES = ["host/scene_host.c"]
 
 

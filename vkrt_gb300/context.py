@@ -39,6 +39,8 @@ class Scene:
     rgb2spec: np.ndarray | None = None    # float32 table in vkrt's layout
     emissive_mesh_materials: np.ndarray | None = None  # uint32, material of each emissive-mesh entry
     name: str = ""
+    mesh_names: list = field(default_factory=list)  # per MeshInfo (scene files)
+    notes: list = field(default_factory=list)       # what a loader dropped or ignored
 
     @property
     def triangle_count(self) -> int:
@@ -250,6 +252,28 @@ class RenderContext:
         self._check(self.lib.vkrt_cuda_read_output(self.handle, abi.ptr(out), out.nbytes), "read output")
         return out
 
+    # ---- selection passes and frame timing ---------------------------------------------------------------------
+    def render_selection_overlay(self, scene_data: np.ndarray) -> None:
+        """Selection mask of scene_data's selectedMeshIndex and its outline drawn into the output image."""
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA).reshape(1)
+        self._check(self.lib.vkrt_cuda_render_selection_overlay(self.handle, abi.ptr(sd)), "selection overlay")
+
+    def read_selection_mask(self) -> np.ndarray:
+        out = np.empty((self.height, self.width), dtype=np.uint32)
+        self._check(self.lib.vkrt_cuda_read_selection_mask(self.handle, abi.ptr(out), out.nbytes), "selection mask")
+        return out
+
+    def pick_mesh(self, scene_data: np.ndarray, x: int, y: int) -> int:
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA).reshape(1)
+        out = np.zeros(1, np.uint32)
+        self._check(self.lib.vkrt_cuda_pick_mesh(self.handle, abi.ptr(sd), x, y, abi.ptr(out)), "pick")
+        return int(out[0])
+
+    def last_frame_ms(self) -> float:
+        out = np.zeros(1, np.float32)
+        self._check(self.lib.vkrt_cuda_last_frame_ms(self.handle, abi.ptr(out)), "frame time")
+        return float(out[0])
+
     # ---- path-replay adjoint -----------------------------------------------------------------------------------
     def render_adjoint(self, scene_data: np.ndarray, d_image: np.ndarray, sample_base: int = 0, gradients: int = 0,
                        accumulate: bool = False) -> None:
@@ -378,3 +402,23 @@ def autotune_batch(contexts: list, scene_datas: np.ndarray, frames_per_trial: in
                                                  frames_per_trial, abi.ptr(best), C.byref(ms))
     contexts[0]._check(r, "autotune batch")
     return best, ms.value
+
+
+class AutoSpp:
+    """vkrt's auto-SPP controller (vkrt_host_auto_spp_*): feed it each frame's render milliseconds and the spp the
+    frame used; it returns the spp for the next frame."""
+
+    def __init__(self, target_fps: int = 60):
+        self.lib = abi.load()
+        self.state = np.zeros(1, dtype=abi.AUTO_SPP)
+        self.lib.vkrt_host_auto_spp_init(abi.ptr(self.state), int(target_fps))
+
+    @property
+    def target_ms(self) -> float:
+        return float(self.state["targetFrameMs"][0])
+
+    def update(self, render_ms: float, spp: int) -> int:
+        s = np.array([spp], np.uint32)
+        if self.lib.vkrt_host_auto_spp_update(abi.ptr(self.state), float(render_ms), abi.ptr(s)) < 0:
+            raise VkrtError("auto-SPP update: invalid arguments")
+        return int(s[0])

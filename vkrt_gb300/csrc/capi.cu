@@ -18,6 +18,7 @@
 #include "adjoint.h"
 #include "bvh_build.h"
 #include "nrc.h"
+#include "overlay.h"
 #include "context_view.h"
 #include "render.h"
 #include "wavefront.h"
@@ -134,6 +135,13 @@ struct VKRT_CudaContext {
     DeviceArray<NrcInput> nrcIn;
     DeviceArray<float4> nrcTarget, nrcOut;
     DeviceArray<float> nrcLoss;
+
+    // selection passes: mask of the selected mesh, pick result
+    DeviceArray<uint32_t> selectionMask;
+    DeviceArray<uint32_t> pickResult;
+    // device time of the last render call (events on the context's stream around it)
+    cudaEvent_t frameStart = nullptr, frameEnd = nullptr;
+    bool frameTimed = false;
 };
 
 namespace {
@@ -325,8 +333,11 @@ int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** out) 
     c->device = cfg.deviceIndex;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->order, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&c->frameStart) != cudaSuccess || cudaEventCreate(&c->frameEnd) != cudaSuccess ||
         cudaMalloc(&c->counters, sizeof(RenderCounters)) != cudaSuccess) {
         if (c->order) cudaEventDestroy(c->order);
+        if (c->frameStart) cudaEventDestroy(c->frameStart);
+        if (c->frameEnd) cudaEventDestroy(c->frameEnd);
         if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return VKRT_CUDA_ERROR_INITIALIZATION_FAILED;
@@ -376,9 +387,13 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     c->materialGrad.release();
     c->emissiveMeshMaterial.release();
     c->dImage.release();
+    c->selectionMask.release();
+    c->pickResult.release();
     if (c->counters) cudaFree(c->counters);
     c->wavefront.reset();
     if (c->order) cudaEventDestroy(c->order);
+    if (c->frameStart) cudaEventDestroy(c->frameStart);
+    if (c->frameEnd) cudaEventDestroy(c->frameEnd);
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -645,9 +660,15 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     int32_t v = validateFrame(c, sd);
     if (v != VKRT_CUDA_SUCCESS) return v;
     cudaSetDevice(c->device);
+    VKRT_TRY(c, cudaEventRecord(c->frameStart, c->stream), "frame timing");
     if (c->cfg.integrator == VKRT_CUDA_INTEGRATOR_WAVEFRONT) {
         VKRT_CudaContext* one[1] = {c};
-        return vkrt_cuda_render_batch(one, sd, 1);
+        int32_t r = vkrt_cuda_render_batch(one, sd, 1);
+        if (r == VKRT_CUDA_SUCCESS) {
+            VKRT_TRY(c, cudaEventRecord(c->frameEnd, c->stream), "frame timing");
+            c->frameTimed = true;
+        }
+        return r;
     }
     const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
     (void)spectral;
@@ -662,8 +683,62 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     FilmBuffers film{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "render");
     VKRT_TRY(c, launchRender(scene, *sd, rp, film, c->counters, c->cfg.threadsPerBlock, c->stream), "render launch");
+    VKRT_TRY(c, cudaEventRecord(c->frameEnd, c->stream), "frame timing");
+    c->frameTimed = true;
     c->readIndex ^= 1;  // VKRT_endFrame's ping-pong swap (frame.c:386-389)
     c->countersPending = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_last_frame_ms(VKRT_CudaContext* c, float* ms) {
+    if (!c || !ms) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!c->frameTimed) return invalid(c, "no frame rendered yet");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, cudaEventSynchronize(c->frameEnd), "frame timing");
+    VKRT_TRY(c, cudaEventElapsedTime(ms, c->frameStart, c->frameEnd), "frame timing");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_render_selection_overlay(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    int32_t v = validateFrame(c, sd);
+    if (v != VKRT_CUDA_SUCCESS) return v;
+    if (sd->selectionEnabled != 0u && sd->selectedMeshIndex != VKRT_CUDA_INVALID_INDEX &&
+        sd->selectedMeshIndex >= uint32_t(c->hostMeshes.size()))
+        return invalid(c, "selected mesh index out of range");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->selectionMask.reserve(size_t(c->width) * c->height), "selection mask");
+    DeviceScene scene = makeDeviceScene(c);
+    VKRT_TRY(c, launchSelectionMask(scene, *sd, c->width, c->height, c->selectionMask.ptr, c->stream), "selection mask");
+    if (sd->selectionEnabled != 0u)
+        VKRT_TRY(c, launchOutline(c->selectionMask.ptr, c->width, c->height, c->output.ptr, c->stream), "outline");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_read_selection_mask(VKRT_CudaContext* c, uint32_t* mask, size_t bytes) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    const size_t need = size_t(c->width) * c->height * sizeof(uint32_t);
+    if (!mask || bytes < need || !need) return invalid(c, "selection mask buffer too small");
+    if (c->selectionMask.count * sizeof(uint32_t) < need) return invalid(c, "no selection mask rendered yet");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, cudaMemcpyAsync(mask, c->selectionMask.ptr, need, cudaMemcpyDeviceToHost, c->stream), "read mask");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read mask");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_pick_mesh(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, uint32_t x, uint32_t y,
+                            uint32_t* meshIndex) {
+    if (!c || !meshIndex) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    int32_t v = validateFrame(c, sd);
+    if (v != VKRT_CUDA_SUCCESS) return v;
+    if (x >= c->width || y >= c->height) return invalid(c, "pick pixel outside the film");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->pickResult.reserve(1), "pick");
+    DeviceScene scene = makeDeviceScene(c);
+    VKRT_TRY(c, launchPick(scene, *sd, x, y, c->pickResult.ptr, c->stream), "pick");
+    VKRT_TRY(c, cudaMemcpyAsync(meshIndex, c->pickResult.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream),
+             "pick");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "pick");
     return VKRT_CUDA_SUCCESS;
 }
 

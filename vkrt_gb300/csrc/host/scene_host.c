@@ -453,3 +453,46 @@ int32_t vkrt_host_build_light_tables(VKRT_CudaMeshInfo* meshInfos, uint32_t mesh
     free(pmfScratch);
     return 0;
 }
+
+/* ---- auto-SPP: VKRT_setAutoSPPTargetFPS (src/core/api/settings.c:68-79), updateAutoSPP (scene/timing.c:121-178) */
+
+void vkrt_host_auto_spp_init(VKRT_CudaAutoSpp* state, uint32_t targetFPS) {
+    if (!state) return;
+    uint32_t fps = targetFPS ? targetFPS : 60u;
+    if (fps < 30u) fps = 30u;
+    if (fps > 360u) fps = 360u;
+    state->targetFrameMs = 1000.0f / (float)fps;
+    state->controlMs = 0.0f;
+}
+
+int32_t vkrt_host_auto_spp_update(VKRT_CudaAutoSpp* state, float renderMs, uint32_t* samplesPerPixel) {
+    /* exponential smoothing of the cost per sample, a 90% budget, asymmetric deadbands and step limits */
+    const float smoothing = 0.35f, budget = 0.90f;
+    const float upBand = 0.18f, downBand = 0.08f, upStep = 1.25f, downStep = 0.60f;
+    const uint32_t maxSpp = 2048u;
+    if (!state || !samplesPerPixel) return -1;
+    if (!(state->targetFrameMs > 0.0f) || !(renderMs > 0.0f)) return 0;
+    const uint32_t spp = *samplesPerPixel ? *samplesPerPixel : 1u;
+    const float sppf = (float)spp;
+    const float perSample = renderMs / sppf;
+    if (!(perSample > 0.0f)) return 0;
+    state->controlMs = state->controlMs <= 0.0f ? perSample
+                                                : state->controlMs * (1.0f - smoothing) + perSample * smoothing;
+    float desired = state->targetFrameMs * budget / state->controlMs;
+    desired = desired < 1.0f ? 1.0f : (desired > (float)maxSpp ? (float)maxSpp : desired);
+    const float delta = desired - sppf;
+    const float band = fmaxf(sppf * (delta > 0.0f ? upBand : downBand), 1.0f);
+    if (fabsf(delta) <= band) return 0;
+    uint32_t next;
+    if (delta > 0.0f) {
+        next = (uint32_t)floorf(fminf(desired, ceilf(sppf * upStep)));
+        if (next <= spp && spp < maxSpp) next = spp + 1u;
+    } else {
+        next = (uint32_t)ceilf(fmaxf(desired, floorf(sppf * downStep)));
+        if (next >= spp && spp > 1u) next = spp - 1u;
+    }
+    next = next < 1u ? 1u : (next > maxSpp ? maxSpp : next);
+    if (next == spp) return 0;
+    *samplesPerPixel = next;
+    return 1;
+}

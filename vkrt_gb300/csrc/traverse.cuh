@@ -192,9 +192,11 @@ struct TraversalStack {
 };
 
 // Closest hit (anyHit = false) or first accepted hit (anyHit = true).
-template <bool kAnyHit, bool kCount>
+// kMeshFilter: only triangles of mesh `meshFilter` count as hits (the selection-mask rays, which vkrt traces
+// against a TLAS holding the selected mesh alone).
+template <bool kAnyHit, bool kCount, bool kMeshFilter = false>
 VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* smemColumn, uint32_t smemStride,
-                           RenderCounters* counters) {
+                           RenderCounters* counters, uint32_t meshFilter = 0u) {
     TraceHit best;
     best.mesh = VKRT_CUDA_INVALID_INDEX;
     best.prim = VKRT_CUDA_INVALID_INDEX;
@@ -265,6 +267,7 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
             const float4* tp = reinterpret_cast<const float4*>(sc.tris + ti);
             float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
             if (kCount) triBytes += 48u;
+            if (kMeshFilter && __float_as_uint(b.w) != meshFilter) continue;
             float t, b1, b2;
             if (watertightHit(wr, org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
                               make_float3(c.x, c.y, c.z), tmin, tmax, t, b1, b2)) {
