@@ -205,6 +205,15 @@ int32_t vkrt_cuda_read_output(VKRT_CudaContext* context, uint16_t* rgba, size_t 
 
 int32_t vkrt_cuda_get_stats(VKRT_CudaContext* context, VKRT_CudaStats* stats);
 
+/* Denoiser features (integrator/path/loop.slang:83-111, writeback.slang:87-114): with enabled = 1, forward frames of
+ * either integrator also accumulate, per pixel, the albedo and shading normal of each sample's first vertex that is
+ * not followed through a sharp specular lobe (bsdf/principled/denoiser.slang), as running means weighted by the
+ * number of samples whose feature resolved (.w). The feature films are cleared with the accumulation.
+ * vkrt_cuda_read_denoiser_features copies the latest albedo and normal films (RGBA32F, width*height*16 bytes each;
+ * either pointer may be NULL). */
+int32_t vkrt_cuda_set_denoiser_features(VKRT_CudaContext* context, uint32_t enabled);
+int32_t vkrt_cuda_read_denoiser_features(VKRT_CudaContext* context, float* albedo, float* normal, size_t bytes);
+
 /* CUDA stream (cudaStream_t) the context launches on, for callers that time or order work around it. */
 void* vkrt_cuda_stream(VKRT_CudaContext* context);
 

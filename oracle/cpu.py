@@ -53,6 +53,7 @@ def load():
         "oracle_trace_fp64_bruteforce": (_I32, [_V, _V, _U32, _V, _V, _D, _U32]),
         "oracle_render": (_I32, [_V, _V, _V, _V, _V, _V, _V]),
         "oracle_render_f64": (_I32, [_V, _V, _V, _V, _V]),
+        "oracle_render_features": (_I32, [_V, _V, _V, _V, _V, _V, _V]),
         "oracle_hash": (_U32, [_U32]), "oracle_init_pixel_seed": (_U32, [C.c_int32, C.c_int32, _U32, _U32]),
         "oracle_rand": (_F, [_V]), "oracle_pcg32": (_U32, [_V, _U64]),
         "oracle_world_triangles": (_U32, [_V, _V, _U32]),
@@ -160,6 +161,22 @@ class OracleScene:
             raise RuntimeError(f"oracle_render failed ({r})")
         stats = {k: getattr(st, k) for k, _ in OracleRenderStats._fields_}
         return (acc_out, out, stats) if want_output else (acc_out, stats)
+
+    def render_features(self, scene_data, rng_mode=0, rng_seed=1, precision=32, threads=0):
+        """One frame from a cleared film: (accumulation, albedo, normal), each (H, W, 4) float32; the feature
+        images hold the frame's per-pixel means with .w = resolved samples."""
+        from vkrt_gb300 import abi
+        sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA)
+        w = int(sd["viewportRect"][0][0] + sd["viewportRect"][0][2])
+        h = int(sd["viewportRect"][0][1] + sd["viewportRect"][0][3])
+        acc_in = np.zeros((h, w, 4), np.float32)
+        acc_out, alb, nrm = (np.zeros((h, w, 4), np.float32) for _ in range(3))
+        p = OracleRenderParams(rng_mode, rng_seed, precision, threads, 0, 0, 0)
+        r = self.lib.oracle_render_features(self.handle, _p(sd), C.byref(p), _p(acc_in), _p(acc_out), _p(alb),
+                                            _p(nrm))
+        if r != 0:
+            raise RuntimeError(f"oracle_render_features failed ({r})")
+        return acc_out, alb, nrm
 
     def render_f64(self, scene_data, rng_mode=0, rng_seed=1, precision=64, threads=0):
         """One frame from a cleared film, the accumulation returned in float64 (H, W, 4)."""

@@ -861,6 +861,7 @@ struct MaterialR {  // Material fields the restated lobes read, after texturing
     V3<R> baseColor;
     R roughness, metallic, anisotropic, specular, specularTint, ior, transmission, subsurface, clearcoat;
     R sheenWeight;
+    V3<R> sheenTint;
     V3<R> eta, k;
     V3<R> emissionColor;
     R emissionLuminance;
@@ -1387,6 +1388,12 @@ bool envSample(const Scene& s, R u1, R u2, R rotDeg, V3<R>& dir, R& pdf) {
 // Integrators (integrator/path/**)
 // ---------------------------------------------------------------------------------------------------------
 template <class R>
+struct FeatureAcc {  // a sample's denoiser feature (integrator/path/state.slang DenoiserFeatures)
+    V3<R> albedo{R(0)}, normal{R(0)};
+    R weight = R(0);
+};
+
+template <class R>
 struct Ctx {
     const SceneFull& s;
     const VKRT_CudaSceneData& sd;
@@ -1394,7 +1401,44 @@ struct Ctx {
     bool bruteForce;
     const std::vector<std::array<double, 9>>* tri64;
     OracleRenderStats stats{};
+    FeatureAcc<R>* feat = nullptr;  // the current sample's feature, when features are rendered
 };
+
+// bsdf/principled/denoiser.slang:7-22
+template <class R>
+bool denoiserFollowsSpecular(const MaterialR<R>& m, uint32_t frontFace) {
+    R diffuseW = maxc(m.baseColor * (R(1) - m.metallic)) * (R(1) - m.transmission);
+    R subsurfaceW = diffuseW * m.subsurface;
+    R sheenW = maxc(sat(m.sheenTint) * sat(m.sheenWeight)) * (R(1) - m.transmission);
+    R clearcoatW = frontFace != 0u ? m.clearcoat : R(0);
+    const R eps = R(1e-3);
+    if (diffuseW > eps || subsurfaceW > eps || sheenW > eps || clearcoatW > eps) return false;
+    if (m.transmission > eps && m.ior <= R(1) + R(1e-4)) return true;
+    if (m.roughness > R(0.02)) return false;
+    return m.transmission > eps || m.metallic >= R(1) - eps || maxc(dielSpecF0(m)) > eps;
+}
+
+// bsdf/principled/denoiser.slang:24-44
+template <class R>
+V3<R> denoiserAlbedo(const MaterialR<R>& m) {
+    R nonMetal = R(1) - m.metallic;
+    V3<R> diffuse = m.baseColor * nonMetal;
+    V3<R> sheen = sat(m.sheenTint) * sat(m.sheenWeight);
+    V3<R> f0 = dielSpecF0(m);
+    bool conductor = m.k.x > R(0) || m.k.y > R(0) || m.k.z > R(0);
+    V3<R> metalF0 = conductor ? fresnelConductor(R(1), vmax(m.eta, V3<R>(R(1e-3))), vmax(m.k, V3<R>(R(0))))
+                              : sat(m.baseColor);
+    R wd = nonMetal * (R(1) - m.transmission) * (R(1) - m.subsurface);
+    R wss = nonMetal * (R(1) - m.transmission) * m.subsurface;
+    R ws = nonMetal * (R(1) - m.transmission) * sat(lum(f0));
+    R wt = nonMetal * m.transmission;
+    R wm = m.metallic;
+    R wsh = maxc(sheen) * nonMetal * (R(1) - m.transmission);
+    R total = wd + wss + ws + wt + wm + wsh;
+    if (total <= R(0)) return sat(diffuse);
+    V3<R> a = diffuse * wd + diffuse * wss + f0 * ws + V3<R>(R(1)) * wt + metalF0 * wm + sheen * wsh;
+    return sat(a / total);
+}
 
 template <class R>
 HitRec traceClosest(Ctx<R>& c, V3<R> o, V3<R> d, bool primary) {
@@ -1438,6 +1482,7 @@ MaterialR<R> toMaterialR(const VKRT_CudaMaterial& m) {
     r.subsurface = R(m.subsurface);
     r.clearcoat = R(m.clearcoat);
     r.sheenWeight = R(m.sheenTintWeight[3]);
+    r.sheenTint = V3<R>(R(m.sheenTintWeight[0]), R(m.sheenTintWeight[1]), R(m.sheenTintWeight[2]));
     r.eta = V3<R>(R(m.eta[0]), R(m.eta[1]), R(m.eta[2]));
     r.k = V3<R>(R(m.k[0]), R(m.k[1]), R(m.k[2]));
     r.emissionColor = V3<R>(R(m.emissionColor[0]), R(m.emissionColor[1]), R(m.emissionColor[2]));
@@ -1460,6 +1505,15 @@ Vertex<R> makeVertex(Ctx<R>& c, const HitRec& h, V3<R> o, V3<R> d) {  // surface
     v.mat = toMaterialR<R>(m);
     applySurfaceTextures(c.s, m, v.surf.tex, v.mat);
     return v;
+}
+
+// integrator/path/loop.slang:83-103: the first vertex that is not followed through a sharp specular lobe
+template <class R>
+void captureFeature(Ctx<R>& c, const Vertex<R>& v) {
+    if (!c.feat || c.feat->weight > R(0) || denoiserFollowsSpecular(v.mat, v.surf.frontFace)) return;
+    c.feat->albedo = denoiserAlbedo(v.mat);
+    c.feat->normal = v.surf.shadingNormal;
+    c.feat->weight = R(1);
 }
 
 template <class R>
@@ -1570,6 +1624,7 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
         }
         if (!anyPositive(thr)) break;
         Vertex<R> v = makeVertex(c, h, o, d);
+        captureFeature(c, v);
         BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace);
         V3<R> contrib(R(0));
         bool vertexNeeSupported = true;
@@ -1680,6 +1735,7 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
         }
         if (!anyPositive(thr)) break;
         Vertex<R> v = makeVertex(c, h, o, d);
+        captureFeature(c, v);
         BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace);
         V4<R> contrib(R(0));
         bool vertexNeeSupported = true;
@@ -1779,7 +1835,8 @@ void tonemapPixel(const VKRT_CudaSceneData& sd, V3<float> acc, bool spectral, ui
 template <class R>
 void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderParams& p, const float* accIn,
                 float* accOut, uint16_t* outImg, OracleRenderStats* statsOut,
-                const std::vector<std::array<double, 9>>* tri64, double* accOut64 = nullptr) {
+                const std::vector<std::array<double, 9>>* tri64, double* accOut64 = nullptr,
+                float* albedoOut = nullptr, float* normalOut = nullptr) {
     uint32_t W = sd.viewportRect[0] + sd.viewportRect[2];
     uint32_t H = sd.viewportRect[1] + sd.viewportRect[3];
     uint32_t r0 = p.rowBegin, r1 = p.rowEnd ? std::min(p.rowEnd, H) : H;
@@ -1813,10 +1870,28 @@ void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderPa
             float prev[4] = {accIn[pi * 4 + 0], accIn[pi * 4 + 1], accIn[pi * 4 + 2], accIn[pi * 4 + 3]};
             uint32_t prevN = uint32_t(prev[3] + 0.5f);  // state.slang:72
             V3<R> sum(R(0));
+            FeatureAcc<R> fsum;
             for (uint32_t si = 0; si < spp; ++si) {
                 uint32_t gi = prevN + si;
+                FeatureAcc<R> f;
+                c.feat = albedoOut ? &f : nullptr;
                 sum += spectral ? traceHeroSample(c, mf, int(x), int(y), gi, p.rngMode, p.rngSeed)
                                 : traceRgbSample(c, mf, int(x), int(y), gi, p.rngMode, p.rngSeed);
+                fsum.albedo += f.albedo;
+                fsum.normal += f.normal;
+                fsum.weight += f.weight;
+            }
+            if (albedoOut && normalOut) {  // the frame's feature means and their weight (writeback.slang:9-22)
+                V3<R> a = fsum.weight > R(0) ? fsum.albedo / fsum.weight : V3<R>(R(0));
+                V3<R> n = fsum.weight > R(0) ? fsum.normal / fsum.weight : V3<R>(R(0));
+                albedoOut[pi * 4 + 0] = float(a.x);
+                albedoOut[pi * 4 + 1] = float(a.y);
+                albedoOut[pi * 4 + 2] = float(a.z);
+                albedoOut[pi * 4 + 3] = float(fsum.weight);
+                normalOut[pi * 4 + 0] = float(n.x);
+                normalOut[pi * 4 + 1] = float(n.y);
+                normalOut[pi * 4 + 2] = float(n.z);
+                normalOut[pi * 4 + 3] = float(fsum.weight);
             }
             // writeback.slang:9-22,72-114
             V3<R> cur = sum / R(spp);
@@ -2039,6 +2114,19 @@ int32_t oracle_render_f64(void* p, const VKRT_CudaSceneData* sd, const OracleRen
         renderRows<double>(h->s, *sd, *params, accIn, acc32.data(), nullptr, nullptr, &h->tri64, accOut64);
     else
         renderRows<float>(h->s, *sd, *params, accIn, acc32.data(), nullptr, nullptr, &h->tri64, accOut64);
+    return 0;
+}
+
+int32_t oracle_render_features(void* p, const VKRT_CudaSceneData* sd, const OracleRenderParams* params,
+                               const float* accIn, float* accOut, float* albedoOut, float* normalOut) {
+    SceneHandle* h = static_cast<SceneHandle*>(p);
+    if (!h || !sd || !params || !accIn || !accOut || !albedoOut || !normalOut) return -1;
+    if (params->precision == 64)
+        renderRows<double>(h->s, *sd, *params, accIn, accOut, nullptr, nullptr, &h->tri64, nullptr, albedoOut,
+                           normalOut);
+    else
+        renderRows<float>(h->s, *sd, *params, accIn, accOut, nullptr, nullptr, &h->tri64, nullptr, albedoOut,
+                          normalOut);
     return 0;
 }
 

@@ -82,6 +82,10 @@ int32_t oracle_render(void* scene, const VKRT_CudaSceneData* sceneData, const Or
 
 /* Same frame with the accumulation written in double precision (the image before its FP32 store), for
  * finite-difference checks of gradients. */
+/* oracle_render with the denoiser features: albedoOut / normalOut receive the frame's per-pixel feature means
+ * (RGBA32F, .w = number of samples whose feature resolved). */
+int32_t oracle_render_features(void* scene, const VKRT_CudaSceneData* sceneData, const OracleRenderParams* params,
+                               const float* accIn, float* accOut, float* albedoOut, float* normalOut);
 int32_t oracle_render_f64(void* scene, const VKRT_CudaSceneData* sceneData, const OracleRenderParams* params,
                           const float* accumIn, double* accumOut);
 

@@ -199,6 +199,8 @@ EXPORTS = {
     "vkrt_cuda_read_selection_mask": (_I32, [_V, _V, _SZ]),
     "vkrt_cuda_pick_mesh": (_I32, [_V, _V, _U32, _U32, _V]),
     "vkrt_cuda_last_frame_ms": (_I32, [_V, _V]),
+    "vkrt_cuda_set_denoiser_features": (_I32, [_V, _U32]),
+    "vkrt_cuda_read_denoiser_features": (_I32, [_V, _V, _V, _SZ]),
     "vkrt_host_pack_shader_vertices": (None, [_V, _U32, _V]),
     "vkrt_host_mesh_transform": (None, [_V, _V, _V, _V]),
     "vkrt_host_camera_matrices": (None, [_V, _V, _V, _F, _F, _F, _U32, _U32, _V]),

@@ -252,6 +252,18 @@ class RenderContext:
         self._check(self.lib.vkrt_cuda_read_output(self.handle, abi.ptr(out), out.nbytes), "read output")
         return out
 
+    # ---- denoiser features --------------------------------------------------------------------------------------
+    def set_denoiser_features(self, enabled: bool = True) -> None:
+        self._check(self.lib.vkrt_cuda_set_denoiser_features(self.handle, 1 if enabled else 0), "denoiser features")
+
+    def read_denoiser_features(self):
+        """(albedo, normal), each (height, width, 4) float32 with .w = resolved samples."""
+        a = np.empty((self.height, self.width, 4), np.float32)
+        n = np.empty_like(a)
+        self._check(self.lib.vkrt_cuda_read_denoiser_features(self.handle, abi.ptr(a), abi.ptr(n), a.nbytes),
+                    "read features")
+        return a, n
+
     # ---- selection passes and frame timing ---------------------------------------------------------------------
     def render_selection_overlay(self, scene_data: np.ndarray) -> None:
         """Selection mask of scene_data's selectedMeshIndex and its outline drawn into the output image."""

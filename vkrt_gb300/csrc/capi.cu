@@ -106,6 +106,9 @@ struct VKRT_CudaContext {
     // film
     DeviceArray<float4> accum[2];
     DeviceArray<ushort4> output;
+    // denoiser feature films (albedo, shading normal; .w = resolved samples), ping-ponged with the accumulation
+    bool features = false;
+    DeviceArray<float4> albedo[2], normal[2];
     uint32_t width = 0, height = 0;
     int readIndex = 0;
 
@@ -194,6 +197,30 @@ cudaError_t rebuildBvh(VKRT_CudaContext* c) {
     return buildBvh(in, c->bvh, &c->bvhStats, c->stream);
 }
 
+FilmBuffers filmOf(VKRT_CudaContext* c) {
+    FilmBuffers f{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
+    if (c->features) {
+        f.albedoRead = c->albedo[c->readIndex].ptr;
+        f.albedoWrite = c->albedo[c->readIndex ^ 1].ptr;
+        f.normalRead = c->normal[c->readIndex].ptr;
+        f.normalWrite = c->normal[c->readIndex ^ 1].ptr;
+    }
+    return f;
+}
+
+cudaError_t clearFeatureFilms(VKRT_CudaContext* c) {
+    if (!c->features || !c->width) return cudaSuccess;
+    const size_t bytes = size_t(c->width) * c->height * sizeof(float4);
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = c->albedo[i].reserve(size_t(c->width) * c->height);
+        if (e == cudaSuccess) e = c->normal[i].reserve(size_t(c->width) * c->height);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->albedo[i].ptr, 0, bytes, c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->normal[i].ptr, 0, bytes, c->stream);
+    }
+    return e;
+}
+
 DeviceScene makeDeviceScene(VKRT_CudaContext* c) {
     if (c->textureTableDirty) {
         c->textureTable.assign(c->textureDescs.data(), c->textureDescs.size(), c->stream);
@@ -279,7 +306,7 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
     std::memset(&S, 0, sizeof(S));
     S.sc = makeDeviceScene(c);
     S.sd = sd;
-    S.film = FilmBuffers{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
+    S.film = filmOf(c);
     S.filmWidth = c->width;
     S.filmHeight = c->height;
     S.vx0 = sd.viewportRect[0];
@@ -389,6 +416,10 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     c->dImage.release();
     c->selectionMask.release();
     c->pickResult.release();
+    for (int i = 0; i < 2; ++i) {
+        c->albedo[i].release();
+        c->normal[i].release();
+    }
     if (c->counters) cudaFree(c->counters);
     c->wavefront.reset();
     if (c->order) cudaEventDestroy(c->order);
@@ -643,6 +674,7 @@ int32_t vkrt_cuda_resize(VKRT_CudaContext* c, uint32_t w, uint32_t h) {
     c->height = h;
     c->readIndex = 0;
     VKRT_TRY(c, launchClearFilm(c->accum[0].ptr, c->accum[1].ptr, c->output.ptr, n, c->stream), "film clear");
+    VKRT_TRY(c, clearFeatureFilms(c), "feature films");
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -652,6 +684,40 @@ int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* c) {
     cudaSetDevice(c->device);
     VKRT_TRY(c, launchClearFilm(c->accum[0].ptr, c->accum[1].ptr, c->output.ptr, size_t(c->width) * c->height, c->stream),
              "film clear");
+    VKRT_TRY(c, clearFeatureFilms(c), "feature films");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_set_denoiser_features(VKRT_CudaContext* c, uint32_t enabled) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (enabled > 1u) return invalid(c, "denoiser features: 0 or 1");
+    cudaSetDevice(c->device);
+    if ((enabled != 0u) == c->features) return VKRT_CUDA_SUCCESS;
+    c->features = enabled != 0u;
+    if (!c->features) {
+        for (int i = 0; i < 2; ++i) {
+            c->albedo[i].release();
+            c->normal[i].release();
+        }
+        return VKRT_CUDA_SUCCESS;
+    }
+    VKRT_TRY(c, clearFeatureFilms(c), "feature films");
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_read_denoiser_features(VKRT_CudaContext* c, float* albedo, float* normal, size_t bytes) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!c->features) return invalid(c, "denoiser features are off");
+    const size_t need = size_t(c->width) * c->height * sizeof(float4);
+    if (!need || bytes < need || (!albedo && !normal)) return invalid(c, "feature buffers too small");
+    cudaSetDevice(c->device);
+    if (albedo)
+        VKRT_TRY(c, cudaMemcpyAsync(albedo, c->albedo[c->readIndex].ptr, need, cudaMemcpyDeviceToHost, c->stream),
+                 "read features");
+    if (normal)
+        VKRT_TRY(c, cudaMemcpyAsync(normal, c->normal[c->readIndex].ptr, need, cudaMemcpyDeviceToHost, c->stream),
+                 "read features");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read features");
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -680,7 +746,7 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     rp.width = c->width;
     rp.height = c->height;
     rp.countBytes = c->cfg.countRays;
-    FilmBuffers film{c->accum[c->readIndex].ptr, c->accum[c->readIndex ^ 1].ptr, c->output.ptr};
+    FilmBuffers film = filmOf(c);
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "render");
     VKRT_TRY(c, launchRender(scene, *sd, rp, film, c->counters, c->cfg.threadsPerBlock, c->stream), "render launch");
     VKRT_TRY(c, cudaEventRecord(c->frameEnd, c->stream), "frame timing");

@@ -19,6 +19,7 @@ namespace vkrt {
 
 constexpr uint32_t kPathPrevNee = 1u;  // the previous vertex sampled NEE (loop.slang:69-71)
 constexpr uint32_t kPathDone = 2u;
+constexpr uint32_t kPathFeatureDone = 4u;  // the sample's denoiser feature was taken at an earlier vertex
 
 struct PathState {
     Rng rng;
@@ -103,6 +104,26 @@ struct NoVertexHook {
     VKRT_DEV void neeEnvironment(uint32_t, const Bsdf&, float3, float3, float3, float3) {}
     VKRT_DEV void bsdfSample(const Bsdf&, float3, float3) {}
     VKRT_DEV void cacheQuery(const Surface&, const ShadeMaterial&) {}
+};
+
+// A sample's denoiser feature (integrator/path/state.slang DenoiserFeatures): albedo and shading normal of the first
+// vertex that is not followed through a sharp specular lobe (integrator/path/loop.slang:83-103); weight 1 once taken.
+struct DenoiserFeature {
+    float3 albedo;
+    float3 normal;
+    float weight;
+};
+
+VKRT_DEV void captureFeature(DenoiserFeature& f, const Surface& s, const ShadeMaterial& m) {
+    if (f.weight > 0.0f || denoiserFollowsSpecular(m)) return;
+    f.albedo = denoiserAlbedo(m);
+    f.normal = s.shadingNormal;
+    f.weight = 1.0f;
+}
+
+struct FeatureHook : NoVertexHook {
+    DenoiserFeature* f;
+    VKRT_DEV void surface(const Surface& s, const ShadeMaterial& m, const Bsdf&) { captureFeature(*f, s, m); }
 };
 
 // Processes the hit of p's current ray. Returns true when the path continues with a new ray in p.o / p.d.

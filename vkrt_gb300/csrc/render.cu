@@ -19,7 +19,7 @@ namespace {
 
 // One pixel: SceneData.samplesPerPixel paths, each traced to the end (shadow rays traced inline), blended into the
 // running mean (writeback.slang:72-114) and encoded for display.
-template <bool kSpectral, bool kCountBytes>
+template <bool kSpectral, bool kCountBytes, bool kFeatures>
 __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, VKRT_CudaSceneData sd, RenderParams rp,
                                                                FilmBuffers film, RenderCounters* counters) {
     extern __shared__ uint2 smemStack[];
@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
         if (!inside) {
             film.accumWrite[pixel] = f4(0.0f);
             film.output[pixel] = make_ushort4(0, 0, 0, 0);
+            if (kFeatures) film.albedoWrite[pixel] = film.normalWrite[pixel] = f4(0.0f);
         } else {
             KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
             const float4 prev = film.accumRead[pixel];
@@ -43,8 +44,10 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                            rp.rngSeed};
             SpecTable tab = makeSpecTable(sc, sd);
             float3 sum = f3(0.0f);
+            DenoiserFeature fsum{f3(0.0f), f3(0.0f), 0.0f};
             for (uint32_t si = 0; si < spp; ++si) {
                 PathState p = beginPath<kSpectral>(cfg, sd, px, py, prevN + si);
+                DenoiserFeature feat{f3(0.0f), f3(0.0f), 0.0f};
                 pc.samples++;
                 for (;;) {
                     if (p.depth == 0) pc.primary++;
@@ -52,7 +55,11 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     TraceHit h = closest<kCountBytes>(k, p.o, p.d);
                     ShadowRequest sh[2];
                     uint32_t ns;
-                    bool cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
+                    bool cont;
+                    if (kFeatures)
+                        cont = shadePathVertex<kSpectral, FeatureHook>(sc, sd, cfg, tab, p, h, sh, ns,
+                                                                       FeatureHook{{}, &feat});
+                    else cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
                     for (uint32_t i = 0; i < ns; ++i) {
                         pc.shadow++;
                         TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
@@ -63,6 +70,15 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     if (!cont) break;
                 }
                 sum += pathResult<kSpectral>(cfg, p);
+                if (kFeatures) {
+                    fsum.albedo += feat.albedo;
+                    fsum.normal += feat.normal;
+                    fsum.weight += feat.weight;
+                }
+            }
+            if (kFeatures) {
+                blendFeature(film.albedoRead, film.albedoWrite, pixel, fsum.albedo, fsum.weight);
+                blendFeature(film.normalRead, film.normalWrite, pixel, fsum.normal, fsum.weight);
             }
             float3 cur = sum / float(spp);
             float pw = float(prevN), tw = pw + float(spp);
@@ -353,13 +369,26 @@ cudaError_t launchRender(const DeviceScene& sc, const VKRT_CudaSceneData& sd, co
     const uint32_t blocks = uint32_t((pixels + threads - 1) / threads);
     const size_t smem = size_t(threads) * VKRT_SMEM_STACK * sizeof(uint2);
     const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
+    const bool features = film.albedoWrite != nullptr;
+#define VKRT_MEGA(S, C, F) kRenderMega<S, C, F><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters)
     if (spectral) {
-        if (rp.countBytes) kRenderMega<true, true><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters);
-        else kRenderMega<true, false><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters);
+        if (features) {
+            if (rp.countBytes) VKRT_MEGA(true, true, true);
+            else VKRT_MEGA(true, false, true);
+        } else {
+            if (rp.countBytes) VKRT_MEGA(true, true, false);
+            else VKRT_MEGA(true, false, false);
+        }
     } else {
-        if (rp.countBytes) kRenderMega<false, true><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters);
-        else kRenderMega<false, false><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters);
+        if (features) {
+            if (rp.countBytes) VKRT_MEGA(false, true, true);
+            else VKRT_MEGA(false, false, true);
+        } else {
+            if (rp.countBytes) VKRT_MEGA(false, true, false);
+            else VKRT_MEGA(false, false, false);
+        }
     }
+#undef VKRT_MEGA
     return cudaGetLastError();
 }
 

@@ -20,7 +20,22 @@ struct FilmBuffers {
     float4* accumRead;
     float4* accumWrite;
     ushort4* output;
+    // denoiser feature films (albedo, shading normal; .w = resolved samples), ping-ponged like the accumulation;
+    // null when the context does not render features
+    float4* albedoRead = nullptr;
+    float4* albedoWrite = nullptr;
+    float4* normalRead = nullptr;
+    float4* normalWrite = nullptr;
 };
+
+// writeback.slang:72-114 for a feature film: the frame mean (sum / weight) blended into the running mean by weight
+VKRT_DEV void blendFeature(const float4* read, float4* write, size_t pix, float3 sum, float weight) {
+    const float4 prev = read[pix];
+    const float tw = prev.w + weight;
+    float3 v = f3(0.0f);
+    if (tw > 0.0f) v = (xyz(prev) * prev.w + sum) / tw;
+    write[pix] = make_float4(v.x, v.y, v.z, tw);
+}
 
 // One frame of vkrt's ray-generation pass (entry/path/raygen_rgb.slang / raygen_spectral_hero.slang).
 cudaError_t launchRender(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const RenderParams& rp,

@@ -410,6 +410,30 @@ VKRT_DEV float3 dielSpecF0(const ShadeMaterial& m) {  // fresnel.slang:15-20
     return sat(tt * (d * (m.specular / 0.5f)));
 }
 
+VKRT_DEV float3 fresnelConductor(float cosT, float3 eta, float3 k);
+
+// Denoiser features (bsdf/principled/denoiser.slang:7-46) on the shaded subset, where the transmission, subsurface,
+// sheen and clearcoat layers are absent: a vertex whose only visible response is a sharp specular lobe is followed
+// through; the first other vertex gives the feature albedo (a weighted mix of the diffuse colour, the dielectric
+// and the metallic F0) and its shading normal.
+VKRT_DEV bool denoiserFollowsSpecular(const ShadeMaterial& m) {
+    if (maxc(m.baseColor * (1.0f - m.metallic)) > 1e-3f) return false;  // a visible base layer
+    if (m.roughness > 0.02f) return false;
+    return m.metallic >= 1.0f - 1e-3f || maxc(dielSpecF0(m)) > 1e-3f;
+}
+
+VKRT_DEV float3 denoiserAlbedo(const ShadeMaterial& m) {
+    const float nonMetal = 1.0f - m.metallic;
+    const float3 diffuse = m.baseColor * nonMetal;
+    const float3 f0 = dielSpecF0(m);
+    const float3 metalF0 =
+        m.conductor ? fresnelConductor(1.0f, fmax3(m.eta, f3(1e-3f)), fmax3(m.k, f3(0.0f))) : sat(m.baseColor);
+    const float wd = nonMetal, ws = nonMetal * sat(lum(f0)), wm = m.metallic;
+    const float total = wd + ws + wm;
+    if (total <= 0.0f) return sat(diffuse);
+    return sat((diffuse * wd + f0 * ws + metalF0 * wm) / total);
+}
+
 VKRT_DEV float fresnelDielectric(float cosT, float eta) {  // fresnel.slang:31-48
     float ci = fminf(fmaxf(cosT, -1.0f), 1.0f);
     if (ci < 0.0f) {

@@ -118,6 +118,11 @@ struct WfGlobals {
     NrcInput* nrcQueries;  // Q inputs of the iteration's queries
     uint32_t* slotQuery;   // query position of a slot whose path ended at the cache
     float4* nrcPred;       // predictions, by query position
+    // denoiser features (forward frames of scenes with feature films): per (pixel, sample) item, albedo and shading
+    // normal of the first non-specular vertex, .w = 1 once taken
+    uint32_t features;
+    float4* itemFeatA;
+    float4* itemFeatN;
 };
 
 VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
@@ -264,6 +269,10 @@ VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t sl
         if (startSample<kSpectral>(g, scenes, slot, sceneId, local / S.spp, local % S.spp)) {
             g.slotScene[slot] = sceneId;
             g.slotItem[slot] = local;
+            if (g.features) {
+                g.itemFeatA[size_t(S.itemBase) + local] = f4(0.0f);
+                g.itemFeatN[size_t(S.itemBase) + local] = f4(0.0f);
+            }
             if (g.mode == kWavefrontAdjoint) g.adjTotal[slot] = g.sampleBuf[size_t(S.itemBase) + local];
             return true;
         }
@@ -309,6 +318,19 @@ __global__ void kWfResolve(WfGlobals g) {
         float3 acc = tw <= 0.0f ? f3(0.0f) : (xyz(prev) * pw + cur * float(S.spp)) / tw;
         S.film.accumWrite[pix] = make_float4(acc.x, acc.y, acc.z, tw);
         S.film.output[pix] = encodeOutput(S.sd, acc, kSpectral);
+        if (g.features && S.film.albedoWrite) {
+            const float4* fa = g.itemFeatA + size_t(S.itemBase) + size_t(local) * S.spp;
+            const float4* fn = g.itemFeatN + size_t(S.itemBase) + size_t(local) * S.spp;
+            float3 as = f3(0.0f), ns = f3(0.0f);
+            float wsum = 0.0f;
+            for (uint32_t s = 0; s < S.spp; ++s) {
+                as += xyz(fa[s]);
+                ns += xyz(fn[s]);
+                wsum += fa[s].w;
+            }
+            blendFeature(S.film.albedoRead, S.film.albedoWrite, pix, as, wsum);
+            blendFeature(S.film.normalRead, S.film.normalWrite, pix, ns, wsum);
+        }
     }
 }
 
@@ -323,6 +345,7 @@ __global__ void kWfClearOutside(WfGlobals g) {
             if (x >= S.vx0 && y >= S.vy0 && x < S.vx0 + S.vw && y < S.vy0 + S.vh) continue;
             S.film.accumWrite[p] = f4(0.0f);
             S.film.output[p] = make_ushort4(0, 0, 0, 0);
+            if (S.film.albedoWrite) S.film.albedoWrite[p] = S.film.normalWrite[p] = f4(0.0f);
         }
     }
 }
@@ -453,11 +476,16 @@ VKRT_DEV NrcInput nrcInputOf(const Surface& s, const ShadeMaterial& m, float3 ra
     return in;
 }
 
-// forward-pass hook: records the radiance-cache query of a path that ends at the cache
+// forward-pass hook: records the radiance-cache query of a path that ends at the cache, and the denoiser feature
+// (feat = null when features are off)
 struct CacheHook : NoVertexHook {
     NrcInput* in;
     bool* queried;
     float3 rayDir;
+    DenoiserFeature* feat;
+    VKRT_DEV void surface(const Surface& s, const ShadeMaterial& m, const Bsdf&) {
+        if (feat) captureFeature(*feat, s, m);
+    }
     VKRT_DEV void cacheQuery(const Surface& s, const ShadeMaterial& m) {
         *in = nrcInputOf(s, m, rayDir);
         *queried = true;
@@ -611,7 +639,9 @@ VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t sl
                  xyz(g.adjTotal[slot]), xyz(radiance));
 }
 
-template <bool kSpectral, bool kAdjoint, int kMinBlocks>
+// kFeatures: the frame also takes denoiser features (a separate instantiation, so frames without them keep the
+// register budget of the plain kernel)
+template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFeatures = false>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
     const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
@@ -659,8 +689,17 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                 if (g.adj.wantEmission && av.emitted) scatterHitEmission(S.sc, g.adj, smemMat, av);
                 adjStoreVertex(g, slot, av, cont);
             } else {
+                const bool featDone = (p.flags & kPathFeatureDone) != 0u;
+                DenoiserFeature feat{f3(0.0f), f3(0.0f), featDone ? 1.0f : 0.0f};
                 cont = shadePathVertex<kSpectral, CacheHook>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
-                                                             CacheHook{{}, &query, &queried, p.d});
+                                                             CacheHook{{}, &query, &queried, p.d,
+                                                                       kFeatures ? &feat : nullptr});
+                if (kFeatures && !featDone && feat.weight > 0.0f) {
+                    const size_t item = size_t(S.itemBase) + g.slotItem[slot];
+                    g.itemFeatA[item] = make_float4(feat.albedo.x, feat.albedo.y, feat.albedo.z, 1.0f);
+                    g.itemFeatN[item] = make_float4(feat.normal.x, feat.normal.y, feat.normal.z, 0.0f);
+                    p.flags |= kPathFeatureDone;
+                }
             }
             storePath(g, slot, p);
             uint32_t flags = queried ? kPendCache : 0u;
@@ -829,7 +868,8 @@ struct WavefrontEngine::Buffers {
     size_t capQ = 0, capKeys = 0, capScenes = 0;
     size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
            c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
-           c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0;
+           c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0,
+           c_fA = 0, c_fN = 0;
     size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
     WfScene* scenes = nullptr;
     uint32_t* bases = nullptr;  // itemBase of every scene, then workBase
@@ -936,6 +976,14 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(slotScene, c_scene, Q);
     WF_GROW(slotItem, c_work, Q);
     WF_GROW(sampleBuf, c_sum, std::max<size_t>(totalItems, 1));
+    bool features = false;  // forward frames render denoiser features when any scene has feature films
+    if (mode == kWavefrontForward)
+        for (const WfScene& S : scenes)
+            if (S.film.albedoWrite) features = true;
+    if (features) {
+        WF_GROW(itemFeatA, c_fA, std::max<size_t>(totalItems, 1));
+        WF_GROW(itemFeatN, c_fN, std::max<size_t>(totalItems, 1));
+    }
     WF_GROW(hitA, c_hitA, Q);
     WF_GROW(hitV, c_hitV, Q);
     WF_GROW(hitKey, c_key, Q);
@@ -990,6 +1038,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         if (e != cudaSuccess) return e;
     }
     g.mode = uint32_t(mode);
+    g.features = features ? 1u : 0u;
     g.adj = adjoint ? *adjoint : AdjointParams{};
     g.cacheDepth = useCache ? cache->cacheDepth : 0xFFFFFFFFu;
     g.scenes = B.scenes;
@@ -1046,6 +1095,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         stage(kStageShade, [&] {
             // register budget follows the requested residency: 128 (4 blocks/SM), 80 (6) or 64 (8) registers
             if (adjMode) kWfShade<false, true, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (features && spectral) kWfShade<true, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (features) kWfShade<false, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 8) kWfShade<true, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 6) kWfShade<true, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
