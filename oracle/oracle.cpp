@@ -860,6 +860,7 @@ template <class R>
 struct MaterialR {  // Material fields the restated lobes read, after texturing
     V3<R> baseColor;
     R roughness, metallic, anisotropic, specular, specularTint, ior, transmission, subsurface, clearcoat;
+    R clearcoatGloss, diffuseRoughness;
     R sheenWeight;
     V3<R> sheenTint;
     V3<R> eta, k;
@@ -1066,8 +1067,71 @@ template <class R> bool sampleVndf(V3<R> wo, const Ggx<R>& g, R u1, R u2, V3<R>&
 
 template <class R>
 struct Weights {
-    R metal = 0, dielectric = 0, diffuse = 0;
+    R metal = 0, dielectric = 0, diffuse = 0, coat = 0, subsurface = 0;
 };
+
+// Disney clearcoat (bsdf/lobes/clearcoat.slang) and the coat's directional attenuation (attenuation.slang:13-24)
+template <class R> R clearcoatAlpha(const MaterialR<R>& m) {
+    R g = sat(m.clearcoatGloss);
+    return std::max(R(0.1) + (R(0.001) - R(0.1)) * g, R(1e-3));
+}
+template <class R> R clearcoatG1(R c, R a) {
+    R a2 = a * a, c2 = std::max(c * c, R(1e-6));
+    R t2 = std::max(R(1) - c2, R(0)) / c2;
+    return R(2) / (R(1) + std::sqrt(R(1) + a2 * t2));
+}
+template <class R> R clearcoatD(R cm, R a) {
+    R a2 = a * a;
+    if (a2 >= R(1) - R(1e-6)) return R(kInvPi);
+    R den = R(kPi) * std::log(a2) * (R(1) + (a2 - R(1)) * cm * cm);
+    return (a2 - R(1)) / std::min(den, R(-1e-6));
+}
+template <class R> R evalClearcoat(R weight, R a, V3<R> wo, V3<R> wi, R& pdf) {
+    pdf = R(0);
+    if (weight <= R(0) || wo.z <= R(0) || wi.z <= R(0)) return R(0);
+    V3<R> h = safeNormalize(wo + wi);
+    R woh = sat(dot(wo, h));
+    if (woh <= R(0)) return R(0);
+    R D = clearcoatD(sat(h.z), a);
+    R F = R(0.04) + (R(1) - R(0.04)) * schlickW(woh);
+    R G = clearcoatG1(wo.z, R(0.25)) * clearcoatG1(wi.z, R(0.25));
+    pdf = D * sat(h.z) / std::max(R(4) * woh, R(1e-6));
+    return R(0.25) * weight * D * F * G / std::max(R(4) * wo.z * wi.z, R(1e-6));
+}
+template <class R> R coatDirAtten(const MaterialR<R>& m, V3<R> w) {
+    if (m.clearcoat <= R(0)) return R(1);
+    R c = std::fabs(w.z);
+    if (c <= R(0)) return R(0);
+    return R(1) - sat(R(0.25) * m.clearcoat * (R(0.04) + (R(1) - R(0.04)) * schlickW(c)));
+}
+
+// Oren-Nayar and the Disney fake subsurface for a unit colour (bsdf/lobes/diffuse.slang:20-53, subsurface.slang)
+template <class R> R orenNayarUnit(R rough, V3<R> wo, V3<R> wi) {
+    if (wo.z <= R(0) || wi.z <= R(0)) return R(0);
+    R sg = sat(rough) * (R(0.5) * R(kPi)), sg2 = sg * sg;
+    R A = R(1) - sg2 / (R(2) * (sg2 + R(0.33)));
+    R B = R(0.45) * sg2 / (sg2 + R(0.09));
+    R s2i = sat(R(1) - wi.z * wi.z), s2o = sat(R(1) - wo.z * wo.z);
+    R si = std::sqrt(s2i), so = std::sqrt(s2o);
+    R cphi = R(0);
+    if (s2i > R(0) && s2o > R(0))
+        cphi = std::min(std::max((wi.x * wo.x + wi.y * wo.y) / std::sqrt(s2i * s2o), R(-1)), R(1));
+    R mc = std::max(R(0), cphi);
+    bool inSteeper = std::fabs(wi.z) > std::fabs(wo.z);
+    R sinA = inSteeper ? so : si;
+    R tanB = inSteeper ? si / std::max(std::fabs(wi.z), R(1e-6)) : so / std::max(std::fabs(wo.z), R(1e-6));
+    return R(kInvPi) * (A + B * mc * sinA * tanB);
+}
+template <class R> R fakeSubsurfaceUnit(R rough, V3<R> wo, V3<R> wi) {
+    if (wo.z <= R(0) || wi.z <= R(0)) return R(0);
+    V3<R> h = safeNormalize(wo + wi);
+    R wih = sat(dot(wi, h));
+    R f90 = wih * wih * rough;
+    R fin = R(1) + (f90 - R(1)) * schlickW(wi.z);
+    R fout = R(1) + (f90 - R(1)) * schlickW(wo.z);
+    R ss = R(1.25) * (fin * fout * (R(1) / std::max(wi.z + wo.z, R(1e-6)) - R(0.5)) + R(0.5));
+    return R(kInvPi) * ss;
+}
 
 template <class R> V3<R> dielDirAlbedo(const MaterialR<R>& m, V3<R> w) {  // attenuation.slang:30-47
     if (std::fabs(w.z) <= R(0)) return V3<R>(R(1));
@@ -1088,19 +1152,24 @@ template <class R> Weights<R> branchWeights(const MaterialR<R>& m, V3<R> wo) {  
     R baseScatter = nonMetal * (R(1) - m.transmission);
     R dielSpecW = nonMetal * std::max(sat(lum(dielSpecF0(m))) + R(0), R(0));
     R dielAtt = lum(dielDirAtten(m, wo));
+    R viewCoat = coatDirAtten(m, wo);
     Weights<R> w;
-    w.metal = m.metallic * baseW;
-    w.dielectric = dielSpecW;
-    w.diffuse = dielAtt * baseScatter * (R(1) - m.subsurface) * diffW;
-    R total = w.metal + w.dielectric + w.diffuse;
+    w.coat = m.clearcoat * R(0.25);
+    w.metal = viewCoat * m.metallic * baseW;
+    w.dielectric = viewCoat * dielSpecW;
+    w.diffuse = viewCoat * dielAtt * baseScatter * (R(1) - m.subsurface) * diffW;
+    w.subsurface = viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
+    R total = w.coat + w.metal + w.dielectric + w.diffuse + w.subsurface;
     if (total <= R(0)) {
-        w.metal = w.dielectric = R(0);
+        w.metal = w.dielectric = w.coat = w.subsurface = R(0);
         w.diffuse = R(1);
         return w;
     }
+    w.coat /= total;
     w.metal /= total;
     w.dielectric /= total;
     w.diffuse /= total;
+    w.subsurface /= total;
     return w;
 }
 
@@ -1166,15 +1235,29 @@ template <class R> void evalRgb(const BsdfState<R>& s, V3<R> wi, V3<R>& value, R
             }
         }
     }
-    if (s.w.diffuse > R(0)) {  // evalLambertian (diffuse.slang:13-18)
-        V3<R> dc = s.mat.baseColor * (R(1) - s.mat.metallic);
+    R coat = R(0);
+    if (s.w.coat > R(0)) {
+        R cp;
+        coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
+        pdf += s.w.coat * cp;
+    }
+    V3<R> dc = s.mat.baseColor * (R(1) - s.mat.metallic);
+    if (s.w.diffuse > R(0)) {  // evalLambertian / evalOrenNayar (diffuse.slang:13-53)
         V3<R> dw = dc * ((R(1) - s.mat.transmission) * (R(1) - s.mat.subsurface));
-        sub = wi.z > R(0) ? dw * R(kInvPi) : V3<R>(R(0));
+        R unit = s.mat.diffuseRoughness <= R(0) ? (wi.z > R(0) ? R(kInvPi) : R(0))
+                                                 : orenNayarUnit(s.mat.diffuseRoughness, s.wo, wi);
+        sub = dw * unit;
         pdf += s.w.diffuse * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0));
+    }
+    if (s.w.subsurface > R(0)) {  // evalFakeSubsurface (subsurface.slang:12-31)
+        V3<R> sw = dc * ((R(1) - s.mat.transmission) * s.mat.subsurface);
+        sub += sw * fakeSubsurfaceUnit(s.mat.diffuseRoughness, s.wo, wi);
+        pdf += s.w.subsurface * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0));
     }
     V3<R> viewAtt = dielDirAtten(s.mat, s.wo);
     R nonMetal = R(1) - s.mat.metallic;
-    value = metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal;
+    R att = coatDirAtten(s.mat, s.wo) * coatDirAtten(s.mat, wi);  // reflectionStackAttenuation
+    value = V3<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att;
 }
 
 // 4-lane spectral reflection stack (principled/eval_spectral.slang:4-94), same subset
@@ -1212,21 +1295,49 @@ template <class R> V4<R> evalSpectral(const BsdfState<R>& s, const Rgb2Spec& tab
             }
         }
     }
-    if (s.w.diffuse > R(0)) {
+    R coat = R(0);
+    if (s.w.coat > R(0)) {
+        R cp;
+        coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
+        tp += V4<R>(s.w.coat * cp);
+    }
+    if (s.w.diffuse > R(0) || s.w.subsurface > R(0)) {
         V4<R> dc = spectralScalar4(tab, sat(s.mat.baseColor * (R(1) - s.mat.metallic)), l);
-        R scale = (R(1) - s.mat.transmission) * (R(1) - s.mat.subsurface);
-        R val = wi.z > R(0) ? scale * R(kInvPi) : R(0);
-        sub = dc * val;
-        tp += V4<R>(s.w.diffuse * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0)));
+        if (s.w.diffuse > R(0)) {
+            R scale = (R(1) - s.mat.transmission) * (R(1) - s.mat.subsurface);
+            R unit = s.mat.diffuseRoughness <= R(0) ? (wi.z > R(0) ? R(kInvPi) : R(0))
+                                                     : orenNayarUnit(s.mat.diffuseRoughness, s.wo, wi);
+            sub = dc * (scale * unit);
+            tp += V4<R>(s.w.diffuse * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0)));
+        }
+        if (s.w.subsurface > R(0)) {
+            R scale = (R(1) - s.mat.transmission) * s.mat.subsurface;
+            sub += dc * (scale * fakeSubsurfaceUnit(s.mat.diffuseRoughness, s.wo, wi));
+            tp += V4<R>(s.w.subsurface * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0)));
+        }
     }
     V4<R> viewAtt = spectralScalar4(tab, sat(dielDirAtten(s.mat, s.wo)), l);
     R nonMetal = R(1) - s.mat.metallic;
-    return metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal;
+    R att = coatDirAtten(s.mat, s.wo) * coatDirAtten(s.mat, wi);
+    return V4<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att;
 }
 
 // sampleBSDFDirection (principled/sample.slang:4-51), subset
 template <class R> bool sampleDirection(const BsdfState<R>& s, Rng& rng, V3<R>& wi) {
     R sel = R(rng.next());
+    if (sel < s.w.coat) {  // sampleClearcoat (clearcoat.slang:73-97)
+        R u1 = R(rng.next()), u2 = R(rng.next());
+        R a = clearcoatAlpha(s.mat), a2 = a * a, cm;
+        if (a2 >= R(1) - R(1e-6)) cm = std::sqrt(std::max(R(0), R(1) - u1));
+        else cm = std::sqrt(sat((R(1) - std::pow(a2, R(1) - u1)) / std::max(R(1) - a2, R(1e-6))));
+        R sm = std::sqrt(sat(R(1) - cm * cm)), phi = R(2) * R(kPi) * u2;
+        V3<R> m(sm * std::cos(phi), sm * std::sin(phi), cm);
+        R wom = dot(s.wo, m);
+        if (wom <= R(0)) return false;
+        wi = m * (R(2) * wom) - s.wo;
+        return wi.z > R(0);
+    }
+    sel -= s.w.coat;
     if (sel < s.w.metal) {  // sampleGGX (ggx.slang:211-227)
         R u1 = R(rng.next()), u2 = R(rng.next());
         V3<R> m;
@@ -1248,7 +1359,7 @@ template <class R> bool sampleDirection(const BsdfState<R>& s, Rng& rng, V3<R>& 
         wi = m * (R(2) * wom) - s.wo;
         return wi.z > R(0);
     }
-    // diffuse (and the fallback branch) -> cosine hemisphere (math.slang:42-48)
+    // diffuse, subsurface (and the fallback branch) -> cosine hemisphere (math.slang:42-48)
     R u1 = R(rng.next()), u2 = R(rng.next());
     R r = std::sqrt(u1), phi = R(2) * R(kPi) * u2;
     wi = V3<R>(r * std::cos(phi), r * std::sin(phi), std::sqrt(std::max(R(0), R(1) - u1)));
@@ -1481,6 +1592,8 @@ MaterialR<R> toMaterialR(const VKRT_CudaMaterial& m) {
     r.transmission = R(m.transmission);
     r.subsurface = R(m.subsurface);
     r.clearcoat = R(m.clearcoat);
+    r.clearcoatGloss = R(m.clearcoatGloss);
+    r.diffuseRoughness = R(m.diffuseRoughness);
     r.sheenWeight = R(m.sheenTintWeight[3]);
     r.sheenTint = V3<R>(R(m.sheenTintWeight[0]), R(m.sheenTintWeight[1]), R(m.sheenTintWeight[2]));
     r.eta = V3<R>(R(m.eta[0]), R(m.eta[1]), R(m.eta[2]));

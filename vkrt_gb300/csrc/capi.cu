@@ -79,6 +79,7 @@ struct VKRT_CudaContext {
     DeviceArray<VKRT_CudaMaterial> materials;
     std::vector<VKRT_CudaMaterial> hostMaterials;
     uint32_t materialCount = 0;
+    bool extendedMaterials = false;  // some material has clearcoat, subsurface or diffuseRoughness above 0
     DeviceArray<VKRT_CudaEmissiveMesh> emissiveMeshes;
     DeviceArray<VKRT_CudaEmissiveTriangle> emissiveTriangles;
     DeviceArray<float> meshAliasQ, triAliasQ;
@@ -317,6 +318,7 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
     S.spectral = spectral ? 1u : 0u;
     S.neeEnabled = (sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u) ? 1u : 0u;
     S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
+    S.extended = c->extendedMaterials ? 1u : 0u;
     return S;
 }
 
@@ -516,6 +518,10 @@ int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* c, const VKRT_CudaMaterial*
     VKRT_TRY(c, c->materials.assign(materials, count, c->stream), "upload materials");
     c->hostMaterials.assign(materials, materials + count);
     c->materialCount = count;
+    c->extendedMaterials = false;
+    for (uint32_t i = 0; i < count; ++i)
+        if (materials[i].clearcoat > 0.0f || materials[i].subsurface > 0.0f || materials[i].diffuseRoughness > 0.0f)
+            c->extendedMaterials = true;
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -746,6 +752,7 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     rp.width = c->width;
     rp.height = c->height;
     rp.countBytes = c->cfg.countRays;
+    rp.extended = c->extendedMaterials ? 1u : 0u;
     FilmBuffers film = filmOf(c);
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "render");
     VKRT_TRY(c, launchRender(scene, *sd, rp, film, c->counters, c->cfg.threadsPerBlock, c->stream), "render launch");
@@ -1190,8 +1197,11 @@ int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const f
     if (v != VKRT_CUDA_SUCCESS) return v;
     if (VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL)
         return invalid(c, "the adjoint differentiates the RGB render mode only");
-    for (const VKRT_CudaMaterial& m : c->hostMaterials)
+    for (const VKRT_CudaMaterial& m : c->hostMaterials) {
         if (m.specularTint != 0.0f) return invalid(c, "the adjoint needs specularTint 0 on every material");
+        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f)
+            return invalid(c, "the adjoint covers the metal / dielectric / Lambert stack only");
+    }
     VKRT_CudaAdjointConfig a{};
     if (cfg) a = *cfg;
     const uint32_t want = a.gradients ? a.gradients

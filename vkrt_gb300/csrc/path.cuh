@@ -128,7 +128,7 @@ struct FeatureHook : NoVertexHook {
 
 // Processes the hit of p's current ray. Returns true when the path continues with a new ray in p.o / p.d.
 // `shadows` receives up to two requests (count in `numShadows`).
-template <bool kSpectral, class Hook = NoVertexHook>
+template <bool kSpectral, class Hook = NoVertexHook, bool kExt = false>
 VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const StepConfig& cfg,
                               const SpecTable& tab, PathState& p, const TraceHit& h, ShadowRequest* shadows,
                               uint32_t& numShadows, Hook hook = Hook()) {
@@ -163,7 +163,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
     ShadeMaterial mat;
     Basis basis;
     shadeVertex(sc, s, p.d, mat, basis);
-    Bsdf bsdf = makeBsdf(mat, toLocal(-p.d, basis), s.frontFace);
+    Bsdf bsdf = makeBsdf<kExt>(mat, toLocal(-p.d, basis), s.frontFace);
     const float4 lam = heroLambdas(p.lamUnit);
     hook.surface(s, mat, bsdf);
 
@@ -204,13 +204,13 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             float pdf;
             float4 c = f4(0.0f);
             if (kSpectral) {
-                float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
+                float4 fcos = evalSpectral<kExt>(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
                 float lt = p.techPath * ls.pdfSA, bt = p.techPath * pdf;
                 float den = 4.0f * lt + 4.0f * bt;
                 float mis = den > 0.0f ? lt / den : 0.0f;
                 if (mis > 0.0f) c = p.thr * (fcos * spectral4(tab, ls.emission, lam) * (mis / ls.pdfSA));
             } else {
-                float3 f = evalRgb(bsdf, wl, pdf);
+                float3 f = evalRgb<kExt>(bsdf, wl, pdf);
                 if (pdf > 0.0f) {
                     float3 v = thr3(p) * (f * fabsf(wl.z) * ls.emission * (powerHeuristic(ls.pdfSA, pdf) / ls.pdfSA));
                     c = make_float4(v.x, v.y, v.z, 0.0f);
@@ -233,13 +233,13 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             float pdf;
             float4 c = f4(0.0f);
             if (kSpectral) {
-                float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
+                float4 fcos = evalSpectral<kExt>(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
                 float lt = p.techPath * pe, bt = p.techPath * pdf;
                 float den = 4.0f * lt + 4.0f * bt;
                 float mis = den > 0.0f ? lt / den : 0.0f;
                 if (mis > 0.0f) c = p.thr * (fcos * spectral4(tab, envRadiance(sc, sd, wi), lam) * (mis / pe));
             } else {
-                float3 f = evalRgb(bsdf, wl, pdf);
+                float3 f = evalRgb<kExt>(bsdf, wl, pdf);
                 if (pdf > 0.0f) {
                     float3 Le = envRadiance(sc, sd, wi);
                     float3 v = thr3(p) * (f * fabsf(wl.z) * Le * (powerHeuristic(pe, pdf) / pe));
@@ -256,10 +256,10 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
     // next direction (sample_rgb.slang:6-23 / sample_spectral.slang:6-24)
     if (bsdf.wo.z <= 0.0f) return false;
     float3 wl;
-    if (!sampleDirection(bsdf, p.rng, wl)) return false;
+    if (!sampleDirection<kExt>(bsdf, p.rng, wl)) return false;
     float pdf;
     if (kSpectral) {
-        float4 val = evalSpectral(bsdf, tab, wl, lam, pdf);
+        float4 val = evalSpectral<kExt>(bsdf, tab, wl, lam, pdf);
         if (!(pdf > 0.0f)) return false;
         float4 weight = val * (fabsf(wl.z) / pdf);
         if (!anyPos(weight)) return false;
@@ -268,7 +268,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
         p.techPath *= pdf;
         p.thr *= weight;
     } else {
-        float3 f = evalRgb(bsdf, wl, pdf);
+        float3 f = evalRgb<kExt>(bsdf, wl, pdf);
         if (!(pdf > 0.0f)) return false;
         float3 weight = f * (fabsf(wl.z) / pdf);
         if (!anyPos(weight)) return false;

@@ -19,7 +19,8 @@ namespace {
 
 // One pixel: SceneData.samplesPerPixel paths, each traced to the end (shadow rays traced inline), blended into the
 // running mean (writeback.slang:72-114) and encoded for display.
-template <bool kSpectral, bool kCountBytes, bool kFeatures>
+// kFull: the extended reflection stack and the denoiser features (written when the film has feature images)
+template <bool kSpectral, bool kCountBytes, bool kFull>
 __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, VKRT_CudaSceneData sd, RenderParams rp,
                                                                FilmBuffers film, RenderCounters* counters) {
     extern __shared__ uint2 smemStack[];
@@ -34,7 +35,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
         if (!inside) {
             film.accumWrite[pixel] = f4(0.0f);
             film.output[pixel] = make_ushort4(0, 0, 0, 0);
-            if (kFeatures) film.albedoWrite[pixel] = film.normalWrite[pixel] = f4(0.0f);
+            if (kFull && film.albedoWrite) film.albedoWrite[pixel] = film.normalWrite[pixel] = f4(0.0f);
         } else {
             KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
             const float4 prev = film.accumRead[pixel];
@@ -56,9 +57,9 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     ShadowRequest sh[2];
                     uint32_t ns;
                     bool cont;
-                    if (kFeatures)
-                        cont = shadePathVertex<kSpectral, FeatureHook>(sc, sd, cfg, tab, p, h, sh, ns,
-                                                                       FeatureHook{{}, &feat});
+                    if (kFull)
+                        cont = shadePathVertex<kSpectral, FeatureHook, true>(sc, sd, cfg, tab, p, h, sh, ns,
+                                                                             FeatureHook{{}, &feat});
                     else cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
                     for (uint32_t i = 0; i < ns; ++i) {
                         pc.shadow++;
@@ -70,13 +71,13 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     if (!cont) break;
                 }
                 sum += pathResult<kSpectral>(cfg, p);
-                if (kFeatures) {
+                if (kFull) {
                     fsum.albedo += feat.albedo;
                     fsum.normal += feat.normal;
                     fsum.weight += feat.weight;
                 }
             }
-            if (kFeatures) {
+            if (kFull && film.albedoWrite) {
                 blendFeature(film.albedoRead, film.albedoWrite, pixel, fsum.albedo, fsum.weight);
                 blendFeature(film.normalRead, film.normalWrite, pixel, fsum.normal, fsum.weight);
             }
@@ -369,7 +370,7 @@ cudaError_t launchRender(const DeviceScene& sc, const VKRT_CudaSceneData& sd, co
     const uint32_t blocks = uint32_t((pixels + threads - 1) / threads);
     const size_t smem = size_t(threads) * VKRT_SMEM_STACK * sizeof(uint2);
     const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
-    const bool features = film.albedoWrite != nullptr;
+    const bool features = film.albedoWrite != nullptr || rp.extended != 0u;
 #define VKRT_MEGA(S, C, F) kRenderMega<S, C, F><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters)
     if (spectral) {
         if (features) {

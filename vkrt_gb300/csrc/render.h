@@ -14,6 +14,7 @@ struct RenderParams {
     uint32_t width;      // film size (the viewport rectangle lives in SceneData)
     uint32_t height;
     uint32_t countBytes; // accumulate node / triangle fetch bytes
+    uint32_t extended;   // some material uses the extended reflection stack (clearcoat, Oren-Nayar, subsurface)
 };
 
 struct FilmBuffers {

@@ -3,8 +3,9 @@
 // importance distribution, and rgb2spec hero-wavelength spectral upsampling. Each function names the vkrt shader it
 // computes the same quantity as (paths relative to src/shaders/).
 //
-// Material subset: sheen, clearcoat, transmission, subsurface and Oren-Nayar (diffuseRoughness) are not evaluated;
-// their lobes have zero weight for materials with those parameters at 0, which is what this backend renders.
+// Material coverage: metal, dielectric specular and diffuse lobes always; clearcoat, Oren-Nayar (diffuseRoughness)
+// and fake subsurface in the extended instantiations (kExt), chosen when a scene's materials use them. Sheen (its
+// LTC fit table) and transmission (refraction, media, dispersion) are not evaluated: their lobes get no weight.
 #pragma once
 
 #include "scene.cuh"
@@ -342,6 +343,7 @@ struct ShadeMaterial {
     float3 eta, k;
     float3 emission;  // emissionColor * emissionLuminance after the emissive texture
     bool conductor;
+    float clearcoat, clearcoatGloss, subsurface, diffuseRoughness;  // the extended reflection stack's inputs
 };
 
 VKRT_DEV void shadeVertex(const DeviceScene& sc, Surface& s, float3 dir, ShadeMaterial& mat, Basis& basis) {
@@ -371,6 +373,10 @@ VKRT_DEV void shadeVertex(const DeviceScene& sc, Surface& s, float3 dir, ShadeMa
     mat.eta = make_float3(m.eta[0], m.eta[1], m.eta[2]);
     mat.k = make_float3(m.k[0], m.k[1], m.k[2]);
     mat.conductor = m.k[0] > 0.0f || m.k[1] > 0.0f || m.k[2] > 0.0f;
+    mat.clearcoat = m.clearcoat;
+    mat.clearcoatGloss = m.clearcoatGloss;
+    mat.subsurface = m.subsurface;
+    mat.diffuseRoughness = m.diffuseRoughness;
     float4 bc = sampleMaterialTexture(sc, m.baseColorTextureIndex, m.baseColorTextureWrap, m.baseColorTextureTransform,
                                       m.textureRotations[0], m.textureTexcoordSets & 0xffu, s.tex, f4(1.0f));
     mat.baseColor = mat.baseColor * xyz(bc) * xyz(s.tex.color);
@@ -518,12 +524,94 @@ VKRT_DEV bool sampleVndf(float3 wo, const Ggx& g, float u1, float u2, float3& m)
     return m.z > 0.0f;
 }
 
+// Extended reflection stack (principled/eval_rgb.slang:4-105 beyond the glTF subset): Disney clearcoat
+// (lobes/clearcoat.slang: GTR1 distribution, gloss-remapped alpha, fixed 0.25 masking roughness, Schlick F0 0.04, its
+// directional attenuation on everything below it), Oren-Nayar diffuse for diffuseRoughness > 0 and the Disney fake
+// subsurface lobe (lobes/diffuse.slang, lobes/subsurface.slang). Used by the kExt instantiations.
+VKRT_DEV float coatAlpha(const ShadeMaterial& m) {  // clearcoat.slang:20-28
+    return fmaxf(0.1f + (0.001f - 0.1f) * sat(m.clearcoatGloss), 1e-3f);
+}
+VKRT_DEV float coatG1(float c, float a) {  // clearcoat.slang:30-35
+    float a2 = a * a, c2 = fmaxf(c * c, 1e-6f);
+    float t2 = fmaxf(1.0f - c2, 0.0f) / c2;
+    return 2.0f / (1.0f + sqrtf(1.0f + a2 * t2));
+}
+VKRT_DEV float coatD(float cm, float a) {  // clearcoat.slang:37-45
+    float a2 = a * a;
+    if (a2 >= 1.0f - 1e-6f) return kInvPi;
+    float den = kPi * logf(a2) * (1.0f + (a2 - 1.0f) * cm * cm);
+    return (a2 - 1.0f) / fminf(den, -1e-6f);
+}
+VKRT_DEV float coatEval(float weight, float a, float3 wo, float3 wi, float& pdf) {  // clearcoat.slang:47-71
+    pdf = 0.0f;
+    if (weight <= 0.0f || wo.z <= 0.0f || wi.z <= 0.0f) return 0.0f;
+    float3 h = safeNormalize(wo + wi);
+    float woh = sat(dot(wo, h));
+    if (woh <= 0.0f) return 0.0f;
+    float D = coatD(sat(h.z), a);
+    float F = 0.04f + (1.0f - 0.04f) * pow5(1.0f - woh);
+    float G = coatG1(wo.z, 0.25f) * coatG1(wi.z, 0.25f);
+    pdf = D * sat(h.z) / fmaxf(4.0f * woh, 1e-6f);
+    return 0.25f * weight * D * F * G / fmaxf(4.0f * wo.z * wi.z, 1e-6f);
+}
+VKRT_DEV bool coatSample(float3 wo, float a, float u1, float u2, float3& wi) {  // clearcoat.slang:73-97
+    float a2 = a * a, cm;
+    if (a2 >= 1.0f - 1e-6f) cm = sqrtf(fmaxf(0.0f, 1.0f - u1));
+    else cm = sqrtf(sat((1.0f - powf(a2, 1.0f - u1)) / fmaxf(1.0f - a2, 1e-6f)));
+    float sm = sqrtf(sat(1.0f - cm * cm)), sp, cp;
+    sincosf(2.0f * kPi * u2, &sp, &cp);
+    float3 m = make_float3(sm * cp, sm * sp, cm);
+    float wom = dot(wo, m);
+    if (wom <= 0.0f) return false;
+    wi = m * (2.0f * wom) - wo;
+    return wi.z > 0.0f;
+}
+VKRT_DEV float coatAtten(const ShadeMaterial& m, float3 w) {  // attenuation.slang:13-24
+    if (m.clearcoat <= 0.0f) return 1.0f;
+    float c = fabsf(w.z);
+    if (c <= 0.0f) return 0.0f;
+    float f = 0.04f + (1.0f - 0.04f) * pow5(1.0f - sat(c));
+    return 1.0f - sat(0.25f * m.clearcoat * f);
+}
+VKRT_DEV float sin2Th(float3 w) { return sat(1.0f - w.z * w.z); }
+VKRT_DEV float orenNayar(float rough, float3 wo, float3 wi) {  // diffuse.slang:20-53, for a unit colour
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return 0.0f;
+    float sg = sat(rough) * (0.5f * kPi), sg2 = sg * sg;
+    float A = 1.0f - sg2 / (2.0f * (sg2 + 0.33f));
+    float B = 0.45f * sg2 / (sg2 + 0.09f);
+    float s2i = sin2Th(wi), s2o = sin2Th(wo);
+    float si = sqrtf(s2i), so = sqrtf(s2o);
+    float cphi = 0.0f;
+    if (s2i > 0.0f && s2o > 0.0f) cphi = fminf(fmaxf((wi.x * wo.x + wi.y * wo.y) * rsqrtf(s2i * s2o), -1.0f), 1.0f);
+    float maxCos = fmaxf(0.0f, cphi), sinA, tanB;
+    if (fabsf(wi.z) > fabsf(wo.z)) {
+        sinA = so;
+        tanB = si / fmaxf(fabsf(wi.z), 1e-6f);
+    } else {
+        sinA = si;
+        tanB = so / fmaxf(fabsf(wo.z), 1e-6f);
+    }
+    return kInvPi * (A + B * maxCos * sinA * tanB);
+}
+VKRT_DEV float fakeSss(float rough, float3 wo, float3 wi) {  // subsurface.slang:12-31, for a unit colour
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return 0.0f;
+    float3 h = safeNormalize(wo + wi);
+    float wih = sat(dot(wi, h));
+    float f90 = wih * wih * rough;
+    float fin = 1.0f + (f90 - 1.0f) * pow5(1.0f - sat(wi.z));
+    float fout = 1.0f + (f90 - 1.0f) * pow5(1.0f - sat(wo.z));
+    float ss = 1.25f * (fin * fout * (1.0f / fmaxf(wi.z + wo.z, 1e-6f) - 0.5f) + 0.5f);
+    return kInvPi * ss;
+}
+
 struct Bsdf {
     ShadeMaterial mat;
     float3 wo;
     Ggx ggx;
     uint32_t frontFace;
     float wMetal, wDiel, wDiff;  // normalised branch weights (principled/weights.slang:27-62)
+    float wCoat, wSub;           // extended stack only (0 otherwise)
+    float coatA, viewCoat;       // clearcoat alpha, coat attenuation toward wo (extended stack)
     float3 f0Diel;               // dielectric specular F0
     float3 viewAtten;            // dielectric directional attenuation at wo
 };
@@ -537,6 +625,7 @@ VKRT_DEV float3 dielDirAtten(float roughness, float3 f0, float cosT) {  // atten
     return sat(f3(1.0f) - sat(f0 * A + f3(B)));
 }
 
+template <bool kExt = false>
 VKRT_DEV Bsdf makeBsdf(const ShadeMaterial& m, float3 wo, uint32_t frontFace) {
     Bsdf s;
     s.mat = m;
@@ -550,14 +639,28 @@ VKRT_DEV Bsdf makeBsdf(const ShadeMaterial& m, float3 wo, uint32_t frontFace) {
     float wm = m.metallic * fmaxf(lum(m.baseColor), 1e-3f);
     float wd = nonMetal * fmaxf(sat(lum(s.f0Diel)), 0.0f);
     float wf = lum(s.viewAtten) * nonMetal * fmaxf(lum(diff), 1e-3f);
-    float tot = wm + wd + wf;
+    float wc = 0.0f, ws = 0.0f;
+    s.viewCoat = 1.0f;
+    s.coatA = 0.1f;
+    if (kExt) {
+        s.coatA = coatAlpha(m);
+        s.viewCoat = coatAtten(m, wo);
+        wc = m.clearcoat * 0.25f;
+        wm *= s.viewCoat;
+        wd *= s.viewCoat;
+        ws = s.viewCoat * wf * m.subsurface;
+        wf = s.viewCoat * wf * (1.0f - m.subsurface);
+    }
+    float tot = wc + wm + wd + wf + ws;
     if (tot <= 0.0f) {
-        s.wMetal = s.wDiel = 0.0f;
+        s.wMetal = s.wDiel = s.wCoat = s.wSub = 0.0f;
         s.wDiff = 1.0f;
     } else {
+        s.wCoat = wc / tot;
         s.wMetal = wm / tot;
         s.wDiel = wd / tot;
         s.wDiff = wf / tot;
+        s.wSub = ws / tot;
     }
     return s;
 }
@@ -569,11 +672,47 @@ VKRT_DEV float3 metalFresnel(const Bsdf& s, float c) {
                            : schlick(c, s.mat.baseColor);
 }
 
-// RGB reflection stack (principled/eval_rgb.slang:4-121 restricted to metal + dielectric + Lambert)
+// The extended stack's coat value and substrate factor for unit colours: value = coat + att * (metal + ...), with
+// substrate = diffuseColour * (diffuse + subsurface) (scalars for a unit colour)
+struct ExtTerms {
+    float coat, att, diffuse, subsurface;
+};
+
+template <bool kExt>
+VKRT_DEV ExtTerms extTerms(const Bsdf& s, float3 wi, float& pdf) {
+    ExtTerms t{0.0f, 1.0f, 0.0f, 0.0f};
+    if (!kExt) {
+        if (s.wDiff > 0.0f) {
+            t.diffuse = kInvPi;
+            pdf += s.wDiff * (wi.z * kInvPi);
+        }
+        return t;
+    }
+    if (s.wCoat > 0.0f) {
+        float cp;
+        t.coat = coatEval(s.mat.clearcoat, s.coatA, s.wo, wi, cp);
+        pdf += s.wCoat * cp;
+    }
+    if (s.wDiff > 0.0f) {
+        t.diffuse = (1.0f - s.mat.subsurface) *
+                    (s.mat.diffuseRoughness <= 0.0f ? kInvPi : orenNayar(s.mat.diffuseRoughness, s.wo, wi));
+        pdf += s.wDiff * (wi.z * kInvPi);
+    }
+    if (s.wSub > 0.0f) {
+        t.subsurface = s.mat.subsurface * fakeSss(s.mat.diffuseRoughness, s.wo, wi);
+        pdf += s.wSub * (wi.z * kInvPi);
+    }
+    t.att = s.viewCoat * coatAtten(s.mat, wi);
+    return t;
+}
+
+// RGB reflection stack (principled/eval_rgb.slang:4-121: metal + dielectric + diffuse; with kExt also clearcoat,
+// Oren-Nayar and fake subsurface)
+template <bool kExt = false>
 VKRT_DEV float3 evalRgb(const Bsdf& s, float3 wi, float& pdf) {
     pdf = 0.0f;
     if (wi.z <= 0.0f) return f3(0.0f);
-    float3 metal = f3(0.0f), diel = f3(0.0f), sub = f3(0.0f);
+    float3 metal = f3(0.0f), diel = f3(0.0f);
     float3 h = s.wo + wi;
     float h2 = dot(h, h);
     float3 m = h * rsqrtf(h2);
@@ -593,18 +732,18 @@ VKRT_DEV float3 evalRgb(const Bsdf& s, float3 wi, float& pdf) {
         diel = schlick(wom, s.f0Diel) * DG;
         pdf += s.wDiel * reflPdf;
     }
-    if (s.wDiff > 0.0f) {
-        sub = s.mat.baseColor * ((1.0f - s.mat.metallic) * kInvPi);
-        pdf += s.wDiff * (wi.z * kInvPi);
-    }
-    return metal * s.mat.metallic + (diel + s.viewAtten * sub) * (1.0f - s.mat.metallic);
+    ExtTerms t = extTerms<kExt>(s, wi, pdf);
+    float3 sub = s.mat.baseColor * ((1.0f - s.mat.metallic) * (t.diffuse + t.subsurface));
+    float3 base = metal * s.mat.metallic + (diel + s.viewAtten * sub) * (1.0f - s.mat.metallic);
+    return kExt ? f3(t.coat) + base * t.att : base;
 }
 
 // 4-lane spectral stack (principled/eval_spectral.slang:4-94); all lanes share one technique pdf in this subset
+template <bool kExt = false>
 VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, float4 l, float& pdf) {
     pdf = 0.0f;
     if (wi.z <= 0.0f) return f4(0.0f);
-    float4 metal = f4(0.0f), diel = f4(0.0f), sub = f4(0.0f);
+    float4 metal = f4(0.0f), diel = f4(0.0f);
     float3 h = s.wo + wi;
     float h2 = dot(h, h);
     float3 m = h * rsqrtf(h2);
@@ -624,17 +763,26 @@ VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, flo
         diel = spectral4(tab, sat(schlick(wom, s.f0Diel)), l) * DG;
         pdf += s.wDiel * reflPdf;
     }
-    if (s.wDiff > 0.0f) {
-        sub = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l) * kInvPi;
-        pdf += s.wDiff * (wi.z * kInvPi);
-    }
+    ExtTerms t = extTerms<kExt>(s, wi, pdf);
+    float4 sub = f4(0.0f);
+    if (s.wDiff > 0.0f || s.wSub > 0.0f)
+        sub = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l) * (t.diffuse + t.subsurface);
     float4 va = spectral4(tab, sat(s.viewAtten), l);
-    return metal * s.mat.metallic + (diel + va * sub) * (1.0f - s.mat.metallic);
+    float4 base = metal * s.mat.metallic + (diel + va * sub) * (1.0f - s.mat.metallic);
+    return kExt ? f4(t.coat) + base * t.att : base;
 }
 
-// sampleBSDFDirection (principled/sample.slang:4-51), same subset
+// sampleBSDFDirection (principled/sample.slang:4-51): lobe by weight (coat, metal, dielectric, diffuse, subsurface)
+template <bool kExt = false>
 VKRT_DEV bool sampleDirection(const Bsdf& s, Rng& rng, float3& wi) {
     float sel = rng.next();
+    if (kExt) {
+        if (sel < s.wCoat) {
+            float u1 = rng.next(), u2 = rng.next();
+            return coatSample(s.wo, s.coatA, u1, u2, wi);
+        }
+        sel -= s.wCoat;
+    }
     if (sel < s.wMetal || (sel - s.wMetal) < s.wDiel) {
         bool diel = !(sel < s.wMetal);
         if (diel && (s.wo.z <= 0.0f || dielIdentity(s.mat))) return false;

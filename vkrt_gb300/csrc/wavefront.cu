@@ -510,7 +510,7 @@ constexpr uint32_t kNrcTrainVerts = 16;  // vertices of a training path that bec
 // the radiance the path gathered after the vertex's own emission, divided by the throughput that reached it: an
 // unbiased estimate of what the vertex scatters toward the previous one (linear sRGB; hero paths convert the four
 // wavelengths as a sample result is converted).
-template <bool kSpectral>
+template <bool kSpectral, bool kExt>
 __global__ void __launch_bounds__(kWfThreads) kNrcTrainPaths(const WfScene* __restrict__ scenes, uint32_t paths,
                                                              uint32_t frame, uint32_t seed, uint32_t rngMode,
                                                              uint64_t rngSeed, uint32_t maxRecords,
@@ -540,8 +540,8 @@ __global__ void __launch_bounds__(kWfThreads) kNrcTrainPaths(const WfScene* __re
             const float4 thrBefore = p.thr;
             ShadowRequest sh[2];
             uint32_t ns;
-            bool cont = shadePathVertex<kSpectral, TrainHook>(S.sc, S.sd, cfg, tab, p, hit, sh, ns,
-                                                              TrainHook{{}, &in, &has, p.d});
+            bool cont = shadePathVertex<kSpectral, TrainHook, kExt>(S.sc, S.sd, cfg, tab, p, hit, sh, ns,
+                                                                    TrainHook{{}, &in, &has, p.d});
             if (has && nv < kNrcTrainVerts) {
                 vin[nv] = in;
                 vthr[nv] = thrBefore;
@@ -639,9 +639,9 @@ VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t sl
                  xyz(g.adjTotal[slot]), xyz(radiance));
 }
 
-// kFeatures: the frame also takes denoiser features (a separate instantiation, so frames without them keep the
-// register budget of the plain kernel)
-template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFeatures = false>
+// kFull: the extended reflection stack and the denoiser features (taken when g.features is set); a separate
+// instantiation, so frames that need neither keep the register budget of the plain kernel
+template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFull = false>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
     const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
@@ -691,10 +691,10 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
             } else {
                 const bool featDone = (p.flags & kPathFeatureDone) != 0u;
                 DenoiserFeature feat{f3(0.0f), f3(0.0f), featDone ? 1.0f : 0.0f};
-                cont = shadePathVertex<kSpectral, CacheHook>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
-                                                             CacheHook{{}, &query, &queried, p.d,
-                                                                       kFeatures ? &feat : nullptr});
-                if (kFeatures && !featDone && feat.weight > 0.0f) {
+                cont = shadePathVertex<kSpectral, CacheHook, kFull>(
+                    S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
+                    CacheHook{{}, &query, &queried, p.d, (kFull && g.features) ? &feat : nullptr});
+                if (kFull && g.features && !featDone && feat.weight > 0.0f) {
                     const size_t item = size_t(S.itemBase) + g.slotItem[slot];
                     g.itemFeatA[item] = make_float4(feat.albedo.x, feat.albedo.y, feat.albedo.z, 1.0f);
                     g.itemFeatN[item] = make_float4(feat.normal.x, feat.normal.y, feat.normal.z, 0.0f);
@@ -977,9 +977,12 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(slotItem, c_work, Q);
     WF_GROW(sampleBuf, c_sum, std::max<size_t>(totalItems, 1));
     bool features = false;  // forward frames render denoiser features when any scene has feature films
-    if (mode == kWavefrontForward)
-        for (const WfScene& S : scenes)
-            if (S.film.albedoWrite) features = true;
+    bool extended = false;  // some scene's materials use the extended reflection stack
+    for (const WfScene& S : scenes) {
+        if (mode == kWavefrontForward && S.film.albedoWrite) features = true;
+        if (S.extended) extended = true;
+    }
+    const bool full = features || extended;
     if (features) {
         WF_GROW(itemFeatA, c_fA, std::max<size_t>(totalItems, 1));
         WF_GROW(itemFeatN, c_fN, std::max<size_t>(totalItems, 1));
@@ -1095,8 +1098,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         stage(kStageShade, [&] {
             // register budget follows the requested residency: 128 (4 blocks/SM), 80 (6) or 64 (8) registers
             if (adjMode) kWfShade<false, true, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (features && spectral) kWfShade<true, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (features) kWfShade<false, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (full && spectral) kWfShade<true, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (full) kWfShade<false, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 8) kWfShade<true, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 6) kWfShade<true, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
@@ -1142,14 +1145,15 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         const uint32_t maxRecords = cache->trainingPaths * kNrcTrainVerts;
         const uint32_t tb = (cache->trainingPaths + kWfThreads - 1u) / kWfThreads;
         if (cache->trainingPaths) {
-            if (spectral)
-                kNrcTrainPaths<true><<<tb, kWfThreads, smem, stream>>>(B.scenes, cache->trainingPaths, cache->frame,
-                                                                       cache->seed, rngMode, rngSeed, maxRecords, B.recIn,
-                                                                       B.recTarget, B.recCount, counters);
-            else
-                kNrcTrainPaths<false><<<tb, kWfThreads, smem, stream>>>(B.scenes, cache->trainingPaths, cache->frame,
-                                                                        cache->seed, rngMode, rngSeed, maxRecords,
-                                                                        B.recIn, B.recTarget, B.recCount, counters);
+#define VKRT_TRAIN(S, X)                                                                                            \
+    kNrcTrainPaths<S, X><<<tb, kWfThreads, smem, stream>>>(B.scenes, cache->trainingPaths, cache->frame, cache->seed, \
+                                                          rngMode, rngSeed, maxRecords, B.recIn, B.recTarget,       \
+                                                          B.recCount, counters)
+            if (spectral && extended) VKRT_TRAIN(true, true);
+            else if (spectral) VKRT_TRAIN(true, false);
+            else if (extended) VKRT_TRAIN(false, true);
+            else VKRT_TRAIN(false, false);
+#undef VKRT_TRAIN
         }
         if (!B.hostCount) e = cudaMallocHost(&B.hostCount, sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.hostCount, B.recCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);

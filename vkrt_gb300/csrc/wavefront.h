@@ -23,6 +23,7 @@ struct WfScene {
     uint32_t spectral;
     uint32_t neeEnabled;
     uint32_t envNee;
+    uint32_t extended;  // some material uses the extended reflection stack
     // filled by the engine
     uint32_t tileW, tileH, tilesX;
     uint32_t workBase, workCount;  // padded pixel work items (tile order)
