@@ -51,12 +51,13 @@ def test_extended_stack_rgb_parity(built, integrator):
 def test_extended_stack_spectral_parity(built, integrator):
     from oracle import cpu
     s = extended_cornell(48, 48, spp=2)
-    sd = s.scene_data.copy()
     with RenderContext(rng_mode=abi.RNG_PCG32, integrator=integrator) as ctx:
         table, info = ctx.generate_rgb2spec(32)
         s.rgb2spec = table
-        sd["rgb2specSRGB"] = info
-        sd["packedRenderSettings"] = abi.pack_render_settings(1, abi.RENDER_MODE_SPECTRAL, 1)
+        s.scene_data["rgb2specSRGB"] = info
+        s.scene_data["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES,
+                                                                         abi.RENDER_MODE_SPECTRAL, abi.SPECTRAL_HERO)
+        sd = s.scene_data.copy()
         ctx.upload_scene(s)
         ctx.render_frame(sd)
         gpu = ctx.read_accumulation()
