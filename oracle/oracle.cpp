@@ -597,6 +597,43 @@ HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float
     return best;
 }
 
+bool meshTransmissive(const Scene& s, uint32_t mesh) {
+    return s.materials[s.meshes[mesh].materialIndex].transmission > 0.0f;
+}
+
+// Shadow query of a scene with transmissive materials (rt/payloads/shadow_payload.slang, entry/shadow/closest_hit.slang):
+// a shadow ray whose reported hit is transmissive answers "unsupported" instead of "occluded". vkrt reports the first
+// hit the driver accepts, in an unspecified order; here an opaque hit anywhere on the segment wins, and the segment
+// is unsupported when its only hits are transmissive.
+enum : int { kShadowVisible = 0, kShadowOccluded = 1, kShadowTransmission = 2 };
+int shadowFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float tmax) {
+    if (s.bvh.nodes.empty()) return kShadowVisible;
+    RayPre<float> rp = prepRay(o, d, tmin, tmax);
+    V3<float> inv(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool sawTransmissive = false;
+    while (sp > 0) {
+        uint32_t ni = stack[--sp];
+        const BvhNode& n = s.bvh.nodes[ni];
+        if (!boxHit(n, o, inv, tmin, tmax)) continue;
+        if (n.count == 0) {
+            stack[sp++] = s.bvh.right[ni];
+            stack[sp++] = n.left;
+            continue;
+        }
+        for (uint32_t i = 0; i < n.count; ++i) {
+            const WorldTri& tr = s.tris[n.left + i];
+            float t, b1, b2;
+            if (!watertight(rp, tr.v[0], tr.v[1], tr.v[2], t, b1, b2)) continue;
+            if (!meshTransmissive(s, tr.mesh)) return kShadowOccluded;
+            sawTransmissive = true;
+        }
+    }
+    return sawTransmissive ? kShadowTransmission : kShadowVisible;
+}
+
 // FP64 brute-force closest hit over world triangles (optionally reporting ambiguity)
 HitRec traceFp64Brute(const SceneFull& s, const std::vector<std::array<double, 9>>& tri64, V3<double> o,
                       V3<double> d, double tmin, double tmax, bool* ambiguous, double eps) {
@@ -867,6 +904,8 @@ struct MaterialR {  // Material fields the restated lobes read, after texturing
     V3<R> emissionColor;
     R emissionLuminance;
     R abbe;
+    R absorptionCoefficient;
+    V3<R> attenuationColor;
 };
 
 template <class R>
@@ -1144,21 +1183,73 @@ template <class R> V3<R> dielDirAlbedo(const MaterialR<R>& m, V3<R> w) {  // att
 }
 template <class R> V3<R> dielDirAtten(const MaterialR<R>& m, V3<R> w) { return sat(V3<R>(R(1)) - dielDirAlbedo(m, w)); }
 
-template <class R> Weights<R> branchWeights(const MaterialR<R>& m, V3<R> wo) {  // weights.slang:27-62 (subset)
+// Dispersion by the Cauchy fit through the Fraunhofer D line and the Abbe number (utility/spectral.slang:124-136)
+template <class R> R dispersiveIor(R ior, R abbe, R lambdaNm) {
+    if (ior <= R(1) + R(1e-4) || abbe <= R(0)) return std::max(ior, R(1));
+    const R cUm = R(0.6562725), dUm = R(0.5875618), fUm = R(0.4861327);
+    R lUm = std::max(lambdaNm * R(0.001), R(1e-4));
+    R dn = (ior - R(1)) / std::max(abbe, R(1e-6));
+    R B = dn / (R(1) / (fUm * fUm) - R(1) / (cUm * cUm));
+    R A = ior - B / (dUm * dUm);
+    return std::max(A + B / (lUm * lUm), R(1));
+}
+// bsdf/base/interface.slang:4-32: the interface IOR (dispersive in the spectral modes) and the two eta conventions
+template <class R> R interfaceIor(const MaterialR<R>& m, R lambdaNm, bool spectral) {
+    R ior = std::max(m.ior, R(1));
+    return spectral ? dispersiveIor(ior, m.abbe, lambdaNm) : ior;
+}
+template <class R> R interfaceEta(const MaterialR<R>& m, uint32_t front, R lambdaNm = R(0), bool spectral = false) {
+    R ior = interfaceIor(m, lambdaNm, spectral);
+    return front ? ior : R(1) / ior;
+}
+template <class R> R refractionEta(const MaterialR<R>& m, uint32_t front, R lambdaNm, bool spectral) {
+    R ior = interfaceIor(m, lambdaNm, spectral);
+    return front ? R(1) / ior : ior;
+}
+template <class R> bool dielIdentity(const MaterialR<R>& m) { return std::max(m.ior, R(1)) <= R(1) + R(1e-4); }
+template <class R> V3<R> transmissionColor(const MaterialR<R>& m) {  // material.slang:75-77
+    return m.transmission > R(0) && m.metallic <= R(0) ? V3<R>(R(1)) : m.baseColor;
+}
+template <class R> R transmissionProbability(const MaterialR<R>& m, R F) {  // dielectric/interface.slang:68-72
+    R tw = m.transmission * (R(1) - F), tot = F + tw;
+    return tot <= R(0) ? R(0) : tw / tot;
+}
+template <class R> bool mediumIsRefractive(const MaterialR<R>& m) {  // base/medium.slang:40-42
+    return m.transmission > R(0) && std::max(m.ior, R(1)) > R(1) + R(1e-4);
+}
+template <class R> bool hasAbsorption(const MaterialR<R>& m) {  // base/medium.slang:36-38
+    return m.absorptionCoefficient > R(0) &&
+           (m.attenuationColor.x < R(0.9999) || m.attenuationColor.y < R(0.9999) || m.attenuationColor.z < R(0.9999));
+}
+// HLSL refract(i, n, eta): the zero vector on total internal reflection
+template <class R> V3<R> refractDir(V3<R> i, V3<R> n, R eta) {
+    R c = dot(n, i);
+    R k = R(1) - eta * eta * (R(1) - c * c);
+    if (k < R(0)) return V3<R>(R(0));
+    return i * eta - n * (eta * c + std::sqrt(k));
+}
+
+template <class R> Weights<R> branchWeights(const MaterialR<R>& m, V3<R> wo, uint32_t frontFace) {  // weights.slang:27-62
     V3<R> diff = m.baseColor * (R(1) - m.metallic);
     R nonMetal = R(1) - m.metallic;
     R baseW = std::max(lum(m.baseColor), R(1e-3));
     R diffW = std::max(lum(diff), R(1e-3));
     R baseScatter = nonMetal * (R(1) - m.transmission);
-    R dielSpecW = nonMetal * std::max(sat(lum(dielSpecF0(m))) + R(0), R(0));
-    R dielAtt = lum(dielDirAtten(m, wo));
-    R viewCoat = coatDirAtten(m, wo);
+    R transW = m.transmission * std::max(lum(transmissionColor(m)), R(1e-3));
+    R dielSpecW = nonMetal * std::max(sat(lum(dielSpecF0(m))) + transW, R(0));
     Weights<R> w;
-    w.coat = m.clearcoat * R(0.25);
-    w.metal = viewCoat * m.metallic * baseW;
-    w.dielectric = viewCoat * dielSpecW;
-    w.diffuse = viewCoat * dielAtt * baseScatter * (R(1) - m.subsurface) * diffW;
-    w.subsurface = viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
+    if (m.transmission > R(0) && frontFace == 0u) {  // interior side of a transmissive interface
+        w.metal = m.metallic * baseW;
+        w.dielectric = dielSpecW;
+    } else {
+        R dielAtt = lum(dielDirAtten(m, wo));
+        R viewCoat = coatDirAtten(m, wo);
+        w.coat = m.clearcoat * R(0.25);
+        w.metal = viewCoat * m.metallic * baseW;
+        w.dielectric = viewCoat * dielSpecW;
+        w.diffuse = viewCoat * dielAtt * baseScatter * (R(1) - m.subsurface) * diffW;
+        w.subsurface = viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
+    }
     R total = w.coat + w.metal + w.dielectric + w.diffuse + w.subsurface;
     if (total <= R(0)) {
         w.metal = w.dielectric = w.coat = w.subsurface = R(0);
@@ -1181,6 +1272,7 @@ struct BsdfState {
     uint32_t frontFace;
     Weights<R> w;
     bool conductor;
+    bool interior;  // useInteriorDielectricInterface (attenuation.slang:4-6)
 };
 
 template <class R> BsdfState<R> makeBsdf(const MaterialR<R>& m, V3<R> wo, uint32_t frontFace) {
@@ -1189,8 +1281,9 @@ template <class R> BsdfState<R> makeBsdf(const MaterialR<R>& m, V3<R> wo, uint32
     s.wo = wo;
     s.frontFace = frontFace;
     s.ggx = makeGgx(m, wo);
-    s.w = branchWeights(m, wo);
+    s.w = branchWeights(m, wo, frontFace);
     s.conductor = m.k.x > R(0) || m.k.y > R(0) || m.k.z > R(0);
+    s.interior = m.transmission > R(0) && frontFace == 0u;
     return s;
 }
 
@@ -1199,131 +1292,195 @@ template <class R> V3<R> metalFresnelRgb(const BsdfState<R>& s, R c) {  // ggx.s
                        : schlick(c, s.mat.baseColor);
 }
 
-template <class R> R interfaceEta(const MaterialR<R>& m, uint32_t front) {  // base/interface.slang:13-16 (no dispersion)
-    R ior = std::max(m.ior, R(1));
-    return front ? ior : R(1) / ior;
+// One transmission lane (dielectric/eval_rgb.slang:40-95, eval_spectral.slang:45-97): the rough dielectric BTDF of
+// Walter et al. 2007 with the Fresnel-weighted choice between reflection and refraction; `color` is the lane's
+// transmission colour, `coatAtt` the attenuation of the layers above the interface.
+template <class R> R evalTransmissionLane(const BsdfState<R>& s, V3<R> wi, R coatAtt, R color, R lambdaNm,
+                                          bool spectral, R& pdf) {
+    pdf = R(0);
+    if (s.mat.transmission <= R(0) || s.wo.z <= R(0) || wi.z >= R(0)) return R(0);
+    if (dielIdentity(s.mat)) {
+        if (dot(wi, -s.wo) < R(0.9999)) return R(0);
+        pdf = R(1);
+        return coatAtt * color / std::max(std::fabs(wi.z), R(kGgxEps));
+    }
+    R etap = interfaceEta(s.mat, s.frontFace, lambdaNm, spectral);
+    V3<R> h = s.wo + wi * etap;
+    if (dot(h, h) <= R(kGgxEps)) return R(0);
+    V3<R> wm = safeNormalize(h);
+    if (wm.z < R(0)) wm = -wm;
+    R woM = dot(s.wo, wm), wiM = dot(wi, wm);
+    R denom = wiM + woM / etap;
+    if (!(woM > R(0) && wiM < R(0) && std::fabs(denom) > R(kGgxEps))) return R(0);
+    R F = fresnelDielectric(woM, etap);
+    R tprob = transmissionProbability(s.mat, F);
+    if (tprob <= R(0)) return R(0);
+    R D = ggxD(wm, s.ggx), G = ggxG(s.wo, wi, s.ggx);
+    R d2 = denom * denom;
+    R scale = R(1) / std::max(etap * etap, R(kGgxEps));
+    R term = std::fabs((wiM * woM) / std::max(std::fabs(wi.z) * s.wo.z * d2, R(kGgxEps)));
+    R dwm = std::fabs(wiM) / std::max(d2, R(kGgxEps));
+    pdf = tprob * visibleNormalPdf(s.wo, wm, s.ggx) * dwm;
+    return coatAtt * color * ((R(1) - F) * D * G * term * scale);
 }
-template <class R> bool dielIdentity(const MaterialR<R>& m) { return std::max(m.ior, R(1)) <= R(1) + R(1e-4); }
 
-// RGB reflection stack (principled/eval_rgb.slang:4-102), subset: no sheen/clearcoat/transmission/subsurface
-template <class R> void evalRgb(const BsdfState<R>& s, V3<R> wi, V3<R>& value, R& pdf) {
+template <class R> R transmissionCoatAtt(const BsdfState<R>& s) {  // materialTransmissionStackAttenuation
+    return s.interior ? R(1) : coatDirAtten(s.mat, s.wo);
+}
+
+// The scalar stack (principled/eval_rgb.slang:4-141): RGB (single = false) or one wavelength of the single-wavelength
+// path (single = true: colours become spectral scalars at lambda; the dielectric view attenuation stays RGB, as in
+// evalScalarReflectionStack, and callers read the first component).
+template <class R> void evalScalar(const BsdfState<R>& s, const Rgb2Spec* tab, V3<R> wi, R lambda, bool single,
+                                   V3<R>& value, R& pdf) {
     value = V3<R>(R(0));
     pdf = R(0);
-    if (wi.z <= R(0)) return;  // transmission lobe absent (evalDielectricTransmission returns 0 with transmission 0)
+    auto spec = [&](V3<R> c) { return single ? V3<R>(spectralScalar(*tab, sat(c), lambda)) : c; };
+    if (wi.z <= R(0)) {  // evalDielectricTransmission
+        V3<R> tc = transmissionColor(s.mat) * ((R(1) - s.mat.metallic) * s.mat.transmission);
+        tc = spec(tc);
+        R coatAtt = transmissionCoatAtt(s);
+        R tp = R(0);
+        for (int i = 0; i < 3; ++i) value[i] = evalTransmissionLane(s, wi, coatAtt, tc[i], lambda, single, tp);
+        pdf = tp * s.w.dielectric;
+        return;
+    }
+    R coat = R(0);
     V3<R> metal(R(0)), diel(R(0)), sub(R(0));
+    if (s.w.coat > R(0)) {
+        R cp;
+        coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
+        pdf += s.w.coat * cp;
+    }
     if (s.w.metal > R(0)) {  // evalGGX (ggx.slang:118-152)
         V3<R> m;
         R wom;
-        if (s.wo.z > R(0) && wi.z > R(0) && halfVector(s.wo, wi, m, wom)) {
+        if (s.wo.z > R(0) && halfVector(s.wo, wi, m, wom)) {
             R D = ggxD(m, s.ggx), G = ggxG(s.wo, wi, s.ggx);
-            metal = metalFresnelRgb(s, wom) * (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
+            metal = spec(metalFresnelRgb(s, wom)) * (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
             pdf += s.w.metal * reflectionPdf(s.wo, m, s.ggx);
         }
     }
     if (s.w.dielectric > R(0)) {  // evalDielectricReflection (dielectric/eval_rgb.slang:6-38)
         V3<R> m;
         R wom;
-        if (!dielIdentity(s.mat) && s.wo.z > R(0) && wi.z > R(0) && halfVector(s.wo, wi, m, wom)) {
-            R F = fresnelDielectric(wom, interfaceEta(s.mat, s.frontFace));
-            R tw = s.mat.transmission * (R(1) - F), tot = F + tw;
-            R tp = tot <= R(0) ? R(0) : tw / tot;
-            R reflP = R(1) - tp;
+        if (!dielIdentity(s.mat) && s.wo.z > R(0) && halfVector(s.wo, wi, m, wom)) {
+            R F = fresnelDielectric(wom, interfaceEta(s.mat, s.frontFace, lambda, single));
+            R reflP = R(1) - transmissionProbability(s.mat, F);
             if (reflP > R(0)) {
                 R D = ggxD(m, s.ggx), G = ggxG(s.wo, wi, s.ggx);
-                diel = schlick(wom, dielSpecF0(s.mat)) * (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
+                V3<R> color = s.mat.transmission > R(0) && s.mat.metallic <= R(0) ? V3<R>(F)
+                                                                                  : spec(schlick(wom, dielSpecF0(s.mat)));
+                diel = color * (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
                 pdf += s.w.dielectric * (reflP * reflectionPdf(s.wo, m, s.ggx));
             }
         }
     }
-    R coat = R(0);
-    if (s.w.coat > R(0)) {
-        R cp;
-        coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
-        pdf += s.w.coat * cp;
+    if (s.w.diffuse > R(0) || s.w.subsurface > R(0)) {
+        V3<R> dc = spec(s.mat.baseColor * (R(1) - s.mat.metallic));
+        if (s.w.diffuse > R(0)) {  // evalLambertian / evalOrenNayar (diffuse.slang:13-53)
+            V3<R> dw = dc * ((R(1) - s.mat.transmission) * (R(1) - s.mat.subsurface));
+            R unit = s.mat.diffuseRoughness <= R(0) ? R(kInvPi) : orenNayarUnit(s.mat.diffuseRoughness, s.wo, wi);
+            sub += dw * unit;
+            pdf += s.w.diffuse * (wi.z * R(kInvPi));
+        }
+        if (s.w.subsurface > R(0)) {  // evalFakeSubsurface (subsurface.slang:12-31)
+            V3<R> sw = dc * ((R(1) - s.mat.transmission) * s.mat.subsurface);
+            sub += sw * fakeSubsurfaceUnit(s.mat.diffuseRoughness, s.wo, wi);
+            pdf += s.w.subsurface * (wi.z * R(kInvPi));
+        }
     }
-    V3<R> dc = s.mat.baseColor * (R(1) - s.mat.metallic);
-    if (s.w.diffuse > R(0)) {  // evalLambertian / evalOrenNayar (diffuse.slang:13-53)
-        V3<R> dw = dc * ((R(1) - s.mat.transmission) * (R(1) - s.mat.subsurface));
-        R unit = s.mat.diffuseRoughness <= R(0) ? (wi.z > R(0) ? R(kInvPi) : R(0))
-                                                 : orenNayarUnit(s.mat.diffuseRoughness, s.wo, wi);
-        sub = dw * unit;
-        pdf += s.w.diffuse * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0));
-    }
-    if (s.w.subsurface > R(0)) {  // evalFakeSubsurface (subsurface.slang:12-31)
-        V3<R> sw = dc * ((R(1) - s.mat.transmission) * s.mat.subsurface);
-        sub += sw * fakeSubsurfaceUnit(s.mat.diffuseRoughness, s.wo, wi);
-        pdf += s.w.subsurface * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0));
+    R nonMetal = R(1) - s.mat.metallic;
+    if (s.interior) {
+        value = metal * s.mat.metallic + diel * nonMetal;
+        return;
     }
     V3<R> viewAtt = dielDirAtten(s.mat, s.wo);
-    R nonMetal = R(1) - s.mat.metallic;
     R att = coatDirAtten(s.mat, s.wo) * coatDirAtten(s.mat, wi);  // reflectionStackAttenuation
     value = V3<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att;
 }
 
-// 4-lane spectral reflection stack (principled/eval_spectral.slang:4-94), same subset
+template <class R> void evalRgb(const BsdfState<R>& s, V3<R> wi, V3<R>& value, R& pdf) {
+    evalScalar(s, static_cast<const Rgb2Spec*>(nullptr), wi, R(0), false, value, pdf);
+}
+
+// 4-lane hero stack (principled/eval_spectral.slang:4-117): per-lane technique pdfs `tp` (they differ across lanes
+// only at dispersive interfaces)
 template <class R> V4<R> evalSpectral(const BsdfState<R>& s, const Rgb2Spec& tab, V3<R> wi, V4<R> l, V4<R>& tp) {
     tp = V4<R>(R(0));
-    if (wi.z <= R(0)) return V4<R>(R(0));
+    if (wi.z <= R(0)) {  // evalSpectralDielectricTransmission
+        R coatAtt = transmissionCoatAtt(s);
+        V4<R> tc = spectralScalar4(tab, sat(transmissionColor(s.mat)), l) *
+                   ((R(1) - s.mat.metallic) * s.mat.transmission);
+        V4<R> v;
+        for (int i = 0; i < 4; ++i) v[i] = evalTransmissionLane(s, wi, coatAtt, tc[i], l[i], true, tp[i]);
+        tp = tp * s.w.dielectric;
+        return v;
+    }
+    R coat = R(0);
     V4<R> metal(R(0)), diel(R(0)), sub(R(0));
+    if (s.w.coat > R(0)) {
+        R cp;
+        coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
+        tp += V4<R>(s.w.coat * cp);
+    }
     if (s.w.metal > R(0)) {  // evalSpectralGGX
         V3<R> m;
         R wom;
-        if (s.wo.z > R(0) && wi.z > R(0) && halfVector(s.wo, wi, m, wom)) {
+        if (s.wo.z > R(0) && halfVector(s.wo, wi, m, wom)) {
             R D = ggxD(m, s.ggx), G = ggxG(s.wo, wi, s.ggx);
             R p = reflectionPdf(s.wo, m, s.ggx);
-            metal = spectralScalar4(tab, sat(metalFresnelRgb(s, wom)), l) * (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
+            metal = spectralScalar4(tab, sat(metalFresnelRgb(s, wom)), l) *
+                    (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
             tp += V4<R>(s.w.metal * p);
         }
     }
     if (s.w.dielectric > R(0)) {  // evalSpectralDielectricReflection
         V3<R> m;
         R wom;
-        if (!dielIdentity(s.mat) && s.wo.z > R(0) && wi.z > R(0) && halfVector(s.wo, wi, m, wom)) {
+        if (!dielIdentity(s.mat) && s.wo.z > R(0) && halfVector(s.wo, wi, m, wom)) {
             R D = ggxD(m, s.ggx), G = ggxG(s.wo, wi, s.ggx);
             R base = reflectionPdf(s.wo, m, s.ggx);
-            V4<R> lanes;
+            V4<R> F, lanes;
             for (int i = 0; i < 4; ++i) {
-                R F = fresnelDielectric(wom, interfaceEta(s.mat, s.frontFace));
-                R tw = s.mat.transmission * (R(1) - F), tot = F + tw;
-                R tprob = tot <= R(0) ? R(0) : tw / tot;
-                lanes[i] = (R(1) - tprob) * base;
+                F[i] = fresnelDielectric(wom, interfaceEta(s.mat, s.frontFace, l[i], true));
+                lanes[i] = (R(1) - transmissionProbability(s.mat, F[i])) * base;
             }
             if (anyPositive(lanes)) {
-                diel = spectralScalar4(tab, sat(schlick(wom, dielSpecF0(s.mat))), l) *
-                       (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
+                V4<R> color = s.mat.transmission > R(0) && s.mat.metallic <= R(0)
+                                  ? F
+                                  : spectralScalar4(tab, sat(schlick(wom, dielSpecF0(s.mat))), l);
+                diel = color * (D * G / std::max(R(4) * s.wo.z * wi.z, R(kGgxEps)));
                 tp += lanes * s.w.dielectric;
             }
         }
-    }
-    R coat = R(0);
-    if (s.w.coat > R(0)) {
-        R cp;
-        coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
-        tp += V4<R>(s.w.coat * cp);
     }
     if (s.w.diffuse > R(0) || s.w.subsurface > R(0)) {
         V4<R> dc = spectralScalar4(tab, sat(s.mat.baseColor * (R(1) - s.mat.metallic)), l);
         if (s.w.diffuse > R(0)) {
             R scale = (R(1) - s.mat.transmission) * (R(1) - s.mat.subsurface);
-            R unit = s.mat.diffuseRoughness <= R(0) ? (wi.z > R(0) ? R(kInvPi) : R(0))
-                                                     : orenNayarUnit(s.mat.diffuseRoughness, s.wo, wi);
-            sub = dc * (scale * unit);
-            tp += V4<R>(s.w.diffuse * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0)));
+            R unit = s.mat.diffuseRoughness <= R(0) ? R(kInvPi) : orenNayarUnit(s.mat.diffuseRoughness, s.wo, wi);
+            sub += dc * (scale * unit);
+            tp += V4<R>(s.w.diffuse * (wi.z * R(kInvPi)));
         }
         if (s.w.subsurface > R(0)) {
             R scale = (R(1) - s.mat.transmission) * s.mat.subsurface;
             sub += dc * (scale * fakeSubsurfaceUnit(s.mat.diffuseRoughness, s.wo, wi));
-            tp += V4<R>(s.w.subsurface * (wi.z > R(0) ? wi.z * R(kInvPi) : R(0)));
+            tp += V4<R>(s.w.subsurface * (wi.z * R(kInvPi)));
         }
     }
-    V4<R> viewAtt = spectralScalar4(tab, sat(dielDirAtten(s.mat, s.wo)), l);
     R nonMetal = R(1) - s.mat.metallic;
+    if (s.interior) return metal * s.mat.metallic + diel * nonMetal;
+    V4<R> viewAtt = spectralScalar4(tab, sat(dielDirAtten(s.mat, s.wo)), l);
     R att = coatDirAtten(s.mat, s.wo) * coatDirAtten(s.mat, wi);
     return V4<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att;
 }
 
-// sampleBSDFDirection (principled/sample.slang:4-51), subset
-template <class R> bool sampleDirection(const BsdfState<R>& s, Rng& rng, V3<R>& wi) {
+// sampleBSDFDirection (principled/sample.slang:4-51) with sampleDielectric (dielectric/sample.slang:7-53); the
+// dielectric lobe refracts at the IOR of `lambda` when `spectral`
+template <class R> bool sampleDirection(const BsdfState<R>& s, Rng& rng, V3<R>& wi, bool& isTrans, R lambda = R(0),
+                                        bool spectral = false) {
+    isTrans = false;
     R sel = R(rng.next());
     if (sel < s.w.coat) {  // sampleClearcoat (clearcoat.slang:73-97)
         R u1 = R(rng.next()), u2 = R(rng.next());
@@ -1348,14 +1505,28 @@ template <class R> bool sampleDirection(const BsdfState<R>& s, Rng& rng, V3<R>& 
         return wi.z > R(0);
     }
     sel -= s.w.metal;
-    if (sel < s.w.dielectric) {  // sampleDielectric (dielectric/sample.slang:7-53) with transmission 0
+    if (sel < s.w.dielectric) {  // sampleDielectric
         if (s.wo.z <= R(0)) return false;
-        if (dielIdentity(s.mat)) return false;
+        if (dielIdentity(s.mat)) {
+            wi = -s.wo;
+            isTrans = s.mat.transmission > R(0);
+            return s.mat.transmission > R(0);
+        }
         R u1 = R(rng.next()), u2 = R(rng.next());
         V3<R> m;
         if (!sampleVndf(s.wo, s.ggx, u1, u2, m)) return false;
         R wom = dot(s.wo, m);
         if (wom <= R(0)) return false;
+        R F = fresnelDielectric(wom, interfaceEta(s.mat, s.frontFace, lambda, spectral));
+        R tprob = transmissionProbability(s.mat, F);
+        if (tprob > R(0) && R(rng.next()) < tprob) {
+            V3<R> t = refractDir(-s.wo, m, refractionEta(s.mat, s.frontFace, lambda, spectral));
+            if (dot(t, t) > R(0) && t.z < R(0)) {
+                wi = t;
+                isTrans = true;
+                return true;
+            }
+        }
         wi = m * (R(2) * wom) - s.wo;
         return wi.z > R(0);
     }
@@ -1601,6 +1772,8 @@ MaterialR<R> toMaterialR(const VKRT_CudaMaterial& m) {
     r.emissionColor = V3<R>(R(m.emissionColor[0]), R(m.emissionColor[1]), R(m.emissionColor[2]));
     r.emissionLuminance = R(m.emissionLuminance);
     r.abbe = R(m.abbeNumber);
+    r.absorptionCoefficient = R(m.absorptionCoefficient);
+    r.attenuationColor = V3<R>(R(m.attenuationColor[0]), R(m.attenuationColor[1]), R(m.attenuationColor[2]));
     return r;
 }
 
@@ -1704,10 +1877,67 @@ bool shadowVisible(Ctx<R>& c, V3<R> p, V3<R> gn, V3<R> wi, R tmax) {  // light/d
     return !occluded(c, o, wi, tmax);
 }
 
+// The emissive-NEE shadow ray: visible, occluded, or unsupported (through a transmissive surface). Scenes without
+// transmissive materials take the any-hit query above; with them the segment is scanned by shadowFp32 (the FP32
+// traversal also in brute-force mode).
+template <class R>
+int shadowResult(Ctx<R>& c, bool transmissiveScene, V3<R> p, V3<R> gn, V3<R> wi, R tmax) {
+    if (!transmissiveScene) return shadowVisible(c, p, gn, wi, tmax) ? kShadowVisible : kShadowOccluded;
+    c.stats.shadowRays++;
+    V3<R> off = dot(wi, gn) >= R(0) ? gn : -gn;
+    V3<R> o = p + off * R(kShadowOrigin);
+    return shadowFp32(c.s, V3<float>(o), V3<float>(wi), kTMin, float(tmax));
+}
+
 struct ModeFlags {
     bool neeEnabled;   // misNeeEnabled && emissiveMeshCount > 0 (state.slang:50-52)
     bool envNee;       // environment importance sampling enabled and a distribution exists
+    bool transmissive; // some material has transmission > 0 (environment NEE is then off: vkrt has none)
 };
+
+// MediumState (bsdf/base/medium.slang:7-33): the medium a path entered through a transmissive interface
+template <class R>
+struct Medium {
+    bool refractive = false, absorbing = false;
+    V4<R> sigma = V4<R>(R(0));  // absorption: RGB in xyz, the four hero lanes, or the single wavelength in x
+    bool boundary() const { return refractive || absorbing; }
+};
+
+template <class R>
+R absorptionSigma1(R tint, R coeff) {  // materialAbsorptionSigma (medium.slang:44-64)
+    return -std::log(std::max(tint, R(1e-6))) * coeff;
+}
+
+// updateMediumStateFromTransmission / ...Spectral (medium.slang:79-115); `mode` 0 RGB, 1 hero lanes, 2 one wavelength
+template <class R>
+void updateMedium(Medium<R>& med, const Rgb2Spec* tab, const MaterialR<R>& m, uint32_t frontFace, bool isTrans,
+                  int mode, V4<R> lam) {
+    if (!isTrans) return;
+    bool entering = frontFace != 0u;
+    med.refractive = entering && mediumIsRefractive(m);
+    med.absorbing = entering && hasAbsorption(m);
+    med.sigma = V4<R>(R(0));
+    if (!med.absorbing) return;
+    V3<R> tint = sat(m.attenuationColor);
+    if (mode == 0) {
+        med.sigma = V4<R>(absorptionSigma1(tint.x, m.absorptionCoefficient),
+                          absorptionSigma1(tint.y, m.absorptionCoefficient),
+                          absorptionSigma1(tint.z, m.absorptionCoefficient), R(0));
+    } else if (mode == 1) {
+        V4<R> s4 = spectralScalar4(*tab, tint, lam);
+        for (int i = 0; i < 4; ++i) med.sigma[i] = absorptionSigma1(s4[i], m.absorptionCoefficient);
+    } else {
+        med.sigma = V4<R>(absorptionSigma1(spectralScalar(*tab, tint, lam.x), m.absorptionCoefficient));
+    }
+}
+
+template <class R>
+V4<R> mediumTransmittance(const Medium<R>& med, R dist) {
+    if (!med.absorbing) return V4<R>(R(1));
+    V4<R> T;
+    for (int i = 0; i < 4; ++i) T[i] = std::exp(-med.sigma[i] * dist);
+    return T;
+}
 
 template <class R>
 V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sampleIndexGlobal, uint32_t rngMode,
@@ -1722,10 +1952,12 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
     V3<R> radiance(R(0)), thr(R(1));
     R prevBsdfPdf = R(0);
     bool prevNee = false;
+    Medium<R> med;
     R rot = R(c.sd.environmentRotation);
     for (uint32_t depth = 0; depth < c.sd.rrMaxDepth; ++depth) {
         HitRec h = traceClosest(c, o, d, depth == 0);
         if (!h.hit()) {
+            if (med.boundary()) break;  // shouldAccumulateEnvironmentMiss (loop.slang:4-6)
             V3<R> L = envRadiance<R>(c.s, c.sd, d);
             R w = R(1);
             if (mf.envNee && prevNee && depth > 0 && prevBsdfPdf > R(0)) {
@@ -1735,22 +1967,32 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
             radiance += thr * L * w;
             break;
         }
+        if (med.absorbing) {  // applyRgbMediumTransmittance (rgb/transport.slang:10-17)
+            V4<R> T = mediumTransmittance(med, R(h.t));
+            thr = thr * V3<R>(T.x, T.y, T.z);
+        }
         if (!anyPositive(thr)) break;
         Vertex<R> v = makeVertex(c, h, o, d);
         captureFeature(c, v);
         BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace);
         V3<R> contrib(R(0));
-        bool vertexNeeSupported = true;
-        if (mf.neeEnabled && st.wo.z > R(0)) {  // sampleDirectLightRgb (rgb_lighting.slang:7-31)
+        const bool neeAllowedHere = !med.refractive;  // rgb/integrator.slang:61
+        bool vertexNeeSupported = neeAllowedHere;
+        if (mf.neeEnabled && neeAllowedHere && st.wo.z > R(0)) {  // sampleDirectLightRgb (rgb_lighting.slang:7-31)
             LightSampleR<R> ls = sampleEmissive(c, v.hitPoint, rng);
-            if (ls.valid && shadowVisible(c, v.hitPoint, v.surf.geometricNormal, ls.wi, ls.shadowDist)) {
-                V3<R> wl = toLocal(ls.wi, v.basis);
+            int vis = ls.valid ? shadowResult(c, mf.transmissive, v.hitPoint, v.surf.geometricNormal, ls.wi,
+                                              ls.shadowDist)
+                               : kShadowOccluded;
+            if (vis == kShadowTransmission) vertexNeeSupported = false;
+            V3<R> wl = toLocal(ls.wi, v.basis);
+            if (vis == kShadowVisible && !(mediumIsRefractive(v.mat) && wl.z <= R(0))) {
                 V3<R> f;
                 R pdf;
                 evalRgb(st, wl, f, pdf);
                 if (pdf > R(0)) {
                     R mis = (ls.pdfSA * ls.pdfSA) / (ls.pdfSA * ls.pdfSA + pdf * pdf);
-                    contrib += (f * std::fabs(wl.z)) * ls.emission * mis / ls.pdfSA;
+                    V4<R> T = mediumTransmittance(med, ls.shadowDist);
+                    contrib += V3<R>(T.x, T.y, T.z) * (f * std::fabs(wl.z)) * ls.emission * mis / ls.pdfSA;
                 }
             }
         }
@@ -1790,7 +2032,8 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
         // sampleRgbNextDirection (rgb/transport.slang:23-45) via sampleBSDF (sample_rgb.slang:6-23)
         if (st.wo.z <= R(0)) break;
         V3<R> wl;
-        if (!sampleDirection(st, rng, wl)) break;
+        bool isTrans;
+        if (!sampleDirection(st, rng, wl, isTrans)) break;
         V3<R> f;
         R pdf;
         evalRgb(st, wl, f, pdf);
@@ -1800,13 +2043,15 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
         thr *= weight;
         if (!anyPositive(thr)) break;
         prevBsdfPdf = pdf;
-        prevNee = vertexNeeSupported;
+        prevNee = vertexNeeSupported && !isTrans;
+        updateMedium(med, static_cast<const Rgb2Spec*>(nullptr), v.mat, v.surf.frontFace, isTrans, 0, V4<R>(R(0)));
         if (depth + 1u >= c.sd.rrMinDepth) {  // rgb/integrator.slang:100-106
             R p = clampr(maxc(thr), R(kRRMin), R(kRRMax));
             if (R(rng.next()) > p) break;
             thr /= p;
         }
-        o = v.hitPoint + v.surf.geometricNormal * R(kShadowOrigin);  // loop.slang:113-120
+        // advancePathRay (loop.slang:113-120): a refracted ray starts below the surface
+        o = v.hitPoint + (isTrans ? -v.surf.geometricNormal : v.surf.geometricNormal) * R(kShadowOrigin);
         d = toWorld(wl, v.basis);
     }
     return radiance;
@@ -1815,7 +2060,8 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
 template <class R>
 V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sampleIndexGlobal, uint32_t rngMode,
                       uint64_t seed) {
-    // spectral_hero/integrator.slang:16-172 (hero lanes stay active: no dispersive transmission in the subset)
+    // spectral_hero/integrator.slang:16-172 with spectral_hero/transport.slang: four hero lanes until a dispersive
+    // refraction collapses the path to its first lane, which then continues as a single-wavelength path
     Rng rng = makeRng(rngMode, seed, px, py, c.sd.frameNumber, sampleIndexGlobal);
     c.stats.pathSamples++;
     R jx = R(rng.next()) - R(0.5);
@@ -1830,12 +2076,21 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
     for (int i = 0; i < 4; ++i) lam[i] = R(kLambdaMin) + fracr(R(unit) + R(offs[i])) * R(kLambdaRange);
     V4<R> invPdf = V4<R>(R(kLambdaRange));
     V4<R> thr(R(1)), techPath(R(1)), prevVertexTech(R(0)), prevBsdfTech(R(0)), spec(R(0));
+    bool collapsed = false;  // !spectralHeroPathActive
+    R thrS = R(0), specS = R(0), prevBsdfPdf = R(0);
+    V3<R> xyzDone(R(0));  // the hero lanes' radiance, moved to XYZ at the collapse
     bool prevNee = false;
+    Medium<R> med;
     R rot = R(c.sd.environmentRotation);
     for (uint32_t depth = 0; depth < c.sd.rrMaxDepth; ++depth) {
         HitRec h = traceClosest(c, o, d, depth == 0);
         if (!h.hit()) {
+            if (med.boundary()) break;
             V3<R> L = envRadiance<R>(c.s, c.sd, d);
+            if (collapsed) {
+                specS += thrS * spectralScalar(c.tab, L, lam.x);
+                break;
+            }
             R w = heroBalance(techPath);
             if (mf.envNee && prevNee && depth > 0) {
                 R pe = envPdf(c.s, d, rot);
@@ -1846,25 +2101,50 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
             spec += thr * (spectralScalar4(c.tab, L, lam) * w);
             break;
         }
-        if (!anyPositive(thr)) break;
+        if (med.absorbing) {  // applySpectralHeroMediumTransmittance (spectral_hero/transport.slang:22-35)
+            V4<R> T = mediumTransmittance(med, R(h.t));
+            if (collapsed) thrS *= T.x;
+            else thr = thr * T;
+        }
+        if (collapsed ? !(thrS > R(0)) : !anyPositive(thr)) break;
         Vertex<R> v = makeVertex(c, h, o, d);
         captureFeature(c, v);
         BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace);
         V4<R> contrib(R(0));
-        bool vertexNeeSupported = true;
-        if (mf.neeEnabled && st.wo.z > R(0)) {  // sampleDirectLightSpectralHero (spectral_lighting.slang:34-64)
+        R contribS = R(0);
+        const bool neeAllowedHere = !med.refractive;
+        bool vertexNeeSupported = neeAllowedHere;
+        if (mf.neeEnabled && neeAllowedHere && st.wo.z > R(0)) {
+            // sampleDirectLightSpectralHero / sampleDirectLightSpectralSingle (spectral_lighting.slang:7-64)
             LightSampleR<R> ls = sampleEmissive(c, v.hitPoint, rng);
-            if (ls.valid && shadowVisible(c, v.hitPoint, v.surf.geometricNormal, ls.wi, ls.shadowDist)) {
-                V3<R> wl = toLocal(ls.wi, v.basis);
-                V4<R> tp;
-                V4<R> fcos = evalSpectral(st, c.tab, wl, lam, tp) * std::fabs(wl.z);
-                V4<R> lt = techPath * ls.pdfSA, bt = techPath * tp;
-                R den = sum4(lt) + sum4(bt);
-                R mis = den > R(0) ? lt.x / den : R(0);
-                if (mis > R(0)) contrib += fcos * spectralScalar4(c.tab, ls.emission, lam) * (mis / ls.pdfSA);
+            int vis = ls.valid ? shadowResult(c, mf.transmissive, v.hitPoint, v.surf.geometricNormal, ls.wi,
+                                              ls.shadowDist)
+                               : kShadowOccluded;
+            if (vis == kShadowTransmission) vertexNeeSupported = false;
+            V3<R> wl = toLocal(ls.wi, v.basis);
+            if (vis == kShadowVisible && !(mediumIsRefractive(v.mat) && wl.z <= R(0))) {
+                V4<R> T = mediumTransmittance(med, ls.shadowDist);
+                if (collapsed) {
+                    V3<R> f;
+                    R pdf;
+                    evalScalar(st, &c.tab, wl, lam.x, true, f, pdf);
+                    if (pdf > R(0)) {
+                        R value = f.x * std::fabs(wl.z) * spectralScalar(c.tab, ls.emission, lam.x);
+                        R mis = (ls.pdfSA * ls.pdfSA) / (ls.pdfSA * ls.pdfSA + pdf * pdf);
+                        contribS += mis * T.x * value / ls.pdfSA;
+                    }
+                } else {
+                    V4<R> tp;
+                    V4<R> fcos = evalSpectral(st, c.tab, wl, lam, tp) * std::fabs(wl.z);
+                    V4<R> lt = techPath * ls.pdfSA, bt = techPath * tp;
+                    R den = sum4(lt) + sum4(bt);
+                    R mis = den > R(0) ? lt.x / den : R(0);
+                    if (mis > R(0))
+                        contrib += T * fcos * spectralScalar4(c.tab, ls.emission, lam) * (mis / ls.pdfSA);
+                }
             }
         }
-        if (mf.envNee && st.wo.z > R(0)) {
+        if (mf.envNee && st.wo.z > R(0)) {  // never with transmissive materials, so never on a collapsed path
             V3<R> wi;
             R pe;
             R u1 = R(rng.next()), u2 = R(rng.next());
@@ -1883,46 +2163,83 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
         }
         V3<R> emission = v.mat.emissionColor * v.mat.emissionLuminance;
         if (anyPositive(emission)) {
-            R w = heroBalance(techPath);
-            if (mf.neeEnabled && prevNee && depth > 0) {
-                R lpa = R(c.s.meshes[h.mesh].lightPdfArea);
-                R lps = R(0);
-                if (lpa > R(0)) {
-                    R d2 = R(h.t) * R(h.t);
-                    R cl = std::fabs(dot(d, v.surf.geometricNormal));
-                    if (d2 > R(0) && cl > R(0)) lps = lpa * d2 / cl;
-                }
-                V4<R> bt = prevVertexTech * prevBsdfTech, lt = prevVertexTech * lps;
-                R den = sum4(bt) + sum4(lt);
-                w = den > R(0) ? bt.x / den : R(0);
+            R lps = R(0);
+            R lpa = R(c.s.meshes[h.mesh].lightPdfArea);
+            if (lpa > R(0)) {
+                R d2 = R(h.t) * R(h.t);
+                R cl = std::fabs(dot(d, v.surf.geometricNormal));
+                if (d2 > R(0) && cl > R(0)) lps = lpa * d2 / cl;
             }
-            contrib += spectralScalar4(c.tab, emission, lam) * w;
+            if (collapsed) {  // bsdfEmitterMisWeight (loop.slang:60-80)
+                R w = R(1);
+                if (mf.neeEnabled && prevNee && depth > 0 && prevBsdfPdf > R(0))
+                    w = lps <= R(0) ? R(1) : (prevBsdfPdf * prevBsdfPdf) / (prevBsdfPdf * prevBsdfPdf + lps * lps);
+                contribS += spectralScalar(c.tab, emission, lam.x) * w;
+            } else {
+                R w = heroBalance(techPath);
+                if (mf.neeEnabled && prevNee && depth > 0) {
+                    V4<R> bt = prevVertexTech * prevBsdfTech, lt = prevVertexTech * lps;
+                    R den = sum4(bt) + sum4(lt);
+                    w = den > R(0) ? bt.x / den : R(0);
+                }
+                contrib += spectralScalar4(c.tab, emission, lam) * w;
+            }
         }
-        spec += thr * contrib;
-        // sampleSpectralBSDF (sample_spectral.slang:6-24)
+        if (collapsed) specS += thrS * contribS;
+        else spec += thr * contrib;
+        // sampleSpectralHeroNextDirection (spectral_hero/transport.slang:49-109)
         if (st.wo.z <= R(0)) break;
         V3<R> wl;
-        if (!sampleDirection(st, rng, wl)) break;
-        V4<R> tp;
-        V4<R> val = evalSpectral(st, c.tab, wl, lam, tp);
-        if (!(tp.x > R(0))) break;
-        V4<R> weight = val * (std::fabs(wl.z) / tp.x);
-        if (!anyPositive(weight)) break;
-        prevVertexTech = techPath;
-        prevBsdfTech = tp;
-        techPath *= tp;
-        thr *= weight;
-        if (!anyPositive(thr)) break;
-        prevNee = vertexNeeSupported;
-        if (depth + 1u >= c.sd.rrMinDepth) {
-            R p = clampr(max4(thr), R(kRRMin), R(kRRMax));
-            if (R(rng.next()) > p) break;
-            techPath = techPath * p;
-            thr = thr / p;
+        bool isTrans;
+        if (!sampleDirection(st, rng, wl, isTrans, lam.x, true)) break;
+        if (collapsed) {
+            V3<R> f;
+            R pdf;
+            evalScalar(st, &c.tab, wl, lam.x, true, f, pdf);
+            if (pdf <= R(0)) break;
+            V3<R> weight = f * (std::fabs(wl.z) / pdf);
+            if (!anyPositive(weight)) break;
+            thrS *= weight.x;
+            if (!(thrS > R(0))) break;
+            prevBsdfPdf = pdf;
+        } else {
+            V4<R> tp;
+            V4<R> val = evalSpectral(st, c.tab, wl, lam, tp);
+            if (!(tp.x > R(0))) break;
+            V4<R> weight = val * (std::fabs(wl.z) / tp.x);
+            if (!anyPositive(weight)) break;
+            prevVertexTech = techPath;
+            prevBsdfTech = tp;
+            techPath *= tp;
+            thr *= weight;
+            if (!anyPositive(thr)) break;
+            if (isTrans && mediumIsRefractive(v.mat) && v.mat.abbe > R(0)) {  // collapse to the first lane
+                xyzDone += spectral4ToXYZ(spec, lam, invPdf);
+                spec = V4<R>(R(0));
+                thrS = thr.x;
+                thr = V4<R>(R(0));
+                prevBsdfPdf = tp.x;
+                collapsed = true;
+            }
         }
-        o = v.hitPoint + v.surf.geometricNormal * R(kShadowOrigin);
+        prevNee = vertexNeeSupported && !isTrans;
+        updateMedium(med, &c.tab, v.mat, v.surf.frontFace, isTrans, collapsed ? 2 : 1, lam);
+        if (depth + 1u >= c.sd.rrMinDepth) {
+            if (collapsed) {
+                R p = clampr(thrS, R(kRRMin), R(kRRMax));
+                if (R(rng.next()) > p) break;
+                thrS /= p;
+            } else {
+                R p = clampr(max4(thr), R(kRRMin), R(kRRMax));
+                if (R(rng.next()) > p) break;
+                techPath = techPath * p;
+                thr = thr / p;
+            }
+        }
+        o = v.hitPoint + (isTrans ? -v.surf.geometricNormal : v.surf.geometricNormal) * R(kShadowOrigin);
         d = toWorld(wl, v.basis);
     }
+    if (collapsed) return xyzDone + cieXYZ(lam.x) * ((specS * invPdf.x) / R(kCieY));
     return spectral4ToXYZ(spec, lam, invPdf);
 }
 
@@ -1956,8 +2273,10 @@ void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderPa
     bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
     ModeFlags mf;
     mf.neeEnabled = sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u;
+    mf.transmissive = false;
+    for (const VKRT_CudaMaterial& m : s.materials) mf.transmissive = mf.transmissive || m.transmission > 0.0f;
     mf.envNee = s.envSampling == VKRT_CUDA_ENV_IMPORTANCE && s.env.valid && sd.misNeeEnabled != 0u &&
-                sd.environmentTextureIndex == s.envTexture;
+                sd.environmentTextureIndex == s.envTexture && !mf.transmissive;
     Rgb2Spec tab;
     if (!s.rgb2spec.empty()) {
         tab.table = s.rgb2spec.data();
@@ -2332,7 +2651,8 @@ int32_t oracle_bsdf_sample_rgb(const VKRT_CudaMaterial* m, const float wo[3], ui
     rng.h = rngState;
     V3<float> w;
     *pdf = 0.0f;
-    if (st.wo.z <= 0.0f || !sampleDirection(st, rng, w)) return -1;
+    bool isTrans;
+    if (st.wo.z <= 0.0f || !sampleDirection(st, rng, w, isTrans)) return -1;
     V3<float> f;
     float p;
     evalRgb(st, w, f, p);

@@ -10,23 +10,38 @@ from vkrt_gb300 import RenderContext, abi, scenes
 pytestmark = pytest.mark.gpu
 
 
-def _mirror_cornell():
+def _mirror_cornell(coat=False):
+    """With `coat`, the mirror box wears a clear coat (a visible layer: features stop there) and the short box is a
+    subsurface material with an Oren-Nayar base."""
     s = scenes.cornell(64, 64, spp=4)
     mirror = s.materials[int(s.meshes["materialIndex"][-1])].copy()  # the last box gets its own smooth mirror
     mirror["metallic"] = 1.0
     mirror["roughness"] = 0.0
     mirror["baseColor"] = [0.9, 0.9, 0.9]
-    s.materials = np.concatenate([s.materials, mirror.reshape(1)])
+    mats = [mirror]
+    if coat:
+        mirror["clearcoat"] = 1.0
+        mirror["clearcoatGloss"] = 1.0
+        sss = s.materials[0].copy()
+        sss["baseColor"] = [0.8, 0.6, 0.4]
+        sss["subsurface"] = 0.8
+        sss["diffuseRoughness"] = 0.6
+        mats.append(sss)
+    first = len(s.materials)
+    s.materials = np.concatenate([s.materials] + [m.reshape(1) for m in mats])
     meshes = s.meshes.copy()
-    meshes["materialIndex"][-1] = len(s.materials) - 1
+    meshes["materialIndex"][-1] = first
+    if coat:
+        meshes["materialIndex"][-2] = first + 1
     s.meshes = meshes
     return s
 
 
+@pytest.mark.parametrize("coat", [False, True])
 @pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
-def test_features_match_oracle(built, integrator):
+def test_features_match_oracle(built, integrator, coat):
     from oracle import cpu
-    s = _mirror_cornell()
+    s = _mirror_cornell(coat)
     sd = s.scene_data
     with RenderContext(rng_mode=abi.RNG_REFERENCE, integrator=integrator) as ctx:
         ctx.upload_scene(s)
@@ -44,6 +59,9 @@ def test_features_match_oracle(built, integrator):
     # pixels that see the mirror carry the albedo of what it reflects, not the mirror's 0.9 grey
     assert (alb[..., 3] > 0).mean() > 0.9
     assert np.all(alb[..., 3] <= 4.0)
+    # a clear-coated mirror is a visible layer: its pixels keep the mirror's own F0 (0.9) instead of following it
+    mirror_albedo = (np.abs(alb[..., :3] - 0.9) < 1e-4).all(-1).mean()
+    assert (mirror_albedo > 0.05) if coat else (mirror_albedo == 0.0), mirror_albedo
 
 
 def test_features_accumulate_over_frames(built):

@@ -79,7 +79,8 @@ struct VKRT_CudaContext {
     DeviceArray<VKRT_CudaMaterial> materials;
     std::vector<VKRT_CudaMaterial> hostMaterials;
     uint32_t materialCount = 0;
-    bool extendedMaterials = false;  // some material has clearcoat, subsurface or diffuseRoughness above 0
+    bool extendedMaterials = false;     // some material has clearcoat, subsurface, diffuseRoughness or transmission
+    bool transmissiveMaterials = false;  // some material has transmission above 0
     DeviceArray<VKRT_CudaEmissiveMesh> emissiveMeshes;
     DeviceArray<VKRT_CudaEmissiveTriangle> emissiveTriangles;
     DeviceArray<float> meshAliasQ, triAliasQ;
@@ -297,9 +298,11 @@ int32_t validateFrame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
     return VKRT_CUDA_SUCCESS;
 }
 
+// Environment NEE (this backend's addition) is off in scenes with transmissive materials, where vkrt's estimator
+// (NEE unsupported through transmissive surfaces, no environment light inside media) has no environment technique.
 bool envNeeActive(const VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
     return c->cfg.environmentSampling == VKRT_CUDA_ENV_IMPORTANCE && c->envTexture != VKRT_CUDA_INVALID_INDEX &&
-           sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u;
+           sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u && !c->transmissiveMaterials;
 }
 
 WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spectral) {
@@ -319,6 +322,7 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
     S.neeEnabled = (sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u) ? 1u : 0u;
     S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
     S.extended = c->extendedMaterials ? 1u : 0u;
+    S.transmissive = c->transmissiveMaterials ? 1u : 0u;
     return S;
 }
 
@@ -519,9 +523,13 @@ int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* c, const VKRT_CudaMaterial*
     c->hostMaterials.assign(materials, materials + count);
     c->materialCount = count;
     c->extendedMaterials = false;
-    for (uint32_t i = 0; i < count; ++i)
-        if (materials[i].clearcoat > 0.0f || materials[i].subsurface > 0.0f || materials[i].diffuseRoughness > 0.0f)
+    c->transmissiveMaterials = false;
+    for (uint32_t i = 0; i < count; ++i) {
+        const VKRT_CudaMaterial& m = materials[i];
+        if (m.transmission > 0.0f) c->transmissiveMaterials = true;
+        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f)
             c->extendedMaterials = true;
+    }
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -892,6 +900,8 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     // a single context with an enabled radiance cache trains it and renders cache-terminated paths
     WfCacheFrame cache{};
     const bool useCache = count == 1 && c0->nrc && c0->nrc->ready() && c0->nrcCfg.enabled;
+    if (useCache && c0->transmissiveMaterials)
+        return invalid(c0, "the radiance cache covers reflection-only materials (a material has transmission)");
     if (useCache)
         cache = WfCacheFrame{c0->nrc.get(), c0->nrcCfg.terminationDepth, c0->nrcCfg.trainingPaths,
                              c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber};
@@ -1199,7 +1209,7 @@ int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const f
         return invalid(c, "the adjoint differentiates the RGB render mode only");
     for (const VKRT_CudaMaterial& m : c->hostMaterials) {
         if (m.specularTint != 0.0f) return invalid(c, "the adjoint needs specularTint 0 on every material");
-        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f)
+        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f)
             return invalid(c, "the adjoint covers the metal / dielectric / Lambert stack only");
     }
     VKRT_CudaAdjointConfig a{};

@@ -13,6 +13,7 @@
 // then the environment NEE request), so the result does not depend on when the shadow rays are traced.
 #pragma once
 
+#include "bsdf_full.cuh"
 #include "integrator.cuh"
 
 namespace vkrt {
@@ -20,6 +21,9 @@ namespace vkrt {
 constexpr uint32_t kPathPrevNee = 1u;  // the previous vertex sampled NEE (loop.slang:69-71)
 constexpr uint32_t kPathDone = 2u;
 constexpr uint32_t kPathFeatureDone = 4u;  // the sample's denoiser feature was taken at an earlier vertex
+constexpr uint32_t kPathRefractive = 8u;   // inside a refractive medium: no NEE (MediumState, medium.slang:7-33)
+constexpr uint32_t kPathAbsorbing = 16u;   // inside an absorbing medium: Beer-Lambert along each segment
+constexpr uint32_t kPathCollapsed = 32u;   // spectral path collapsed to its first hero lane by dispersion
 
 struct PathState {
     Rng rng;
@@ -28,9 +32,15 @@ struct PathState {
     float4 radiance;  // RGB radiance in xyz, or the four hero-lane spectral radiances
     float lamUnit;    // hero wavelength unit sample; lane i at 360 + frac(lamUnit + i/4) * 470
     float techPath, prevVertexTech, prevBsdfTech;  // hero MIS (shared by the four lanes)
-    float prevBsdfPdf;                             // RGB MIS
+    float prevBsdfPdf;                             // RGB MIS, and the single-wavelength MIS of a collapsed path
     uint32_t depth;
     uint32_t flags;
+    // full instantiations: hero lanes 1-3 of the technique pdfs (lane 0 in the scalars above; the lanes differ after
+    // dispersive interfaces) and the absorption of the medium the path is in (RGB in xyz, the four hero lanes, or the
+    // collapsed lane in x). A collapsed path keeps its throughput in thr.x, the XYZ of its hero lanes in
+    // radiance.xyz and its single-wavelength radiance in radiance.w.
+    float3 techYZW, prevVertexYZW, prevBsdfYZW;
+    float4 sigma;
 };
 
 struct ShadowRequest {
@@ -76,6 +86,10 @@ VKRT_DEV PathState beginPath(const StepConfig& cfg, const VKRT_CudaSceneData& sd
     p.prevBsdfPdf = 0.0f;
     p.depth = 0;
     p.flags = 0;
+    p.techYZW = f3(1.0f);
+    p.prevVertexYZW = f3(0.0f);
+    p.prevBsdfYZW = f3(0.0f);
+    p.sigma = f4(0.0f);
     return p;
 }
 
@@ -83,6 +97,8 @@ VKRT_DEV PathState beginPath(const StepConfig& cfg, const VKRT_CudaSceneData& sd
 template <bool kSpectral>
 VKRT_DEV float3 pathResult(const StepConfig& cfg, const PathState& p) {
     if (!kSpectral) return xyz(p.radiance);
+    if (p.flags & kPathCollapsed)  // spectralSampleToXYZ of the surviving lane (spectral.slang:99-102)
+        return xyz(p.radiance) + cieXYZ(heroLambdas(p.lamUnit).x) * (p.radiance.w * (kLambdaRange / kCieYIntegral));
     return spectral4ToXYZ(p.radiance, heroLambdas(p.lamUnit), kLambdaRange);
 }
 
@@ -115,7 +131,7 @@ struct DenoiserFeature {
 };
 
 VKRT_DEV void captureFeature(DenoiserFeature& f, const Surface& s, const ShadeMaterial& m) {
-    if (f.weight > 0.0f || denoiserFollowsSpecular(m)) return;
+    if (f.weight > 0.0f || denoiserFollowsSpecular(m, s.frontFace)) return;
     f.albedo = denoiserAlbedo(m);
     f.normal = s.shadingNormal;
     f.weight = 1.0f;
@@ -126,12 +142,270 @@ struct FeatureHook : NoVertexHook {
     VKRT_DEV void surface(const Surface& s, const ShadeMaterial& m, const Bsdf&) { captureFeature(*f, s, m); }
 };
 
-// Processes the hit of p's current ray. Returns true when the path continues with a new ray in p.o / p.d.
-// `shadows` receives up to two requests (count in `numShadows`).
-template <bool kSpectral, class Hook = NoVertexHook, bool kExt = false>
-VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const StepConfig& cfg,
-                              const SpecTable& tab, PathState& p, const TraceHit& h, ShadowRequest* shadows,
-                              uint32_t& numShadows, Hook hook = Hook()) {
+VKRT_DEV float sum4f(float4 a) { return a.x + a.y + a.z + a.w; }
+VKRT_DEV float heroBalance(float4 t) {  // heroWavelengthBalanceWeight (spectral.slang:115-118)
+    const float c = sum4f(t);
+    return c > 0.0f ? t.x / c : 0.0f;
+}
+VKRT_DEV float4 mediumTransmittance(const PathState& p, float dist) {  // medium.slang:66-72
+    if (!(p.flags & kPathAbsorbing)) return f4(1.0f);
+    return make_float4(expf(-p.sigma.x * dist), expf(-p.sigma.y * dist), expf(-p.sigma.z * dist),
+                       expf(-p.sigma.w * dist));
+}
+VKRT_DEV float absorptionSigma(float tint, float coeff) {  // materialAbsorptionSigma (medium.slang:44-64)
+    return -logf(fmaxf(tint, 1e-6f)) * coeff;
+}
+
+// One vertex of the full integrators: shadePathVertex with vkrt's whole reflection stack, its transmissive
+// interface and the media behind it (rgb/integrator.slang:15-113, spectral_hero/integrator.slang:16-172,
+// spectral_hero/transport.slang): Beer-Lambert absorption along segments inside a medium, no NEE and no environment
+// inside a refractive medium, NEE that the shadow tracer marks unsupported when its ray meets a transmissive
+// surface (then p loses kPathPrevNee), refraction below the surface, and the collapse of a hero path to its first
+// lane after a dispersive refraction (the path then runs as a single-wavelength path).
+template <bool kSpectral, class Hook>
+VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const StepConfig& cfg,
+                                  const SpecTable& tab, PathState& p, const TraceHit& h, ShadowRequest* shadows,
+                                  uint32_t& numShadows, Hook hook) {
+    numShadows = 0;
+    const uint32_t depth = p.depth;
+    const float rot = sd.environmentRotation;
+    const bool prevNee = (p.flags & kPathPrevNee) != 0u;
+    bool collapsed = kSpectral && (p.flags & kPathCollapsed) != 0u;
+    const float4 lam = heroLambdas(p.lamUnit);
+    float4 tech = make_float4(p.techPath, p.techYZW.x, p.techYZW.y, p.techYZW.z);
+    const float4 pvt = make_float4(p.prevVertexTech, p.prevVertexYZW.x, p.prevVertexYZW.y, p.prevVertexYZW.z);
+    const float4 pbt = make_float4(p.prevBsdfTech, p.prevBsdfYZW.x, p.prevBsdfYZW.y, p.prevBsdfYZW.z);
+    if (h.mesh == VKRT_CUDA_INVALID_INDEX) {  // environment, unless a medium boundary is active (loop.slang:4-6)
+        if (p.flags & (kPathRefractive | kPathAbsorbing)) return false;
+        const float3 L = envRadiance(sc, sd, p.d);
+        if (kSpectral) {
+            if (collapsed) {
+                p.radiance.w += p.thr.x * spectral1(tab, L, lam.x);
+                return false;
+            }
+            float w = heroBalance(tech);
+            if (cfg.envNee && prevNee && depth > 0) {
+                const float pe = envPdf(sc.env, p.d, rot);
+                const float4 bt = pvt * pbt, lt = pvt * pe;
+                const float den = sum4f(bt) + sum4f(lt);
+                w = den > 0.0f ? bt.x / den : 0.0f;
+            }
+            p.radiance += p.thr * spectral4(tab, L, lam) * w;
+        } else {
+            float w = 1.0f;
+            if (cfg.envNee && prevNee && depth > 0 && p.prevBsdfPdf > 0.0f) {
+                const float pe = envPdf(sc.env, p.d, rot);
+                if (pe > 0.0f) w = powerHeuristic(p.prevBsdfPdf, pe);
+            }
+            const float3 c = thr3(p) * L * w;
+            p.radiance += make_float4(c.x, c.y, c.z, 0.0f);
+        }
+        return false;
+    }
+    if (p.flags & kPathAbsorbing) {  // apply*MediumTransmittance (rgb/transport.slang:10-17, hero :22-35)
+        const float4 T = mediumTransmittance(p, h.t);
+        if (collapsed) p.thr.x *= T.x;
+        else p.thr = kSpectral ? p.thr * T : make_float4(p.thr.x * T.x, p.thr.y * T.y, p.thr.z * T.z, 0.0f);
+    }
+    if (collapsed ? !(p.thr.x > 0.0f) : !anyPos(p.thr)) return false;
+    Surface s = reconstructSurface(sc, h.mesh, h.prim, h.u, h.v, p.o, p.d, h.t);
+    ShadeMaterial mat;
+    Basis basis;
+    shadeVertex(sc, s, p.d, mat, basis);
+    const BsdfFull bsdf = makeBsdfFull(mat, toLocal(-p.d, basis), s.frontFace);
+    hook.surface(s, mat, bsdf);
+
+    if (anyPos(mat.emission)) {  // emission, MIS against emissive NEE at the previous vertex (loop.slang:62-80)
+        const bool misNee = cfg.neeEnabled && prevNee && depth > 0;
+        if (kSpectral && !collapsed) {
+            float w = heroBalance(tech);
+            if (misNee) {
+                const float lps = emitterLightPdfSA(sc, h.mesh, h.t, p.d, s.geometricNormal);
+                const float4 bt = pvt * pbt, lt = pvt * lps;
+                const float den = sum4f(bt) + sum4f(lt);
+                w = den > 0.0f ? bt.x / den : 0.0f;
+            }
+            p.radiance += p.thr * spectral4(tab, mat.emission, lam) * w;
+        } else {
+            float w = 1.0f;
+            if (misNee && p.prevBsdfPdf > 0.0f) {
+                const float lps = emitterLightPdfSA(sc, h.mesh, h.t, p.d, s.geometricNormal);
+                w = lps <= 0.0f ? 1.0f : powerHeuristic(p.prevBsdfPdf, lps);
+            }
+            if (collapsed) {
+                p.radiance.w += p.thr.x * spectral1(tab, mat.emission, lam.x) * w;
+            } else {
+                const float3 c = thr3(p) * mat.emission * w;
+                p.radiance += make_float4(c.x, c.y, c.z, 0.0f);
+                hook.emission(thr3(p) * w);
+            }
+        }
+    }
+
+    if (depth == cfg.cacheDepth) {
+        hook.cacheQuery(s, mat);
+        return false;
+    }
+
+    const bool neeHere = (p.flags & kPathRefractive) == 0u;  // currentVertexNeeAllowed
+    if (cfg.neeEnabled && neeHere && bsdf.wo.z > 0.0f) {
+        // sampleDirectLight{Rgb, SpectralHero, SpectralSingle} (light/direct/*.slang): the shadow ray is traced even
+        // when the light lies below a refractive surface, since its answer may mark NEE unsupported
+        LightSample ls;
+        if (sampleEmissive(sc, s.hitPoint, p.rng, ls)) {
+            const float3 wl = toLocal(ls.wi, basis);
+            float4 c = f4(0.0f);
+            if (!(mediumIsRefractive(mat) && wl.z <= 0.0f)) {
+                const float4 T = mediumTransmittance(p, ls.shadowDist);
+                float pdf;
+                if (!kSpectral) {
+                    const float3 f = evalScalarFull<false>(bsdf, tab, wl, 0.0f, pdf);
+                    if (pdf > 0.0f) {
+                        const float3 v = thr3(p) * (make_float3(T.x, T.y, T.z) * f * fabsf(wl.z) * ls.emission *
+                                                    (powerHeuristic(ls.pdfSA, pdf) / ls.pdfSA));
+                        c = make_float4(v.x, v.y, v.z, 0.0f);
+                    }
+                } else if (collapsed) {
+                    const float3 f = evalScalarFull<true>(bsdf, tab, wl, lam.x, pdf);
+                    if (pdf > 0.0f) {
+                        const float value = f.x * fabsf(wl.z) * spectral1(tab, ls.emission, lam.x);
+                        c.w = p.thr.x * (powerHeuristic(ls.pdfSA, pdf) * T.x * value / ls.pdfSA);
+                    }
+                } else {
+                    float4 tp;
+                    const float4 fcos = evalHeroFull(bsdf, tab, wl, lam, tp) * fabsf(wl.z);
+                    const float4 lt = tech * ls.pdfSA, bt = tech * tp;
+                    const float den = sum4f(lt) + sum4f(bt);
+                    const float mis = den > 0.0f ? lt.x / den : 0.0f;
+                    if (mis > 0.0f) c = p.thr * (T * fcos * spectral4(tab, ls.emission, lam) * (mis / ls.pdfSA));
+                }
+            }
+            const float3 off = dot(ls.wi, s.geometricNormal) >= 0.0f ? s.geometricNormal : -s.geometricNormal;
+            shadows[numShadows++] = ShadowRequest{s.hitPoint + off * kShadowOriginOffset, ls.wi, ls.shadowDist, c};
+        }
+    }
+    // environment NEE: off when any material is transmissive (vkrt has none), so never on a collapsed path
+    if (cfg.envNee && bsdf.wo.z > 0.0f) {
+        const float u1 = p.rng.next(), u2 = p.rng.next();
+        float3 wi;
+        float pe;
+        if (envSample(sc.env, u1, u2, rot, wi, pe)) {
+            const float3 wl = toLocal(wi, basis);
+            float4 c = f4(0.0f);
+            if (kSpectral) {
+                float4 tp;
+                const float4 fcos = evalHeroFull(bsdf, tab, wl, lam, tp) * fabsf(wl.z);
+                const float4 lt = tech * pe, bt = tech * tp;
+                const float den = sum4f(lt) + sum4f(bt);
+                const float mis = den > 0.0f ? lt.x / den : 0.0f;
+                if (mis > 0.0f) c = p.thr * (fcos * spectral4(tab, envRadiance(sc, sd, wi), lam) * (mis / pe));
+            } else {
+                float pdf;
+                const float3 f = evalScalarFull<false>(bsdf, tab, wl, 0.0f, pdf);
+                if (pdf > 0.0f) {
+                    const float3 v = thr3(p) * (f * fabsf(wl.z) * envRadiance(sc, sd, wi) * (powerHeuristic(pe, pdf) / pe));
+                    c = make_float4(v.x, v.y, v.z, 0.0f);
+                }
+            }
+            const float3 off = dot(wi, s.geometricNormal) >= 0.0f ? s.geometricNormal : -s.geometricNormal;
+            shadows[numShadows++] = ShadowRequest{s.hitPoint + off * kShadowOriginOffset, wi, kTMax, c};
+        }
+    }
+
+    // next direction (sample_rgb.slang:6-23, sample_spectral.slang:6-24, spectral_hero/transport.slang:49-109)
+    if (bsdf.wo.z <= 0.0f) return false;
+    float3 wl;
+    bool isTrans;
+    if (!sampleFull(bsdf, p.rng, lam.x, kSpectral, wl, isTrans)) return false;
+    float pdf;
+    if (!kSpectral) {
+        const float3 f = evalScalarFull<false>(bsdf, tab, wl, 0.0f, pdf);
+        if (!(pdf > 0.0f)) return false;
+        const float3 weight = f * (fabsf(wl.z) / pdf);
+        if (!anyPos(weight)) return false;
+        p.thr = make_float4(p.thr.x * weight.x, p.thr.y * weight.y, p.thr.z * weight.z, 0.0f);
+        if (!anyPos(p.thr)) return false;
+        p.prevBsdfPdf = pdf;
+    } else if (collapsed) {
+        const float3 f = evalScalarFull<true>(bsdf, tab, wl, lam.x, pdf);
+        if (!(pdf > 0.0f)) return false;
+        const float3 weight = f * (fabsf(wl.z) / pdf);
+        if (!anyPos(weight)) return false;
+        p.thr.x *= weight.x;
+        if (!(p.thr.x > 0.0f)) return false;
+        p.prevBsdfPdf = pdf;
+    } else {
+        float4 tp;
+        const float4 val = evalHeroFull(bsdf, tab, wl, lam, tp);
+        if (!(tp.x > 0.0f)) return false;
+        const float4 weight = val * (fabsf(wl.z) / tp.x);
+        if (!anyPos(weight)) return false;
+        p.prevVertexTech = tech.x;
+        p.prevVertexYZW = make_float3(tech.y, tech.z, tech.w);
+        p.prevBsdfTech = tp.x;
+        p.prevBsdfYZW = make_float3(tp.y, tp.z, tp.w);
+        tech = tech * tp;
+        p.thr *= weight;
+        if (!anyPos(p.thr)) return false;
+        if (isTrans && mediumIsRefractive(mat) && mat.abbe > 0.0f) {
+            // dispersion: the hero lanes' radiance (and this vertex's pending NEE) moves to XYZ, lane 0 goes on
+            const float3 done = spectral4ToXYZ(p.radiance, lam, kLambdaRange);
+            p.radiance = make_float4(done.x, done.y, done.z, 0.0f);
+            for (uint32_t r = 0; r < numShadows; ++r) {
+                const float3 c = spectral4ToXYZ(shadows[r].contribution, lam, kLambdaRange);
+                shadows[r].contribution = make_float4(c.x, c.y, c.z, 0.0f);
+            }
+            p.thr = make_float4(p.thr.x, 0.0f, 0.0f, 0.0f);
+            p.prevBsdfPdf = tp.x;
+            p.flags |= kPathCollapsed;
+            collapsed = true;
+        }
+    }
+    if (neeHere && !isTrans) p.flags |= kPathPrevNee;
+    else p.flags &= ~kPathPrevNee;
+    if (isTrans) {  // updateMediumStateFromTransmission[Spectral] (medium.slang:79-115)
+        const bool entering = s.frontFace != 0u;
+        const bool absorbing = entering && hasAbsorption(mat);
+        p.flags &= ~(kPathRefractive | kPathAbsorbing);
+        if (entering && mediumIsRefractive(mat)) p.flags |= kPathRefractive;
+        p.sigma = f4(0.0f);
+        if (absorbing) {
+            p.flags |= kPathAbsorbing;
+            const float3 tint = sat(mat.attenuationColor);
+            const float k = mat.absorption;
+            if (!kSpectral) {
+                p.sigma = make_float4(absorptionSigma(tint.x, k), absorptionSigma(tint.y, k), absorptionSigma(tint.z, k),
+                                      0.0f);
+            } else if (collapsed) {
+                p.sigma = f4(absorptionSigma(spectral1(tab, tint, lam.x), k));
+            } else {
+                const float4 s4 = spectral4(tab, tint, lam);
+                p.sigma = make_float4(absorptionSigma(s4.x, k), absorptionSigma(s4.y, k), absorptionSigma(s4.z, k),
+                                      absorptionSigma(s4.w, k));
+            }
+        }
+    }
+    if (depth + 1u >= sd.rrMinDepth) {  // Russian roulette
+        const float q = !kSpectral ? maxc(thr3(p)) : (collapsed ? p.thr.x : max4(p.thr));
+        const float prob = fminf(fmaxf(q, kRRMin), kRRMax);
+        if (p.rng.next() > prob) return false;
+        if (kSpectral && !collapsed) tech = tech * prob;
+        p.thr = p.thr / prob;
+    }
+    p.techPath = tech.x;
+    p.techYZW = make_float3(tech.y, tech.z, tech.w);
+    // advancePathRay (loop.slang:113-120): a refracted ray starts below the surface
+    p.o = s.hitPoint + (isTrans ? -s.geometricNormal : s.geometricNormal) * kShadowOriginOffset;
+    p.d = toWorld(wl, basis);
+    p.depth = depth + 1u;
+    return p.depth < sd.rrMaxDepth;
+}
+
+// The vertex step of the reflection-only instantiations (the glTF subset of shading.cuh).
+template <bool kSpectral, class Hook>
+VKRT_DEV bool shadePathVertexSubset(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const StepConfig& cfg,
+                                    const SpecTable& tab, PathState& p, const TraceHit& h, ShadowRequest* shadows,
+                                    uint32_t& numShadows, Hook hook) {
     numShadows = 0;
     const uint32_t depth = p.depth;
     const float rot = sd.environmentRotation;
@@ -163,7 +437,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
     ShadeMaterial mat;
     Basis basis;
     shadeVertex(sc, s, p.d, mat, basis);
-    Bsdf bsdf = makeBsdf<kExt>(mat, toLocal(-p.d, basis), s.frontFace);
+    Bsdf bsdf = makeBsdf(mat, toLocal(-p.d, basis), s.frontFace);
     const float4 lam = heroLambdas(p.lamUnit);
     hook.surface(s, mat, bsdf);
 
@@ -204,13 +478,13 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             float pdf;
             float4 c = f4(0.0f);
             if (kSpectral) {
-                float4 fcos = evalSpectral<kExt>(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
+                float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
                 float lt = p.techPath * ls.pdfSA, bt = p.techPath * pdf;
                 float den = 4.0f * lt + 4.0f * bt;
                 float mis = den > 0.0f ? lt / den : 0.0f;
                 if (mis > 0.0f) c = p.thr * (fcos * spectral4(tab, ls.emission, lam) * (mis / ls.pdfSA));
             } else {
-                float3 f = evalRgb<kExt>(bsdf, wl, pdf);
+                float3 f = evalRgb(bsdf, wl, pdf);
                 if (pdf > 0.0f) {
                     float3 v = thr3(p) * (f * fabsf(wl.z) * ls.emission * (powerHeuristic(ls.pdfSA, pdf) / ls.pdfSA));
                     c = make_float4(v.x, v.y, v.z, 0.0f);
@@ -233,13 +507,13 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
             float pdf;
             float4 c = f4(0.0f);
             if (kSpectral) {
-                float4 fcos = evalSpectral<kExt>(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
+                float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
                 float lt = p.techPath * pe, bt = p.techPath * pdf;
                 float den = 4.0f * lt + 4.0f * bt;
                 float mis = den > 0.0f ? lt / den : 0.0f;
                 if (mis > 0.0f) c = p.thr * (fcos * spectral4(tab, envRadiance(sc, sd, wi), lam) * (mis / pe));
             } else {
-                float3 f = evalRgb<kExt>(bsdf, wl, pdf);
+                float3 f = evalRgb(bsdf, wl, pdf);
                 if (pdf > 0.0f) {
                     float3 Le = envRadiance(sc, sd, wi);
                     float3 v = thr3(p) * (f * fabsf(wl.z) * Le * (powerHeuristic(pe, pdf) / pe));
@@ -256,10 +530,10 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
     // next direction (sample_rgb.slang:6-23 / sample_spectral.slang:6-24)
     if (bsdf.wo.z <= 0.0f) return false;
     float3 wl;
-    if (!sampleDirection<kExt>(bsdf, p.rng, wl)) return false;
+    if (!sampleDirection(bsdf, p.rng, wl)) return false;
     float pdf;
     if (kSpectral) {
-        float4 val = evalSpectral<kExt>(bsdf, tab, wl, lam, pdf);
+        float4 val = evalSpectral(bsdf, tab, wl, lam, pdf);
         if (!(pdf > 0.0f)) return false;
         float4 weight = val * (fabsf(wl.z) / pdf);
         if (!anyPos(weight)) return false;
@@ -268,7 +542,7 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
         p.techPath *= pdf;
         p.thr *= weight;
     } else {
-        float3 f = evalRgb<kExt>(bsdf, wl, pdf);
+        float3 f = evalRgb(bsdf, wl, pdf);
         if (!(pdf > 0.0f)) return false;
         float3 weight = f * (fabsf(wl.z) / pdf);
         if (!anyPos(weight)) return false;
@@ -290,6 +564,16 @@ VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& s
     p.d = toWorld(wl, basis);
     p.depth = depth + 1u;
     return p.depth < sd.rrMaxDepth;
+}
+
+// Processes the hit of p's current ray. Returns true when the path continues with a new ray in p.o / p.d.
+// `shadows` receives up to two requests (count in `numShadows`). kExt selects vkrt's whole material stack.
+template <bool kSpectral, class Hook = NoVertexHook, bool kExt = false>
+VKRT_DEV bool shadePathVertex(const DeviceScene& sc, const VKRT_CudaSceneData& sd, const StepConfig& cfg,
+                              const SpecTable& tab, PathState& p, const TraceHit& h, ShadowRequest* shadows,
+                              uint32_t& numShadows, Hook hook = Hook()) {
+    if constexpr (kExt) return shadePathVertexFull<kSpectral>(sc, sd, cfg, tab, p, h, shadows, numShadows, hook);
+    else return shadePathVertexSubset<kSpectral>(sc, sd, cfg, tab, p, h, shadows, numShadows, hook);
 }
 
 }  // namespace vkrt

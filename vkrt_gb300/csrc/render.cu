@@ -64,9 +64,17 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     for (uint32_t i = 0; i < ns; ++i) {
                         pc.shadow++;
                         TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
-                        if (traceBvh<true, kCountBytes>(sc, r, k.stackColumn, k.stackStride, counters).mesh ==
-                            VKRT_CUDA_INVALID_INDEX)
+                        if (kFull) {  // a transmissive occluder makes the vertex's NEE unsupported
+                            const TraceHit o = traceBvh<true, kCountBytes, false, true>(sc, r, k.stackColumn,
+                                                                                         k.stackStride, counters);
+                            if (o.mesh == VKRT_CUDA_INVALID_INDEX) {
+                                if (o.prim == kShadowThroughTransmission) p.flags &= ~kPathPrevNee;
+                                else p.radiance += sh[i].contribution;
+                            }
+                        } else if (traceBvh<true, kCountBytes>(sc, r, k.stackColumn, k.stackStride, counters).mesh ==
+                                   VKRT_CUDA_INVALID_INDEX) {
                             p.radiance += sh[i].contribution;
+                        }
                     }
                     if (!cont) break;
                 }

@@ -3,9 +3,10 @@
 // importance distribution, and rgb2spec hero-wavelength spectral upsampling. Each function names the vkrt shader it
 // computes the same quantity as (paths relative to src/shaders/).
 //
-// Material coverage: metal, dielectric specular and diffuse lobes always; clearcoat, Oren-Nayar (diffuseRoughness)
-// and fake subsurface in the extended instantiations (kExt), chosen when a scene's materials use them. Sheen (its
-// LTC fit table) and transmission (refraction, media, dispersion) are not evaluated: their lobes get no weight.
+// Material coverage here: the glTF metallic-roughness subset (metal, dielectric specular and Lambert lobes), which the
+// reflection-only instantiations use. The rest of vkrt's stack (clearcoat, Oren-Nayar, fake subsurface, the
+// transmissive interface with dispersion and media) is in bsdf_full.cuh for the full instantiations. Sheen (its LTC
+// fit table) is not evaluated: its lobe gets no weight.
 #pragma once
 
 #include "scene.cuh"
@@ -262,6 +263,14 @@ VKRT_DEV float rgb2specEval(float3 c, float l) {
     return 0.5f * x * rsqrtf(x * x + 1.0f) + 0.5f;
 }
 
+// spectralScalarFromLinearSrgb (spectral.slang:37-48)
+VKRT_DEV float spectral1(const SpecTable& tab, float3 rgb, float l) {
+    float m = maxc(rgb);
+    if (m <= 0.0f) return 0.0f;
+    float scale = m <= 1.0f ? 1.0f : m;
+    return rgb2specEval(rgb2specFetch(tab, rgb / scale), l) * scale;
+}
+
 // spectralScalarFromLinearSrgb4 (spectral.slang:50-64)
 VKRT_DEV float4 spectral4(const SpecTable& tab, float3 rgb, float4 l) {
     float m = maxc(rgb);
@@ -344,6 +353,8 @@ struct ShadeMaterial {
     float3 emission;  // emissionColor * emissionLuminance after the emissive texture
     bool conductor;
     float clearcoat, clearcoatGloss, subsurface, diffuseRoughness;  // the extended reflection stack's inputs
+    float transmission, abbe, absorption;                            // the transmissive interface and its medium
+    float3 attenuationColor;
 };
 
 VKRT_DEV void shadeVertex(const DeviceScene& sc, Surface& s, float3 dir, ShadeMaterial& mat, Basis& basis) {
@@ -377,6 +388,10 @@ VKRT_DEV void shadeVertex(const DeviceScene& sc, Surface& s, float3 dir, ShadeMa
     mat.clearcoatGloss = m.clearcoatGloss;
     mat.subsurface = m.subsurface;
     mat.diffuseRoughness = m.diffuseRoughness;
+    mat.transmission = m.transmission;
+    mat.abbe = m.abbeNumber;
+    mat.absorption = m.absorptionCoefficient;
+    mat.attenuationColor = make_float3(m.attenuationColor[0], m.attenuationColor[1], m.attenuationColor[2]);
     float4 bc = sampleMaterialTexture(sc, m.baseColorTextureIndex, m.baseColorTextureWrap, m.baseColorTextureTransform,
                                       m.textureRotations[0], m.textureTexcoordSets & 0xffu, s.tex, f4(1.0f));
     mat.baseColor = mat.baseColor * xyz(bc) * xyz(s.tex.color);
@@ -418,12 +433,15 @@ VKRT_DEV float3 dielSpecF0(const ShadeMaterial& m) {  // fresnel.slang:15-20
 
 VKRT_DEV float3 fresnelConductor(float cosT, float3 eta, float3 k);
 
-// Denoiser features (bsdf/principled/denoiser.slang:7-46) on the shaded subset, where the transmission, subsurface,
-// sheen and clearcoat layers are absent: a vertex whose only visible response is a sharp specular lobe is followed
-// through; the first other vertex gives the feature albedo (a weighted mix of the diffuse colour, the dielectric
-// and the metallic F0) and its shading normal.
-VKRT_DEV bool denoiserFollowsSpecular(const ShadeMaterial& m) {
-    if (maxc(m.baseColor * (1.0f - m.metallic)) > 1e-3f) return false;  // a visible base layer
+// Denoiser features (bsdf/principled/denoiser.slang:7-46) on the shaded layers, where transmission and sheen are
+// absent: a vertex whose only visible response is a sharp specular lobe is followed through (a front-facing clear
+// coat is a visible layer); the first other vertex gives the feature albedo (a weighted mix of the diffuse colour,
+// the dielectric and the metallic F0) and its shading normal. Subsurface changes neither rule: its share of the
+// albedo weight is taken from the diffuse share with the same colour, and its layer weight never exceeds it.
+VKRT_DEV bool denoiserFollowsSpecular(const ShadeMaterial& m, uint32_t frontFace) {
+    // a visible base layer: diffuse (its subsurface share is no larger) or a clear coat seen from the front
+    if (maxc(m.baseColor * (1.0f - m.metallic)) > 1e-3f) return false;
+    if (frontFace != 0u && m.clearcoat > 1e-3f) return false;
     if (m.roughness > 0.02f) return false;
     return m.metallic >= 1.0f - 1e-3f || maxc(dielSpecF0(m)) > 1e-3f;
 }
@@ -527,7 +545,7 @@ VKRT_DEV bool sampleVndf(float3 wo, const Ggx& g, float u1, float u2, float3& m)
 // Extended reflection stack (principled/eval_rgb.slang:4-105 beyond the glTF subset): Disney clearcoat
 // (lobes/clearcoat.slang: GTR1 distribution, gloss-remapped alpha, fixed 0.25 masking roughness, Schlick F0 0.04, its
 // directional attenuation on everything below it), Oren-Nayar diffuse for diffuseRoughness > 0 and the Disney fake
-// subsurface lobe (lobes/diffuse.slang, lobes/subsurface.slang). Used by the kExt instantiations.
+// subsurface lobe (lobes/diffuse.slang, lobes/subsurface.slang). Used by bsdf_full.cuh.
 VKRT_DEV float coatAlpha(const ShadeMaterial& m) {  // clearcoat.slang:20-28
     return fmaxf(0.1f + (0.001f - 0.1f) * sat(m.clearcoatGloss), 1e-3f);
 }
@@ -625,7 +643,7 @@ VKRT_DEV float3 dielDirAtten(float roughness, float3 f0, float cosT) {  // atten
     return sat(f3(1.0f) - sat(f0 * A + f3(B)));
 }
 
-template <bool kExt = false>
+// Branch weights of the glTF subset (principled/weights.slang:27-62 with no coat, subsurface or transmission)
 VKRT_DEV Bsdf makeBsdf(const ShadeMaterial& m, float3 wo, uint32_t frontFace) {
     Bsdf s;
     s.mat = m;
@@ -634,33 +652,22 @@ VKRT_DEV Bsdf makeBsdf(const ShadeMaterial& m, float3 wo, uint32_t frontFace) {
     s.ggx = makeGgx(m, wo);
     s.f0Diel = dielSpecF0(m);
     s.viewAtten = dielDirAtten(m.roughness, s.f0Diel, wo.z);
+    s.wCoat = s.wSub = 0.0f;
+    s.coatA = 0.1f;
+    s.viewCoat = 1.0f;
     float3 diff = m.baseColor * (1.0f - m.metallic);
     float nonMetal = 1.0f - m.metallic;
     float wm = m.metallic * fmaxf(lum(m.baseColor), 1e-3f);
     float wd = nonMetal * fmaxf(sat(lum(s.f0Diel)), 0.0f);
     float wf = lum(s.viewAtten) * nonMetal * fmaxf(lum(diff), 1e-3f);
-    float wc = 0.0f, ws = 0.0f;
-    s.viewCoat = 1.0f;
-    s.coatA = 0.1f;
-    if (kExt) {
-        s.coatA = coatAlpha(m);
-        s.viewCoat = coatAtten(m, wo);
-        wc = m.clearcoat * 0.25f;
-        wm *= s.viewCoat;
-        wd *= s.viewCoat;
-        ws = s.viewCoat * wf * m.subsurface;
-        wf = s.viewCoat * wf * (1.0f - m.subsurface);
-    }
-    float tot = wc + wm + wd + wf + ws;
+    float tot = wm + wd + wf;
     if (tot <= 0.0f) {
-        s.wMetal = s.wDiel = s.wCoat = s.wSub = 0.0f;
+        s.wMetal = s.wDiel = 0.0f;
         s.wDiff = 1.0f;
     } else {
-        s.wCoat = wc / tot;
         s.wMetal = wm / tot;
         s.wDiel = wd / tot;
         s.wDiff = wf / tot;
-        s.wSub = ws / tot;
     }
     return s;
 }
@@ -672,43 +679,7 @@ VKRT_DEV float3 metalFresnel(const Bsdf& s, float c) {
                            : schlick(c, s.mat.baseColor);
 }
 
-// The extended stack's coat value and substrate factor for unit colours: value = coat + att * (metal + ...), with
-// substrate = diffuseColour * (diffuse + subsurface) (scalars for a unit colour)
-struct ExtTerms {
-    float coat, att, diffuse, subsurface;
-};
-
-template <bool kExt>
-VKRT_DEV ExtTerms extTerms(const Bsdf& s, float3 wi, float& pdf) {
-    ExtTerms t{0.0f, 1.0f, 0.0f, 0.0f};
-    if (!kExt) {
-        if (s.wDiff > 0.0f) {
-            t.diffuse = kInvPi;
-            pdf += s.wDiff * (wi.z * kInvPi);
-        }
-        return t;
-    }
-    if (s.wCoat > 0.0f) {
-        float cp;
-        t.coat = coatEval(s.mat.clearcoat, s.coatA, s.wo, wi, cp);
-        pdf += s.wCoat * cp;
-    }
-    if (s.wDiff > 0.0f) {
-        t.diffuse = (1.0f - s.mat.subsurface) *
-                    (s.mat.diffuseRoughness <= 0.0f ? kInvPi : orenNayar(s.mat.diffuseRoughness, s.wo, wi));
-        pdf += s.wDiff * (wi.z * kInvPi);
-    }
-    if (s.wSub > 0.0f) {
-        t.subsurface = s.mat.subsurface * fakeSss(s.mat.diffuseRoughness, s.wo, wi);
-        pdf += s.wSub * (wi.z * kInvPi);
-    }
-    t.att = s.viewCoat * coatAtten(s.mat, wi);
-    return t;
-}
-
-// RGB reflection stack (principled/eval_rgb.slang:4-121: metal + dielectric + diffuse; with kExt also clearcoat,
-// Oren-Nayar and fake subsurface)
-template <bool kExt = false>
+// RGB reflection stack of the subset (principled/eval_rgb.slang:4-121: metal + dielectric + Lambert)
 VKRT_DEV float3 evalRgb(const Bsdf& s, float3 wi, float& pdf) {
     pdf = 0.0f;
     if (wi.z <= 0.0f) return f3(0.0f);
@@ -732,14 +703,15 @@ VKRT_DEV float3 evalRgb(const Bsdf& s, float3 wi, float& pdf) {
         diel = schlick(wom, s.f0Diel) * DG;
         pdf += s.wDiel * reflPdf;
     }
-    ExtTerms t = extTerms<kExt>(s, wi, pdf);
-    float3 sub = s.mat.baseColor * ((1.0f - s.mat.metallic) * (t.diffuse + t.subsurface));
-    float3 base = metal * s.mat.metallic + (diel + s.viewAtten * sub) * (1.0f - s.mat.metallic);
-    return kExt ? f3(t.coat) + base * t.att : base;
+    float3 sub = f3(0.0f);
+    if (s.wDiff > 0.0f) {
+        sub = s.mat.baseColor * ((1.0f - s.mat.metallic) * kInvPi);
+        pdf += s.wDiff * (wi.z * kInvPi);
+    }
+    return metal * s.mat.metallic + (diel + s.viewAtten * sub) * (1.0f - s.mat.metallic);
 }
 
-// 4-lane spectral stack (principled/eval_spectral.slang:4-94); all lanes share one technique pdf in this subset
-template <bool kExt = false>
+// 4-lane spectral stack of the subset (principled/eval_spectral.slang:4-94); all lanes share one technique pdf
 VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, float4 l, float& pdf) {
     pdf = 0.0f;
     if (wi.z <= 0.0f) return f4(0.0f);
@@ -763,26 +735,18 @@ VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, flo
         diel = spectral4(tab, sat(schlick(wom, s.f0Diel)), l) * DG;
         pdf += s.wDiel * reflPdf;
     }
-    ExtTerms t = extTerms<kExt>(s, wi, pdf);
     float4 sub = f4(0.0f);
-    if (s.wDiff > 0.0f || s.wSub > 0.0f)
-        sub = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l) * (t.diffuse + t.subsurface);
+    if (s.wDiff > 0.0f) {
+        sub = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l) * kInvPi;
+        pdf += s.wDiff * (wi.z * kInvPi);
+    }
     float4 va = spectral4(tab, sat(s.viewAtten), l);
-    float4 base = metal * s.mat.metallic + (diel + va * sub) * (1.0f - s.mat.metallic);
-    return kExt ? f4(t.coat) + base * t.att : base;
+    return metal * s.mat.metallic + (diel + va * sub) * (1.0f - s.mat.metallic);
 }
 
-// sampleBSDFDirection (principled/sample.slang:4-51): lobe by weight (coat, metal, dielectric, diffuse, subsurface)
-template <bool kExt = false>
+// sampleBSDFDirection (principled/sample.slang:4-51) of the subset: metal, dielectric reflection, diffuse
 VKRT_DEV bool sampleDirection(const Bsdf& s, Rng& rng, float3& wi) {
     float sel = rng.next();
-    if (kExt) {
-        if (sel < s.wCoat) {
-            float u1 = rng.next(), u2 = rng.next();
-            return coatSample(s.wo, s.coatA, u1, u2, wi);
-        }
-        sel -= s.wCoat;
-    }
     if (sel < s.wMetal || (sel - s.wMetal) < s.wDiel) {
         bool diel = !(sel < s.wMetal);
         if (diel && (s.wo.z <= 0.0f || dielIdentity(s.mat))) return false;

@@ -191,10 +191,16 @@ struct TraversalStack {
     }
 };
 
+// prim of a kTransmissive any-hit answer whose segment met transmissive surfaces only
+constexpr uint32_t kShadowThroughTransmission = 0xFFFFFFFEu;
+
 // Closest hit (anyHit = false) or first accepted hit (anyHit = true).
 // kMeshFilter: only triangles of mesh `meshFilter` count as hits (the selection-mask rays, which vkrt traces
 // against a TLAS holding the selected mesh alone).
-template <bool kAnyHit, bool kCount, bool kMeshFilter = false>
+// kTransmissive (any-hit shadow rays of scenes with transmissive materials, rt/payloads/shadow_payload.slang): hits on
+// meshes whose material has transmission > 0 do not end the search but leave prim = kShadowThroughTransmission;
+// an opaque hit anywhere on the segment answers occluded (vkrt reports whichever hit the driver accepts first).
+template <bool kAnyHit, bool kCount, bool kMeshFilter = false, bool kTransmissive = false>
 VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* smemColumn, uint32_t smemStride,
                            RenderCounters* counters, uint32_t meshFilter = 0u) {
     TraceHit best;
@@ -272,6 +278,10 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
             if (watertightHit(wr, org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
                               make_float3(c.x, c.y, c.z), tmin, tmax, t, b1, b2)) {
                 uint32_t gid = __float_as_uint(a.w);
+                if (kTransmissive && sc.materials[sc.meshes[__float_as_uint(b.w)].materialIndex].transmission > 0.0f) {
+                    best.prim = kShadowThroughTransmission;
+                    continue;
+                }
                 if (t < tmax || gid < best.gid) {
                     tmax = t;
                     best.t = t;

@@ -51,7 +51,8 @@ enum : uint32_t {
     kCntClass0 = 8,  // class-partitioned shade queue: misses, dielectric hits, metal hits
     kCntQueries = 11,  // radiance-cache queries of the iteration
 };
-constexpr uint32_t kPendCache = 16u;  // pendFlags: the path ended at a radiance-cache query
+constexpr uint32_t kPendCache = 16u;        // pendFlags: the path ended at a radiance-cache query
+constexpr uint32_t kPendUnsupported = 32u;  // pendFlags: an NEE shadow ray met a transmissive surface
 constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;  // kSortMaterial sorts by (scene, class)
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
 
@@ -123,6 +124,13 @@ struct WfGlobals {
     uint32_t features;
     float4* itemFeatA;
     float4* itemFeatN;
+    // scenes with transmissive materials: per slot, hero lanes 1-3 of the technique pdfs and the medium's absorption
+    // (extA = techYZW + sigma.x, extB = prevVertexYZW + sigma.y, extC = prevBsdfYZW + sigma.z, extD = sigma.w)
+    uint32_t transmissive;
+    float4* extA;
+    float4* extB;
+    float4* extC;
+    float* extD;
 };
 
 VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
@@ -217,6 +225,31 @@ VKRT_DEV PathState loadPath(const WfGlobals& g, uint32_t s) {
     return p;
 }
 
+// The full instantiations' part of the slot state. Without transmissive materials the hero lanes stay equal and no
+// medium is entered, so lanes 1-3 repeat lane 0.
+VKRT_DEV void storePathExt(const WfGlobals& g, uint32_t s, const PathState& p) {
+    if (!g.transmissive) return;
+    g.extA[s] = make_float4(p.techYZW.x, p.techYZW.y, p.techYZW.z, p.sigma.x);
+    g.extB[s] = make_float4(p.prevVertexYZW.x, p.prevVertexYZW.y, p.prevVertexYZW.z, p.sigma.y);
+    g.extC[s] = make_float4(p.prevBsdfYZW.x, p.prevBsdfYZW.y, p.prevBsdfYZW.z, p.sigma.z);
+    g.extD[s] = p.sigma.w;
+}
+
+VKRT_DEV void loadPathExt(const WfGlobals& g, uint32_t s, PathState& p) {
+    if (!g.transmissive) {
+        p.techYZW = f3(p.techPath);
+        p.prevVertexYZW = f3(p.prevVertexTech);
+        p.prevBsdfYZW = f3(p.prevBsdfTech);
+        p.sigma = f4(0.0f);
+        return;
+    }
+    const float4 a = g.extA[s], b = g.extB[s], c = g.extC[s];
+    p.techYZW = xyz(a);
+    p.prevVertexYZW = xyz(b);
+    p.prevBsdfYZW = xyz(c);
+    p.sigma = make_float4(a.w, b.w, c.w, g.extD[s]);
+}
+
 VKRT_DEV StepConfig stepConfig(const WfGlobals& g, const WfScene& S) {
     return StepConfig{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed, g.cacheDepth};
 }
@@ -238,6 +271,7 @@ VKRT_DEV bool startSample(const WfGlobals& g, const WfScene* scenes, uint32_t sl
     StepConfig cfg = stepConfig(g, S);
     PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, first + sample);
     storePath(g, slot, p);
+    storePathExt(g, slot, p);
     g.pendFlags[slot] = 0u;
     if (g.mode == kWavefrontAdjoint) {
         float inv = 1.0f / float(g.adj.sampleBase + S.spp);
@@ -675,6 +709,10 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
             applyPending(g, slot, p.radiance);
+            if constexpr (kFull) {
+                loadPathExt(g, slot, p);
+                if (pf & kPendUnsupported) p.flags &= ~kPathPrevNee;  // the previous vertex's NEE was unsupported
+            }
             if constexpr (kAdjoint) adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
             g.pendFlags[slot] = 0u;
             uint4 a = g.hitA[slot];
@@ -702,6 +740,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                 }
             }
             storePath(g, slot, p);
+            if constexpr (kFull) storePathExt(g, slot, p);
             uint32_t flags = queried ? kPendCache : 0u;
             if (ns > 0) {
                 g.pend0[slot] = sh[0].contribution;
@@ -766,6 +805,31 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g)
         nodeVisits, triTests);
     warpCount(&g.counters->shadowRays, traced);
     if (kCount) warpCountBytes(&g.counters->shadowNodeBytes, &g.counters->shadowTriBytes, nodeVisits, triTests);
+}
+
+// Shadow rays of scenes with transmissive materials: one ray per thread through traceBvh's transmissive any-hit
+// mode; a ray whose segment meets only transmissive surfaces marks its request unsupported.
+template <bool kCount>
+__global__ void __launch_bounds__(kWfThreads) kWfShadowTransmissive(WfGlobals g) {
+    extern __shared__ uint2 smemStack[];
+    const uint32_t n = g.counts[kCntShadow];
+    uint32_t traced = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        if (i < n) {
+            const float4 a = g.shadowA[i], b = g.shadowB[i];
+            const uint32_t tag = __float_as_uint(b.w);
+            const uint32_t slot = tag & 0x7FFFFFFFu;
+            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            const TraceRay r{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
+            const TraceHit h = traceBvh<true, kCount, false, true>(sc, r, smemStack + threadIdx.x, blockDim.x,
+                                                                   kCount ? g.counters : nullptr);
+            ++traced;
+            if (h.mesh == VKRT_CUDA_INVALID_INDEX)
+                atomicOr(&g.pendFlags[slot], h.prim == kShadowThroughTransmission ? kPendUnsupported : 4u << (tag >> 31));
+        }
+    }
+    warpCount(&g.counters->shadowRays, traced);
 }
 
 template <bool kSpectral, bool kAdjoint>
@@ -869,7 +933,7 @@ struct WavefrontEngine::Buffers {
     size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
            c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
            c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0,
-           c_fA = 0, c_fN = 0;
+           c_fA = 0, c_fN = 0, c_eA = 0, c_eB = 0, c_eC = 0, c_eD = 0;
     size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
     WfScene* scenes = nullptr;
     uint32_t* bases = nullptr;  // itemBase of every scene, then workBase
@@ -910,7 +974,8 @@ void WavefrontEngine::release() {
                     g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, b_->bases,
                     g.nrcQueries, g.slotQuery, g.nrcPred, b_->recIn, b_->recTarget, b_->recCount, g.adjDelta,
                     g.adjTotal,
-                    g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR};
+                    g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR,
+                    g.itemFeatA, g.itemFeatN, g.extA, g.extB, g.extC, g.extD};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b_->hostCount) cudaFreeHost(b_->hostCount);
@@ -977,12 +1042,20 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(slotItem, c_work, Q);
     WF_GROW(sampleBuf, c_sum, std::max<size_t>(totalItems, 1));
     bool features = false;  // forward frames render denoiser features when any scene has feature films
-    bool extended = false;  // some scene's materials use the extended reflection stack
+    bool extended = false;      // some scene's materials use the full material stack
+    bool transmissive = false;  // ... with transmission (media and per-lane hero state per slot)
     for (const WfScene& S : scenes) {
         if (mode == kWavefrontForward && S.film.albedoWrite) features = true;
         if (S.extended) extended = true;
+        if (S.transmissive) transmissive = true;
     }
     const bool full = features || extended;
+    if (transmissive) {
+        WF_GROW(extA, c_eA, Q);
+        WF_GROW(extB, c_eB, Q);
+        WF_GROW(extC, c_eC, Q);
+        WF_GROW(extD, c_eD, Q);
+    }
     if (features) {
         WF_GROW(itemFeatA, c_fA, std::max<size_t>(totalItems, 1));
         WF_GROW(itemFeatN, c_fN, std::max<size_t>(totalItems, 1));
@@ -1042,6 +1115,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     }
     g.mode = uint32_t(mode);
     g.features = features ? 1u : 0u;
+    g.transmissive = transmissive ? 1u : 0u;
     g.adj = adjoint ? *adjoint : AdjointParams{};
     g.cacheDepth = useCache ? cache->cacheDepth : 0xFFFFFFFFu;
     g.scenes = B.scenes;
@@ -1108,7 +1182,9 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             else kWfShade<false, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
         });
         stage(kStageShadow, [&] {
-            if (profile) kWfShadow<true, 8><<<gridI, kWfThreads, smem, stream>>>(g);
+            if (transmissive && profile) kWfShadowTransmissive<true><<<gridS, kWfThreads, smem, stream>>>(g);
+            else if (transmissive) kWfShadowTransmissive<false><<<gridS, kWfThreads, smem, stream>>>(g);
+            else if (profile) kWfShadow<true, 8><<<gridI, kWfThreads, smem, stream>>>(g);
             else kWfShadow<false, 8><<<gridI, kWfThreads, smem, stream>>>(g);
         });
         if (useCache)  // predictions for the paths that ended at the cache in this iteration

@@ -23,7 +23,8 @@ struct WfScene {
     uint32_t spectral;
     uint32_t neeEnabled;
     uint32_t envNee;
-    uint32_t extended;  // some material uses the extended reflection stack
+    uint32_t extended;      // some material uses vkrt's stack beyond the glTF subset (the full instantiations)
+    uint32_t transmissive;  // some material has transmission (media, per-lane hero pdfs, transmissive shadows)
     // filled by the engine
     uint32_t tileW, tileH, tilesX;
     uint32_t workBase, workCount;  // padded pixel work items (tile order)
