@@ -153,6 +153,13 @@ int32_t vkrt_cuda_set_environment(VKRT_CudaContext* context, uint32_t textureInd
 int32_t vkrt_cuda_upload_rgb2spec(VKRT_CudaContext* context, const float* table, uint32_t floatCount,
                                   const VKRT_CudaRGB2SpecTableInfo* info);
 
+/* The sheen lobe's LTC fit table, SHEEN_LTC_TABLE of vkrt (src/shaders/bsdf/data/sheen_ltc.slang:6-8): three
+ * 32 x 32 layers (transform a, transform b, directional albedo) over (cos theta_o, sheen roughness), row-major by
+ * roughness; floatCount must be 3072. Materials with a sheen colour (sheenTintWeight) render only once it is
+ * installed (a frame without it returns VKRT_CUDA_ERROR_INVALID_ARGUMENT). */
+#define VKRT_CUDA_SHEEN_TABLE_FLOATS 3072u
+int32_t vkrt_cuda_upload_sheen_table(VKRT_CudaContext* context, const float* table, uint32_t floatCount);
+
 /* Generates the sRGB rgb2spec table on the device (Jakob & Hanika 2019 Gauss-Newton fit against the CIE 1931
  * analytic fits under illuminant E, the colour space of vkrt's spectral output transform) and installs it.
  * Returns the table layout in outInfo; the table stays resident. */

@@ -24,7 +24,8 @@ class OracleSceneDesc(C.Structure):
                 ("emissiveMeshCount", _U32), ("emissiveTriangles", _V), ("emissiveTriangleCount", _U32),
                 ("meshAliasQ", _V), ("meshAliasIdx", _V), ("triAliasQ", _V), ("triAliasIdx", _V),
                 ("textures", C.POINTER(OracleTexture)), ("textureCount", _U32), ("rgb2spec", _V),
-                ("rgb2specFloatCount", _U32), ("environmentSampling", _U32), ("envTextureIndex", _U32)]
+                ("rgb2specFloatCount", _U32), ("environmentSampling", _U32), ("envTextureIndex", _U32),
+                ("sheenLtc", _V), ("sheenLtcFloatCount", _U32)]
 
 
 class OracleRenderParams(C.Structure):
@@ -109,6 +110,8 @@ class OracleScene:
             d.rgb2spec, d.rgb2specFloatCount = _p(scene.rgb2spec), len(scene.rgb2spec)
         d.environmentSampling = environment_sampling
         d.envTextureIndex = scene.env_texture
+        if scene.sheen_table is not None:
+            d.sheenLtc, d.sheenLtcFloatCount = _p(scene.sheen_table), len(scene.sheen_table)
         self.handle = self.lib.oracle_scene_create(C.byref(d))
         self.scene = scene
 

@@ -288,6 +288,7 @@ struct Scene {
     std::vector<uint32_t> meshIdx, triIdx;
     std::vector<Tex> textures;
     std::vector<float> rgb2spec;
+    std::vector<float> sheenLtc;  // 3 x 32 x 32 (transform a, transform b, albedo), empty: no sheen lobe
     std::vector<WorldTri> tris;        // BVH order after build
     std::vector<uint32_t> meshTriBase; // global id of the first triangle of each mesh
     std::vector<BvhNode> nodes;
@@ -597,6 +598,8 @@ HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float
     return best;
 }
 
+const float* sheenTable(const Scene& s) { return s.sheenLtc.empty() ? nullptr : s.sheenLtc.data(); }
+
 bool meshTransmissive(const Scene& s, uint32_t mesh) {
     return s.materials[s.meshes[mesh].materialIndex].transmission > 0.0f;
 }
@@ -898,7 +901,7 @@ struct MaterialR {  // Material fields the restated lobes read, after texturing
     V3<R> baseColor;
     R roughness, metallic, anisotropic, specular, specularTint, ior, transmission, subsurface, clearcoat;
     R clearcoatGloss, diffuseRoughness;
-    R sheenWeight;
+    R sheenWeight, sheenRoughness;
     V3<R> sheenTint;
     V3<R> eta, k;
     V3<R> emissionColor;
@@ -1106,7 +1109,7 @@ template <class R> bool sampleVndf(V3<R> wo, const Ggx<R>& g, R u1, R u2, V3<R>&
 
 template <class R>
 struct Weights {
-    R metal = 0, dielectric = 0, diffuse = 0, coat = 0, subsurface = 0;
+    R metal = 0, dielectric = 0, diffuse = 0, coat = 0, subsurface = 0, sheen = 0;
 };
 
 // Disney clearcoat (bsdf/lobes/clearcoat.slang) and the coat's directional attenuation (attenuation.slang:13-24)
@@ -1229,7 +1232,61 @@ template <class R> V3<R> refractDir(V3<R> i, V3<R> n, R eta) {
     return i * eta - n * (eta * c + std::sqrt(k));
 }
 
-template <class R> Weights<R> branchWeights(const MaterialR<R>& m, V3<R> wo, uint32_t frontFace) {  // weights.slang:27-62
+// Microfiber sheen through its LTC fit (bsdf/lobes/sheen.slang): a 32 x 32 table per layer over (cos theta_o,
+// roughness), looked up bilinearly (:23-39); the lobe is a linearly transformed cosine in the frame whose tangent
+// is wo's projection (:41-85)
+template <class R> R lerpr(R a, R b, R t) { return a * (R(1) - t) + b * t; }
+template <class R> R sheenLookup(const float* T, R cosT, R rough, uint32_t layer) {
+    R ux = sat(cosT) * R(31), uy = sat(rough) * R(31);
+    uint32_t x0 = std::min(uint32_t(ux), 31u), y0 = std::min(uint32_t(uy), 31u);
+    uint32_t x1 = std::min(x0 + 1u, 31u), y1 = std::min(y0 + 1u, 31u);
+    R tx = ux - std::floor(ux), ty = uy - std::floor(uy);
+    const float* L = T + layer * 1024u;
+    R e00 = R(L[y0 * 32u + x0]), e10 = R(L[y0 * 32u + x1]), e01 = R(L[y1 * 32u + x0]), e11 = R(L[y1 * 32u + x1]);
+    return lerpr(lerpr(e00, e10, tx), lerpr(e01, e11, tx), ty);
+}
+template <class R> V3<R> sheenColor(const MaterialR<R>& m, const float* T) {  // material.slang:63-73
+    return T ? sat(m.sheenTint) * sat(m.sheenWeight) : V3<R>(R(0));
+}
+template <class R> R sheenAlbedo(const float* T, R cosT, R rough) {  // sheenDirectionalAlbedo (sheen.slang:87-89)
+    return T ? sheenLookup(T, cosT, std::min(std::max(rough, R(1e-3)), R(1)), 2u) : R(0);
+}
+template <class R> R sheenAtten(const float* T, R weight, R cosT, R rough) {  // sheenLayerAttenuation (:91-93)
+    return sat(R(1) - weight * sheenAlbedo(T, cosT, rough));
+}
+template <class R> struct SheenLtc {
+    Basis<R> basis;
+    R a = R(0), b = R(0), albedo = R(0);
+};
+template <class R> SheenLtc<R> sheenLtcAt(const float* T, V3<R> wo, R sheenRough) {  // makeSheenParams (:41-57)
+    SheenLtc<R> p;
+    p.basis = makeBasis(V3<R>(R(0), R(0), R(1)), V4<R>(wo.x, wo.y, wo.z, R(1)));
+    if (!T || wo.z <= R(0)) return p;
+    R r = std::min(std::max(sheenRough, R(1e-3)), R(1));
+    p.a = sheenLookup(T, wo.z, r, 0u);
+    p.b = sheenLookup(T, wo.z, r, 1u);
+    p.albedo = sheenLookup(T, wo.z, r, 2u);
+    return p;
+}
+template <class R> R sheenDistribution(V3<R> lw, const SheenLtc<R>& p) {  // sheenDistributionValue (:59-74)
+    R z = std::max(lw.z, R(0));
+    if (z <= R(0) || std::fabs(p.a) < R(1e-5) || p.albedo < R(1e-5)) return R(0);
+    R axbz = p.a * lw.x + p.b * lw.z;
+    R len2 = axbz * axbz + (p.a * lw.y) * (p.a * lw.y) + lw.z * lw.z;
+    if (len2 <= R(1e-6)) return R(0);
+    R scale = p.a / len2;
+    return R(kInvPi) * z * scale * scale;
+}
+template <class R> R evalSheenUnit(const SheenLtc<R>& p, V3<R> wo, V3<R> wi, R& pdf) {  // evalSheen (:95-111)
+    pdf = R(0);
+    if (wo.z <= R(0) || wi.z <= R(0)) return R(0);
+    R D = sheenDistribution(toLocal(wi, p.basis), p);
+    pdf = D;
+    return p.albedo * D;
+}
+
+template <class R> Weights<R> branchWeights(const MaterialR<R>& m, V3<R> wo, uint32_t frontFace,
+                                            const float* sheenT) {  // weights.slang:27-62
     V3<R> diff = m.baseColor * (R(1) - m.metallic);
     R nonMetal = R(1) - m.metallic;
     R baseW = std::max(lum(m.baseColor), R(1e-3));
@@ -1238,24 +1295,28 @@ template <class R> Weights<R> branchWeights(const MaterialR<R>& m, V3<R> wo, uin
     R transW = m.transmission * std::max(lum(transmissionColor(m)), R(1e-3));
     R dielSpecW = nonMetal * std::max(sat(lum(dielSpecF0(m))) + transW, R(0));
     Weights<R> w;
+    V3<R> sc = sheenColor(m, sheenT);
     if (m.transmission > R(0) && frontFace == 0u) {  // interior side of a transmissive interface
         w.metal = m.metallic * baseW;
         w.dielectric = dielSpecW;
     } else {
         R dielAtt = lum(dielDirAtten(m, wo));
         R viewCoat = coatDirAtten(m, wo);
-        w.coat = m.clearcoat * R(0.25);
-        w.metal = viewCoat * m.metallic * baseW;
-        w.dielectric = viewCoat * dielSpecW;
-        w.diffuse = viewCoat * dielAtt * baseScatter * (R(1) - m.subsurface) * diffW;
-        w.subsurface = viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
+        R viewSheen = sheenAtten(sheenT, maxc(sc), wo.z, m.sheenRoughness);
+        w.sheen = lum(sc);
+        w.coat = viewSheen * m.clearcoat * R(0.25);
+        w.metal = viewSheen * viewCoat * m.metallic * baseW;
+        w.dielectric = viewSheen * viewCoat * dielSpecW;
+        w.diffuse = viewSheen * viewCoat * dielAtt * baseScatter * (R(1) - m.subsurface) * diffW;
+        w.subsurface = viewSheen * viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
     }
-    R total = w.coat + w.metal + w.dielectric + w.diffuse + w.subsurface;
+    R total = w.sheen + w.coat + w.metal + w.dielectric + w.diffuse + w.subsurface;
     if (total <= R(0)) {
-        w.metal = w.dielectric = w.coat = w.subsurface = R(0);
+        w.metal = w.dielectric = w.coat = w.subsurface = w.sheen = R(0);
         w.diffuse = R(1);
         return w;
     }
+    w.sheen /= total;
     w.coat /= total;
     w.metal /= total;
     w.dielectric /= total;
@@ -1273,15 +1334,20 @@ struct BsdfState {
     Weights<R> w;
     bool conductor;
     bool interior;  // useInteriorDielectricInterface (attenuation.slang:4-6)
+    const float* sheenT;  // the sheen LTC table, or null
+    SheenLtc<R> sheen;    // the sheen lobe's transform at wo
 };
 
-template <class R> BsdfState<R> makeBsdf(const MaterialR<R>& m, V3<R> wo, uint32_t frontFace) {
+template <class R> BsdfState<R> makeBsdf(const MaterialR<R>& m, V3<R> wo, uint32_t frontFace,
+                                         const float* sheenT = nullptr) {
     BsdfState<R> s;
     s.mat = m;
     s.wo = wo;
     s.frontFace = frontFace;
     s.ggx = makeGgx(m, wo);
-    s.w = branchWeights(m, wo, frontFace);
+    s.sheenT = sheenT;
+    s.sheen = sheenLtcAt(sheenT, wo, m.sheenRoughness);
+    s.w = branchWeights(m, wo, frontFace, sheenT);
     s.conductor = m.k.x > R(0) || m.k.y > R(0) || m.k.z > R(0);
     s.interior = m.transmission > R(0) && frontFace == 0u;
     return s;
@@ -1325,7 +1391,9 @@ template <class R> R evalTransmissionLane(const BsdfState<R>& s, V3<R> wi, R coa
 }
 
 template <class R> R transmissionCoatAtt(const BsdfState<R>& s) {  // materialTransmissionStackAttenuation
-    return s.interior ? R(1) : coatDirAtten(s.mat, s.wo);
+    if (s.interior) return R(1);
+    return sheenAtten(s.sheenT, maxc(sheenColor(s.mat, s.sheenT)), s.wo.z, s.mat.sheenRoughness) *
+           coatDirAtten(s.mat, s.wo);
 }
 
 // The scalar stack (principled/eval_rgb.slang:4-141): RGB (single = false) or one wavelength of the single-wavelength
@@ -1346,7 +1414,13 @@ template <class R> void evalScalar(const BsdfState<R>& s, const Rgb2Spec* tab, V
         return;
     }
     R coat = R(0);
-    V3<R> metal(R(0)), diel(R(0)), sub(R(0));
+    V3<R> metal(R(0)), diel(R(0)), sub(R(0)), sheenV(R(0)), sc(R(0));
+    if (s.w.sheen > R(0) || !s.interior) sc = spec(sheenColor(s.mat, s.sheenT));
+    if (s.w.sheen > R(0)) {
+        R sp;
+        sheenV = sc * evalSheenUnit(s.sheen, s.wo, wi, sp);
+        pdf += s.w.sheen * sp;
+    }
     if (s.w.coat > R(0)) {
         R cp;
         coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
@@ -1397,7 +1471,8 @@ template <class R> void evalScalar(const BsdfState<R>& s, const Rgb2Spec* tab, V
     }
     V3<R> viewAtt = dielDirAtten(s.mat, s.wo);
     R att = coatDirAtten(s.mat, s.wo) * coatDirAtten(s.mat, wi);  // reflectionStackAttenuation
-    value = V3<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att;
+    R viewSheen = sheenAtten(s.sheenT, maxc(sc), s.wo.z, s.mat.sheenRoughness);
+    value = sheenV + (V3<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att) * viewSheen;
 }
 
 template <class R> void evalRgb(const BsdfState<R>& s, V3<R> wi, V3<R>& value, R& pdf) {
@@ -1418,7 +1493,13 @@ template <class R> V4<R> evalSpectral(const BsdfState<R>& s, const Rgb2Spec& tab
         return v;
     }
     R coat = R(0);
-    V4<R> metal(R(0)), diel(R(0)), sub(R(0));
+    V4<R> metal(R(0)), diel(R(0)), sub(R(0)), sheenV(R(0)), sc(R(0));
+    if (s.w.sheen > R(0) || !s.interior) sc = spectralScalar4(tab, sat(sheenColor(s.mat, s.sheenT)), l);
+    if (s.w.sheen > R(0)) {
+        R sp;
+        sheenV = sc * evalSheenUnit(s.sheen, s.wo, wi, sp);
+        tp += V4<R>(s.w.sheen * sp);
+    }
     if (s.w.coat > R(0)) {
         R cp;
         coat = evalClearcoat(s.mat.clearcoat, clearcoatAlpha(s.mat), s.wo, wi, cp);
@@ -1473,7 +1554,10 @@ template <class R> V4<R> evalSpectral(const BsdfState<R>& s, const Rgb2Spec& tab
     if (s.interior) return metal * s.mat.metallic + diel * nonMetal;
     V4<R> viewAtt = spectralScalar4(tab, sat(dielDirAtten(s.mat, s.wo)), l);
     R att = coatDirAtten(s.mat, s.wo) * coatDirAtten(s.mat, wi);
-    return V4<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att;
+    R alb = sheenAlbedo(s.sheenT, s.wo.z, s.mat.sheenRoughness);
+    V4<R> viewSheen;
+    for (int i = 0; i < 4; ++i) viewSheen[i] = sat(R(1) - sc[i] * alb);
+    return sheenV + (V4<R>(coat) + (metal * s.mat.metallic + (diel + viewAtt * sub) * nonMetal) * att) * viewSheen;
 }
 
 // sampleBSDFDirection (principled/sample.slang:4-51) with sampleDielectric (dielectric/sample.slang:7-53); the
@@ -1482,6 +1566,18 @@ template <class R> bool sampleDirection(const BsdfState<R>& s, Rng& rng, V3<R>& 
                                         bool spectral = false) {
     isTrans = false;
     R sel = R(rng.next());
+    if (sel < s.w.sheen) {  // sampleSheen (sheen.slang:113-128)
+        const SheenLtc<R>& p = s.sheen;
+        if (std::fabs(p.a) < R(1e-5) || p.albedo < R(1e-5)) return false;
+        R r = std::sqrt(R(rng.next()));
+        R phi = R(2) * R(kPi) * R(rng.next());
+        R dx = r * std::cos(phi), dy = r * std::sin(phi);
+        R dz = std::sqrt(std::max(R(1) - (dx * dx + dy * dy), R(0)));
+        V3<R> lw = normalize(V3<R>(dx - dz * p.b, dy, dz * p.a));
+        wi = toWorld(lw, p.basis);
+        return wi.z > R(0);
+    }
+    sel -= s.w.sheen;
     if (sel < s.w.coat) {  // sampleClearcoat (clearcoat.slang:73-97)
         R u1 = R(rng.next()), u2 = R(rng.next());
         R a = clearcoatAlpha(s.mat), a2 = a * a, cm;
@@ -1767,6 +1863,7 @@ MaterialR<R> toMaterialR(const VKRT_CudaMaterial& m) {
     r.diffuseRoughness = R(m.diffuseRoughness);
     r.sheenWeight = R(m.sheenTintWeight[3]);
     r.sheenTint = V3<R>(R(m.sheenTintWeight[0]), R(m.sheenTintWeight[1]), R(m.sheenTintWeight[2]));
+    r.sheenRoughness = R(m.sheenRoughness);
     r.eta = V3<R>(R(m.eta[0]), R(m.eta[1]), R(m.eta[2]));
     r.k = V3<R>(R(m.k[0]), R(m.k[1]), R(m.k[2]));
     r.emissionColor = V3<R>(R(m.emissionColor[0]), R(m.emissionColor[1]), R(m.emissionColor[2]));
@@ -1974,7 +2071,7 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
         if (!anyPositive(thr)) break;
         Vertex<R> v = makeVertex(c, h, o, d);
         captureFeature(c, v);
-        BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace);
+        BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace, sheenTable(c.s));
         V3<R> contrib(R(0));
         const bool neeAllowedHere = !med.refractive;  // rgb/integrator.slang:61
         bool vertexNeeSupported = neeAllowedHere;
@@ -2109,7 +2206,7 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
         if (collapsed ? !(thrS > R(0)) : !anyPositive(thr)) break;
         Vertex<R> v = makeVertex(c, h, o, d);
         captureFeature(c, v);
-        BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace);
+        BsdfState<R> st = makeBsdf(v.mat, toLocal(-d, v.basis), v.surf.frontFace, sheenTable(c.s));
         V4<R> contrib(R(0));
         R contribS = R(0);
         const bool neeAllowedHere = !med.refractive;
@@ -2395,6 +2492,7 @@ void* oracle_scene_create(const OracleSceneDesc* d) {
         s.textures[i].rgba.assign(t.rgba, t.rgba + size_t(t.width) * t.height * 4);
     }
     if (d->rgb2spec && d->rgb2specFloatCount) s.rgb2spec.assign(d->rgb2spec, d->rgb2spec + d->rgb2specFloatCount);
+    if (d->sheenLtc && d->sheenLtcFloatCount >= 3072u) s.sheenLtc.assign(d->sheenLtc, d->sheenLtc + 3072);
     s.envSampling = d->environmentSampling;
     s.envTexture = d->envTextureIndex;
     if (s.envSampling == VKRT_CUDA_ENV_IMPORTANCE && d->envTextureIndex < s.textures.size() &&

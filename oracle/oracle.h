@@ -45,6 +45,8 @@ typedef struct OracleSceneDesc {
     uint32_t rgb2specFloatCount;
     uint32_t environmentSampling; /* VKRT_CUDA_ENV_*: 1 builds the importance distribution of envTextureIndex */
     uint32_t envTextureIndex;
+    const float* sheenLtc; /* 3 x 32 x 32 sheen LTC table (bsdf/data/sheen_ltc.slang layout), NULL: no sheen lobe */
+    uint32_t sheenLtcFloatCount;
 } OracleSceneDesc;
 
 typedef struct OracleRenderParams {

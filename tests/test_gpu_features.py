@@ -96,3 +96,20 @@ def test_features_accumulate_over_frames(built):
         b.render_frame(s.scene_data)
         np.testing.assert_array_equal(a.read_accumulation(), b.read_accumulation())
     del acc_on
+
+
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
+def test_features_through_glass_match_oracle(built, integrator):
+    """Smooth glass is followed through (denoiser.slang:13-21): the albedo behind it is taken."""
+    from oracle import cpu
+    from tests.test_gpu_materials import glass_cornell
+    s = glass_cornell()
+    with RenderContext(rng_mode=abi.RNG_REFERENCE, integrator=integrator) as ctx:
+        ctx.upload_scene(s)
+        ctx.set_denoiser_features(True)
+        ctx.render_frame(s.scene_data)
+        alb, nrm = ctx.read_denoiser_features()
+    _, ref_alb, ref_nrm = cpu.OracleScene(s).render_features(s.scene_data, rng_mode=abi.RNG_REFERENCE)
+    close_a = (np.abs(alb[..., :3] - ref_alb[..., :3]) <= 1e-4).all(-1)
+    close_n = (np.abs(nrm[..., :3] - ref_nrm[..., :3]) <= 1e-4).all(-1)
+    assert close_a.mean() > 0.97 and close_n.mean() > 0.97, (close_a.mean(), close_n.mean())

@@ -151,3 +151,86 @@ def test_transmissive_materials_rejected_by_the_adjoint_and_the_cache(built):
         ctx.nrc_configure(seed=3, enabled=1)
         with pytest.raises(Exception):
             ctx.render_frame(s.scene_data)
+
+
+def synthetic_sheen_table():
+    """A smooth stand-in for vkrt's sheen LTC table with the same layout and value ranges ([layer][roughness][cos]):
+    parity does not depend on the table's values, since the device and the oracle read the same table."""
+    c = np.linspace(0.0, 1.0, 32, dtype=np.float32)[None, :]
+    r = np.linspace(0.0, 1.0, 32, dtype=np.float32)[:, None]
+    a = 0.25 + 0.6 * r + 0.1 * c
+    b = 0.2 * (c - 0.5) * (1.0 - r)
+    albedo = 0.05 + 0.3 * r * (1.0 - 0.5 * c)
+    return np.stack([a + 0 * c, b + 0 * r, albedo]).astype(np.float32).reshape(-1)
+
+
+def sheen_cornell(width=64, height=64, spp=4, table=True):
+    s = scenes.cornell(width, height, spp=spp)
+    velvet = s.materials[0].copy()  # red velvet: diffuse base under a bright sheen layer
+    velvet["baseColor"] = [0.5, 0.05, 0.05]
+    velvet["sheenTintWeight"] = [1.0, 0.9, 0.8, 1.0]
+    velvet["sheenRoughness"] = 0.5
+    satin = s.materials[0].copy()  # sheen over clear coat over a metal
+    satin["metallic"] = 1.0
+    satin["roughness"] = 0.4
+    satin["baseColor"] = [0.8, 0.7, 0.3]
+    satin["sheenTintWeight"] = [0.6, 0.7, 1.0, 0.7]
+    satin["sheenRoughness"] = 0.2
+    satin["clearcoat"] = 0.5
+    first = len(s.materials)
+    s.materials = np.concatenate([s.materials, velvet.reshape(1), satin.reshape(1)])
+    meshes = s.meshes.copy()
+    meshes["materialIndex"][-1] = first
+    meshes["materialIndex"][-2] = first + 1
+    s.meshes = meshes
+    if table:
+        s.sheen_table = synthetic_sheen_table()
+    return s
+
+
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
+def test_sheen_rgb_parity(built, integrator):
+    from oracle import cpu
+    s = sheen_cornell()
+    with RenderContext(rng_mode=abi.RNG_REFERENCE, integrator=integrator) as ctx:
+        ctx.upload_scene(s)
+        ctx.render_frame(s.scene_data)
+        gpu = ctx.read_accumulation()
+    ref, _ = cpu.OracleScene(s).render(s.scene_data, rng_mode=abi.RNG_REFERENCE)
+    close = (np.abs(gpu[..., :3] - ref[..., :3]) <= 1e-3 + 1e-3 * np.abs(ref[..., :3])).all(-1)
+    assert close.mean() > 0.97, close.mean()
+    # the sheen layer changes the image against the same scene without it
+    plain = sheen_cornell(table=False)
+    plain.materials["sheenTintWeight"] = 0.0
+    ref0, _ = cpu.OracleScene(plain).render(plain.scene_data, rng_mode=abi.RNG_REFERENCE)
+    assert np.abs(ref0[..., :3] - ref[..., :3]).max(-1).mean() > 1e-3
+
+
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
+def test_sheen_spectral_parity(built, integrator):
+    from oracle import cpu
+    s = sheen_cornell(48, 48, spp=2)
+    with RenderContext(rng_mode=abi.RNG_REFERENCE, integrator=integrator) as ctx:
+        table, info = ctx.generate_rgb2spec(32)
+        s.rgb2spec = table
+        s.scene_data["rgb2specSRGB"] = info
+        s.scene_data["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES,
+                                                                         abi.RENDER_MODE_SPECTRAL, abi.SPECTRAL_HERO)
+        ctx.upload_scene(s)
+        ctx.render_frame(s.scene_data)
+        gpu = ctx.read_accumulation()
+    ref, _ = cpu.OracleScene(s).render(s.scene_data, rng_mode=abi.RNG_REFERENCE)
+    close = (np.abs(gpu[..., :3] - ref[..., :3]) <= 2e-3 + 2e-3 * np.abs(ref[..., :3])).all(-1)
+    assert close.mean() > 0.95, close.mean()
+
+
+def test_sheen_needs_the_table(built):
+    s = sheen_cornell(32, 32, spp=1, table=False)
+    with RenderContext(rng_mode=abi.RNG_PCG32) as ctx:
+        ctx.upload_scene(s)
+        with pytest.raises(Exception):
+            ctx.render_frame(s.scene_data)
+        with pytest.raises(Exception):
+            ctx.upload_sheen_table(np.zeros(100, np.float32))
+        ctx.upload_sheen_table(synthetic_sheen_table())
+        ctx.render_frame(s.scene_data)

@@ -162,6 +162,7 @@ EXPORTS = {
     "vkrt_cuda_upload_texture": (_I32, [_V, _U32, _V, _U32, _U32, _U32, _U32]),
     "vkrt_cuda_set_environment": (_I32, [_V, _U32]),
     "vkrt_cuda_upload_rgb2spec": (_I32, [_V, _V, _U32, _V]),
+    "vkrt_cuda_upload_sheen_table": (_I32, [_V, _V, _U32]),
     "vkrt_cuda_generate_rgb2spec": (_I32, [_V, _U32, _V]),
     "vkrt_cuda_download_rgb2spec": (_I32, [_V, _V, _U32]),
     "vkrt_cuda_resize": (_I32, [_V, _U32, _U32]),

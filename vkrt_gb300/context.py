@@ -37,6 +37,7 @@ class Scene:
     tri_alias_q: np.ndarray | None = None
     tri_alias_idx: np.ndarray | None = None
     rgb2spec: np.ndarray | None = None    # float32 table in vkrt's layout
+    sheen_table: np.ndarray | None = None  # float32 [3][32][32] sheen LTC table (vkrt's SHEEN_LTC_TABLE layout)
     emissive_mesh_materials: np.ndarray | None = None  # uint32, material of each emissive-mesh entry
     name: str = ""
     mesh_names: list = field(default_factory=list)  # per MeshInfo (scene files)
@@ -159,6 +160,8 @@ class RenderContext:
             self.upload_texture(slot, tex)
         if scene.env_texture != abi.INVALID_INDEX:
             self._check(self.lib.vkrt_cuda_set_environment(self.handle, scene.env_texture), "set environment")
+        if scene.sheen_table is not None:
+            self.upload_sheen_table(scene.sheen_table)
         if scene.rgb2spec is not None:
             info = np.array([scene.scene_data["rgb2specSRGB"][0]], dtype=np.uint32).reshape(3)
             self._check(self.lib.vkrt_cuda_upload_rgb2spec(self.handle, abi.ptr(scene.rgb2spec), len(scene.rgb2spec),
@@ -201,6 +204,11 @@ class RenderContext:
 
     def update_meshes(self, meshes: np.ndarray) -> None:
         self._check(self.lib.vkrt_cuda_update_meshes(self.handle, abi.ptr(meshes), len(meshes)), "update meshes")
+
+    def upload_sheen_table(self, table: np.ndarray) -> None:
+        """vkrt's sheen LTC table: 3 x 32 x 32 float32 (transform a, transform b, albedo over cos theta, roughness)."""
+        t = np.ascontiguousarray(table, dtype=np.float32).reshape(-1)
+        self._check(self.lib.vkrt_cuda_upload_sheen_table(self.handle, abi.ptr(t), len(t)), "upload sheen table")
 
     def generate_rgb2spec(self, res: int) -> tuple[np.ndarray, np.ndarray]:
         info = np.zeros(3, dtype=np.uint32)

@@ -8,6 +8,7 @@
 //   * the rough dielectric BTDF of lobes/dielectric/** (Walter et al. 2007) with Abbe-number dispersion
 //     (utility/spectral.slang:124-136) and the Fresnel choice between reflection and refraction;
 //   * sampleBSDFDirection (principled/sample.slang:4-51) reporting whether the sample refracted.
+//   * the microfiber sheen lobe on top, through the LTC table the host installs.
 // The reflection-only instantiations keep the smaller Bsdf of shading.cuh.
 #pragma once
 
@@ -18,7 +19,47 @@ namespace vkrt {
 struct BsdfFull : Bsdf {
     bool interior;   // useInteriorDielectricInterface (attenuation.slang:4-6)
     float transAtt;  // attenuation of the layers above the interface on the transmission lobe
+    // sheen: branch weight, LTC transform and albedo at wo, colour (zero without a table)
+    float wSheen, sheenA, sheenB, sheenAlb;
+    float3 sheenColor;
+    const float* sheenLtc;
 };
+
+// Microfiber sheen through its LTC fit (lobes/sheen.slang, Zeltner, Burley and Chiang 2022): three 32 x 32 layers
+// over (cos theta_o, roughness), looked up bilinearly (:23-39); the lobe is a linearly transformed cosine in the
+// frame whose tangent is wo's projection (:41-85).
+VKRT_DEV float sheenLookup(const float* T, float cosT, float rough, uint32_t layer) {
+    const float ux = sat(cosT) * 31.0f, uy = sat(rough) * 31.0f;
+    const uint32_t x0 = min(uint32_t(ux), 31u), y0 = min(uint32_t(uy), 31u);
+    const uint32_t x1 = min(x0 + 1u, 31u), y1 = min(y0 + 1u, 31u);
+    const float tx = ux - floorf(ux), ty = uy - floorf(uy);
+    const float* L = T + layer * 1024u;
+    const float e00 = __ldg(L + y0 * 32u + x0), e10 = __ldg(L + y0 * 32u + x1);
+    const float e01 = __ldg(L + y1 * 32u + x0), e11 = __ldg(L + y1 * 32u + x1);
+    const float a = e00 * (1.0f - tx) + e10 * tx, b = e01 * (1.0f - tx) + e11 * tx;
+    return a * (1.0f - ty) + b * ty;
+}
+VKRT_DEV float sheenAlbedo(const float* T, float cosT, float rough) {  // sheenDirectionalAlbedo (:87-89)
+    return T ? sheenLookup(T, cosT, fminf(fmaxf(rough, 1e-3f), 1.0f), 2u) : 0.0f;
+}
+VKRT_DEV float sheenAtten(const float* T, float weight, float cosT, float rough) {  // sheenLayerAttenuation (:91-93)
+    return sat(1.0f - weight * sheenAlbedo(T, cosT, rough));
+}
+VKRT_DEV Basis sheenBasis(float3 wo) { return makeBasis(make_float3(0.0f, 0.0f, 1.0f), make_float4(wo.x, wo.y, wo.z, 1.0f)); }
+// evalSheen (:95-111) for a unit colour: value albedo * D, pdf D
+VKRT_DEV float evalSheenUnit(const BsdfFull& s, float3 wi, float& pdf) {
+    pdf = 0.0f;
+    if (s.wo.z <= 0.0f || wi.z <= 0.0f) return 0.0f;
+    const float3 lw = toLocal(wi, sheenBasis(s.wo));
+    const float z = fmaxf(lw.z, 0.0f);
+    if (z <= 0.0f || fabsf(s.sheenA) < 1e-5f || s.sheenAlb < 1e-5f) return 0.0f;
+    const float axbz = s.sheenA * lw.x + s.sheenB * lw.z;
+    const float len2 = axbz * axbz + (s.sheenA * lw.y) * (s.sheenA * lw.y) + lw.z * lw.z;
+    if (len2 <= 1e-6f) return 0.0f;
+    const float scale = s.sheenA / len2;
+    pdf = kInvPi * z * scale * scale;
+    return s.sheenAlb * pdf;
+}
 
 VKRT_DEV float dispersiveIor(float ior, float abbe, float lambdaNm) {  // utility/spectral.slang:124-136
     if (ior <= 1.0f + 1e-4f || abbe <= 0.0f) return fmaxf(ior, 1.0f);
@@ -63,11 +104,20 @@ VKRT_DEV float3 refractDir(float3 i, float3 n, float eta) {  // HLSL refract: ze
     return i * eta - n * (eta * c + sqrtf(k));
 }
 
-VKRT_DEV BsdfFull makeBsdfFull(const ShadeMaterial& m, float3 wo, uint32_t frontFace) {
+VKRT_DEV BsdfFull makeBsdfFull(const ShadeMaterial& m, float3 wo, uint32_t frontFace, const float* sheenLtc) {
     BsdfFull s;
     s.mat = m;
     s.wo = wo;
     s.frontFace = frontFace;
+    s.sheenLtc = sheenLtc;
+    s.sheenColor = sheenLtc ? m.sheenColor : f3(0.0f);
+    s.sheenA = s.sheenB = s.sheenAlb = 0.0f;
+    if (sheenLtc && wo.z > 0.0f) {  // makeSheenParams (sheen.slang:41-57)
+        const float r = fminf(fmaxf(m.sheenRoughness, 1e-3f), 1.0f);
+        s.sheenA = sheenLookup(sheenLtc, wo.z, r, 0u);
+        s.sheenB = sheenLookup(sheenLtc, wo.z, r, 1u);
+        s.sheenAlb = sheenLookup(sheenLtc, wo.z, r, 2u);
+    }
     s.ggx = makeGgx(m, wo);
     s.f0Diel = dielSpecF0(m);
     s.viewAtten = dielDirAtten(m.roughness, s.f0Diel, wo.z);
@@ -79,7 +129,7 @@ VKRT_DEV BsdfFull makeBsdfFull(const ShadeMaterial& m, float3 wo, uint32_t front
     const float baseScatter = nonMetal * (1.0f - m.transmission);
     const float transW = m.transmission * fmaxf(lum(transmissionColor(m)), 1e-3f);
     const float dielW = nonMetal * fmaxf(sat(lum(s.f0Diel)) + transW, 0.0f);
-    float wc = 0.0f, wm, wd, wf = 0.0f, ws = 0.0f;
+    float wsh = 0.0f, wc = 0.0f, wm, wd, wf = 0.0f, ws = 0.0f;
     if (s.interior) {
         s.viewCoat = 1.0f;
         s.transAtt = 1.0f;
@@ -87,19 +137,22 @@ VKRT_DEV BsdfFull makeBsdfFull(const ShadeMaterial& m, float3 wo, uint32_t front
         wd = dielW;
     } else {
         s.viewCoat = coatAtten(m, wo);
-        s.transAtt = s.viewCoat;  // materialTransmissionStackAttenuation without a sheen layer
+        const float viewSheen = sheenAtten(sheenLtc, maxc(s.sheenColor), wo.z, m.sheenRoughness);
+        s.transAtt = viewSheen * s.viewCoat;  // materialTransmissionStackAttenuation
         const float dielAtt = lum(s.viewAtten);
-        wc = m.clearcoat * 0.25f;
-        wm = s.viewCoat * m.metallic * baseW;
-        wd = s.viewCoat * dielW;
-        wf = s.viewCoat * dielAtt * baseScatter * (1.0f - m.subsurface) * diffW;
-        ws = s.viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
+        wsh = lum(s.sheenColor);
+        wc = viewSheen * m.clearcoat * 0.25f;
+        wm = viewSheen * s.viewCoat * m.metallic * baseW;
+        wd = viewSheen * s.viewCoat * dielW;
+        wf = viewSheen * s.viewCoat * dielAtt * baseScatter * (1.0f - m.subsurface) * diffW;
+        ws = viewSheen * s.viewCoat * dielAtt * baseScatter * m.subsurface * diffW;
     }
-    const float tot = wc + wm + wd + wf + ws;
+    const float tot = wsh + wc + wm + wd + wf + ws;
     if (tot <= 0.0f) {
-        s.wCoat = s.wMetal = s.wDiel = s.wSub = 0.0f;
+        s.wSheen = s.wCoat = s.wMetal = s.wDiel = s.wSub = 0.0f;
         s.wDiff = 1.0f;
     } else {
+        s.wSheen = wsh / tot;
         s.wCoat = wc / tot;
         s.wMetal = wm / tot;
         s.wDiel = wd / tot;
@@ -179,7 +232,13 @@ VKRT_DEV float3 evalScalarFull(const BsdfFull& s, const SpecTable& tab, float3 w
         return v;
     }
     float coat = 0.0f;
-    float3 metal = f3(0.0f), diel = f3(0.0f), sub = f3(0.0f);
+    float3 metal = f3(0.0f), diel = f3(0.0f), sub = f3(0.0f), sheenV = f3(0.0f), sc = f3(0.0f);
+    if (s.wSheen > 0.0f || !s.interior) sc = spec(s.sheenColor);
+    if (s.wSheen > 0.0f) {
+        float sp;
+        sheenV = sc * evalSheenUnit(s, wi, sp);
+        pdf += s.wSheen * sp;
+    }
     if (s.wCoat > 0.0f) {
         float cp;
         coat = coatEval(s.mat.clearcoat, s.coatA, s.wo, wi, cp);
@@ -216,7 +275,8 @@ VKRT_DEV float3 evalScalarFull(const BsdfFull& s, const SpecTable& tab, float3 w
     const float nonMetal = 1.0f - s.mat.metallic;
     if (s.interior) return metal * s.mat.metallic + diel * nonMetal;
     const float att = s.viewCoat * coatAtten(s.mat, wi);
-    return f3(coat) + (metal * s.mat.metallic + (diel + s.viewAtten * sub) * nonMetal) * att;
+    const float viewSheen = sheenAtten(s.sheenLtc, maxc(sc), s.wo.z, s.mat.sheenRoughness);
+    return sheenV + (f3(coat) + (metal * s.mat.metallic + (diel + s.viewAtten * sub) * nonMetal) * att) * viewSheen;
 }
 
 // Four hero lanes with one technique pdf per lane in `tp`
@@ -234,7 +294,13 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
         return v;
     }
     float coat = 0.0f;
-    float4 metal = f4(0.0f), diel = f4(0.0f), sub = f4(0.0f);
+    float4 metal = f4(0.0f), diel = f4(0.0f), sub = f4(0.0f), sheenV = f4(0.0f), sc = f4(0.0f);
+    if (s.wSheen > 0.0f || !s.interior) sc = spectral4(tab, sat(s.sheenColor), l);
+    if (s.wSheen > 0.0f) {
+        float sp;
+        sheenV = sc * evalSheenUnit(s, wi, sp);
+        tp = tp + f4(s.wSheen * sp);
+    }
     if (s.wCoat > 0.0f) {
         float cp;
         coat = coatEval(s.mat.clearcoat, s.coatA, s.wo, wi, cp);
@@ -280,7 +346,10 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
     if (s.interior) return metal * s.mat.metallic + diel * nonMetal;
     const float4 va = spectral4(tab, sat(s.viewAtten), l);
     const float att = s.viewCoat * coatAtten(s.mat, wi);
-    return f4(coat) + (metal * s.mat.metallic + (diel + va * sub) * nonMetal) * att;
+    const float alb = sheenAlbedo(s.sheenLtc, s.wo.z, s.mat.sheenRoughness);
+    const float4 viewSheen = make_float4(sat(1.0f - sc.x * alb), sat(1.0f - sc.y * alb), sat(1.0f - sc.z * alb),
+                                         sat(1.0f - sc.w * alb));
+    return sheenV + (f4(coat) + (metal * s.mat.metallic + (diel + va * sub) * nonMetal) * att) * viewSheen;
 }
 
 // sampleBSDFDirection with sampleDielectric (dielectric/sample.slang:7-53); the dielectric lobe refracts at the IOR
@@ -288,6 +357,18 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
 VKRT_DEV bool sampleFull(const BsdfFull& s, Rng& rng, float lambda, bool spectral, float3& wi, bool& isTrans) {
     isTrans = false;
     float sel = rng.next();
+    if (sel < s.wSheen) {  // sampleSheen (sheen.slang:113-128)
+        if (fabsf(s.sheenA) < 1e-5f || s.sheenAlb < 1e-5f) return false;
+        const float r = sqrtf(rng.next());
+        float sp, cp;
+        sincosf(2.0f * kPi * rng.next(), &sp, &cp);
+        const float dx = r * cp, dy = r * sp;
+        const float dz = sqrtf(fmaxf(1.0f - (dx * dx + dy * dy), 0.0f));
+        const float3 lw = normalize(make_float3(dx - dz * s.sheenB, dy, dz * s.sheenA));
+        wi = toWorld(lw, sheenBasis(s.wo));
+        return wi.z > 0.0f;
+    }
+    sel -= s.wSheen;
     if (sel < s.wCoat) {
         float u1 = rng.next(), u2 = rng.next();
         return coatSample(s.wo, s.coatA, u1, u2, wi);

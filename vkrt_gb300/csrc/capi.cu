@@ -96,6 +96,8 @@ struct VKRT_CudaContext {
     // spectral table
     DeviceArray<float> rgb2spec;
     uint32_t rgb2specFloats = 0;
+    DeviceArray<float> sheenTable;  // the sheen LTC table once uploaded (VKRT_CUDA_SHEEN_TABLE_FLOATS)
+    bool sheenMaterials = false;    // some material has a sheen colour
     VKRT_CudaRGB2SpecTableInfo rgb2specInfo{};
     DeviceArray<float4> rgb2specCells;  // the table of rgb2specInfo repacked one float4 per cell
 
@@ -250,6 +252,7 @@ DeviceScene makeDeviceScene(VKRT_CudaContext* c) {
     s.textures = c->textureTable.ptr;
     s.rgb2spec = c->rgb2spec.ptr;
     s.rgb2specFloatCount = c->rgb2specFloats;
+    s.sheenLtc = c->sheenTable.ptr;
     s.rgb2specCells = c->rgb2specCells.ptr;
     s.rgb2specCellsInfo = c->rgb2specInfo;
     s.env.marginal = c->envMarginal.ptr;
@@ -285,6 +288,8 @@ int32_t validateFrame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
     if (sd->emissiveMeshCount > c->emissiveMeshCount) return invalid(c, "SceneData.emissiveMeshCount exceeds the uploaded lights");
     for (const VKRT_CudaMeshInfo& m : c->hostMeshes)
         if (m.materialIndex >= c->materialCount) return invalid(c, "mesh material index out of range");
+    if (c->sheenMaterials && !c->sheenTable.ptr)
+        return invalid(c, "a material has sheen: install vkrt's sheen LTC table (vkrt_cuda_upload_sheen_table)");
     const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
     if (spectral) {
         const VKRT_CudaRGB2SpecTableInfo& ti = sd->rgb2specSRGB;
@@ -524,10 +529,16 @@ int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* c, const VKRT_CudaMaterial*
     c->materialCount = count;
     c->extendedMaterials = false;
     c->transmissiveMaterials = false;
+    c->sheenMaterials = false;
     for (uint32_t i = 0; i < count; ++i) {
         const VKRT_CudaMaterial& m = materials[i];
+        // bsdfSheenColor (material.slang:63-73) is saturate(tint) * saturate(weight)
+        const float w = std::min(std::max(m.sheenTintWeight[3], 0.0f), 1.0f);
+        const float tint = std::max({m.sheenTintWeight[0], m.sheenTintWeight[1], m.sheenTintWeight[2]});
+        if (w > 0.0f && tint > 0.0f) c->sheenMaterials = true;
         if (m.transmission > 0.0f) c->transmissiveMaterials = true;
-        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f)
+        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f ||
+            (w > 0.0f && tint > 0.0f))
             c->extendedMaterials = true;
     }
     return VKRT_CUDA_SUCCESS;
@@ -631,6 +642,15 @@ int32_t vkrt_cuda_set_environment(VKRT_CudaContext* c, uint32_t textureIndex) {
     c->envWidth = W;
     c->envHeight = H;
     c->envTexture = textureIndex;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_upload_sheen_table(VKRT_CudaContext* c, const float* table, uint32_t floatCount) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!table || floatCount != VKRT_CUDA_SHEEN_TABLE_FLOATS) return invalid(c, "sheen table: 3072 floats");
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->sheenTable.assign(table, floatCount, c->stream), "upload sheen table");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "upload sheen table");
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -1211,6 +1231,7 @@ int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const f
         if (m.specularTint != 0.0f) return invalid(c, "the adjoint needs specularTint 0 on every material");
         if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f)
             return invalid(c, "the adjoint covers the metal / dielectric / Lambert stack only");
+    if (c->sheenMaterials) return invalid(c, "the adjoint covers the metal / dielectric / Lambert stack only");
     }
     VKRT_CudaAdjointConfig a{};
     if (cfg) a = *cfg;

@@ -212,7 +212,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
     ShadeMaterial mat;
     Basis basis;
     shadeVertex(sc, s, p.d, mat, basis);
-    const BsdfFull bsdf = makeBsdfFull(mat, toLocal(-p.d, basis), s.frontFace);
+    const BsdfFull bsdf = makeBsdfFull(mat, toLocal(-p.d, basis), s.frontFace, sc.sheenLtc);
     hook.surface(s, mat, bsdf);
 
     if (anyPos(mat.emission)) {  // emission, MIS against emissive NEE at the previous vertex (loop.slang:62-80)

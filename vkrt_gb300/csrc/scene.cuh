@@ -75,6 +75,7 @@ struct DeviceScene {
     const float4* rgb2specCells;
     VKRT_CudaRGB2SpecTableInfo rgb2specCellsInfo;
     EnvDistribution env;
+    const float* sheenLtc;  // sheen LTC table (3 x 32 x 32), null until uploaded
 };
 
 struct RenderCounters {

@@ -6,7 +6,7 @@
 // Material coverage here: the glTF metallic-roughness subset (metal, dielectric specular and Lambert lobes), which the
 // reflection-only instantiations use. The rest of vkrt's stack (clearcoat, Oren-Nayar, fake subsurface, the
 // transmissive interface with dispersion and media) is in bsdf_full.cuh for the full instantiations. Sheen (its LTC
-// fit table) is not evaluated: its lobe gets no weight.
+// fit table) is in bsdf_full.cuh too.
 #pragma once
 
 #include "scene.cuh"
@@ -355,6 +355,8 @@ struct ShadeMaterial {
     float clearcoat, clearcoatGloss, subsurface, diffuseRoughness;  // the extended reflection stack's inputs
     float transmission, abbe, absorption;                            // the transmissive interface and its medium
     float3 attenuationColor;
+    float3 sheenColor;  // bsdfSheenColor: saturate(tint) * saturate(weight) (material.slang:63-73)
+    float sheenRoughness;
 };
 
 VKRT_DEV void shadeVertex(const DeviceScene& sc, Surface& s, float3 dir, ShadeMaterial& mat, Basis& basis) {
@@ -392,6 +394,9 @@ VKRT_DEV void shadeVertex(const DeviceScene& sc, Surface& s, float3 dir, ShadeMa
     mat.abbe = m.abbeNumber;
     mat.absorption = m.absorptionCoefficient;
     mat.attenuationColor = make_float3(m.attenuationColor[0], m.attenuationColor[1], m.attenuationColor[2]);
+    mat.sheenColor = sat(make_float3(m.sheenTintWeight[0], m.sheenTintWeight[1], m.sheenTintWeight[2])) *
+                     sat(m.sheenTintWeight[3]);
+    mat.sheenRoughness = m.sheenRoughness;
     float4 bc = sampleMaterialTexture(sc, m.baseColorTextureIndex, m.baseColorTextureWrap, m.baseColorTextureTransform,
                                       m.textureRotations[0], m.textureTexcoordSets & 0xffu, s.tex, f4(1.0f));
     mat.baseColor = mat.baseColor * xyz(bc) * xyz(s.tex.color);
@@ -433,17 +438,18 @@ VKRT_DEV float3 dielSpecF0(const ShadeMaterial& m) {  // fresnel.slang:15-20
 
 VKRT_DEV float3 fresnelConductor(float cosT, float3 eta, float3 k);
 
-// Denoiser features (bsdf/principled/denoiser.slang:7-46) on the shaded layers, where transmission and sheen are
-// absent: a vertex whose only visible response is a sharp specular lobe is followed through (a front-facing clear
-// coat is a visible layer); the first other vertex gives the feature albedo (a weighted mix of the diffuse colour,
-// the dielectric and the metallic F0) and its shading normal. Subsurface changes neither rule: its share of the
-// albedo weight is taken from the diffuse share with the same colour, and its layer weight never exceeds it.
+// Denoiser features (bsdf/principled/denoiser.slang:7-46): a vertex whose only visible response is a sharp specular
+// lobe (or an identity transmissive interface) is followed through; the first other vertex gives the feature albedo
+// (a weighted mix of the diffuse, dielectric, transmission, metallic and sheen colours) and its shading normal.
 VKRT_DEV bool denoiserFollowsSpecular(const ShadeMaterial& m, uint32_t frontFace) {
-    // a visible base layer: diffuse (its subsurface share is no larger) or a clear coat seen from the front
-    if (maxc(m.baseColor * (1.0f - m.metallic)) > 1e-3f) return false;
-    if (frontFace != 0u && m.clearcoat > 1e-3f) return false;
+    const float diffuseW = maxc(m.baseColor * (1.0f - m.metallic)) * (1.0f - m.transmission);
+    const float subsurfaceW = diffuseW * m.subsurface;
+    const float sheenW = maxc(m.sheenColor) * (1.0f - m.transmission);
+    const float coatW = frontFace != 0u ? m.clearcoat : 0.0f;
+    if (diffuseW > 1e-3f || subsurfaceW > 1e-3f || sheenW > 1e-3f || coatW > 1e-3f) return false;
+    if (m.transmission > 1e-3f && fmaxf(m.ior, 1.0f) <= 1.0f + 1e-4f) return true;
     if (m.roughness > 0.02f) return false;
-    return m.metallic >= 1.0f - 1e-3f || maxc(dielSpecF0(m)) > 1e-3f;
+    return m.transmission > 1e-3f || m.metallic >= 1.0f - 1e-3f || maxc(dielSpecF0(m)) > 1e-3f;
 }
 
 VKRT_DEV float3 denoiserAlbedo(const ShadeMaterial& m) {
@@ -452,10 +458,12 @@ VKRT_DEV float3 denoiserAlbedo(const ShadeMaterial& m) {
     const float3 f0 = dielSpecF0(m);
     const float3 metalF0 =
         m.conductor ? fresnelConductor(1.0f, fmax3(m.eta, f3(1e-3f)), fmax3(m.k, f3(0.0f))) : sat(m.baseColor);
-    const float wd = nonMetal, ws = nonMetal * sat(lum(f0)), wm = m.metallic;
-    const float total = wd + ws + wm;
+    const float base = nonMetal * (1.0f - m.transmission);
+    const float wd = base * (1.0f - m.subsurface), wss = base * m.subsurface, ws = base * sat(lum(f0));
+    const float wt = nonMetal * m.transmission, wm = m.metallic, wsh = maxc(m.sheenColor) * base;
+    const float total = wd + wss + ws + wt + wm + wsh;
     if (total <= 0.0f) return sat(diffuse);
-    return sat((diffuse * wd + f0 * ws + metalF0 * wm) / total);
+    return sat((diffuse * wd + diffuse * wss + f0 * ws + f3(1.0f) * wt + metalF0 * wm + m.sheenColor * wsh) / total);
 }
 
 VKRT_DEV float fresnelDielectric(float cosT, float eta) {  // fresnel.slang:31-48
