@@ -558,8 +558,21 @@ struct HitRec {
     bool hit() const { return mesh != VKRT_CUDA_INVALID_INDEX; }
 };
 
-// closest hit (anyHit = false) or first accepted hit; ties on t go to the smaller global triangle id
-HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float tmax, bool anyHit) {
+// Alpha test of a candidate hit (rt/alpha_test.slang), defined with the texture sampler below. vkrt draws its
+// stochastic decisions from the path stream in any-hit order, which the driver leaves unspecified; here a triangle's
+// decision hashes the ray's seed (the path stream's state when the ray starts, salted per shadow request) with the
+// triangle id, so the closest accepted hit does not depend on traversal order.
+bool alphaAccepts(const Scene& s, uint32_t mesh, uint32_t prim, float u, float v, uint32_t seed, uint32_t gid);
+bool sceneAlphaTested(const Scene& s);
+uint32_t alphaShadowSeed(uint32_t seed, uint32_t request) { return seed ^ (0x68bc21ebu * (request + 1u)); }
+float alphaRandom(uint32_t seed, uint32_t gid) {
+    return float(hash32(seed ^ hash32(gid + 0x632be5abu)) & 0x00ffffffu) * (1.0f / 16777216.0f);
+}
+
+// closest hit (anyHit = false) or first accepted hit; ties on t go to the smaller global triangle id; with `alpha`,
+// candidate hits must pass alphaAccepts under `alphaSeed`
+HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float tmax, bool anyHit, bool alpha = false,
+                 uint32_t alphaSeed = 0u) {
     HitRec best;
     if (s.bvh.nodes.empty()) return best;
     RayPre<float> rp = prepRay(o, d, tmin, tmax);
@@ -583,6 +596,7 @@ HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float
             r2.tmax = bestT;
             float t, b1, b2;
             if (!watertight(r2, tr.v[0], tr.v[1], tr.v[2], t, b1, b2)) continue;
+            if (alpha && !alphaAccepts(s, tr.mesh, tr.prim, b1, b2, alphaSeed, tr.gid)) continue;
             if (t < bestT || (t == bestT && tr.gid < best.gid)) {
                 bestT = t;
                 best.mesh = tr.mesh;
@@ -609,7 +623,8 @@ bool meshTransmissive(const Scene& s, uint32_t mesh) {
 // hit the driver accepts, in an unspecified order; here an opaque hit anywhere on the segment wins, and the segment
 // is unsupported when its only hits are transmissive.
 enum : int { kShadowVisible = 0, kShadowOccluded = 1, kShadowTransmission = 2 };
-int shadowFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float tmax) {
+int shadowFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float tmax, bool alpha = false,
+               uint32_t alphaSeed = 0u) {
     if (s.bvh.nodes.empty()) return kShadowVisible;
     RayPre<float> rp = prepRay(o, d, tmin, tmax);
     V3<float> inv(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
@@ -630,6 +645,7 @@ int shadowFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float t
             const WorldTri& tr = s.tris[n.left + i];
             float t, b1, b2;
             if (!watertight(rp, tr.v[0], tr.v[1], tr.v[2], t, b1, b2)) continue;
+            if (alpha && !alphaAccepts(s, tr.mesh, tr.prim, b1, b2, alphaSeed, tr.gid)) continue;
             if (!meshTransmissive(s, tr.mesh)) return kShadowOccluded;
             sawTransmissive = true;
         }
@@ -894,6 +910,52 @@ V4<R> sampleMaterialTexture(const Scene& s, uint32_t idx, uint32_t wrap, const f
     R tu = cs * sx - sn * sy + R(xf[2]);
     R tv = sn * sx + cs * sy + R(xf[3]);
     return sampleBilinear(s.textures[idx], tu, tv, wrapAxisMode(wrap & 0xffffu), wrapAxisMode((wrap >> 16) & 0xffffu));
+}
+
+bool alphaAccepts(const Scene& s, uint32_t mesh, uint32_t prim, float u, float v, uint32_t seed, uint32_t gid) {
+    const VKRT_CudaMeshInfo& m = s.meshes[mesh];
+    const VKRT_CudaMaterial& mat = s.materials[m.materialIndex];
+    const uint32_t mask = 1u, blend = 2u;  // VKRT_MATERIAL_ALPHA_MODE_MASK / _BLEND (shared/constants.h:56-58)
+    if (!(mat.alphaMode == mask || mat.alphaMode == blend || mat.opacity < 0.999f || m.opacity < 0.999f)) return true;
+    // evaluateSurfaceTextureData (geometry/surface/interpolation.slang:46-60)
+    uint32_t base = m.indexBase + prim * 3u;
+    const VKRT_CudaShaderVertex& a = s.vertices[s.indices[base + 0] + m.vertexBase];
+    const VKRT_CudaShaderVertex& b = s.vertices[s.indices[base + 1] + m.vertexBase];
+    const VKRT_CudaShaderVertex& c = s.vertices[s.indices[base + 2] + m.vertexBase];
+    TexData<float> td;
+    td.color = interp4(unpackColor<float>(a.packedColor), unpackColor<float>(b.packedColor),
+                       unpackColor<float>(c.packedColor), u, v);
+    float w = 1.0f - u - v;
+    for (int k = 0; k < 2; ++k) {
+        td.uv0[k] = a.texcoord0[k] * w + b.texcoord0[k] * u + c.texcoord0[k] * v;
+        td.uv1[k] = a.texcoord1[k] * w + b.texcoord1[k] * u + c.texcoord1[k] * v;
+    }
+    // evaluateMaterialTextureAlpha, alphaPass (rt/alpha_test.slang:19-57)
+    float texAlpha = td.color.w;
+    if (mat.alphaMode != VKRT_CUDA_ALPHA_MODE_OPAQUE)
+        texAlpha *= sampleMaterialTexture(s, mat.baseColorTextureIndex, mat.baseColorTextureWrap,
+                                          mat.baseColorTextureTransform, mat.textureRotations[0],
+                                          mat.textureTexcoordSets & 0xffu, td, V4<float>(1.0f)).w;
+    if (mat.alphaMode == mask) {
+        if (texAlpha < mat.alphaCutoff) return false;
+        float o = sat(m.opacity * mat.opacity * td.color.w);
+        if (o >= 1.0f) return true;
+        if (o <= 0.0f) return false;
+        return alphaRandom(seed, gid) <= o;
+    }
+    float o = sat(m.opacity * mat.opacity * texAlpha);
+    if (o <= 0.0f) return false;
+    if (o >= 1.0f) return true;
+    return alphaRandom(seed, gid) <= o;
+}
+
+bool sceneAlphaTested(const Scene& s) {
+    for (const VKRT_CudaMeshInfo& m : s.meshes) {
+        if (m.materialIndex >= s.materials.size()) continue;
+        const VKRT_CudaMaterial& mat = s.materials[m.materialIndex];
+        if (mat.alphaMode != VKRT_CUDA_ALPHA_MODE_OPAQUE || mat.opacity < 0.999f || m.opacity < 0.999f) return true;
+    }
+    return false;
 }
 
 template <class R>
@@ -1818,10 +1880,12 @@ V3<R> denoiserAlbedo(const MaterialR<R>& m) {
     return sat(a / total);
 }
 
+// Alpha-tested scenes take the FP32 traversal with alpha tests, also in brute-force mode.
 template <class R>
-HitRec traceClosest(Ctx<R>& c, V3<R> o, V3<R> d, bool primary) {
+HitRec traceClosest(Ctx<R>& c, V3<R> o, V3<R> d, bool primary, bool alpha = false, uint32_t alphaSeed = 0u) {
     if (primary) c.stats.primaryRays++;
     else c.stats.extensionRays++;
+    if (alpha) return traceFp32(c.s, V3<float>(o), V3<float>(d), kTMin, kTMax, false, true, alphaSeed);
     if (c.bruteForce) {
         return traceFp64Brute(c.s, *c.tri64, V3<double>(o), V3<double>(d), double(kTMin), double(kTMax), nullptr, 0.0);
     }
@@ -1974,23 +2038,29 @@ bool shadowVisible(Ctx<R>& c, V3<R> p, V3<R> gn, V3<R> wi, R tmax) {  // light/d
     return !occluded(c, o, wi, tmax);
 }
 
-// The emissive-NEE shadow ray: visible, occluded, or unsupported (through a transmissive surface). Scenes without
-// transmissive materials take the any-hit query above; with them the segment is scanned by shadowFp32 (the FP32
-// traversal also in brute-force mode).
-template <class R>
-int shadowResult(Ctx<R>& c, bool transmissiveScene, V3<R> p, V3<R> gn, V3<R> wi, R tmax) {
-    if (!transmissiveScene) return shadowVisible(c, p, gn, wi, tmax) ? kShadowVisible : kShadowOccluded;
-    c.stats.shadowRays++;
-    V3<R> off = dot(wi, gn) >= R(0) ? gn : -gn;
-    V3<R> o = p + off * R(kShadowOrigin);
-    return shadowFp32(c.s, V3<float>(o), V3<float>(wi), kTMin, float(tmax));
-}
-
 struct ModeFlags {
     bool neeEnabled;   // misNeeEnabled && emissiveMeshCount > 0 (state.slang:50-52)
     bool envNee;       // environment importance sampling enabled and a distribution exists
     bool transmissive; // some material has transmission > 0 (environment NEE is then off: vkrt has none)
+    bool alpha;        // some mesh is alpha-tested
 };
+
+// A shadow ray: visible, occluded, or unsupported (through a transmissive surface). Scenes without transmissive or
+// alpha-tested materials take the any-hit query above; others scan the segment with shadowFp32 (the FP32 traversal
+// also in brute-force mode). `alphaSeed` is the ray's alpha seed (alphaShadowSeed of the vertex's seed).
+template <class R>
+int shadowResult(Ctx<R>& c, const ModeFlags& mf, V3<R> p, V3<R> gn, V3<R> wi, R tmax, uint32_t alphaSeed) {
+    if (!mf.transmissive && !mf.alpha) return shadowVisible(c, p, gn, wi, tmax) ? kShadowVisible : kShadowOccluded;
+    c.stats.shadowRays++;
+    V3<R> off = dot(wi, gn) >= R(0) ? gn : -gn;
+    V3<R> o = p + off * R(kShadowOrigin);
+    return shadowFp32(c.s, V3<float>(o), V3<float>(wi), kTMin, float(tmax), mf.alpha, alphaSeed);
+}
+
+uint32_t alphaSeedOf(const Rng& r) {  // the seed of a ray that starts with the stream in state r
+    if (r.mode == VKRT_CUDA_RNG_REFERENCE) return r.h;
+    return uint32_t(r.state) ^ uint32_t(r.state >> 32);
+}
 
 // MediumState (bsdf/base/medium.slang:7-33): the medium a path entered through a transmissive interface
 template <class R>
@@ -2052,7 +2122,9 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
     Medium<R> med;
     R rot = R(c.sd.environmentRotation);
     for (uint32_t depth = 0; depth < c.sd.rrMaxDepth; ++depth) {
-        HitRec h = traceClosest(c, o, d, depth == 0);
+        const uint32_t vseed = alphaSeedOf(rng);  // the ray's alpha seed, reused salted by the vertex's shadow rays
+        uint32_t requests = 0;                    // shadow requests of the vertex so far
+        HitRec h = traceClosest(c, o, d, depth == 0, mf.alpha, vseed);
         if (!h.hit()) {
             if (med.boundary()) break;  // shouldAccumulateEnvironmentMiss (loop.slang:4-6)
             V3<R> L = envRadiance<R>(c.s, c.sd, d);
@@ -2077,8 +2149,8 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
         bool vertexNeeSupported = neeAllowedHere;
         if (mf.neeEnabled && neeAllowedHere && st.wo.z > R(0)) {  // sampleDirectLightRgb (rgb_lighting.slang:7-31)
             LightSampleR<R> ls = sampleEmissive(c, v.hitPoint, rng);
-            int vis = ls.valid ? shadowResult(c, mf.transmissive, v.hitPoint, v.surf.geometricNormal, ls.wi,
-                                              ls.shadowDist)
+            int vis = ls.valid ? shadowResult(c, mf, v.hitPoint, v.surf.geometricNormal, ls.wi, ls.shadowDist,
+                                              alphaShadowSeed(vseed, requests++))
                                : kShadowOccluded;
             if (vis == kShadowTransmission) vertexNeeSupported = false;
             V3<R> wl = toLocal(ls.wi, v.basis);
@@ -2098,7 +2170,8 @@ V3<R> traceRgbSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t sa
             R pe;
             R u1 = R(rng.next()), u2 = R(rng.next());
             if (envSample(c.s, u1, u2, rot, wi, pe)) {
-                if (shadowVisible(c, v.hitPoint, v.surf.geometricNormal, wi, R(kTMax))) {
+                if (shadowResult(c, mf, v.hitPoint, v.surf.geometricNormal, wi, R(kTMax),
+                                 alphaShadowSeed(vseed, requests++)) == kShadowVisible) {
                     V3<R> wl = toLocal(wi, v.basis);
                     V3<R> f;
                     R pdf;
@@ -2180,7 +2253,9 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
     Medium<R> med;
     R rot = R(c.sd.environmentRotation);
     for (uint32_t depth = 0; depth < c.sd.rrMaxDepth; ++depth) {
-        HitRec h = traceClosest(c, o, d, depth == 0);
+        const uint32_t vseed = alphaSeedOf(rng);  // the ray's alpha seed, reused salted by the vertex's shadow rays
+        uint32_t requests = 0;                    // shadow requests of the vertex so far
+        HitRec h = traceClosest(c, o, d, depth == 0, mf.alpha, vseed);
         if (!h.hit()) {
             if (med.boundary()) break;
             V3<R> L = envRadiance<R>(c.s, c.sd, d);
@@ -2214,8 +2289,8 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
         if (mf.neeEnabled && neeAllowedHere && st.wo.z > R(0)) {
             // sampleDirectLightSpectralHero / sampleDirectLightSpectralSingle (spectral_lighting.slang:7-64)
             LightSampleR<R> ls = sampleEmissive(c, v.hitPoint, rng);
-            int vis = ls.valid ? shadowResult(c, mf.transmissive, v.hitPoint, v.surf.geometricNormal, ls.wi,
-                                              ls.shadowDist)
+            int vis = ls.valid ? shadowResult(c, mf, v.hitPoint, v.surf.geometricNormal, ls.wi, ls.shadowDist,
+                                              alphaShadowSeed(vseed, requests++))
                                : kShadowOccluded;
             if (vis == kShadowTransmission) vertexNeeSupported = false;
             V3<R> wl = toLocal(ls.wi, v.basis);
@@ -2246,7 +2321,8 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
             R pe;
             R u1 = R(rng.next()), u2 = R(rng.next());
             if (envSample(c.s, u1, u2, rot, wi, pe)) {
-                if (shadowVisible(c, v.hitPoint, v.surf.geometricNormal, wi, R(kTMax))) {
+                if (shadowResult(c, mf, v.hitPoint, v.surf.geometricNormal, wi, R(kTMax),
+                                 alphaShadowSeed(vseed, requests++)) == kShadowVisible) {
                     V3<R> wl = toLocal(wi, v.basis);
                     V4<R> tp;
                     V4<R> fcos = evalSpectral(st, c.tab, wl, lam, tp) * std::fabs(wl.z);
@@ -2372,6 +2448,7 @@ void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderPa
     mf.neeEnabled = sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u;
     mf.transmissive = false;
     for (const VKRT_CudaMaterial& m : s.materials) mf.transmissive = mf.transmissive || m.transmission > 0.0f;
+    mf.alpha = sceneAlphaTested(s);
     mf.envNee = s.envSampling == VKRT_CUDA_ENV_IMPORTANCE && s.env.valid && sd.misNeeEnabled != 0u &&
                 sd.environmentTextureIndex == s.envTexture && !mf.transmissive;
     Rgb2Spec tab;

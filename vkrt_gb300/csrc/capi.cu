@@ -98,6 +98,7 @@ struct VKRT_CudaContext {
     uint32_t rgb2specFloats = 0;
     DeviceArray<float> sheenTable;  // the sheen LTC table once uploaded (VKRT_CUDA_SHEEN_TABLE_FLOATS)
     bool sheenMaterials = false;    // some material has a sheen colour
+    bool alphaTested = false;       // some mesh's material (or the mesh) is alpha-tested
     VKRT_CudaRGB2SpecTableInfo rgb2specInfo{};
     DeviceArray<float4> rgb2specCells;  // the table of rgb2specInfo repacked one float4 per cell
 
@@ -305,6 +306,27 @@ int32_t validateFrame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
 
 // Environment NEE (this backend's addition) is off in scenes with transmissive materials, where vkrt's estimator
 // (NEE unsupported through transmissive surfaces, no environment light inside media) has no environment technique.
+// Which instantiations and kernels the scene's materials and meshes need (refreshed on every material or mesh upload)
+void refreshMaterialFlags(VKRT_CudaContext* c) {
+    c->extendedMaterials = c->transmissiveMaterials = c->sheenMaterials = c->alphaTested = false;
+    for (const VKRT_CudaMaterial& m : c->hostMaterials) {
+        // bsdfSheenColor (material.slang:63-73) is saturate(tint) * saturate(weight)
+        const float w = std::min(std::max(m.sheenTintWeight[3], 0.0f), 1.0f);
+        const float tint = std::max({m.sheenTintWeight[0], m.sheenTintWeight[1], m.sheenTintWeight[2]});
+        if (w > 0.0f && tint > 0.0f) c->sheenMaterials = true;
+        if (m.transmission > 0.0f) c->transmissiveMaterials = true;
+        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f)
+            c->extendedMaterials = true;
+    }
+    for (const VKRT_CudaMeshInfo& mesh : c->hostMeshes) {  // alphaMayRejectHit (rt/alpha_test.slang:8-10)
+        if (mesh.materialIndex >= c->hostMaterials.size()) continue;
+        const VKRT_CudaMaterial& m = c->hostMaterials[mesh.materialIndex];
+        if (m.alphaMode != VKRT_CUDA_ALPHA_MODE_OPAQUE || m.opacity < 0.999f || mesh.opacity < 0.999f)
+            c->alphaTested = true;
+    }
+    if (c->sheenMaterials || c->alphaTested) c->extendedMaterials = true;
+}
+
 bool envNeeActive(const VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
     return c->cfg.environmentSampling == VKRT_CUDA_ENV_IMPORTANCE && c->envTexture != VKRT_CUDA_INVALID_INDEX &&
            sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u && !c->transmissiveMaterials;
@@ -328,6 +350,7 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
     S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
     S.extended = c->extendedMaterials ? 1u : 0u;
     S.transmissive = c->transmissiveMaterials ? 1u : 0u;
+    S.alpha = c->alphaTested ? 1u : 0u;
     return S;
 }
 
@@ -464,6 +487,7 @@ int32_t vkrt_cuda_upload_geometry(VKRT_CudaContext* c, const VKRT_CudaShaderVert
     VKRT_TRY(c, c->indices.assign(indices, indexCount, c->stream), "upload indices");
     VKRT_TRY(c, c->meshes.assign(meshes, meshCount, c->stream), "upload meshes");
     c->hostMeshes.assign(meshes, meshes + meshCount);
+    refreshMaterialFlags(c);
     c->vertexCount = vertexCount;
     c->indexCount = indexCount;
     c->triCount = uint32_t(tris);
@@ -511,6 +535,7 @@ int32_t vkrt_cuda_update_meshes(VKRT_CudaContext* c, const VKRT_CudaMeshInfo* me
     cudaSetDevice(c->device);
     VKRT_TRY(c, c->meshes.assign(meshes, meshCount, c->stream), "upload meshes");
     c->hostMeshes.assign(meshes, meshes + meshCount);
+    refreshMaterialFlags(c);
     if (geometryChanged) {
         uint64_t tris = 0;
         for (auto& m : c->hostMeshes) tris += m.indexCount / 3u;
@@ -527,20 +552,7 @@ int32_t vkrt_cuda_upload_materials(VKRT_CudaContext* c, const VKRT_CudaMaterial*
     VKRT_TRY(c, c->materials.assign(materials, count, c->stream), "upload materials");
     c->hostMaterials.assign(materials, materials + count);
     c->materialCount = count;
-    c->extendedMaterials = false;
-    c->transmissiveMaterials = false;
-    c->sheenMaterials = false;
-    for (uint32_t i = 0; i < count; ++i) {
-        const VKRT_CudaMaterial& m = materials[i];
-        // bsdfSheenColor (material.slang:63-73) is saturate(tint) * saturate(weight)
-        const float w = std::min(std::max(m.sheenTintWeight[3], 0.0f), 1.0f);
-        const float tint = std::max({m.sheenTintWeight[0], m.sheenTintWeight[1], m.sheenTintWeight[2]});
-        if (w > 0.0f && tint > 0.0f) c->sheenMaterials = true;
-        if (m.transmission > 0.0f) c->transmissiveMaterials = true;
-        if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f ||
-            (w > 0.0f && tint > 0.0f))
-            c->extendedMaterials = true;
-    }
+    refreshMaterialFlags(c);
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -781,6 +793,7 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     rp.height = c->height;
     rp.countBytes = c->cfg.countRays;
     rp.extended = c->extendedMaterials ? 1u : 0u;
+    rp.alpha = c->alphaTested ? 1u : 0u;
     FilmBuffers film = filmOf(c);
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "render");
     VKRT_TRY(c, launchRender(scene, *sd, rp, film, c->counters, c->cfg.threadsPerBlock, c->stream), "render launch");
@@ -920,8 +933,8 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     // a single context with an enabled radiance cache trains it and renders cache-terminated paths
     WfCacheFrame cache{};
     const bool useCache = count == 1 && c0->nrc && c0->nrc->ready() && c0->nrcCfg.enabled;
-    if (useCache && c0->transmissiveMaterials)
-        return invalid(c0, "the radiance cache covers reflection-only materials (a material has transmission)");
+    if (useCache && (c0->transmissiveMaterials || c0->alphaTested))
+        return invalid(c0, "the radiance cache covers opaque reflection-only materials (transmission or alpha)");
     if (useCache)
         cache = WfCacheFrame{c0->nrc.get(), c0->nrcCfg.terminationDepth, c0->nrcCfg.trainingPaths,
                              c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber};
@@ -1231,7 +1244,8 @@ int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const f
         if (m.specularTint != 0.0f) return invalid(c, "the adjoint needs specularTint 0 on every material");
         if (m.clearcoat > 0.0f || m.subsurface > 0.0f || m.diffuseRoughness > 0.0f || m.transmission > 0.0f)
             return invalid(c, "the adjoint covers the metal / dielectric / Lambert stack only");
-    if (c->sheenMaterials) return invalid(c, "the adjoint covers the metal / dielectric / Lambert stack only");
+    if (c->sheenMaterials || c->alphaTested)
+        return invalid(c, "the adjoint covers the opaque metal / dielectric / Lambert stack only");
     }
     VKRT_CudaAdjointConfig a{};
     if (cfg) a = *cfg;

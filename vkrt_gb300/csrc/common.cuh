@@ -112,6 +112,16 @@ struct Rng {
     }
 };
 
+// Alpha-tested hits (rt/alpha_test.slang). vkrt draws a stochastic alpha decision from the path's random stream in
+// any-hit order, which the driver leaves unspecified; here the decision for a triangle is a hash of a per-ray seed
+// (the path stream's state when the ray starts, salted per shadow request) and the triangle's id, so the closest
+// accepted hit does not depend on traversal order and the path stream is not advanced.
+VKRT_DEV uint32_t alphaSeedOf(const Rng& r) { return uint32_t(r.state) ^ uint32_t(r.state >> 32); }
+VKRT_HD uint32_t alphaShadowSeed(uint32_t seed, uint32_t request) { return seed ^ (0x68bc21ebu * (request + 1u)); }
+VKRT_HD float alphaRandom(uint32_t seed, uint32_t gid) {
+    return float(wellonsHash(seed ^ wellonsHash(gid + 0x632be5abu)) & 0x00ffffffu) * (1.0f / 16777216.0f);
+}
+
 VKRT_DEV Rng makeRng(uint32_t mode, uint64_t seed, int32_t x, int32_t y, uint32_t frame, uint32_t sampleIndex) {
     Rng r;
     if (mode == VKRT_CUDA_RNG_REFERENCE) {

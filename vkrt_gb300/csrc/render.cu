@@ -19,7 +19,8 @@ namespace {
 
 // One pixel: SceneData.samplesPerPixel paths, each traced to the end (shadow rays traced inline), blended into the
 // running mean (writeback.slang:72-114) and encoded for display.
-// kFull: the extended reflection stack and the denoiser features (written when the film has feature images)
+// kFull: vkrt's whole material stack, alpha tests and the denoiser features (written when the film has feature
+// images)
 template <bool kSpectral, bool kCountBytes, bool kFull>
 __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, VKRT_CudaSceneData sd, RenderParams rp,
                                                                FilmBuffers film, RenderCounters* counters) {
@@ -53,7 +54,14 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                 for (;;) {
                     if (p.depth == 0) pc.primary++;
                     else pc.extension++;
-                    TraceHit h = closest<kCountBytes>(k, p.o, p.d);
+                    // alpha-tested scenes: the ray's alpha seed, which the vertex's shadow rays reuse salted
+                    const uint32_t alphaSeed = alphaSeedOf(p.rng);
+                    TraceHit h;
+                    if (kFull && rp.alpha)
+                        h = traceBvh<false, kCountBytes, false, false, true>(sc, TraceRay{p.o, p.d, kTMin, kTMax},
+                                                                             k.stackColumn, k.stackStride, counters,
+                                                                             0u, alphaSeed);
+                    else h = closest<kCountBytes>(k, p.o, p.d);
                     ShadowRequest sh[2];
                     uint32_t ns;
                     bool cont;
@@ -65,8 +73,12 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                         pc.shadow++;
                         TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
                         if (kFull) {  // a transmissive occluder makes the vertex's NEE unsupported
-                            const TraceHit o = traceBvh<true, kCountBytes, false, true>(sc, r, k.stackColumn,
-                                                                                         k.stackStride, counters);
+                            const TraceHit o =
+                                rp.alpha ? traceBvh<true, kCountBytes, false, true, true>(
+                                               sc, r, k.stackColumn, k.stackStride, counters, 0u,
+                                               alphaShadowSeed(alphaSeed, i))
+                                         : traceBvh<true, kCountBytes, false, true>(sc, r, k.stackColumn,
+                                                                                    k.stackStride, counters);
                             if (o.mesh == VKRT_CUDA_INVALID_INDEX) {
                                 if (o.prim == kShadowThroughTransmission) p.flags &= ~kPathPrevNee;
                                 else p.radiance += sh[i].contribution;

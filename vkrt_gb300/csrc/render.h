@@ -14,7 +14,8 @@ struct RenderParams {
     uint32_t width;      // film size (the viewport rectangle lives in SceneData)
     uint32_t height;
     uint32_t countBytes; // accumulate node / triangle fetch bytes
-    uint32_t extended;   // some material uses the extended reflection stack (clearcoat, Oren-Nayar, subsurface)
+    uint32_t extended;   // some material uses vkrt's stack beyond the glTF subset, alpha tests included
+    uint32_t alpha;      // some material or mesh is alpha-tested (rt/alpha_test.slang)
 };
 
 struct FilmBuffers {

@@ -185,6 +185,53 @@ VKRT_DEV float4 sampleMaterialTexture(const DeviceScene& sc, uint32_t idx, uint3
 }
 
 // ---------------------------------------------------------------------------------------------------------------
+// alpha test (rt/alpha_test.slang:8-68): mask (cut-out against alphaCutoff, then mesh x material x vertex opacity)
+// and blend (mesh x material x texture opacity) decided with alphaRandom
+// ---------------------------------------------------------------------------------------------------------------
+constexpr uint32_t kAlphaModeMask = 1u, kAlphaModeBlend = 2u;  // VKRT_MATERIAL_ALPHA_MODE_* (shared/constants.h)
+
+VKRT_DEV bool alphaMayReject(const VKRT_CudaMaterial& mat, float meshOpacity) {  // alphaMayRejectHit (:8-10)
+    return mat.alphaMode == kAlphaModeMask || mat.alphaMode == kAlphaModeBlend || mat.opacity < 0.999f ||
+           meshOpacity < 0.999f;
+}
+
+VKRT_DEV bool alphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32_t prim, float u, float v, uint32_t seed,
+                           uint32_t gid) {
+    const VKRT_CudaMeshInfo& m = sc.meshes[mesh];
+    const VKRT_CudaMaterial& mat = sc.materials[m.materialIndex];
+    if (!alphaMayReject(mat, m.opacity)) return true;
+    // evaluateSurfaceTextureData (geometry/surface/interpolation.slang:46-60)
+    const uint32_t base = m.indexBase + prim * 3u;
+    const float4* va = reinterpret_cast<const float4*>(sc.vertices + __ldg(sc.indices + base) + m.vertexBase);
+    const float4* vb = reinterpret_cast<const float4*>(sc.vertices + __ldg(sc.indices + base + 1) + m.vertexBase);
+    const float4* vc = reinterpret_cast<const float4*>(sc.vertices + __ldg(sc.indices + base + 2) + m.vertexBase);
+    const float4 ta = __ldg(va + 1), tb = __ldg(vb + 1), tc = __ldg(vc + 1);
+    const float w = 1.0f - u - v;
+    TexCoords tex;
+    tex.color = lerpTri(unpackColor(__float_as_uint(__ldg(va + 2).z)), unpackColor(__float_as_uint(__ldg(vb + 2).z)),
+                        unpackColor(__float_as_uint(__ldg(vc + 2).z)), u, v);
+    tex.uv0 = make_float2(ta.x * w + tb.x * u + tc.x * v, ta.y * w + tb.y * u + tc.y * v);
+    tex.uv1 = make_float2(ta.z * w + tb.z * u + tc.z * v, ta.w * w + tb.w * u + tc.w * v);
+    // evaluateMaterialTextureAlpha (:19-25)
+    float texAlpha = tex.color.w;
+    if (mat.alphaMode != VKRT_CUDA_ALPHA_MODE_OPAQUE)
+        texAlpha *= sampleMaterialTexture(sc, mat.baseColorTextureIndex, mat.baseColorTextureWrap,
+                                          mat.baseColorTextureTransform, mat.textureRotations[0],
+                                          mat.textureTexcoordSets & 0xffu, tex, f4(1.0f)).w;
+    if (mat.alphaMode == kAlphaModeMask) {  // alphaPass (:31-47)
+        if (texAlpha < mat.alphaCutoff) return false;
+        const float o = sat(m.opacity * mat.opacity * tex.color.w);
+        if (o >= 1.0f) return true;
+        if (o <= 0.0f) return false;
+        return alphaRandom(seed, gid) <= o;
+    }
+    const float o = sat(m.opacity * mat.opacity * texAlpha);
+    if (o <= 0.0f) return false;
+    if (o >= 1.0f) return true;
+    return alphaRandom(seed, gid) <= o;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
 // spectral utilities (utility/rgb2spec.slang, utility/spectral.slang)
 // ---------------------------------------------------------------------------------------------------------------
 struct SpecTable {

@@ -127,6 +127,8 @@ struct WfGlobals {
     // scenes with transmissive materials: per slot, hero lanes 1-3 of the technique pdfs and the medium's absorption
     // (extA = techYZW + sigma.x, extB = prevVertexYZW + sigma.y, extC = prevBsdfYZW + sigma.z, extD = sigma.w)
     uint32_t transmissive;
+    uint32_t alpha;        // some scene has alpha-tested materials: per slot, the alpha seed of the slot's ray
+    uint32_t* alphaSeed;
     float4* extA;
     float4* extB;
     float4* extC;
@@ -411,6 +413,22 @@ VKRT_DEV void warpCountBytes(unsigned long long* nodeBytes, unsigned long long* 
 }
 
 // kMinBlocks: resident blocks per SM the register allocation must allow (the launch grid's blocks per SM)
+// The closest hit of queue entry i (slot `slot`): hit records, and the sort key or class queue entry
+VKRT_DEV void storeHit(const WfGlobals& g, uint32_t i, uint32_t slot, const TraceHit& h) {
+    g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
+    g.hitV[slot] = h.v;
+    if (g.sort == kSortMaterial) {  // histogram of (scene, class) keys for the counting sort
+        const uint32_t sceneId = g.slotScene[slot];
+        const uint32_t key = 3u * sceneId + hitClass(g.scenes[sceneId].sc, h);
+        g.hitKey[i] = key;
+        warpAggregatedSlot(g.keyHist, key);
+    } else if (g.sort == kSortClass) {  // filed straight into the class queues
+        const uint32_t c = hitClass(g.scenes[g.slotScene[slot]].sc, h);
+        const uint32_t pos = warpAggregatedSlot(&g.counts[kCntClass0], c);
+        g.classQueue[size_t(c) * g.Q + pos] = slot;
+    }
+}
+
 template <bool kCount, int kMinBlocks>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals g, uint32_t inQueue) {
     extern __shared__ uint2 smemStack[];
@@ -430,25 +448,37 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
             if (__float_as_uint(o.w) == 0u) ++primary;
             else ++ext;
         },
-        [&](uint32_t i, const TraceHit& h) {
-            uint32_t slot = q[i];
-            g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
-            g.hitV[slot] = h.v;
-            if (g.sort == kSortMaterial) {  // histogram of (scene, class) keys for the counting sort
-                const uint32_t sceneId = g.slotScene[slot];
-                const uint32_t key = 3u * sceneId + hitClass(g.scenes[sceneId].sc, h);
-                g.hitKey[i] = key;
-                warpAggregatedSlot(g.keyHist, key);
-            } else if (g.sort == kSortClass) {  // filed straight into the class queues
-                const uint32_t c = hitClass(g.scenes[g.slotScene[slot]].sc, h);
-                const uint32_t pos = warpAggregatedSlot(&g.counts[kCntClass0], c);
-                g.classQueue[size_t(c) * g.Q + pos] = slot;
-            }
-        },
-        nodeVisits, triTests);
+        [&](uint32_t i, const TraceHit& h) { storeHit(g, i, q[i], h); }, nodeVisits, triTests);
     warpCount(&g.counters->primaryRays, primary);
     warpCount(&g.counters->extensionRays, ext);
     if (kCount) warpCountBytes(&g.counters->nodeBytes, &g.counters->triBytes, nodeVisits, triTests);
+}
+
+// Closest hits of scenes with alpha-tested materials: one ray per thread through traceBvh's alpha mode, seeded from
+// the slot's random stream (the shade kernel keeps the seed for the vertex's shadow rays).
+template <bool kCount>
+__global__ void __launch_bounds__(kWfThreads) kWfIntersectAlpha(WfGlobals g, uint32_t inQueue) {
+    extern __shared__ uint2 smemStack[];
+    const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
+    const uint32_t n = g.counts[inQueue];
+    uint32_t primary = 0, ext = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        if (i < n) {
+            const uint32_t slot = q[i];
+            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            const float4 o = g.o[slot], d = g.d[slot];
+            const uint4 rs = g.rng[slot];
+            const TraceRay r{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
+            const TraceHit h = traceBvh<false, kCount, false, false, true>(
+                sc, r, smemStack + threadIdx.x, blockDim.x, kCount ? g.counters : nullptr, 0u, rs.x ^ rs.y);
+            if (__float_as_uint(o.w) == 0u) ++primary;
+            else ++ext;
+            storeHit(g, i, slot, h);
+        }
+    }
+    warpCount(&g.counters->primaryRays, primary);
+    warpCount(&g.counters->extensionRays, ext);
 }
 
 __global__ void __launch_bounds__(1024) kWfSortScan(WfGlobals g) {
@@ -712,6 +742,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
             if constexpr (kFull) {
                 loadPathExt(g, slot, p);
                 if (pf & kPendUnsupported) p.flags &= ~kPathPrevNee;  // the previous vertex's NEE was unsupported
+                if (g.alpha) g.alphaSeed[slot] = alphaSeedOf(p.rng);  // the seed the intersect kernel used
             }
             if constexpr (kAdjoint) adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
             g.pendFlags[slot] = 0u;
@@ -807,10 +838,11 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g)
     if (kCount) warpCountBytes(&g.counters->shadowNodeBytes, &g.counters->shadowTriBytes, nodeVisits, triTests);
 }
 
-// Shadow rays of scenes with transmissive materials: one ray per thread through traceBvh's transmissive any-hit
-// mode; a ray whose segment meets only transmissive surfaces marks its request unsupported.
-template <bool kCount>
-__global__ void __launch_bounds__(kWfThreads) kWfShadowTransmissive(WfGlobals g) {
+// Shadow rays of scenes with transmissive or alpha-tested materials: one ray per thread through traceBvh's
+// transmissive any-hit mode (and alpha mode); a ray whose segment meets only transmissive surfaces marks its
+// request unsupported.
+template <bool kCount, bool kAlpha>
+__global__ void __launch_bounds__(kWfThreads) kWfShadowScan(WfGlobals g) {
     extern __shared__ uint2 smemStack[];
     const uint32_t n = g.counts[kCntShadow];
     uint32_t traced = 0;
@@ -822,8 +854,9 @@ __global__ void __launch_bounds__(kWfThreads) kWfShadowTransmissive(WfGlobals g)
             const uint32_t slot = tag & 0x7FFFFFFFu;
             const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
             const TraceRay r{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
-            const TraceHit h = traceBvh<true, kCount, false, true>(sc, r, smemStack + threadIdx.x, blockDim.x,
-                                                                   kCount ? g.counters : nullptr);
+            const TraceHit h = traceBvh<true, kCount, false, true, kAlpha>(
+                sc, r, smemStack + threadIdx.x, blockDim.x, kCount ? g.counters : nullptr, 0u,
+                kAlpha ? alphaShadowSeed(g.alphaSeed[slot], tag >> 31) : 0u);
             ++traced;
             if (h.mesh == VKRT_CUDA_INVALID_INDEX)
                 atomicOr(&g.pendFlags[slot], h.prim == kShadowThroughTransmission ? kPendUnsupported : 4u << (tag >> 31));
@@ -933,7 +966,7 @@ struct WavefrontEngine::Buffers {
     size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
            c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
            c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0,
-           c_fA = 0, c_fN = 0, c_eA = 0, c_eB = 0, c_eC = 0, c_eD = 0;
+           c_fA = 0, c_fN = 0, c_eA = 0, c_eB = 0, c_eC = 0, c_eD = 0, c_as = 0;
     size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
     WfScene* scenes = nullptr;
     uint32_t* bases = nullptr;  // itemBase of every scene, then workBase
@@ -975,7 +1008,7 @@ void WavefrontEngine::release() {
                     g.nrcQueries, g.slotQuery, g.nrcPred, b_->recIn, b_->recTarget, b_->recCount, g.adjDelta,
                     g.adjTotal,
                     g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR,
-                    g.itemFeatA, g.itemFeatN, g.extA, g.extB, g.extC, g.extD};
+                    g.itemFeatA, g.itemFeatN, g.extA, g.extB, g.extC, g.extD, g.alphaSeed};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b_->hostCount) cudaFreeHost(b_->hostCount);
@@ -1044,11 +1077,14 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     bool features = false;  // forward frames render denoiser features when any scene has feature films
     bool extended = false;      // some scene's materials use the full material stack
     bool transmissive = false;  // ... with transmission (media and per-lane hero state per slot)
+    bool alpha = false;         // ... with alpha tests
     for (const WfScene& S : scenes) {
         if (mode == kWavefrontForward && S.film.albedoWrite) features = true;
         if (S.extended) extended = true;
         if (S.transmissive) transmissive = true;
+        if (S.alpha) alpha = true;
     }
+    if (alpha) WF_GROW(alphaSeed, c_as, Q);
     const bool full = features || extended;
     if (transmissive) {
         WF_GROW(extA, c_eA, Q);
@@ -1116,6 +1152,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.mode = uint32_t(mode);
     g.features = features ? 1u : 0u;
     g.transmissive = transmissive ? 1u : 0u;
+    g.alpha = alpha ? 1u : 0u;
     g.adj = adjoint ? *adjoint : AdjointParams{};
     g.cacheDepth = useCache ? cache->cacheDepth : 0xFFFFFFFFu;
     g.scenes = B.scenes;
@@ -1160,7 +1197,9 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     auto body = [&](uint32_t in, uint32_t out, bool useGraph) {
         stage(kStageBegin, [&] { kWfBegin<<<4, 1024, 0, stream>>>(g, out); });
         stage(kStageIntersect, [&] {
-            if (profile) kWfIntersect<true, 8><<<gridI, kWfThreads, smem, stream>>>(g, in);
+            if (alpha && profile) kWfIntersectAlpha<true><<<gridS, kWfThreads, smem, stream>>>(g, in);
+            else if (alpha) kWfIntersectAlpha<false><<<gridS, kWfThreads, smem, stream>>>(g, in);
+            else if (profile) kWfIntersect<true, 8><<<gridI, kWfThreads, smem, stream>>>(g, in);
             else kWfIntersect<false, 8><<<gridI, kWfThreads, smem, stream>>>(g, in);
         });
         if (g.sort == kSortMaterial) {
@@ -1182,8 +1221,10 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             else kWfShade<false, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
         });
         stage(kStageShadow, [&] {
-            if (transmissive && profile) kWfShadowTransmissive<true><<<gridS, kWfThreads, smem, stream>>>(g);
-            else if (transmissive) kWfShadowTransmissive<false><<<gridS, kWfThreads, smem, stream>>>(g);
+            if (alpha && profile) kWfShadowScan<true, true><<<gridS, kWfThreads, smem, stream>>>(g);
+            else if (alpha) kWfShadowScan<false, true><<<gridS, kWfThreads, smem, stream>>>(g);
+            else if (transmissive && profile) kWfShadowScan<true, false><<<gridS, kWfThreads, smem, stream>>>(g);
+            else if (transmissive) kWfShadowScan<false, false><<<gridS, kWfThreads, smem, stream>>>(g);
             else if (profile) kWfShadow<true, 8><<<gridI, kWfThreads, smem, stream>>>(g);
             else kWfShadow<false, 8><<<gridI, kWfThreads, smem, stream>>>(g);
         });

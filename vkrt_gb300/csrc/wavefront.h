@@ -25,6 +25,7 @@ struct WfScene {
     uint32_t envNee;
     uint32_t extended;      // some material uses vkrt's stack beyond the glTF subset (the full instantiations)
     uint32_t transmissive;  // some material has transmission (media, per-lane hero pdfs, transmissive shadows)
+    uint32_t alpha;         // some material or mesh is alpha-tested (alpha-aware intersect and shadow kernels)
     // filled by the engine
     uint32_t tileW, tileH, tilesX;
     uint32_t workBase, workCount;  // padded pixel work items (tile order)
