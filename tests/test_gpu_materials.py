@@ -240,9 +240,12 @@ def alpha_cornell(width=64, height=64, spp=4):
     """The tall box is cut out by an alpha-mask checker texture, the short box is half transparent (material
     opacity 0.5, stochastic) and the left wall's mesh opacity is 0.7."""
     s = scenes.cornell(width, height, spp=spp)
-    checker = np.ones((8, 8, 4), np.float32)
+    # 8 x 8 cells of 8 x 8 texels: bilinear alpha crosses the cutoff within 1/8 of a cell, so few pixels sit where
+    # FP32 rounding of the interpolated uv can flip the cut
+    cells = (np.add.outer(np.arange(64) // 8, np.arange(64) // 8) % 2).astype(np.float32)
+    checker = np.ones((64, 64, 4), np.float32)
     checker[..., :3] = 0.73
-    checker[..., 3] = (np.add.outer(np.arange(8), np.arange(8)) % 2).astype(np.float32)
+    checker[..., 3] = cells
     s.textures = dict(s.textures)
     s.textures[0] = checker
     cut = s.materials[0].copy()
