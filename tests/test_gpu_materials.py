@@ -96,6 +96,7 @@ def glass_cornell(width=64, height=64, spp=4, rough=0.0, abbe=0.0, absorb=0.0):
     meshes = s.meshes.copy()
     meshes["materialIndex"][-1] = first
     meshes["materialIndex"][-2] = first
+    meshes["position"][-2:, 2] += 2e-3  # off the floor plane: no coplanar glass / floor faces
     s.meshes = meshes
     return s
 
@@ -115,7 +116,7 @@ def test_transmission_rgb_parity(built, integrator, variant):
         st = ctx.stats()
     ref, ost = cpu.OracleScene(s).render(s.scene_data, rng_mode=abi.RNG_REFERENCE)
     close = (np.abs(gpu[..., :3] - ref[..., :3]) <= 1e-3 + 1e-3 * np.abs(ref[..., :3])).all(-1)
-    assert close.mean() > 0.95, close.mean()
+    assert close.mean() > 0.97, close.mean()
     assert np.isfinite(gpu).all()
     # shadow rays of the device and the oracle agree to the share of diverged paths
     assert abs(st["shadowRays"] - ost["shadowRays"]) <= 0.05 * ost["shadowRays"]
@@ -138,7 +139,7 @@ def test_transmission_spectral_parity(built, integrator, variant):
         gpu = ctx.read_accumulation()
     ref, _ = cpu.OracleScene(s).render(s.scene_data, rng_mode=abi.RNG_REFERENCE)
     close = (np.abs(gpu[..., :3] - ref[..., :3]) <= 2e-3 + 2e-3 * np.abs(ref[..., :3])).all(-1)
-    assert close.mean() > 0.95, close.mean()
+    assert close.mean() > 0.97, close.mean()
     assert np.isfinite(gpu).all()
 
 
@@ -261,6 +262,9 @@ def alpha_cornell(width=64, height=64, spp=4):
     meshes["materialIndex"][-1] = first
     meshes["materialIndex"][-2] = first + 1
     meshes["opacity"][3] = 0.7
+    # the boxes' bottoms lie in the floor plane; lifted a little, so that no ray meets an alpha-tested face and the
+    # floor at the same distance (which of two coplanar faces is nearer is decided by rounding)
+    meshes["position"][-2:, 2] += 2e-3
     s.meshes = meshes
     return s
 
