@@ -95,3 +95,27 @@ def icosphere_mesh(subdivisions=2):
         f = nf
     p = np.array(verts, np.float32)
     return {"positions": p, "normals": p.copy(), "indices": np.array(f, np.uint32).reshape(-1), "name": "Sphere"}
+
+
+def prism_mesh():
+    """Triangular prism with flat faces: an equilateral cross-section (unit circumradius) in glTF's XY plane, extruded
+    from z = -1 to z = 1; faces carry their own vertices so normals stay flat."""
+    ang = np.deg2rad([90.0, 210.0, 330.0])
+    tri = np.stack([np.cos(ang), np.sin(ang)], 1).astype(np.float32)
+    pos, nrm, idx = [], [], []
+
+    def face(pts, n):
+        b = len(pos)
+        pos.extend(pts)
+        nrm.extend([n] * len(pts))
+        idx.extend([b + 0, b + 1, b + 2] if len(pts) == 3 else [b + 0, b + 1, b + 2, b + 0, b + 2, b + 3])
+
+    face([[*tri[0], 1], [*tri[1], 1], [*tri[2], 1]], [0, 0, 1])
+    face([[*tri[0], -1], [*tri[2], -1], [*tri[1], -1]], [0, 0, -1])
+    for k in range(3):
+        a, b = tri[k], tri[(k + 1) % 3]
+        n = np.array([b[1] - a[1], a[0] - b[0], 0.0])  # outward for the counter-clockwise section
+        n = n / np.linalg.norm(n)
+        face([[*a, -1], [*b, -1], [*b, 1], [*a, 1]], n.tolist())
+    return {"positions": np.asarray(pos, np.float32), "normals": np.asarray(nrm, np.float32), "indices": idx,
+            "name": "Prism"}
