@@ -61,7 +61,8 @@ typedef struct VKRT_CudaWavefrontConfig {
     uint32_t sortByMaterial;       /* shade-queue order: 0 as traced; 1 counting-sorted by (scene, material);
                                       2 partitioned into misses, dielectric and metal hits by the intersect kernel */
     uint32_t intersectBlocksPerSM; /* persistent grid of the traversal kernels, per SM */
-    uint32_t shadeBlocksPerSM;     /* persistent grid of the shading kernels, per SM */
+    uint32_t shadeBlocksPerSM;     /* persistent grid of the shading kernels, per SM; also their register budget:
+                                      3 (default) 168 registers, 4: 128, 6: 80, 8: 64 */
     uint32_t useGraph;             /* 1: the frame is one CUDA-graph launch (conditional while node) */
     uint32_t profileStages;        /* 1: stage-by-stage launches with device timers and fetch-byte counting (slower;
                                       for profiling), reported in VKRT_CudaStats.stageMs / *FetchBytes */

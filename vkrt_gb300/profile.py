@@ -31,6 +31,7 @@ def main(argv=None) -> dict:
     ap.add_argument("--stage-launches", action="store_true")
     ap.add_argument("--rgb", action="store_true", help="RGB transport instead of hero spectral")
     ap.add_argument("--cache", action="store_true", help="render with the radiance cache (wavefront only)")
+    ap.add_argument("--shade-blocks", type=int, default=0, help="shade kernel residency (blocks per SM; 0 = default)")
     a = ap.parse_args(argv)
     import torch
 
@@ -44,6 +45,8 @@ def main(argv=None) -> dict:
     ctx.upload_scene(scene)
     if a.stage_launches:
         ctx.set_wavefront_config(profileStages=1)
+    if a.shade_blocks:
+        ctx.set_wavefront_config(shadeBlocksPerSM=a.shade_blocks)
     if a.cache:
         ctx.nrc_configure(enabled=1)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -68,7 +71,8 @@ def main(argv=None) -> dict:
             out["frame_ms"] = round(out.get("frame_ms", 0.0) + ev[0].elapsed_time(ev[1]), 3)
     out["workload"] = {"width": a.width, "height": a.height, "spp": a.spp, "depth": a.depth, "spheres": a.spheres,
                        "triangles": scene.triangle_count, "frames": a.frames, "integrator": a.integrator,
-                       "mode": "rgb" if a.rgb else "hero-spectral", "cache": a.cache}
+                       "mode": "rgb" if a.rgb else "hero-spectral", "cache": a.cache,
+                       "shade_blocks": a.shade_blocks}
     ctx.close()
     print(json.dumps(out))
     return out
