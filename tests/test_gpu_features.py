@@ -86,7 +86,8 @@ def test_features_accumulate_over_frames(built):
         ctx.set_denoiser_features(False)
         with pytest.raises(Exception):
             ctx.read_denoiser_features()
-    # features do not change the image: same frame with features off
+    # features do not change the image: same frame with features off (the feature frame runs the full-stack kernel,
+    # whose arithmetic is ordered differently, so equal to float rounding)
     with RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT) as a, \
             RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT) as b:
         a.upload_scene(s)
@@ -94,7 +95,7 @@ def test_features_accumulate_over_frames(built):
         b.set_denoiser_features(True)
         a.render_frame(s.scene_data)
         b.render_frame(s.scene_data)
-        np.testing.assert_array_equal(a.read_accumulation(), b.read_accumulation())
+        np.testing.assert_allclose(a.read_accumulation(), b.read_accumulation(), rtol=1e-5, atol=1e-7)
     del acc_on
 
 
