@@ -1322,8 +1322,9 @@ template <class R> struct SheenLtc {
 };
 template <class R> SheenLtc<R> sheenLtcAt(const float* T, V3<R> wo, R sheenRough) {  // makeSheenParams (:41-57)
     SheenLtc<R> p;
+    if (!T) return p;  // no table: no sheen lobe (its weight is 0 and the lobe is never evaluated)
     p.basis = makeBasis(V3<R>(R(0), R(0), R(1)), V4<R>(wo.x, wo.y, wo.z, R(1)));
-    if (!T || wo.z <= R(0)) return p;
+    if (wo.z <= R(0)) return p;
     R r = std::min(std::max(sheenRough, R(1e-3)), R(1));
     p.a = sheenLookup(T, wo.z, r, 0u);
     p.b = sheenLookup(T, wo.z, r, 1u);
