@@ -53,7 +53,7 @@ enum : uint32_t {
 };
 constexpr uint32_t kPendCache = 16u;        // pendFlags: the path ended at a radiance-cache query
 constexpr uint32_t kPendUnsupported = 32u;  // pendFlags: an NEE shadow ray met a transmissive surface
-constexpr uint32_t kSortNone = 0, kSortMaterial = 1, kSortClass = 2;  // kSortMaterial sorts by (scene, class)
+constexpr uint32_t kSortMaterial = 1, kSortClass = 2;  // sortByMaterial (0: as traced); 1 sorts by (scene, class)
 constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
 
 
@@ -726,7 +726,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         bool cont = false;
         uint32_t slot = 0, ns = 0;
         ShadowRequest sh[2];
-        NrcInput query;
+        NrcInput query{};
         bool queried = false;
         if (valid) {
             if (g.sort == kSortClass)  // the three class queues read as one
