@@ -703,9 +703,9 @@ VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t sl
                  xyz(g.adjTotal[slot]), xyz(radiance));
 }
 
-// kFull: the extended reflection stack and the denoiser features (taken when g.features is set); a separate
-// instantiation, so frames that need neither keep the register budget of the plain kernel
-template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFull = false>
+// kFull: vkrt's whole material stack (and alpha tests); kFeatures: the denoiser features (taken when g.features is
+// set). Separate instantiations, so frames that need neither keep the register budget of the plain kernel.
+template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFull = false, bool kFeatures = kFull>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
     const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
@@ -762,8 +762,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                 DenoiserFeature feat{f3(0.0f), f3(0.0f), featDone ? 1.0f : 0.0f};
                 cont = shadePathVertex<kSpectral, CacheHook, kFull>(
                     S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
-                    CacheHook{{}, &query, &queried, p.d, (kFull && g.features) ? &feat : nullptr});
-                if (kFull && g.features && !featDone && feat.weight > 0.0f) {
+                    CacheHook{{}, &query, &queried, p.d, (kFeatures && g.features) ? &feat : nullptr});
+                if (kFeatures && g.features && !featDone && feat.weight > 0.0f) {
                     const size_t item = size_t(S.itemBase) + g.slotItem[slot];
                     g.itemFeatA[item] = make_float4(feat.albedo.x, feat.albedo.y, feat.albedo.z, 1.0f);
                     g.itemFeatN[item] = make_float4(feat.normal.x, feat.normal.y, feat.normal.z, 0.0f);
@@ -1085,7 +1085,6 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         if (S.alpha) alpha = true;
     }
     if (alpha) WF_GROW(alphaSeed, c_as, Q);
-    const bool full = features || extended;
     if (transmissive) {
         WF_GROW(extA, c_eA, Q);
         WF_GROW(extB, c_eB, Q);
@@ -1212,8 +1211,11 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             // register budget follows the requested residency: 168 (3 blocks/SM, no spills), 128 (4), 80 (6) or
             // 64 (8) registers
             if (adjMode) kWfShade<false, true, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (full && spectral) kWfShade<true, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (full) kWfShade<false, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (extended && spectral) kWfShade<true, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (extended) kWfShade<false, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (features && spectral)  // reflection-only materials with feature films
+                kWfShade<true, false, 3, false, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            else if (features) kWfShade<false, false, 3, false, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 8) kWfShade<true, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 6) kWfShade<true, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 4) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
