@@ -2044,6 +2044,7 @@ struct ModeFlags {
     bool envNee;       // environment importance sampling enabled and a distribution exists
     bool transmissive; // some material has transmission > 0 (environment NEE is then off: vkrt has none)
     bool alpha;        // some mesh is alpha-tested
+    bool single;       // spectral mode with one wavelength per path (raygen_spectral_single.slang)
 };
 
 // A shadow ray: visible, occluded, or unsupported (through a transmissive surface). Scenes without transmissive or
@@ -2247,8 +2248,11 @@ V3<R> traceHeroSample(Ctx<R>& c, const ModeFlags& mf, int px, int py, uint32_t s
     for (int i = 0; i < 4; ++i) lam[i] = R(kLambdaMin) + fracr(R(unit) + R(offs[i])) * R(kLambdaRange);
     V4<R> invPdf = V4<R>(R(kLambdaRange));
     V4<R> thr(R(1)), techPath(R(1)), prevVertexTech(R(0)), prevBsdfTech(R(0)), spec(R(0));
-    bool collapsed = false;  // !spectralHeroPathActive
-    R thrS = R(0), specS = R(0), prevBsdfPdf = R(0);
+    // spectral_single/integrator.slang:15-120 is the collapsed branch from the start: sampleUniformWavelength
+    // (wavelength.slang:34-42) draws the same unit sample, so its wavelength is hero lane 0
+    bool collapsed = mf.single;  // !spectralHeroPathActive
+    R thrS = collapsed ? R(1) : R(0), specS = R(0), prevBsdfPdf = R(0);
+    if (collapsed) thr = V4<R>(R(0));
     V3<R> xyzDone(R(0));  // the hero lanes' radiance, moved to XYZ at the collapse
     bool prevNee = false;
     Medium<R> med;
@@ -2450,6 +2454,8 @@ void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderPa
     mf.transmissive = false;
     for (const VKRT_CudaMaterial& m : s.materials) mf.transmissive = mf.transmissive || m.transmission > 0.0f;
     mf.alpha = sceneAlphaTested(s);
+    mf.single = spectral && VKRT_CUDA_SPECTRAL_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_SPECTRAL_SINGLE;
+    if (mf.single) mf.envNee = false;
     mf.envNee = s.envSampling == VKRT_CUDA_ENV_IMPORTANCE && s.env.valid && sd.misNeeEnabled != 0u &&
                 sd.environmentTextureIndex == s.envTexture && !mf.transmissive;
     Rgb2Spec tab;

@@ -298,8 +298,9 @@ int32_t validateFrame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
             uint64_t(ti.scaleOffset) + ti.res > c->rgb2specFloats ||
             uint64_t(ti.dataOffset) + 9ull * ti.res * ti.res * ti.res > c->rgb2specFloats)
             return invalid(c, "spectral mode needs an rgb2spec table matching SceneData.rgb2specSRGB");
-        if (VKRT_CUDA_SPECTRAL_MODE_OF(sd->packedRenderSettings) != VKRT_CUDA_SPECTRAL_HERO)
-            return invalid(c, "only hero-wavelength spectral sampling is implemented");
+        const uint32_t sm = VKRT_CUDA_SPECTRAL_MODE_OF(sd->packedRenderSettings);
+        if (sm != VKRT_CUDA_SPECTRAL_HERO && sm != VKRT_CUDA_SPECTRAL_SINGLE)
+            return invalid(c, "unknown spectral sampling mode");
     }
     return VKRT_CUDA_SUCCESS;
 }
@@ -327,9 +328,17 @@ void refreshMaterialFlags(VKRT_CudaContext* c) {
     if (c->sheenMaterials || c->alphaTested) c->extendedMaterials = true;
 }
 
+// Single-wavelength spectral mode (raygen_spectral_single.slang): paths carry one wavelength from the start and run
+// the full-stack kernels, whose collapsed-path branch is that integrator.
+bool singleWavelengthMode(const VKRT_CudaSceneData* sd) {
+    return VKRT_CUDA_RENDER_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL &&
+           VKRT_CUDA_SPECTRAL_MODE_OF(sd->packedRenderSettings) == VKRT_CUDA_SPECTRAL_SINGLE;
+}
+
 bool envNeeActive(const VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
     return c->cfg.environmentSampling == VKRT_CUDA_ENV_IMPORTANCE && c->envTexture != VKRT_CUDA_INVALID_INDEX &&
-           sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u && !c->transmissiveMaterials;
+           sd->environmentTextureIndex == c->envTexture && sd->misNeeEnabled != 0u && !c->transmissiveMaterials &&
+           !singleWavelengthMode(sd);
 }
 
 WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spectral) {
@@ -348,7 +357,7 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
     S.spectral = spectral ? 1u : 0u;
     S.neeEnabled = (sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u) ? 1u : 0u;
     S.envNee = envNeeActive(c, &sd) ? 1u : 0u;
-    S.extended = c->extendedMaterials ? 1u : 0u;
+    S.extended = c->extendedMaterials || singleWavelengthMode(&sd) ? 1u : 0u;
     S.transmissive = c->transmissiveMaterials ? 1u : 0u;
     S.alpha = c->alphaTested ? 1u : 0u;
     return S;
@@ -792,7 +801,7 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     rp.width = c->width;
     rp.height = c->height;
     rp.countBytes = c->cfg.countRays;
-    rp.extended = c->extendedMaterials ? 1u : 0u;
+    rp.extended = c->extendedMaterials || singleWavelengthMode(sd) ? 1u : 0u;
     rp.alpha = c->alphaTested ? 1u : 0u;
     FilmBuffers film = filmOf(c);
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "render");
@@ -935,6 +944,8 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     const bool useCache = count == 1 && c0->nrc && c0->nrc->ready() && c0->nrcCfg.enabled;
     if (useCache && (c0->transmissiveMaterials || c0->alphaTested))
         return invalid(c0, "the radiance cache covers opaque reflection-only materials (transmission or alpha)");
+    if (useCache && singleWavelengthMode(&sds[0]))
+        return invalid(c0, "the radiance cache covers RGB and hero-wavelength frames");
     if (useCache)
         cache = WfCacheFrame{c0->nrc.get(), c0->nrcCfg.terminationDepth, c0->nrcCfg.trainingPaths,
                              c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber};

@@ -57,7 +57,13 @@ struct StepConfig {
     uint32_t rngMode;
     uint64_t rngSeed;
     uint32_t cacheDepth = 0xFFFFFFFFu;  // surface vertex depth at which the path queries the radiance cache and ends
+    bool single = false;  // spectral mode with one wavelength per path (raygen_spectral_single.slang), full kernels
 };
+
+VKRT_DEV bool singleWavelength(const VKRT_CudaSceneData& sd) {
+    return VKRT_CUDA_RENDER_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL &&
+           VKRT_CUDA_SPECTRAL_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_SPECTRAL_SINGLE;
+}
 
 VKRT_DEV float4 heroLambdas(float unit) {
     return make_float4(kLambdaMin + fracf(unit) * kLambdaRange, kLambdaMin + fracf(unit + 0.25f) * kLambdaRange,
@@ -90,6 +96,12 @@ VKRT_DEV PathState beginPath(const StepConfig& cfg, const VKRT_CudaSceneData& sd
     p.prevVertexYZW = f3(0.0f);
     p.prevBsdfYZW = f3(0.0f);
     p.sigma = f4(0.0f);
+    // single-wavelength mode (sampleUniformWavelength, wavelength.slang:34-42): the hero lane-0 wavelength, which is
+    // the same unit sample, carried from the start as a collapsed path
+    if (kSpectral && cfg.single) {
+        p.flags |= kPathCollapsed;
+        p.thr = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    }
     return p;
 }
 

@@ -44,6 +44,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
             const uint32_t spp = max(sd.samplesPerPixel, 1u);
             StepConfig cfg{kSpectral, sd.misNeeEnabled != 0u && sd.emissiveMeshCount > 0u, rp.envNee != 0u, rp.rngMode,
                            rp.rngSeed};
+            cfg.single = kSpectral && kFull && singleWavelength(sd);
             SpecTable tab = makeSpecTable(sc, sd);
             float3 sum = f3(0.0f);
             DenoiserFeature fsum{f3(0.0f), f3(0.0f), 0.0f};

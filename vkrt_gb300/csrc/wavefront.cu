@@ -253,7 +253,9 @@ VKRT_DEV void loadPathExt(const WfGlobals& g, uint32_t s, PathState& p) {
 }
 
 VKRT_DEV StepConfig stepConfig(const WfGlobals& g, const WfScene& S) {
-    return StepConfig{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed, g.cacheDepth};
+    StepConfig cfg{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed, g.cacheDepth};
+    cfg.single = S.spectral != 0u && singleWavelength(S.sd);
+    return cfg;
 }
 
 VKRT_DEV SpecTable specTable(const WfScene& S) {
