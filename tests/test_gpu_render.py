@@ -104,3 +104,22 @@ def test_accumulation_running_mean(built):
     np.testing.assert_array_equal(first[..., 3], 2.0)
     np.testing.assert_array_equal(second[..., 3], 4.0)
     assert not np.array_equal(first[..., :3], second[..., :3])
+
+
+def test_frame_validation(built):
+    """Frames the backend cannot render as vkrt would are refused, not rendered differently: debug views, unknown
+    spectral modes, spectral frames without an rgb2spec table; the context stays usable."""
+    scene = scenes.cornell(16, 16, spp=1)
+    with RenderContext() as ctx:
+        ctx.upload_scene(scene)
+        for field, value in (("debugMode", 3), ("debugMode", 16)):
+            sd = scene.scene_data.copy()
+            sd[field] = value
+            with pytest.raises(Exception):
+                ctx.render_frame(sd)
+        sd = scene.scene_data.copy()
+        sd["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES, abi.RENDER_MODE_SPECTRAL, 7)
+        with pytest.raises(Exception):
+            ctx.render_frame(sd)
+        ctx.render_frame(scene.scene_data)
+        assert np.isfinite(ctx.read_accumulation()).all()

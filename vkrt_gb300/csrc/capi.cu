@@ -286,6 +286,9 @@ int32_t validateFrame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd) {
         uint64_t(sd->viewportRect[1]) + sd->viewportRect[3] > c->height)
         return invalid(c, "viewport outside the film");
     if (sd->rrMaxDepth > 1024u) return invalid(c, "rrMaxDepth above 1024");
+    // vkrt's debug views (constants.h:35-52, integrator/path/debug.slang) are not built: refuse rather than render
+    // a normal frame in their place
+    if (sd->debugMode != VKRT_CUDA_DEBUG_MODE_NONE) return invalid(c, "debug render modes are not built");
     if (sd->emissiveMeshCount > c->emissiveMeshCount) return invalid(c, "SceneData.emissiveMeshCount exceeds the uploaded lights");
     for (const VKRT_CudaMeshInfo& m : c->hostMeshes)
         if (m.materialIndex >= c->materialCount) return invalid(c, "mesh material index out of range");
