@@ -119,12 +119,12 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_per_ray():
-    """DRAM bytes per closest-hit ray of kWfIntersect from the committed ncu summary, when one exists."""
-    p = ROOT / "profiles" / "wavefront_intersect_traffic.json"
+def _traffic_per_launch():
+    """DRAM bytes per kWfIntersect launch of the headline frame from the committed ncu capture, when one exists."""
+    p = ROOT / "profiles" / "kWfIntersect_dram_icosphere1M_1920x1080x16spp.json"
     if p.exists():
         try:
-            return json.loads(p.read_text()).get("dram_bytes_per_ray")
+            return json.loads(p.read_text()).get("dram_bytes_per_launch")
         except Exception:
             return None
     return None
@@ -449,9 +449,7 @@ def run_ours(args) -> dict | None:
     shadow_ms = max(stage_ms["shadow"], 1e-6)
     achieved = closest_bytes / (isect_ms * 1e-3) / 1e9
     isect_launches = 2 * pst["wavefrontBodies"]
-    closest_rays = pst["primaryRays"] + pst["extensionRays"]
-    per_ray = _traffic_per_ray()
-    traffic = None if per_ray is None or not isect_launches else int(per_ray * closest_rays / isect_launches)
+    traffic = _traffic_per_launch()  # the committed capture is of this frame (build_scene's defaults)
 
     # the same frame by the megakernel
     mctx = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE,
