@@ -533,9 +533,12 @@ def cpu_baseline(scene, budget_s: float = 12.0, threads: int = 0) -> dict:
     from oracle import cpu
     from vkrt_gb300 import abi
 
+    import copy
     sd = scene.scene_data.copy()
     if scene.rgb2spec is None:
-        # no device table on this path: the oracle's own fit (the per-lookup cost does not depend on res)
+        # no device table on this path: the oracle's own fit (the per-lookup cost does not depend on res), on a copy
+        # of the scene so that repeated calls see the scene as given
+        scene = copy.copy(scene)
         scene.rgb2spec = cpu.rgb2spec_generate(16, threads)
         sd["rgb2specSRGB"] = (16, 0, 16)
     orc = cpu.OracleScene(scene, environment_sampling=abi.ENV_IMPORTANCE)

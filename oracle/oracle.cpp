@@ -2698,10 +2698,20 @@ int32_t oracle_trace_fp64_bruteforce(void* p, const VKRT_CudaRay* rays, uint32_t
     return 0;
 }
 
+// A spectral frame needs an rgb2spec table that holds the layout SceneData.rgb2specSRGB names (the device's frame
+// validation refuses the same frames).
+bool spectralTableFits(const Scene& s, const VKRT_CudaSceneData& sd) {
+    if (VKRT_CUDA_RENDER_MODE_OF(sd.packedRenderSettings) != VKRT_CUDA_RENDER_MODE_SPECTRAL) return true;
+    const uint64_t res = sd.rgb2specSRGB.res, n = s.rgb2spec.size();
+    return res >= 2 && uint64_t(sd.rgb2specSRGB.scaleOffset) + res <= n &&
+           uint64_t(sd.rgb2specSRGB.dataOffset) + 9ull * res * res * res <= n;
+}
+
 int32_t oracle_render(void* p, const VKRT_CudaSceneData* sd, const OracleRenderParams* params, const float* accIn,
                       float* accOut, uint16_t* out, OracleRenderStats* stats) {
     SceneHandle* h = static_cast<SceneHandle*>(p);
     if (!h || !sd || !params || !accIn || !accOut) return -1;
+    if (!spectralTableFits(h->s, *sd)) return -2;
     SceneFull& s = h->s;
     // the brute-force path needs triangles by global id
     SceneFull* sp = &s;
@@ -2722,6 +2732,7 @@ int32_t oracle_render_f64(void* p, const VKRT_CudaSceneData* sd, const OracleRen
                           double* accOut64) {
     SceneHandle* h = static_cast<SceneHandle*>(p);
     if (!h || !sd || !params || !accIn || !accOut64) return -1;
+    if (!spectralTableFits(h->s, *sd)) return -2;
     size_t n = size_t(sd->viewportRect[0] + sd->viewportRect[2]) * (sd->viewportRect[1] + sd->viewportRect[3]) * 4;
     std::vector<float> acc32(n);
     if (params->precision == 64)
@@ -2735,6 +2746,7 @@ int32_t oracle_render_features(void* p, const VKRT_CudaSceneData* sd, const Orac
                                const float* accIn, float* accOut, float* albedoOut, float* normalOut) {
     SceneHandle* h = static_cast<SceneHandle*>(p);
     if (!h || !sd || !params || !accIn || !accOut || !albedoOut || !normalOut) return -1;
+    if (!spectralTableFits(h->s, *sd)) return -2;
     if (params->precision == 64)
         renderRows<double>(h->s, *sd, *params, accIn, accOut, nullptr, nullptr, &h->tri64, nullptr, albedoOut,
                            normalOut);
