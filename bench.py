@@ -543,19 +543,23 @@ def cpu_baseline(scene, budget_s: float = 12.0, threads: int = 0) -> dict:
         sd["rgb2specSRGB"] = (16, 0, 16)
     orc = cpu.OracleScene(scene, environment_sampling=abi.ENV_IMPORTANCE)
     ncores = threads or os.cpu_count() or 1
-    rows = 2
-    acc = None
+    height = int(sd["viewportRect"][0][1] + sd["viewportRect"][0][3])
+    mid = height // 2
+    # calibration on a block of rows at the frame's centre, then a block sized to the budget (centred, clamped)
+    rows = max(1, min(height, 8))
     t0 = time.perf_counter()
-    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(540, 540 + rows), threads=threads)
+    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(mid - rows // 2, mid - rows // 2 + rows), threads=threads)
     dt = time.perf_counter() - t0
-    rows = int(max(2, min(1080 - 540, rows * budget_s / max(dt, 1e-3))))
+    rows = int(max(1, min(height, rows * budget_s / max(dt, 1e-3))))
+    lo = max(0, min(height - rows, mid - rows // 2))
     t0 = time.perf_counter()
-    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(540 - rows // 2, 540 - rows // 2 + rows), threads=threads)
+    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(lo, lo + rows), threads=threads)
     dt = time.perf_counter() - t0
     rays = st["primaryRays"] + st["extensionRays"] + st["shadowRays"]
     orc.close()
     return {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": ncores, "kind": "port",
-            "sample": f"{rows} rows x 1920 px x 16 spp of the same frame ({rays} rays, {dt:.1f} s)"}
+            "sample": f"{rows} rows x {int(sd['viewportRect'][0][2])} px x {int(sd['samplesPerPixel'][0])} spp of the same "
+                      f"frame ({rays} rays, {dt:.1f} s)"}
 
 
 def run_reference(args) -> dict | None:
