@@ -126,11 +126,13 @@ class OracleScene:
         except Exception:
             pass
 
-    def trace_fp32(self, rays, any_hit=False, threads=0):
+    def trace_fp32(self, rays, any_hit=False, threads=0, selection_alpha=False):
+        """FP32 traversal; selection_alpha drops mask cut-outs as vkrt's selection rays do."""
         from vkrt_gb300 import abi
         r = np.ascontiguousarray(rays, dtype=abi.RAY)
         hits = np.zeros(len(r), dtype=abi.HIT)
-        self.lib.oracle_trace_fp32(self.handle, _p(r), len(r), 1 if any_hit else 0, _p(hits), threads)
+        flags = (1 if any_hit else 0) | (2 if selection_alpha else 0)
+        self.lib.oracle_trace_fp32(self.handle, _p(r), len(r), flags, _p(hits), threads)
         return hits
 
     def trace_fp64(self, rays, eps=1e-5, threads=0):

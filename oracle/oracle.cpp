@@ -563,6 +563,7 @@ struct HitRec {
 // decision hashes the ray's seed (the path stream's state when the ray starts, salted per shadow request) with the
 // triangle id, so the closest accepted hit does not depend on traversal order.
 bool alphaAccepts(const Scene& s, uint32_t mesh, uint32_t prim, float u, float v, uint32_t seed, uint32_t gid);
+bool selectionAlphaAccepts(const Scene& s, uint32_t mesh, uint32_t prim, float u, float v);
 bool sceneAlphaTested(const Scene& s);
 uint32_t alphaShadowSeed(uint32_t seed, uint32_t request) { return seed ^ (0x68bc21ebu * (request + 1u)); }
 float alphaRandom(uint32_t seed, uint32_t gid) {
@@ -572,7 +573,7 @@ float alphaRandom(uint32_t seed, uint32_t gid) {
 // closest hit (anyHit = false) or first accepted hit; ties on t go to the smaller global triangle id; with `alpha`,
 // candidate hits must pass alphaAccepts under `alphaSeed`
 HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float tmax, bool anyHit, bool alpha = false,
-                 uint32_t alphaSeed = 0u) {
+                 uint32_t alphaSeed = 0u, bool selection = false) {
     HitRec best;
     if (s.bvh.nodes.empty()) return best;
     RayPre<float> rp = prepRay(o, d, tmin, tmax);
@@ -597,6 +598,7 @@ HitRec traceFp32(const SceneFull& s, V3<float> o, V3<float> d, float tmin, float
             float t, b1, b2;
             if (!watertight(r2, tr.v[0], tr.v[1], tr.v[2], t, b1, b2)) continue;
             if (alpha && !alphaAccepts(s, tr.mesh, tr.prim, b1, b2, alphaSeed, tr.gid)) continue;
+            if (selection && !selectionAlphaAccepts(s, tr.mesh, tr.prim, b1, b2)) continue;
             if (t < bestT || (t == bestT && tr.gid < best.gid)) {
                 bestT = t;
                 best.mesh = tr.mesh;
@@ -947,6 +949,29 @@ bool alphaAccepts(const Scene& s, uint32_t mesh, uint32_t prim, float u, float v
     if (o <= 0.0f) return false;
     if (o >= 1.0f) return true;
     return alphaRandom(seed, gid) <= o;
+}
+
+// selectionAlphaHitAccepted (rt/alpha_test.slang:68-76): only mask cut-outs are dropped
+bool selectionAlphaAccepts(const Scene& s, uint32_t mesh, uint32_t prim, float u, float v) {
+    const VKRT_CudaMeshInfo& m = s.meshes[mesh];
+    const VKRT_CudaMaterial& mat = s.materials[m.materialIndex];
+    if (mat.alphaMode != 1u) return true;
+    uint32_t base = m.indexBase + prim * 3u;
+    const VKRT_CudaShaderVertex& a = s.vertices[s.indices[base + 0] + m.vertexBase];
+    const VKRT_CudaShaderVertex& b = s.vertices[s.indices[base + 1] + m.vertexBase];
+    const VKRT_CudaShaderVertex& c = s.vertices[s.indices[base + 2] + m.vertexBase];
+    TexData<float> td;
+    td.color = interp4(unpackColor<float>(a.packedColor), unpackColor<float>(b.packedColor),
+                       unpackColor<float>(c.packedColor), u, v);
+    float w = 1.0f - u - v;
+    for (int k = 0; k < 2; ++k) {
+        td.uv0[k] = a.texcoord0[k] * w + b.texcoord0[k] * u + c.texcoord0[k] * v;
+        td.uv1[k] = a.texcoord1[k] * w + b.texcoord1[k] * u + c.texcoord1[k] * v;
+    }
+    float texAlpha = td.color.w * sampleMaterialTexture(s, mat.baseColorTextureIndex, mat.baseColorTextureWrap,
+                                                        mat.baseColorTextureTransform, mat.textureRotations[0],
+                                                        mat.textureTexcoordSets & 0xffu, td, V4<float>(1.0f)).w;
+    return texAlpha >= mat.alphaCutoff;
 }
 
 bool sceneAlphaTested(const Scene& s) {
@@ -2670,7 +2695,8 @@ int32_t oracle_trace_fp32(void* p, const VKRT_CudaRay* rays, uint32_t count, uin
         for (uint32_t i = blk * 256; i < std::min(count, blk * 256 + 256); ++i) {
             const VKRT_CudaRay& r = rays[i];
             HitRec hr = traceFp32(h->s, V3<float>(r.origin[0], r.origin[1], r.origin[2]),
-                                  V3<float>(r.direction[0], r.direction[1], r.direction[2]), r.tMin, r.tMax, anyHit != 0);
+                                  V3<float>(r.direction[0], r.direction[1], r.direction[2]), r.tMin, r.tMax,
+                                  (anyHit & 1u) != 0, false, 0u, (anyHit & 2u) != 0);
             fillHit(hr, &hits[i]);
         }
     });

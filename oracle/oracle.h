@@ -69,7 +69,8 @@ typedef struct OracleRenderStats {
 void* oracle_scene_create(const OracleSceneDesc* desc);
 void oracle_scene_destroy(void* scene);
 
-/* FP32 watertight traversal of the oracle BVH2; hits use the same record as VKRT_CudaHit. */
+/* FP32 watertight traversal of the oracle BVH2; hits use the same record as VKRT_CudaHit. `anyHit` bit 0: first
+ * accepted hit; bit 1: mask cut-outs are dropped as selection rays drop them (rt/alpha_test.slang:68-76). */
 int32_t oracle_trace_fp32(void* scene, const VKRT_CudaRay* rays, uint32_t count, uint32_t anyHit,
                           VKRT_CudaHit* hits, uint32_t threads);
 /* FP64 brute force over all world-space triangles (vertices transformed in FP64 from the FP32 mesh TRS);

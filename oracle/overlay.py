@@ -66,9 +66,15 @@ def selection_mask(scene, scene_data, width: int, height: int):
     if int(sd["selectionEnabled"]) == 0 or sel == abi.INVALID_INDEX:
         return mask, amb
     rays, inside = camera_rays(scene_data, width, height)
-    orc = cpu.OracleScene(single_mesh_scene(scene, sel))
+    sub = single_mesh_scene(scene, sel)
+    sub.textures = scene.textures
+    orc = cpu.OracleScene(sub)
     try:
-        hits, ambiguous = orc.trace_fp64(rays.reshape(-1))
+        if int(sub.materials["alphaMode"][0]) == 1:  # mask cut-outs: the FP32 traversal with the selection alpha test
+            hits = orc.trace_fp32(rays.reshape(-1), any_hit=True, selection_alpha=True)
+            ambiguous = np.zeros(len(hits), bool)
+        else:
+            hits, ambiguous = orc.trace_fp64(rays.reshape(-1))
     finally:
         orc.close()
     hit = (hits["instanceIndex"] != abi.INVALID_INDEX).reshape(height, width)
@@ -110,7 +116,11 @@ def pick_mesh(scene, scene_data, x: int, y: int, oracle_scene=None):
         return abi.INVALID_INDEX, False
     orc = oracle_scene if oracle_scene is not None else cpu.OracleScene(scene)
     try:
-        hits, amb = orc.trace_fp64(rays[y:y + 1, x])
+        if (scene.materials["alphaMode"] == 1).any():  # mask cut-outs: FP32 traversal with the selection alpha test
+            hits = orc.trace_fp32(rays[y:y + 1, x], selection_alpha=True)
+            amb = np.zeros(1, bool)
+        else:
+            hits, amb = orc.trace_fp64(rays[y:y + 1, x])
     finally:
         if oracle_scene is None:
             orc.close()

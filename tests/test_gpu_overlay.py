@@ -114,3 +114,31 @@ def test_auto_spp_follows_the_frame_budget(built):
     last_spp, last_ms = times[-1]
     assert last_spp > 4, times[-8:]
     assert last_ms < 1.1 * c.target_ms, times[-8:]
+
+
+def test_selection_and_pick_drop_mask_cut_outs(built):
+    """A mesh with an alpha-mask checker: its selection mask has the cut-outs as holes, and picks through a hole
+    name what lies behind (selectionAlphaHitAccepted, rt/alpha_test.slang:68-76)."""
+    from oracle import cpu
+    from tests.test_gpu_materials import alpha_cornell
+    s = alpha_cornell(96, 96, spp=1)
+    with RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT) as ctx:
+        ctx.upload_scene(s)
+        sd = s.scene_data.copy()
+        sd["selectionEnabled"] = 1
+        sd["selectedMeshIndex"] = 7  # the cut-out box
+        ctx.render_frame(sd)
+        ctx.render_selection_overlay(sd)
+        mask = ctx.read_selection_mask()
+        want, _ = overlay.selection_mask(s, sd, 96, 96)
+        assert want.sum() > 50
+        assert (mask != want).mean() <= 0.002, int((mask != want).sum())
+        orc = cpu.OracleScene(s)
+        picks = [(x, y) for y in range(8, 96, 6) for x in range(8, 96, 6)]
+        same = sum(ctx.pick_mesh(sd, x, y) == overlay.pick_mesh(s, sd, x, y, orc)[0] for x, y in picks)
+        assert same >= len(picks) - 1, (same, len(picks))
+    # the same box without the cut-out covers more pixels
+    opaque = alpha_cornell(96, 96, spp=1)
+    opaque.materials["alphaMode"][-2] = 0
+    full, _ = overlay.selection_mask(opaque, sd, 96, 96)
+    assert full.sum() > want.sum()

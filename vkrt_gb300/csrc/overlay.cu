@@ -4,11 +4,13 @@
 //   selection mask  src/shaders/entry/select/raygen.slang:5-14 (+ rt/queries/selection_query.slang:7-11): per
 //                   pixel, a pixel-centre camera ray traced with first-hit termination against a TLAS that holds
 //                   the selected mesh alone; mask = hit. Here: the scene BVH with hits restricted to that mesh.
+//                   Mask cut-outs do not count (selectionAlphaHitAccepted, rt/alpha_test.slang:68-76).
 //   outline         src/shaders/entry/post/outline.slang:9-60: 16 x 16 tiles, the mask tile plus a 5-pixel apron
 //                   in shared memory; a pixel outside the mask with a masked pixel within the square of radius
 //                   clamp(round(min(W, H) * 2 / 1080), 1, 5) takes the outline colour (1, 0.55, 0.1)
 //                   (scene/constants.slang:17-18), its alpha kept.
-//   pick            src/shaders/integrator/path/debug.slang:21-29: the closest hit of the pixel-centre camera ray.
+//   pick            src/shaders/integrator/path/debug.slang:21-29: the closest hit of the pixel-centre camera ray,
+//                   mask cut-outs dropped as for the selection rays (the deterministic part of the path any-hit).
 #include <cuda_runtime.h>
 
 #include "integrator.cuh"
@@ -41,7 +43,7 @@ __global__ void __launch_bounds__(kMaskThreads) kSelectionMask(DeviceScene sc, V
         float3 org;
         const float3 dir = primaryRay(sd, px, py, 0.0f, 0.0f, org);
         const TraceRay r{org, dir, kTMin, kTMax};
-        const TraceHit h = traceBvh<true, false, true>(sc, r, smemStack + threadIdx.x, blockDim.x, nullptr,
+        const TraceHit h = traceBvh<true, false, true, false, 2>(sc, r, smemStack + threadIdx.x, blockDim.x, nullptr,
                                                        sd.selectedMeshIndex);
         m = h.mesh != VKRT_CUDA_INVALID_INDEX ? 1u : 0u;
     }
@@ -87,7 +89,7 @@ __global__ void kPick(DeviceScene sc, VKRT_CudaSceneData sd, uint32_t x, uint32_
         float3 org;
         const float3 dir = primaryRay(sd, int(x), int(y), 0.0f, 0.0f, org);
         const TraceRay r{org, dir, kTMin, kTMax};
-        mesh = traceBvh<false, false>(sc, r, smemStack, 1u, nullptr).mesh;
+        mesh = traceBvh<false, false, false, false, 2>(sc, r, smemStack, 1u, nullptr).mesh;
     }
     *out = mesh;
 }

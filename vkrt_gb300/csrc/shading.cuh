@@ -195,11 +195,9 @@ VKRT_DEV bool alphaMayReject(const VKRT_CudaMaterial& mat, float meshOpacity) { 
            meshOpacity < 0.999f;
 }
 
-VKRT_DEV bool alphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32_t prim, float u, float v, uint32_t seed,
-                           uint32_t gid) {
-    const VKRT_CudaMeshInfo& m = sc.meshes[mesh];
-    const VKRT_CudaMaterial& mat = sc.materials[m.materialIndex];
-    if (!alphaMayReject(mat, m.opacity)) return true;
+// The texture alpha of a candidate hit (evaluateMaterialTextureAlpha, :19-25) and its vertex alpha in `vertexAlpha`
+VKRT_DEV float hitTextureAlpha(const DeviceScene& sc, const VKRT_CudaMeshInfo& m, const VKRT_CudaMaterial& mat,
+                               uint32_t prim, float u, float v, float& vertexAlpha) {
     // evaluateSurfaceTextureData (geometry/surface/interpolation.slang:46-60)
     const uint32_t base = m.indexBase + prim * 3u;
     const float4* va = reinterpret_cast<const float4*>(sc.vertices + __ldg(sc.indices + base) + m.vertexBase);
@@ -212,15 +210,25 @@ VKRT_DEV bool alphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32_t prim, 
                         unpackColor(__float_as_uint(__ldg(vc + 2).z)), u, v);
     tex.uv0 = make_float2(ta.x * w + tb.x * u + tc.x * v, ta.y * w + tb.y * u + tc.y * v);
     tex.uv1 = make_float2(ta.z * w + tb.z * u + tc.z * v, ta.w * w + tb.w * u + tc.w * v);
-    // evaluateMaterialTextureAlpha (:19-25)
+    vertexAlpha = tex.color.w;
     float texAlpha = tex.color.w;
     if (mat.alphaMode != VKRT_CUDA_ALPHA_MODE_OPAQUE)
         texAlpha *= sampleMaterialTexture(sc, mat.baseColorTextureIndex, mat.baseColorTextureWrap,
                                           mat.baseColorTextureTransform, mat.textureRotations[0],
                                           mat.textureTexcoordSets & 0xffu, tex, f4(1.0f)).w;
+    return texAlpha;
+}
+
+VKRT_DEV bool alphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32_t prim, float u, float v, uint32_t seed,
+                           uint32_t gid) {
+    const VKRT_CudaMeshInfo& m = sc.meshes[mesh];
+    const VKRT_CudaMaterial& mat = sc.materials[m.materialIndex];
+    if (!alphaMayReject(mat, m.opacity)) return true;
+    float vertexAlpha;
+    const float texAlpha = hitTextureAlpha(sc, m, mat, prim, u, v, vertexAlpha);
     if (mat.alphaMode == kAlphaModeMask) {  // alphaPass (:31-47)
         if (texAlpha < mat.alphaCutoff) return false;
-        const float o = sat(m.opacity * mat.opacity * tex.color.w);
+        const float o = sat(m.opacity * mat.opacity * vertexAlpha);
         if (o >= 1.0f) return true;
         if (o <= 0.0f) return false;
         return alphaRandom(seed, gid) <= o;
@@ -229,6 +237,15 @@ VKRT_DEV bool alphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32_t prim, 
     if (o <= 0.0f) return false;
     if (o >= 1.0f) return true;
     return alphaRandom(seed, gid) <= o;
+}
+
+// selectionAlphaHitAccepted (:68-76): the selection and pick rays drop mask cut-outs only
+VKRT_DEV bool selectionAlphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32_t prim, float u, float v) {
+    const VKRT_CudaMeshInfo& m = sc.meshes[mesh];
+    const VKRT_CudaMaterial& mat = sc.materials[m.materialIndex];
+    if (mat.alphaMode != kAlphaModeMask) return true;
+    float vertexAlpha;
+    return hitTextureAlpha(sc, m, mat, prim, u, v, vertexAlpha) >= mat.alphaCutoff;
 }
 
 // ---------------------------------------------------------------------------------------------------------------

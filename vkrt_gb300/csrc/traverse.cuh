@@ -200,9 +200,10 @@ constexpr uint32_t kShadowThroughTransmission = 0xFFFFFFFEu;
 // kTransmissive (any-hit shadow rays of scenes with transmissive materials, rt/payloads/shadow_payload.slang): hits on
 // meshes whose material has transmission > 0 do not end the search but leave prim = kShadowThroughTransmission;
 // an opaque hit anywhere on the segment answers occluded (vkrt reports whichever hit the driver accepts first).
-// kAlpha (scenes with alpha-tested materials, entry/path/any_hit.slang and entry/shadow/any_hit.slang): a candidate
-// hit on such a material counts only when alphaAccepts it, with the ray's `alphaSeed`.
-template <bool kAnyHit, bool kCount, bool kMeshFilter = false, bool kTransmissive = false, bool kAlpha = false>
+// kAlpha 1 (scenes with alpha-tested materials, entry/path/any_hit.slang and entry/shadow/any_hit.slang): a candidate
+// hit on such a material counts only when alphaAccepts it, with the ray's `alphaSeed`; kAlpha 2 (selection and pick
+// rays, entry/select/any_hit.slang): mask cut-outs are dropped (selectionAlphaAccepts).
+template <bool kAnyHit, bool kCount, bool kMeshFilter = false, bool kTransmissive = false, int kAlpha = 0>
 VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* smemColumn, uint32_t smemStride,
                            RenderCounters* counters, uint32_t meshFilter = 0u, uint32_t alphaSeed = 0u) {
     TraceHit best;
@@ -280,7 +281,9 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
             if (watertightHit(wr, org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
                               make_float3(c.x, c.y, c.z), tmin, tmax, t, b1, b2)) {
                 uint32_t gid = __float_as_uint(a.w);
-                if (kAlpha && !alphaAccepts(sc, __float_as_uint(b.w), __float_as_uint(c.w), b1, b2, alphaSeed, gid))
+                if (kAlpha == 1 && !alphaAccepts(sc, __float_as_uint(b.w), __float_as_uint(c.w), b1, b2, alphaSeed, gid))
+                    continue;
+                if (kAlpha == 2 && !selectionAlphaAccepts(sc, __float_as_uint(b.w), __float_as_uint(c.w), b1, b2))
                     continue;
                 if (kTransmissive && sc.materials[sc.meshes[__float_as_uint(b.w)].materialIndex].transmission > 0.0f) {
                     best.prim = kShadowThroughTransmission;
