@@ -91,3 +91,26 @@ def test_batch_of_uneven_scenes(built):
     finally:
         for c in ctxs:
             c.close()
+
+
+def test_batch_of_mixed_material_scenes(built):
+    """A batch holding a glass scene, an alpha-tested scene and a reflection-only scene runs the full-stack, alpha
+    and transmissive-shadow kernels for all three; each scene's image equals its single-scene wavefront render
+    (the reflection-only scene's to float rounding: it is shaded by the full-stack kernel in the batch)."""
+    from tests.test_gpu_materials import alpha_cornell, glass_cornell
+    ss = [glass_cornell(48, 40, spp=2, abbe=30.0, absorb=2.0), alpha_cornell(40, 48, spp=2), scenes.cornell(32, 32, spp=2)]
+    kw = dict(rng_mode=abi.RNG_PCG32)
+    alone = [_render(s, abi.INTEGRATOR_WAVEFRONT, **kw)[0] for s in ss]
+    ctxs = [RenderContext(integrator=abi.INTEGRATOR_WAVEFRONT, **kw) for _ in ss]
+    try:
+        for c, s in zip(ctxs, ss):
+            c.upload_scene(s)
+        render_batch(ctxs, np.concatenate([s.scene_data for s in ss]))
+        for c, a in zip(ctxs, alone):
+            g = c.read_accumulation()
+            np.testing.assert_array_equal(g[..., 3], a[..., 3])
+            close = (np.abs(g[..., :3] - a[..., :3]) <= 1e-5 + 1e-4 * np.abs(a[..., :3])).all(-1)
+            assert close.mean() > 0.99, close.mean()
+    finally:
+        for c in ctxs:
+            c.close()
