@@ -21,7 +21,9 @@ namespace {
 // running mean (writeback.slang:72-114) and encoded for display.
 // kFull: vkrt's whole material stack, alpha tests and the denoiser features (written when the film has feature
 // images)
-template <bool kSpectral, bool kCountBytes, bool kFull>
+// kFeatures alone: the denoiser features with the reflection-only materials (the plain vertex step plus the feature
+// hook).
+template <bool kSpectral, bool kCountBytes, bool kFull, bool kFeatures = kFull>
 __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, VKRT_CudaSceneData sd, RenderParams rp,
                                                                FilmBuffers film, RenderCounters* counters) {
     extern __shared__ uint2 smemStack[];
@@ -36,7 +38,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
         if (!inside) {
             film.accumWrite[pixel] = f4(0.0f);
             film.output[pixel] = make_ushort4(0, 0, 0, 0);
-            if (kFull && film.albedoWrite) film.albedoWrite[pixel] = film.normalWrite[pixel] = f4(0.0f);
+            if (kFeatures && film.albedoWrite) film.albedoWrite[pixel] = film.normalWrite[pixel] = f4(0.0f);
         } else {
             KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
             const float4 prev = film.accumRead[pixel];
@@ -69,6 +71,9 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     if (kFull)
                         cont = shadePathVertex<kSpectral, FeatureHook, true>(sc, sd, cfg, tab, p, h, sh, ns,
                                                                              FeatureHook{{}, &feat});
+                    else if (kFeatures)
+                        cont = shadePathVertex<kSpectral, FeatureHook>(sc, sd, cfg, tab, p, h, sh, ns,
+                                                                       FeatureHook{{}, &feat});
                     else cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
                     for (uint32_t i = 0; i < ns; ++i) {
                         pc.shadow++;
@@ -92,13 +97,13 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                     if (!cont) break;
                 }
                 sum += pathResult<kSpectral>(cfg, p);
-                if (kFull) {
+                if (kFeatures) {
                     fsum.albedo += feat.albedo;
                     fsum.normal += feat.normal;
                     fsum.weight += feat.weight;
                 }
             }
-            if (kFull && film.albedoWrite) {
+            if (kFeatures && film.albedoWrite) {
                 blendFeature(film.albedoRead, film.albedoWrite, pixel, fsum.albedo, fsum.weight);
                 blendFeature(film.normalRead, film.normalWrite, pixel, fsum.normal, fsum.weight);
             }
@@ -391,23 +396,31 @@ cudaError_t launchRender(const DeviceScene& sc, const VKRT_CudaSceneData& sd, co
     const uint32_t blocks = uint32_t((pixels + threads - 1) / threads);
     const size_t smem = size_t(threads) * VKRT_SMEM_STACK * sizeof(uint2);
     const bool spectral = VKRT_CUDA_RENDER_MODE_OF(sd.packedRenderSettings) == VKRT_CUDA_RENDER_MODE_SPECTRAL;
-    const bool features = film.albedoWrite != nullptr || rp.extended != 0u;
-#define VKRT_MEGA(S, C, F) kRenderMega<S, C, F><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters)
+    const bool features = film.albedoWrite != nullptr;
+#define VKRT_MEGA(S, C, F, X) kRenderMega<S, C, F, X><<<blocks, threads, smem, stream>>>(sc, sd, rp, film, counters)
+    // full stack when the materials need it, the feature-capturing plain kernel for feature films, else plain
+    const bool full = rp.extended != 0u;
     if (spectral) {
-        if (features) {
-            if (rp.countBytes) VKRT_MEGA(true, true, true);
-            else VKRT_MEGA(true, false, true);
+        if (full) {
+            if (rp.countBytes) VKRT_MEGA(true, true, true, true);
+            else VKRT_MEGA(true, false, true, true);
+        } else if (features) {
+            if (rp.countBytes) VKRT_MEGA(true, true, false, true);
+            else VKRT_MEGA(true, false, false, true);
         } else {
-            if (rp.countBytes) VKRT_MEGA(true, true, false);
-            else VKRT_MEGA(true, false, false);
+            if (rp.countBytes) VKRT_MEGA(true, true, false, false);
+            else VKRT_MEGA(true, false, false, false);
         }
     } else {
-        if (features) {
-            if (rp.countBytes) VKRT_MEGA(false, true, true);
-            else VKRT_MEGA(false, false, true);
+        if (full) {
+            if (rp.countBytes) VKRT_MEGA(false, true, true, true);
+            else VKRT_MEGA(false, false, true, true);
+        } else if (features) {
+            if (rp.countBytes) VKRT_MEGA(false, true, false, true);
+            else VKRT_MEGA(false, false, false, true);
         } else {
-            if (rp.countBytes) VKRT_MEGA(false, true, false);
-            else VKRT_MEGA(false, false, false);
+            if (rp.countBytes) VKRT_MEGA(false, true, false, false);
+            else VKRT_MEGA(false, false, false, false);
         }
     }
 #undef VKRT_MEGA
