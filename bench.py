@@ -18,7 +18,9 @@ adjoint : the path-replay adjoint of the inverse-rendering Cornell box (128 x 12
         albedo + roughness textures): device time of the adjoint call / device time of the forward frame.
 batch : 64 uneven icosphere fields (10k-500k triangles, 256^2-1024^2, 8 spp, depth 10, RGB) in one autotuned graph
         launch vs 64 sequential megakernel (and wavefront) frames.
-convergence : time to relMSE <= 1e-3 against a 2048-spp reference, plain wavefront vs radiance-cache frames.
+convergence : time to relMSE <= 1e-3 against a 17,600-spp reference (its own relMSE estimated from two independent
+        halves, its estimator checked against the FP64 oracle on the same seeds), plain wavefront, radiance-cache and
+        plain megakernel frames, each timed directly.
 --impl reference : the CPU restatement of vkrt's integrator (the oracle, a port: vkrt's own renderer needs Vulkan
         and is unavailable here) on all host cores, on a bounded block of rows of the same frame per step.
 """
@@ -42,13 +44,21 @@ METRIC = "Mrays/s"
 WORKLOAD = "icosphere-field-1M-tris 1920x1080 16spp depth12 hero-spectral env-IS"
 
 
-def _config(width, height, spp, depth, tris, extra=None):
-    c = {"workload": WORKLOAD, "triangles": tris, "width": width, "height": height, "spp": spp, "max_depth": depth,
-         "render_mode": "spectral-hero-4", "rng": "pcg32 seed 1", "environment": "1024x512 fp32 sky + sun, IS+MIS",
-         "l2": "flushed before every timed frame (256 MiB write)"}
-    if extra:
-        c.update(extra)
-    return c
+def _config(tris=1_024_000):
+    """The workload, identical in both arms' lines."""
+    return {"workload": WORKLOAD, "triangles": tris, "width": 1920, "height": 1080, "spp": 16, "max_depth": 12,
+            "render_mode": "spectral-hero-4", "rgb2spec_res": 64, "rng": "pcg32 seed 1",
+            "environment": "1024x512 fp32 sky + sun, IS+MIS",
+            "l2": "flushed before every timed frame (256 MiB write)"}
+
+
+CONFIG0 = "cornell 256x256, 64 frames x 1 spp, depth 8, RGB, pcg32 seed 1"
+
+
+def _vkrt_units(spp_frames: float, seconds: float) -> dict:
+    """vkrt's benchmark units (src/app/render/benchmark.c:115-130): a sample is one spp over the whole frame."""
+    return {"samples_per_s": round(spp_frames / seconds, 3) if seconds > 0 else None,
+            "ms_per_sample": round(seconds * 1e3 / spp_frames, 4) if spp_frames > 0 else None}
 
 
 def _dist():
@@ -130,10 +140,11 @@ def _traffic_per_launch():
     return None
 
 
-def build_scene(spp=16, depth=12, width=1920, height=1080, n_spheres=800):
+def build_scene(spp=16, depth=12, width=1920, height=1080, n_spheres=800, host=None):
+    """The headline frame's scene; `host` selects the host layer that makes its records (scenes.py)."""
     from vkrt_gb300 import scenes
     return scenes.icosphere_field(n_spheres=n_spheres, width=width, height=height, spp=spp, max_depth=depth, seed=1,
-                                  spectral=True)
+                                  spectral=True, host=host)
 
 
 def _rays(st):
@@ -203,53 +214,109 @@ def adjoint_ratio(local: int) -> dict:
             "gradients": "albedo texels, roughness texels, emission radiance; FP64 central-difference tests"}
 
 
-def convergence_measure(local: int, scene, mega_ms: float, max_frames: int = 96, ref_frames: int = 128) -> dict:
-    """Time to relMSE <= 1e-3 on the benchmark frame (16 spp per frame) for the plain wavefront tracer and for the
-    radiance-cache tracer, against a 2048-spp reference of the same scene rendered by the GPU tracer (which matches
-    the FP64 oracle per sample in the tests). relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2)."""
+def _relmse(x: np.ndarray, ref: np.ndarray, trim: float = 0.0) -> float:
+    """mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2); trim > 0 drops that share of pixels with the
+    largest error (the firefly-robust variant)."""
+    e = ((x.astype(np.float64) - ref) ** 2 / (ref ** 2 + 1e-2)).mean(-1).ravel()
+    if trim > 0.0:
+        k = int(len(e) * (1.0 - trim))
+        e = np.partition(e, k - 1)[:k]
+    return float(e.mean())
+
+
+def convergence_measure(local: int, scene, max_frames: int = 96, ref_frames: int = 1100) -> dict:
+    """Time to relMSE <= 1e-3 on the benchmark frame (16 spp per frame): plain wavefront tracer, radiance-cache tracer
+    and the plain megakernel, each timed directly (CUDA events around every frame's render).
+
+    Reference: ref_frames x 16 spp of the GPU wavefront tracer with independent seeds (17,600 spp at the default,
+    about 16x the plain tracer's crossing), rendered as two independent halves A and B; its own relMSE is estimated
+    as mean((A - B)^2 / (ref^2 + 1e-2)) / 4. The estimator the reference runs is checked against the FP64 oracle on
+    the same seeds: 8 rows spread over the frame, rendered by the oracle in FP64 with the first timed frame's sample
+    indices. relMSE is reported as is and with the 0.01% of pixels with the largest error dropped (sun fireflies)."""
     import torch
+    from oracle import cpu
     from vkrt_gb300 import RenderContext, abi
 
-    ctx = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE,
-                        integrator=abi.INTEGRATOR_WAVEFRONT)
-    ctx.upload_scene(scene)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
-    sd = scene.scene_data.copy()
-    ctx.reset_accumulation()
-    for f in range(ref_frames):
-        sd["frameNumber"] = 1_000_000 + f
-        ctx.render_frame(sd)
-    ref = ctx.read_accumulation()[..., :3].astype(np.float64)
-    den = ref ** 2 + 1e-2
+    def make(integrator):
+        c = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE,
+                          integrator=integrator)
+        c.upload_scene(scene)
+        return c, torch.cuda.ExternalStream(c.stream, device=torch.device("cuda", local))
 
-    def curve(**cache):
-        ctx.nrc_configure(**cache)
+    ctx, stream = make(abi.INTEGRATOR_WAVEFRONT)
+    sd = scene.scene_data.copy()
+    halves = []
+    t_ref = time.perf_counter()
+    for h in range(2):
         ctx.reset_accumulation()
-        total, pts, reached = 0.0, [], None
+        for f in range(ref_frames // 2):
+            sd["frameNumber"] = 1_000_000 + h * 500_000 + f
+            ctx.render_frame(sd)
+        halves.append(ctx.read_accumulation()[..., :3].astype(np.float64))
+    ref_s = time.perf_counter() - t_ref
+    ref = 0.5 * (halves[0] + halves[1])
+    den = ref ** 2 + 1e-2
+    ref_err = float(np.mean((halves[0] - halves[1]) ** 2 / den)) / 4.0
+    del halves
+
+    def curve(c, st, **cache):
+        if cache:
+            c.nrc_configure(**cache)
+        c.reset_accumulation()
+        total, pts, reached, reached_trim, first = 0.0, [], None, None, None
         for f in range(max_frames):
             sd["frameNumber"] = f
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            ctx.render_frame(sd)
-            b.record(stream)
+            a.record(st)
+            c.render_frame(sd)
+            b.record(st)
             b.synchronize()
             total += a.elapsed_time(b)
-            err = float(np.mean((ctx.read_accumulation()[..., :3] - ref) ** 2 / den))
-            pts.append([f + 1, round(total, 1), round(err, 6)])
+            img = c.read_accumulation()[..., :3]
+            if first is None:
+                first = img.copy()
+            err, err_t = _relmse(img, ref), _relmse(img, ref, 1e-4)
+            pts.append([f + 1, round(total, 1), round(err, 6), round(err_t, 6)])
+            if err_t <= 1e-3 and reached_trim is None:
+                reached_trim = {"frames": f + 1, "spp": 16 * (f + 1), "ms": round(total, 1)}
             if err <= 1e-3:
                 reached = {"frames": f + 1, "spp": 16 * (f + 1), "ms": round(total, 1)}
                 break
-        return {"reached": reached, "curve": pts[:: max(1, len(pts) // 12)] + ([pts[-1]] if pts else [])}
+        return {"reached": reached, "reached_trimmed": reached_trim,
+                "curve": pts[:: max(1, len(pts) // 12)] + ([pts[-1]] if pts else [])}, first
 
-    plain = curve(enabled=0)
-    cached = curve(enabled=1, terminationDepth=2, trainingPaths=65536, trainingSteps=4, learningRate=1e-2, seed=3)
+    plain, first = curve(ctx, stream, enabled=0)
+    cached, _ = curve(ctx, stream, enabled=1, terminationDepth=2, trainingPaths=65536, trainingSteps=4,
+                      learningRate=1e-2, seed=3)
     ctx.close()
-    out = {"threshold": 1e-3, "reference": f"{16 * ref_frames} spp, GPU wavefront tracer, independent seeds",
-           "plain_wavefront": plain, "radiance_cache": cached}
-    if plain["reached"]:
-        # the megakernel renders the same samples (tests: identical images), so it needs the same frames
-        out["megakernel_ms"] = round(plain["reached"]["frames"] * mega_ms, 1)
-        out["wavefront_over_megakernel"] = round(plain["reached"]["ms"] / out["megakernel_ms"], 4)
+    mctx, mstream = make(abi.INTEGRATOR_MEGAKERNEL)
+    mega, _ = curve(mctx, mstream)
+    mctx.close()
+
+    # same-seed check of the estimator against the FP64 oracle on 8 rows of the first frame
+    height = scene.height
+    step = height // 8
+    orc = cpu.OracleScene(scene, environment_sampling=abi.ENV_IMPORTANCE)
+    sd0 = scene.scene_data.copy()
+    sd0["frameNumber"] = 0
+    acc64, _ = orc.render(sd0, rng_mode=abi.RNG_PCG32, rng_seed=1, precision=64, rows=(step // 2, height),
+                          row_step=step)
+    orc.close()
+    rows = list(range(step // 2, height, step))
+    val = _relmse(first[rows], acc64[rows, :, :3].astype(np.float64))
+
+    out = {"threshold": 1e-3,
+           "reference": {"spp": 16 * (ref_frames // 2) * 2, "tracer": "GPU wavefront, independent seeds, two halves",
+                         "relmse_estimate": round(ref_err, 7), "seconds": round(ref_s, 1),
+                         "fp64_same_seed_check": {"rows": len(rows), "spp": 16, "relmse_vs_oracle_fp64": val}},
+           "metric": "relMSE = mean (x - ref)^2 / (ref^2 + 1e-2); reached_trimmed drops the 0.01% worst pixels",
+           "plain_wavefront": plain, "radiance_cache": cached, "plain_megakernel": mega}
+    if plain["reached"] and mega["reached"]:
+        out["wavefront_over_megakernel"] = round(plain["reached"]["ms"] / mega["reached"]["ms"], 4)
+    if plain["reached"] and cached["reached"]:
+        out["cache_over_plain_wavefront"] = round(cached["reached"]["ms"] / plain["reached"]["ms"], 4)
+    if cached["reached"] and mega["reached"]:
+        out["cache_over_megakernel"] = round(cached["reached"]["ms"] / mega["reached"]["ms"], 4)
     return out
 
 
@@ -468,7 +535,7 @@ def run_ours(args) -> dict | None:
     sd_view[:] = sd
     out = torch.empty((ctx.height, ctx.width, 4), dtype=torch.float32, pin_memory=True)
     out_np = out.numpy()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = args.steps
     ctx.sync()
     t0 = time.perf_counter()
     e2e_rays = 0
@@ -489,13 +556,15 @@ def run_ours(args) -> dict | None:
         "warmup": args.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded icosphere field, procedural sky)",
-        "config": _config(1920, 1080, 16, 12, scene.triangle_count,
-                          {"integrator": "wavefront (one CUDA-graph launch per frame)",
-                           "parallelism": f"replicas x{world} (independent sample sets)",
-                           "rays_per_frame": int(rays / args.steps), "bvh_nodes": pst["bvhNodeCount"],
-                           "bvh_mbytes": round(pst["bvhBytes"] / 2 ** 20, 1)}),
+        "config": _config(scene.triangle_count),
+        **_vkrt_units(16.0 * args.steps * world, total_ms * 1e-3),
+        "details": {"integrator": "wavefront (one CUDA-graph launch per frame)",
+                    "parallelism": f"replicas x{world} (independent sample sets)",
+                    "rays_per_frame": int(rays / args.steps), "bvh_nodes": pst["bvhNodeCount"],
+                    "bvh_mbytes": round(pst["bvhBytes"] / 2 ** 20, 1)},
         "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": abi.SCENE_DATA.itemsize,
-                "d2h_bytes_per_step": int(out.numel() * 4), "steps": e2e_steps},
+                "d2h_bytes_per_step": int(out.numel() * 4), "steps": e2e_steps,
+                **_vkrt_units(16.0 * e2e_steps, e2e_s)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": "kWfIntersect",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
@@ -514,76 +583,208 @@ def run_ours(args) -> dict | None:
         "selection_overlay": overlay,
         **extra,
     }
+    if rank == 0 and world == 1:
+        result["config0"] = config0_measure(local)
     if rank == 0 and world == 1 and not args.no_adjoint:
         result["adjoint"] = adjoint_ratio(local)
     if rank == 0 and world == 1 and not args.no_batch:
         result["batch"] = batch_measure(local)
     if rank == 0 and world == 1 and not args.no_convergence:
-        result["convergence"] = convergence_measure(local, scene, mega_ms)
+        result["convergence"] = convergence_measure(local, scene)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(scene, budget_s=args.cpu_seconds)
+        result["cpu_baseline"] = cpu_baseline(build_scene(host=_oracle_host()), budget_s=args.cpu_seconds)
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return result if rank == 0 else None
 
 
-def cpu_baseline(scene, budget_s: float = 12.0, threads: int = 0) -> dict:
-    """The oracle (CPU restatement of vkrt's integrator, FP32) on all host cores, rows of the same frame."""
+def _oracle_host():
+    from oracle.host import OracleHost
+    return OracleHost
+
+
+def _oracle_rgb2spec(scene, res: int = 64, threads: int = 0):
+    """The oracle's own rgb2spec fit at the device table's resolution (setup, not timed), installed in `scene`."""
+    from oracle import cpu
+    scene.rgb2spec = cpu.rgb2spec_generate(res, threads)
+    scene.scene_data["rgb2specSRGB"] = (res, 0, res)
+
+
+def cpu_baseline(scene, budget_s: float = 12.0, threads: int = 0, offset: int = 0, rgb2spec_res: int = 64) -> dict:
+    """The oracle (CPU restatement of vkrt's integrator, FP32) on all host cores, on every k-th row of the frame
+    (k sized so the sample takes about budget_s; rows spread over the whole height, starting at row offset % k).
+    `scene` is built through the oracle's host layer, so nothing of the product is loaded. A scene without an
+    rgb2spec table renders with the oracle's own fit at rgb2spec_res, on a copy (the scene is left as given)."""
+    import copy
     from oracle import cpu
     from vkrt_gb300 import abi
 
-    import copy
-    sd = scene.scene_data.copy()
     if scene.rgb2spec is None:
-        # no device table on this path: the oracle's own fit (the per-lookup cost does not depend on res), on a copy
-        # of the scene so that repeated calls see the scene as given
         scene = copy.copy(scene)
-        scene.rgb2spec = cpu.rgb2spec_generate(16, threads)
-        sd["rgb2specSRGB"] = (16, 0, 16)
+        scene.scene_data = scene.scene_data.copy()
+        _oracle_rgb2spec(scene, rgb2spec_res, threads)
+    sd = scene.scene_data.copy()
     orc = cpu.OracleScene(scene, environment_sampling=abi.ENV_IMPORTANCE)
     ncores = threads or os.cpu_count() or 1
     height = int(sd["viewportRect"][0][1] + sd["viewportRect"][0][3])
-    mid = height // 2
-    # calibration on a block of rows at the frame's centre, then a block sized to the budget (centred, clamped)
-    rows = max(1, min(height, 8))
+    width = int(sd["viewportRect"][0][2])
+    spp = int(sd["samplesPerPixel"][0])
+    # calibration on every 64th row, then a stride sized to the budget
     t0 = time.perf_counter()
-    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(mid - rows // 2, mid - rows // 2 + rows), threads=threads)
+    orc.render(sd, rng_mode=abi.RNG_PCG32, rng_seed=1, threads=threads, row_step=64)
     dt = time.perf_counter() - t0
-    rows = int(max(1, min(height, rows * budget_s / max(dt, 1e-3))))
-    lo = max(0, min(height - rows, mid - rows // 2))
+    rows_per_s = len(range(0, height, 64)) / max(dt, 1e-3)
+    step = max(1, int(round(height / max(rows_per_s * budget_s, 1.0))))
+    start = offset % step
     t0 = time.perf_counter()
-    acc, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rows=(lo, lo + rows), threads=threads)
+    _, st = orc.render(sd, rng_mode=abi.RNG_PCG32, rng_seed=1, threads=threads, rows=(start, height), row_step=step)
     dt = time.perf_counter() - t0
+    rows = len(range(start, height, step))
     rays = st["primaryRays"] + st["extensionRays"] + st["shadowRays"]
     orc.close()
     return {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": ncores, "kind": "port",
-            "sample": f"{rows} rows x {int(sd['viewportRect'][0][2])} px x {int(sd['samplesPerPixel'][0])} spp of the same "
-                      f"frame ({rays} rays, {dt:.1f} s)"}
+            "sample": f"every {step}th row from row {start} ({rows} rows x {width} px x {spp} spp of the frame, "
+                      f"{rays} rays, {dt:.1f} s)",
+            "seconds": dt, "frame_fraction": rows / height,
+            **_vkrt_units(spp * rows / height, dt)}
+
+
+def config0_cpu(threads: int = 0) -> dict:
+    """Config 0 on the host cores: the Cornell box 256 x 256, 64 frames of 1 spp, depth 8, RGB, through the oracle."""
+    from oracle import cpu
+    from vkrt_gb300 import abi, scenes
+    scene = scenes.cornell(256, 256, spp=1, max_depth=8, host=_oracle_host())
+    orc = cpu.OracleScene(scene)
+    sd = scene.scene_data.copy()
+    acc = None
+    rays = 0
+    orc.render(sd, rng_mode=abi.RNG_PCG32, rng_seed=1, threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    for f in range(64):
+        sd["frameNumber"] = f
+        acc, st = orc.render(sd, accum_in=acc, rng_mode=abi.RNG_PCG32, rng_seed=1, threads=threads)
+        rays += st["primaryRays"] + st["extensionRays"] + st["shadowRays"]
+    dt = time.perf_counter() - t0
+    orc.close()
+    return {"workload": CONFIG0, "ms": round(dt * 1e3, 1), "value": round(rays / dt / 1e6, 3), "unit": "Mrays/s",
+            "cores": threads or os.cpu_count() or 1, **_vkrt_units(64.0, dt)}
+
+
+def config0_measure(local: int) -> dict:
+    """Config 0 on the GPU: the Cornell box 256 x 256, 64 frames of 1 spp, depth 8, RGB, PCG32 seed 1, by both
+    integrators; device time of the 64 frames (CUDA events on the context stream)."""
+    import torch
+    from vkrt_gb300 import RenderContext, abi, scenes
+    scene = scenes.cornell(256, 256, spp=1, max_depth=8)
+    out = {"workload": CONFIG0}
+    for name, integ in (("megakernel", abi.INTEGRATOR_MEGAKERNEL), ("wavefront", abi.INTEGRATOR_WAVEFRONT)):
+        with RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, integrator=integ) as ctx:
+            ctx.upload_scene(scene)
+            stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+            sd = scene.scene_data.copy()
+            for f in range(3):  # warm-up frames (graphs, buffers)
+                sd["frameNumber"] = 1000 + f
+                ctx.render_frame(sd)
+            ctx.reset_accumulation()
+            ctx.sync()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            rays = 0
+            a.record(stream)
+            for f in range(64):
+                sd["frameNumber"] = f
+                ctx.render_frame(sd)
+                st = ctx.stats()
+                rays += _rays(st)
+            b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            out[name] = {"ms": round(ms, 3), "value": round(rays / (ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
+                         **_vkrt_units(64.0, ms * 1e-3)}
+    return out
 
 
 def run_reference(args) -> dict | None:
+    """vkrt's own renderer needs Vulkan ray tracing, which neither machine has: the reference arm times the oracle's
+    CPU restatement of vkrt's integrator on all host cores. Its scenes are built through the oracle's restatement of
+    vkrt's host layer and its rgb2spec table by the oracle's own fit at the device table's resolution, so the run
+    loads no product library."""
     rank, world, _ = _dist()
     if rank != 0:
         return None
-    scene = build_scene()
+    scene = build_scene(host=_oracle_host())
+    _oracle_rgb2spec(scene, 64)
     steps = []
     res = None
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(scene, budget_s=args.cpu_seconds)
+        r = cpu_baseline(scene, budget_s=args.cpu_seconds, offset=k)
         if k >= args.warmup:
             steps.append(r)
         res = r
-    value = float(np.mean([s["value"] for s in steps]))
+    secs = sum(r["seconds"] for r in steps)
+    frames = sum(r["frame_fraction"] for r in steps)
+    value = float(np.mean([r["value"] for r in steps]))
     return {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere field, procedural sky)",
-            "config": _config(1920, 1080, 16, 12, scene.triangle_count),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded icosphere field, procedural sky)", "config": _config(scene.triangle_count),
+            **_vkrt_units(16.0 * frames, secs),
             "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": res["cores"], "kind": "port",
-                             "sample": res["sample"]},
+                             "sample": f"per step {res['sample']}"},
             "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config0": config0_cpu(),
             "note": "vkrt's own renderer needs Vulkan ray tracing (no graphics stack on this box): the CPU "
-                    "restatement of its integrator stands in"}
+                    "restatement of its integrator stands in; each step renders a strided sample of the frame's rows"}
+
+
+def run_profile_frame(args) -> dict:
+    """Frames of the seeded icosphere field at a chosen size for profiling runs (the small cases of the ncu
+    summaries): prints one JSON line with rays by kind, node/triangle fetch bytes (with --stage-launches, which also
+    times the wavefront stages one by one), per-stage device milliseconds and the frames' device time. Under ncu the
+    kernels of every rendered frame (warm-up included) are captured; --warmup 0 --frames 1 keeps a capture to one
+    frame. --cache renders with the radiance cache, so its training and inference kernels run in every frame."""
+    import torch
+    from vkrt_gb300 import RenderContext, abi, scenes
+
+    scene = scenes.icosphere_field(n_spheres=args.spheres, width=args.width, height=args.height, spp=args.spp,
+                                   max_depth=args.depth, seed=1, spectral=not args.rgb)
+    integ = abi.INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+    ctx = RenderContext(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE, integrator=integ)
+    if not args.rgb:
+        scene.rgb2spec, info = ctx.generate_rgb2spec(64)
+        scene.scene_data["rgb2specSRGB"] = info
+    ctx.upload_scene(scene)
+    if args.stage_launches:
+        ctx.set_wavefront_config(profileStages=1)
+    if args.shade_blocks:
+        ctx.set_wavefront_config(shadeBlocksPerSM=args.shade_blocks)
+    if args.cache:
+        ctx.nrc_configure(enabled=1)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    sd = scene.scene_data.copy()
+    out = {}
+    for f in range(args.warmup + args.frames):
+        sd["frameNumber"] = f
+        ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev[0].record(stream)
+        ctx.render_frame(sd)
+        ev[1].record(stream)
+        ctx.sync()
+        st = ctx.stats()
+        if f >= args.warmup:
+            for k in ("primaryRays", "extensionRays", "shadowRays", "nodeFetchBytes", "triFetchBytes",
+                      "shadowNodeFetchBytes", "shadowTriFetchBytes", "kernelLaunches", "wavefrontBodies",
+                      "cacheTrainingRecords", "errorFlags"):
+                out[k] = out.get(k, 0) + int(st[k])
+            for k, v in zip(abi.WAVEFRONT_STAGES, st["stageMs"]):
+                out.setdefault("stage_ms", {})[k] = round(out.get("stage_ms", {}).get(k, 0.0) + float(v), 3)
+            out["frame_ms"] = round(out.get("frame_ms", 0.0) + ev[0].elapsed_time(ev[1]), 3)
+    out["workload"] = {"width": args.width, "height": args.height, "spp": args.spp, "depth": args.depth,
+                       "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
+                       "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
+                       "cache": args.cache, "shade_blocks": args.shade_blocks}
+    ctx.close()
+    return out
 
 
 def main():
@@ -600,7 +801,22 @@ def main():
     ap.add_argument("--stage-launches", action="store_true",
                     help="launch the wavefront stages one by one instead of as one CUDA graph (ncu cannot profile "
                          "kernel nodes of graphs with conditional nodes)")
+    prof = ap.add_argument_group("profiling frames (--profile-frame): small cases of the workload for ncu")
+    prof.add_argument("--profile-frame", action="store_true")
+    prof.add_argument("--width", type=int, default=640)
+    prof.add_argument("--height", type=int, default=360)
+    prof.add_argument("--spp", type=int, default=4)
+    prof.add_argument("--depth", type=int, default=12)
+    prof.add_argument("--spheres", type=int, default=800)
+    prof.add_argument("--frames", type=int, default=1)
+    prof.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
+    prof.add_argument("--rgb", action="store_true", help="RGB transport instead of hero spectral")
+    prof.add_argument("--cache", action="store_true", help="render with the radiance cache (wavefront only)")
+    prof.add_argument("--shade-blocks", type=int, default=0, help="shade kernel residency (blocks per SM)")
     args = ap.parse_args()
+    if args.profile_frame:
+        print(json.dumps(run_profile_frame(args)))
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:

@@ -149,6 +149,14 @@ int32_t vkrt_cuda_upload_texture(VKRT_CudaContext* context, uint32_t textureInde
  * uses still come from SceneData.environmentTextureIndex / environmentRotation each frame. */
 int32_t vkrt_cuda_set_environment(VKRT_CudaContext* context, uint32_t textureIndex);
 
+/* Copies the environment importance distribution that vkrt_cuda_set_environment built to host memory: the marginal
+ * CDF over rows (height + 1 floats), the conditional CDFs of the rows (height x (width + 1) floats) and the per-texel
+ * sampling weights (width x height floats, pdf over the unit square). width and height must be the environment
+ * texture's; any output pointer may be NULL. No counterpart in vkrt, which samples the environment only through the
+ * BSDF: it lets a host check the distribution. */
+int32_t vkrt_cuda_read_environment_distribution(VKRT_CudaContext* context, uint32_t width, uint32_t height,
+                                                float* marginal, float* conditional, float* texelPdf);
+
 /* rgb2spec coefficient table in vkrt's buffer layout: `res` z-scale floats followed by 3*res^3*3 coefficients
  * (src/core/scene/rgb2spec.c:17-89). */
 int32_t vkrt_cuda_upload_rgb2spec(VKRT_CudaContext* context, const float* table, uint32_t floatCount,
@@ -225,9 +233,16 @@ int32_t vkrt_cuda_read_denoiser_features(VKRT_CudaContext* context, float* albed
 /* CUDA stream (cudaStream_t) the context launches on, for callers that time or order work around it. */
 void* vkrt_cuda_stream(VKRT_CudaContext* context);
 
-/* Traces `count` rays against the current BVH: anyHit = 0 gives the closest hit (vkrt's scene query,
- * rt/queries/scene_query.slang:10-42), anyHit = 1 stops at the first accepted hit (shadow query,
- * rt/queries/shadow_query.slang:8-28; the record then carries that hit). Host arrays; synchronous. */
+/* Flags of the trace calls' `anyHit` word. VKRT_CUDA_TRACE_ANY_HIT (1) stops at the first accepted hit (shadow
+ * query, rt/queries/shadow_query.slang:8-28; the record then carries that hit); without it the call returns the closest
+ * hit (scene query, rt/queries/scene_query.slang:10-42). VKRT_CUDA_TRACE_PERSISTENT (2) runs the rays through the
+ * wavefront integrator's persistent traversal (dynamic ray fetch, a warp vote per step between node visits and
+ * triangle tests) instead of one ray per thread; both give identical records. */
+#define VKRT_CUDA_TRACE_ANY_HIT 1u
+#define VKRT_CUDA_TRACE_PERSISTENT 2u
+
+/* Traces `count` rays against the current BVH; `anyHit` holds VKRT_CUDA_TRACE_* flags (0 = closest hit by one ray
+ * per thread). Host arrays; synchronous. */
 int32_t vkrt_cuda_trace_rays(VKRT_CudaContext* context, const VKRT_CudaRay* rays, uint32_t count, uint32_t anyHit,
                              VKRT_CudaHit* hits);
 /* Same on device arrays, asynchronous on the context stream. */

@@ -6,8 +6,8 @@ rgb2spec_fit.cpp), compiled with -ffp-contract=off so FP32 expressions round exa
 
 oracle/_ref/libvkrt_ref.so: vkrt's own src/core/utility/packing.c compiled unchanged from the vkrt checkout,
 linked with ref_driver.c, which calls vkrt's vendored cglm (header-only) for camera and mesh matrices. It pins the
-host-side packing and matrix conventions. It is built only here (the vkrt checkout does not travel); tests that
-need it skip when it is absent.
+host-side packing and matrix conventions. It is built only where the environment variable VKRT_REFERENCE names a
+vkrt checkout; tests/golden/make_golden.py uses it to regenerate the golden fixtures the tests read.
 """
 from __future__ import annotations
 
@@ -22,7 +22,8 @@ ROOT = HERE.parent
 LIB = HERE / "liboracle.so"
 REF_DIR = HERE / "_ref"
 REF_LIB = REF_DIR / "libvkrt_ref.so"
-VKRT_SRC = Path(os.environ.get("VKRT_REFERENCE", "/root/reference"))
+# a vkrt checkout, named by the environment; without one the reference-compiled checker is not built
+VKRT_SRC = Path(os.environ["VKRT_REFERENCE"]) if os.environ.get("VKRT_REFERENCE") else None
 
 
 def _run(cmd):
@@ -45,12 +46,14 @@ def build_oracle(force: bool = False) -> Path:
     deps = srcs + [HERE / "oracle.h", HERE / "oracle_math.h", ROOT / "include" / "vkrt_cuda.h",
                    ROOT / "include" / "vkrt_cuda_types.h"]
     if force or not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in deps):
-        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", f"-I{ROOT / 'include'}",
+        _run(["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", f"-I{ROOT / 'include'}",
               f"-I{HERE}", *map(str, srcs), "-o", str(LIB), "-lpthread"])
     return LIB
 
 
 def build_reference(force: bool = False) -> Path | None:
+    if VKRT_SRC is None:
+        return None
     packing = VKRT_SRC / "src/core/utility/packing.c"
     if not packing.exists():
         return None

@@ -30,7 +30,7 @@ class OracleSceneDesc(C.Structure):
 
 class OracleRenderParams(C.Structure):
     _fields_ = [("rngMode", _U32), ("rngSeed", _U64), ("precision", _U32), ("threads", _U32), ("rowBegin", _U32),
-                ("rowEnd", _U32), ("useBruteForce", _U32)]
+                ("rowEnd", _U32), ("useBruteForce", _U32), ("rowStep", _U32)]
 
 
 class OracleRenderStats(C.Structure):
@@ -58,7 +58,7 @@ def load():
         "oracle_hash": (_U32, [_U32]), "oracle_init_pixel_seed": (_U32, [C.c_int32, C.c_int32, _U32, _U32]),
         "oracle_rand": (_F, [_V]), "oracle_pcg32": (_U32, [_V, _U64]),
         "oracle_world_triangles": (_U32, [_V, _V, _U32]),
-        "oracle_env_cdf": (_I32, [_V, _U32, _U32, _V, _V, _V]),
+        "oracle_env_cdf": (_I32, [_V, _U32, _U32, _V, _V, _V, _V]),
         "oracle_env_pdf": (_F, [_V, _V, _F]), "oracle_env_sample": (_I32, [_V, _F, _F, _F, _V, _V]),
         "oracle_rgb2spec_generate": (_I32, [_U32, _V, _U32, _U32]),
         "oracle_rgb2spec_fetch": (None, [_V, _U32, _V, _V]), "oracle_rgb2spec_eval": (_F, [_V, _F]),
@@ -82,7 +82,7 @@ class OracleScene:
     """The oracle's copy of a vkrt_gb300.Scene (world triangles, BVH2, environment distribution)."""
 
     def __init__(self, scene, environment_sampling: int = 0):
-        from vkrt_gb300.context import pack_vertices
+        from .host import pack_vertices  # the oracle's own restatement of vkrt's packing
         self.lib = load()
         if scene.shader_vertices is None:
             scene.shader_vertices = pack_vertices(scene.vertices)
@@ -150,7 +150,8 @@ class OracleScene:
         return out.reshape(n, 3, 3)
 
     def render(self, scene_data, accum_in=None, rng_mode=0, rng_seed=1, precision=32, threads=0, rows=None,
-               brute_force=False, want_output=False):
+               brute_force=False, want_output=False, row_step=1):
+        """One frame; rows = (begin, end) and row_step render every row_step-th row of that range only."""
         from vkrt_gb300 import abi
         sd = np.ascontiguousarray(scene_data, dtype=abi.SCENE_DATA)
         w = int(sd["viewportRect"][0][0] + sd["viewportRect"][0][2])
@@ -159,7 +160,7 @@ class OracleScene:
         acc_out = acc_in.copy()
         out = np.zeros((h, w, 4), np.uint16) if want_output else None
         p = OracleRenderParams(rng_mode, rng_seed, precision, threads, rows[0] if rows else 0, rows[1] if rows else 0,
-                               1 if brute_force else 0)
+                               1 if brute_force else 0, row_step)
         st = OracleRenderStats()
         r = self.lib.oracle_render(self.handle, _p(sd), C.byref(p), _p(acc_in), _p(acc_out), _p(out), C.byref(st))
         if r != 0:
@@ -176,7 +177,7 @@ class OracleScene:
         h = int(sd["viewportRect"][0][1] + sd["viewportRect"][0][3])
         acc_in = np.zeros((h, w, 4), np.float32)
         acc_out, alb, nrm = (np.zeros((h, w, 4), np.float32) for _ in range(3))
-        p = OracleRenderParams(rng_mode, rng_seed, precision, threads, 0, 0, 0)
+        p = OracleRenderParams(rng_mode, rng_seed, precision, threads, 0, 0, 0, 1)
         r = self.lib.oracle_render_features(self.handle, _p(sd), C.byref(p), _p(acc_in), _p(acc_out), _p(alb),
                                             _p(nrm))
         if r != 0:
@@ -191,7 +192,7 @@ class OracleScene:
         h = int(sd["viewportRect"][0][1] + sd["viewportRect"][0][3])
         acc_in = np.zeros((h, w, 4), np.float32)
         acc_out = np.zeros((h, w, 4), np.float64)
-        p = OracleRenderParams(rng_mode, rng_seed, precision, threads, 0, 0, 0)
+        p = OracleRenderParams(rng_mode, rng_seed, precision, threads, 0, 0, 0, 1)
         r = self.lib.oracle_render_f64(self.handle, _p(sd), C.byref(p), _p(acc_in), _p(acc_out))
         if r != 0:
             raise RuntimeError(f"oracle_render_f64 failed ({r})")
@@ -216,12 +217,17 @@ def rgb2spec_generate(res: int, threads: int = 0) -> np.ndarray:
     return out
 
 
-def env_cdf(rgba: np.ndarray):
+def env_cdf(rgba: np.ndarray, texel_pdf: bool = False):
+    """(marginal CDF, conditional CDFs (H, W + 1), FP64 total[, texel weights (H, W)]) of the environment
+    importance distribution."""
     lib = load()
     a = np.ascontiguousarray(rgba, np.float32)
     h, w = a.shape[:2]
     marg = np.zeros(h + 1, np.float32)
     cond = np.zeros(h * (w + 1), np.float32)
     tot = np.zeros(1, np.float64)
-    lib.oracle_env_cdf(_p(a), w, h, _p(marg), _p(cond), _p(tot))
+    pdf = np.zeros((h, w), np.float32)
+    lib.oracle_env_cdf(_p(a), w, h, _p(marg), _p(cond), _p(tot), _p(pdf))
+    if texel_pdf:
+        return marg, cond.reshape(h, w + 1), float(tot[0]), pdf
     return marg, cond.reshape(h, w + 1), float(tot[0])

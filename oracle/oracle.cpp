@@ -695,8 +695,13 @@ HitRec traceFp64Brute(const SceneFull& s, const std::vector<std::array<double, 9
             double s0 = (U + V + W) >= 0 ? 1.0 : -1.0;
             edgeDist = -std::min(s0 * bu, std::min(s0 * bv, s0 * bw));
         }
-        bool uncertain = std::fabs(edgeDist) < eps || (det != 0.0 && (std::fabs(t - tmin) < eps * std::max(1.0, tmin) ||
-                                                                        std::fabs(t - tmax) < eps * std::max(1.0, tmax)));
+        // uncertain: the ray passes within eps (relative to the triangle) of an edge, or through the triangle at a
+        // distance within eps of tmin / tmax; a triangle the ray passes well outside of is never uncertain, whatever
+        // distance its plane is crossed at
+        bool nearOrInside = allPos || allNeg || edgeDist < eps;
+        bool uncertain = nearOrInside && (std::fabs(edgeDist) < eps ||
+                                          (det != 0.0 && (std::fabs(t - tmin) < eps * std::max(1.0, tmin) ||
+                                                          std::fabs(t - tmax) < eps * std::max(1.0, tmax))));
         if (uncertain && det != 0.0 && t > tmin - eps && t < tmax + eps) nearestUncertainT = std::min(nearestUncertainT, t);
         if (!inside || !inRange) continue;
         if (t < bestT || (t == bestT && s.tris[i].gid < best.gid)) {
@@ -2490,10 +2495,12 @@ void renderRows(SceneFull& s, const VKRT_CudaSceneData& sd, const OracleRenderPa
         tab.scaleOffset = sd.rgb2specSRGB.scaleOffset;
         tab.dataOffset = sd.rgb2specSRGB.dataOffset;
     }
-    std::vector<OracleRenderStats> rowStats(r1 > r0 ? r1 - r0 : 0);
+    const uint32_t step = std::max(p.rowStep, 1u);
+    const uint32_t nRows = r1 > r0 ? (r1 - r0 + step - 1u) / step : 0u;
+    std::vector<OracleRenderStats> rowStats(nRows);
     uint32_t spp = std::max(sd.samplesPerPixel, 1u);
-    parallelFor(r1 > r0 ? r1 - r0 : 0, p.threads, [&](uint32_t ri) {
-        uint32_t y = r0 + ri;
+    parallelFor(nRows, p.threads, [&](uint32_t ri) {
+        uint32_t y = r0 + ri * step;
         Ctx<R> c{s, sd, tab, p.useBruteForce != 0, tri64, {}};
         for (uint32_t x = 0; x < W; ++x) {
             size_t pi = size_t(y) * W + x;
@@ -2797,12 +2804,13 @@ float oracle_rand(uint32_t* state) {
 uint32_t oracle_pcg32(uint64_t* state, uint64_t inc) { return pcgNext(*state, inc); }
 
 int32_t oracle_env_cdf(const float* rgba, uint32_t w, uint32_t h, float* marginal, float* conditional,
-                       double* totalOut) {
+                       double* totalOut, float* texelPdf) {
     if (!rgba || !w || !h) return -1;
     std::vector<float> m, c, t;
     buildEnvDistribution(rgba, w, h, m, c, t, totalOut);
     if (marginal) std::memcpy(marginal, m.data(), m.size() * sizeof(float));
     if (conditional) std::memcpy(conditional, c.data(), c.size() * sizeof(float));
+    if (texelPdf) std::memcpy(texelPdf, t.data(), t.size() * sizeof(float));
     return 0;
 }
 

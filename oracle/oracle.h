@@ -57,6 +57,8 @@ typedef struct OracleRenderParams {
     uint32_t rowBegin;  /* render rows [rowBegin, rowEnd) only; other pixels of accumOut are left untouched */
     uint32_t rowEnd;    /* 0 = full height */
     uint32_t useBruteForce; /* 1: FP64 brute-force closest hit instead of the BVH (tiny scenes only) */
+    uint32_t rowStep;   /* render every rowStep-th row of [rowBegin, rowEnd) (0 or 1 = every row): a sample of the
+                           frame spread over its whole height */
 } OracleRenderParams;
 
 typedef struct OracleRenderStats {
@@ -104,7 +106,7 @@ uint32_t oracle_world_triangles(void* scene, float* out, uint32_t capacity);
 /* environment importance distribution: marginal (H+1) and conditional (H*(W+1)) CDFs in FP64 -> FP32, and the
  * solid-angle pdf of directions */
 int32_t oracle_env_cdf(const float* rgba, uint32_t width, uint32_t height, float* marginal, float* conditional,
-                       double* totalOut);
+                       double* totalOut, float* texelPdf);
 float oracle_env_pdf(void* scene, const float dir[3], float rotationDegrees);
 int32_t oracle_env_sample(void* scene, float u1, float u2, float rotationDegrees, float dirOut[3], float* pdfOut);
 

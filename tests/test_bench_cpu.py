@@ -13,10 +13,25 @@ sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
 def test_cpu_baseline_leaves_the_scene_unchanged():
     import bench
     from vkrt_gb300 import scenes
-    scene = scenes.icosphere_field(n_spheres=20, width=64, height=1080, spp=1, max_depth=3, seed=1, spectral=True)
-    for _ in range(2):
-        r = bench.cpu_baseline(scene, budget_s=0.05, threads=2)
+    from oracle.host import OracleHost
+    scene = scenes.icosphere_field(n_spheres=20, width=64, height=1080, spp=1, max_depth=3, seed=1, spectral=True,
+                                   host=OracleHost)
+    for k in range(2):
+        r = bench.cpu_baseline(scene, budget_s=0.05, threads=2, offset=k, rgb2spec_res=8)
         assert r["value"] > 0 and scene.rgb2spec is None
+        assert 0 < r["frame_fraction"] <= 1 and r["samples_per_s"] > 0
+
+
+def test_reference_arm_loads_no_product_library(tmp_path):
+    """The reference arm's scenes come from the oracle's host layer: its process never maps libvkrt_gb300.so."""
+    import subprocess
+    code = ("import sys; sys.path.insert(0, '.'); import bench; from oracle.host import OracleHost; "
+            "s = bench.build_scene(width=64, height=64, n_spheres=10, host=OracleHost); "
+            "r = bench.cpu_baseline(s, budget_s=0.05, threads=2, rgb2spec_res=8); "
+            "print(sorted({l.split()[-1] for l in open('/proc/self/maps') if '.so' in l}))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=Path(__file__).resolve().parents[1], capture_output=True,
+                         text=True, check=True).stdout
+    assert "liboracle.so" in out and "libvkrt_gb300.so" not in out, out
 
 
 def test_oracle_refuses_a_table_smaller_than_its_layout():

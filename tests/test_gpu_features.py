@@ -5,6 +5,8 @@ frames; features off leave the frame untouched."""
 import numpy as np
 import pytest
 
+from parity import assert_match
+
 from vkrt_gb300 import RenderContext, abi, scenes
 
 pytestmark = pytest.mark.gpu
@@ -50,12 +52,10 @@ def test_features_match_oracle(built, integrator, coat):
         acc = ctx.read_accumulation()
         alb, nrm = ctx.read_denoiser_features()
     ref_acc, ref_alb, ref_nrm = cpu.OracleScene(s).render_features(sd, rng_mode=abi.RNG_REFERENCE)
-    same_acc = (np.abs(acc[..., :3] - ref_acc[..., :3]) <= 1e-3 + 1e-3 * np.abs(ref_acc[..., :3])).all(-1)
-    assert same_acc.mean() > 0.97
+    assert_match("features mirror: radiance", acc, ref_acc, 1e-3, 1e-3, max_outside=20)
     np.testing.assert_array_equal(alb[..., 3], ref_alb[..., 3])  # resolved-sample counts
-    close_a = (np.abs(alb[..., :3] - ref_alb[..., :3]) <= 1e-4).all(-1)
-    close_n = (np.abs(nrm[..., :3] - ref_nrm[..., :3]) <= 1e-4).all(-1)
-    assert close_a.mean() > 0.99 and close_n.mean() > 0.99, (close_a.mean(), close_n.mean())
+    assert_match("features mirror: albedo", alb, ref_alb, 1e-4, 0.0, max_outside=2)
+    assert_match("features mirror: normal", nrm, ref_nrm, 1e-4, 0.0, max_outside=2)
     # pixels that see the mirror carry the albedo of what it reflects, not the mirror's 0.9 grey
     assert (alb[..., 3] > 0).mean() > 0.9
     assert np.all(alb[..., 3] <= 4.0)
@@ -111,6 +111,5 @@ def test_features_through_glass_match_oracle(built, integrator):
         ctx.render_frame(s.scene_data)
         alb, nrm = ctx.read_denoiser_features()
     _, ref_alb, ref_nrm = cpu.OracleScene(s).render_features(s.scene_data, rng_mode=abi.RNG_REFERENCE)
-    close_a = (np.abs(alb[..., :3] - ref_alb[..., :3]) <= 1e-4).all(-1)
-    close_n = (np.abs(nrm[..., :3] - ref_nrm[..., :3]) <= 1e-4).all(-1)
-    assert close_a.mean() > 0.97 and close_n.mean() > 0.97, (close_a.mean(), close_n.mean())
+    assert_match("features glass: albedo", alb, ref_alb, 1e-4, 0.0, max_outside=2)
+    assert_match("features glass: normal", nrm, ref_nrm, 1e-4, 0.0, max_outside=2)

@@ -194,10 +194,12 @@ def test_scene_file_rejects_bad_documents(built, tmp_path):
             scene_file.load_scene_file(p, 32, 32)
 
 
-_REF_SCENES = Path(os.environ.get("VKRT_REFERENCE_ROOT", "/root/reference")) / "assets" / "scenes"
+# vkrt's bundled scene files, read from a vkrt checkout named by VKRT_REFERENCE (the tests skip without one)
+_REF_SCENES = Path(os.environ.get("VKRT_REFERENCE", "")) / "assets" / "scenes" if os.environ.get("VKRT_REFERENCE") \
+    else None
 
 
-@pytest.mark.skipif(not _REF_SCENES.exists(), reason="vkrt's own assets are not present")
+@pytest.mark.skipif(_REF_SCENES is None or not _REF_SCENES.exists(), reason="no vkrt checkout named by VKRT_REFERENCE")
 @pytest.mark.parametrize("name", ["cornell", "prism", "caustics"])
 def test_vkrt_scene_files(built, name):
     """vkrt's bundled scene files: every saved mesh whose import exists is loaded with its saved material and the

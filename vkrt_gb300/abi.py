@@ -117,6 +117,7 @@ SPECTRAL_SINGLE, SPECTRAL_HERO = 0, 1
 RNG_REFERENCE, RNG_PCG32 = 0, 1
 ENV_BSDF_ONLY, ENV_IMPORTANCE = 0, 1
 INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT = 0, 1
+TRACE_ANY_HIT, TRACE_PERSISTENT = 1, 2
 TEXTURE_FORMAT_RGBA8_UNORM, TEXTURE_FORMAT_RGBA16_UNORM, TEXTURE_FORMAT_RGBA16_SFLOAT, TEXTURE_FORMAT_RGBA32_SFLOAT = 0, 1, 2, 3
 COLOR_SPACE_SRGB, COLOR_SPACE_LINEAR = 0, 1
 WRAP_REPEAT, WRAP_CLAMP, WRAP_MIRROR = 10497, 33071, 33648
@@ -161,6 +162,7 @@ EXPORTS = {
     "vkrt_cuda_upload_lights": (_I32, [_V, _V, _U32, _V, _U32, _V, _V, _V, _V]),
     "vkrt_cuda_upload_texture": (_I32, [_V, _U32, _V, _U32, _U32, _U32, _U32]),
     "vkrt_cuda_set_environment": (_I32, [_V, _U32]),
+    "vkrt_cuda_read_environment_distribution": (_I32, [_V, _U32, _U32, _V, _V, _V]),
     "vkrt_cuda_upload_rgb2spec": (_I32, [_V, _V, _U32, _V]),
     "vkrt_cuda_upload_sheen_table": (_I32, [_V, _V, _U32]),
     "vkrt_cuda_generate_rgb2spec": (_I32, [_V, _U32, _V]),
@@ -211,6 +213,7 @@ EXPORTS = {
     "vkrt_host_default_material": (None, [_V]),
     "vkrt_host_auto_spp_init": (None, [_V, _U32]),
     "vkrt_host_auto_spp_update": (_I32, [_V, _F, _V]),
+    "vkrt_host_png_unfilter": (_I32, [_V, _U32, _U64, _U32, _V]),
 }
 
 # VKRT_CudaAutoSpp

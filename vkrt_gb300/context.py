@@ -386,12 +386,26 @@ class RenderContext:
         self._check(self.lib.vkrt_cuda_get_stats(self.handle, abi.ptr(st)), "stats")
         return {k: st[k][0].tolist() for k in abi.STATS.names}
 
-    def trace_rays(self, rays: np.ndarray, any_hit: bool = False) -> np.ndarray:
+    def trace_rays(self, rays: np.ndarray, any_hit: bool = False, persistent: bool = False) -> np.ndarray:
+        """Closest (or, with any_hit, first accepted) hits of `rays`; persistent runs them through the wavefront's
+        persistent vote-scheduled traversal instead of one ray per thread."""
         r = np.ascontiguousarray(rays, dtype=abi.RAY)
         hits = np.zeros(len(r), dtype=abi.HIT)
-        self._check(self.lib.vkrt_cuda_trace_rays(self.handle, abi.ptr(r), len(r), 1 if any_hit else 0,
-                                                  abi.ptr(hits)), "trace rays")
+        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_PERSISTENT if persistent else 0)
+        self._check(self.lib.vkrt_cuda_trace_rays(self.handle, abi.ptr(r), len(r), flags, abi.ptr(hits)),
+                    "trace rays")
         return hits
+
+    def read_environment_distribution(self, width: int, height: int):
+        """(marginal CDF (H + 1), conditional CDFs (H, W + 1), texel weights (H, W)) of the environment importance
+        distribution built at upload, float32."""
+        marg = np.zeros(height + 1, np.float32)
+        cond = np.zeros((height, width + 1), np.float32)
+        pdf = np.zeros((height, width), np.float32)
+        self._check(self.lib.vkrt_cuda_read_environment_distribution(self.handle, width, height, abi.ptr(marg),
+                                                                     abi.ptr(cond), abi.ptr(pdf)),
+                    "read environment distribution")
+        return marg, cond, pdf
 
     def trace_rays_device(self, rays_ptr: int, count: int, hits_ptr: int, any_hit: bool = False) -> None:
         self._check(self.lib.vkrt_cuda_trace_rays_device(self.handle, C.c_void_p(rays_ptr), count,

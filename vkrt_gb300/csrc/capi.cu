@@ -669,6 +669,29 @@ int32_t vkrt_cuda_set_environment(VKRT_CudaContext* c, uint32_t textureIndex) {
     return VKRT_CUDA_SUCCESS;
 }
 
+int32_t vkrt_cuda_read_environment_distribution(VKRT_CudaContext* c, uint32_t width, uint32_t height, float* marginal,
+                                                float* conditional, float* texelPdf) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (c->envTexture == VKRT_CUDA_INVALID_INDEX) return invalid(c, "no environment distribution is built");
+    if (width != c->envWidth || height != c->envHeight) return invalid(c, "environment distribution size mismatch");
+    cudaSetDevice(c->device);
+    const size_t W = width, H = height;
+    if (marginal)
+        VKRT_TRY(c, cudaMemcpyAsync(marginal, c->envMarginal.ptr, sizeof(float) * (H + 1), cudaMemcpyDeviceToHost,
+                                    c->stream),
+                 "read environment distribution");
+    if (conditional)
+        VKRT_TRY(c, cudaMemcpyAsync(conditional, c->envConditional.ptr, sizeof(float) * H * (W + 1),
+                                    cudaMemcpyDeviceToHost, c->stream),
+                 "read environment distribution");
+    if (texelPdf)
+        VKRT_TRY(c, cudaMemcpyAsync(texelPdf, c->envTexelPdf.ptr, sizeof(float) * W * H, cudaMemcpyDeviceToHost,
+                                    c->stream),
+                 "read environment distribution");
+    VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read environment distribution");
+    return VKRT_CUDA_SUCCESS;
+}
+
 int32_t vkrt_cuda_upload_sheen_table(VKRT_CudaContext* c, const float* table, uint32_t floatCount) {
     if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     if (!table || floatCount != VKRT_CUDA_SHEEN_TABLE_FLOATS) return invalid(c, "sheen table: 3072 floats");

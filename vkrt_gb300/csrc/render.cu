@@ -7,6 +7,7 @@
 // accumulation image and writes the next accumulation image and the RGBA16 output.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -17,8 +18,14 @@ namespace vkrt {
 
 namespace {
 
-// One pixel: SceneData.samplesPerPixel paths, each traced to the end (shadow rays traced inline), blended into the
-// running mean (writeback.slang:72-114) and encoded for display.
+// One pixel: SceneData.samplesPerPixel paths, blended into the running mean (writeback.slang:72-114) and encoded
+// for display. The loop is flat: every iteration traces exactly one ray of the thread — the next segment of its path
+// or one of the shadow rays its last vertex asked for — through a single inlined copy of the traversal, and a thread
+// whose path ended starts its next sample in the same iteration (path regeneration). With the sample loop nested
+// around the bounce loop instead, a warp waited at the end of every sample for its longest path (3.5 of 32 lanes
+// active on the 1M-triangle field) and held three copies of the traversal code. Each thread still sums its own samples
+// in sample order and applies a vertex's shadow contributions in request order before its next segment, so the image
+// is the nested loop's, bit for bit.
 // kFull: vkrt's whole material stack, alpha tests and the denoiser features (written when the film has feature
 // images)
 // kFeatures alone: the denoiser features with the reflection-only materials (the plain vertex step plus the feature
@@ -40,7 +47,7 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
             film.output[pixel] = make_ushort4(0, 0, 0, 0);
             if (kFeatures && film.albedoWrite) film.albedoWrite[pixel] = film.normalWrite[pixel] = f4(0.0f);
         } else {
-            KernelCtx k{sc, sd, smemStack + threadIdx.x, blockDim.x, counters};
+            uint2* const stackColumn = smemStack + threadIdx.x;
             const float4 prev = film.accumRead[pixel];
             const uint32_t prevN = uint32_t(prev.w + 0.5f);  // integrator/path/state.slang:72
             const uint32_t spp = max(sd.samplesPerPixel, 1u);
@@ -48,59 +55,63 @@ __global__ void __launch_bounds__(kDefaultThreads) kRenderMega(DeviceScene sc, V
                            rp.rngSeed};
             cfg.single = kSpectral && kFull && singleWavelength(sd);
             SpecTable tab = makeSpecTable(sc, sd);
+            const bool alpha = kFull && rp.alpha != 0u;
             float3 sum = f3(0.0f);
             DenoiserFeature fsum{f3(0.0f), f3(0.0f), 0.0f};
-            for (uint32_t si = 0; si < spp; ++si) {
-                PathState p = beginPath<kSpectral>(cfg, sd, px, py, prevN + si);
-                DenoiserFeature feat{f3(0.0f), f3(0.0f), 0.0f};
-                pc.samples++;
-                for (;;) {
-                    if (p.depth == 0) pc.primary++;
-                    else pc.extension++;
-                    // alpha-tested scenes: the ray's alpha seed, which the vertex's shadow rays reuse salted
-                    const uint32_t alphaSeed = alphaSeedOf(p.rng);
-                    TraceHit h;
-                    if (kFull && rp.alpha)
-                        h = traceBvh<false, kCountBytes, false, false, true>(sc, TraceRay{p.o, p.d, kTMin, kTMax},
-                                                                             k.stackColumn, k.stackStride, counters,
-                                                                             0u, alphaSeed);
-                    else h = closest<kCountBytes>(k, p.o, p.d);
-                    ShadowRequest sh[2];
-                    uint32_t ns;
-                    bool cont;
-                    if (kFull)
-                        cont = shadePathVertex<kSpectral, FeatureHook, true>(sc, sd, cfg, tab, p, h, sh, ns,
-                                                                             FeatureHook{{}, &feat});
-                    else if (kFeatures)
-                        cont = shadePathVertex<kSpectral, FeatureHook>(sc, sd, cfg, tab, p, h, sh, ns,
-                                                                       FeatureHook{{}, &feat});
-                    else cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
-                    for (uint32_t i = 0; i < ns; ++i) {
-                        pc.shadow++;
-                        TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
-                        if (kFull) {  // a transmissive occluder makes the vertex's NEE unsupported
-                            const TraceHit o =
-                                rp.alpha ? traceBvh<true, kCountBytes, false, true, true>(
-                                               sc, r, k.stackColumn, k.stackStride, counters, 0u,
-                                               alphaShadowSeed(alphaSeed, i))
-                                         : traceBvh<true, kCountBytes, false, true>(sc, r, k.stackColumn,
-                                                                                    k.stackStride, counters);
-                            if (o.mesh == VKRT_CUDA_INVALID_INDEX) {
-                                if (o.prim == kShadowThroughTransmission) p.flags &= ~kPathPrevNee;
-                                else p.radiance += sh[i].contribution;
-                            }
-                        } else if (traceBvh<true, kCountBytes>(sc, r, k.stackColumn, k.stackStride, counters).mesh ==
-                                   VKRT_CUDA_INVALID_INDEX) {
-                            p.radiance += sh[i].contribution;
-                        }
-                    }
-                    if (!cont) break;
+            DenoiserFeature feat{f3(0.0f), f3(0.0f), 0.0f};
+            PathState p;
+            uint32_t si = 0u;  // samples started
+            bool live = false;
+            for (;;) {
+                if (!live) {
+                    if (si >= spp) break;
+                    p = beginPath<kSpectral>(cfg, sd, px, py, prevN + si);
+                    ++si;
+                    live = true;
+                    feat = DenoiserFeature{f3(0.0f), f3(0.0f), 0.0f};
+                    pc.samples++;
                 }
-                sum += pathResult<kSpectral>(cfg, p);
-                if (kFeatures) {
-                    fsum.albedo += feat.albedo;
-                    fsum.normal += feat.normal;
-                    fsum.weight += feat.weight;
+                if (p.depth == 0) pc.primary++;
+                else pc.extension++;
+                // alpha-tested scenes: the ray's alpha seed, which the vertex's shadow rays reuse salted
+                const uint32_t alphaSeed = alphaSeedOf(p.rng);
+                TraceHit h;
+                if (alpha)
+                    h = traceBvh<false, kCountBytes, false, false, 1>(sc, TraceRay{p.o, p.d, kTMin, kTMax},
+                                                                      stackColumn, blockDim.x, counters, 0u,
+                                                                      alphaSeed);
+                else h = traceBvh<false, kCountBytes>(sc, TraceRay{p.o, p.d, kTMin, kTMax}, stackColumn, blockDim.x,
+                                                      counters);
+                ShadowRequest sh[2];
+                uint32_t ns;
+                bool cont;
+                if (kFull)
+                    cont = shadePathVertex<kSpectral, FeatureHook, true>(sc, sd, cfg, tab, p, h, sh, ns,
+                                                                         FeatureHook{{}, &feat});
+                else if (kFeatures)
+                    cont = shadePathVertex<kSpectral, FeatureHook>(sc, sd, cfg, tab, p, h, sh, ns,
+                                                                   FeatureHook{{}, &feat});
+                else cont = shadePathVertex<kSpectral>(sc, sd, cfg, tab, p, h, sh, ns);
+                for (uint32_t i = 0; i < ns; ++i) {
+                    pc.shadow++;
+                    const TraceRay r{sh[i].origin, sh[i].dir, kTMin, sh[i].tmax};
+                    const TraceHit o = traceBvh<true, kCountBytes, false, false, 0, true>(
+                        sc, r, stackColumn, blockDim.x, counters, 0u, alphaShadowSeed(alphaSeed, i), true, kFull,
+                        alpha);
+                    if (o.mesh == VKRT_CUDA_INVALID_INDEX) {
+                        // a transmissive occluder makes the vertex's NEE unsupported (full stack only)
+                        if (kFull && o.prim == kShadowThroughTransmission) p.flags &= ~kPathPrevNee;
+                        else p.radiance += sh[i].contribution;
+                    }
+                }
+                if (!cont) {
+                    sum += pathResult<kSpectral>(cfg, p);
+                    if (kFeatures) {
+                        fsum.albedo += feat.albedo;
+                        fsum.normal += feat.normal;
+                        fsum.weight += feat.weight;
+                    }
+                    live = false;
                 }
             }
             if (kFeatures && film.albedoWrite) {
@@ -145,6 +156,35 @@ __global__ void __launch_bounds__(kDefaultThreads) kTraceRays(DeviceScene sc, co
     float4* hp = reinterpret_cast<float4*>(hits + i);
     hp[0] = make_float4(__uint_as_float(h.mesh), __uint_as_float(h.prim), hit ? h.t : 0.0f, hit ? h.u : 0.0f);
     hp[1] = make_float4(hit ? h.v : 0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// The same trace through the wavefront's persistent traversal (persistentTraceVote: dynamic ray fetch and a warp vote
+// per step between node visits and triangle tests), so the kernel the wavefront's intersect and shadow stages run can
+// be checked ray by ray. Rays are fetched through counters->workCursor, which the launch clears.
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kDefaultThreads) kTraceRaysPersistent(DeviceScene sc,
+                                                                        const VKRT_CudaRay* __restrict__ rays,
+                                                                        uint32_t count, VKRT_CudaHit* __restrict__ hits,
+                                                                        RenderCounters* counters) {
+    extern __shared__ uint2 smemStack[];
+    uint32_t nodeVisits = 0u, triTests = 0u;
+    persistentTraceVote<kAnyHit, kVoteRefillLanes, false>(
+        count, &counters->workCursor, smemStack + threadIdx.x, blockDim.x, &counters->errorFlags,
+        [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
+            const float4* rp = reinterpret_cast<const float4*>(rays + i);
+            const float4 a = __ldg(rp), b = __ldg(rp + 1);
+            r = TraceRay{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), a.w, b.w};
+            nodes = sc.nodes;
+            tris = sc.tris;
+            nodeCount = sc.nodeCount;
+        },
+        [&](uint32_t i, const TraceHit& h) {
+            const bool hit = h.mesh != VKRT_CUDA_INVALID_INDEX;
+            float4* hp = reinterpret_cast<float4*>(hits + i);
+            hp[0] = make_float4(__uint_as_float(h.mesh), __uint_as_float(h.prim), hit ? h.t : 0.0f, hit ? h.u : 0.0f);
+            hp[1] = make_float4(hit ? h.v : 0.0f, 0.0f, 0.0f, 0.0f);
+        },
+        nodeVisits, triTests);
 }
 
 __global__ void kClearFilm(float4* a, float4* b, ushort4* out, size_t pixels) {
@@ -432,8 +472,21 @@ cudaError_t launchTraceRays(const DeviceScene& sc, const VKRT_CudaRay* rays, uin
     if (count == 0) return cudaSuccess;
     const uint32_t threads = kDefaultThreads;
     const size_t smem = size_t(threads) * VKRT_SMEM_STACK * sizeof(uint2);
+    const bool any = (anyHit & VKRT_CUDA_TRACE_ANY_HIT) != 0u;
+    if (anyHit & VKRT_CUDA_TRACE_PERSISTENT) {
+        int device = 0, sms = 0;
+        cudaError_t e = cudaGetDevice(&device);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&counters->workCursor, 0, sizeof(counters->workCursor), stream);
+        if (e != cudaSuccess) return e;
+        // persistent grid: 8 resident blocks of 128 per SM, as the wavefront's intersect stage
+        const uint32_t grid = std::min(uint32_t(sms) * 8u, (count + threads - 1) / threads);
+        if (any) kTraceRaysPersistent<true><<<grid, threads, smem, stream>>>(sc, rays, count, hits, counters);
+        else kTraceRaysPersistent<false><<<grid, threads, smem, stream>>>(sc, rays, count, hits, counters);
+        return cudaGetLastError();
+    }
     const uint32_t blocks = (count + threads - 1) / threads;
-    if (anyHit) kTraceRays<true><<<blocks, threads, smem, stream>>>(sc, rays, count, hits, counters);
+    if (any) kTraceRays<true><<<blocks, threads, smem, stream>>>(sc, rays, count, hits, counters);
     else kTraceRays<false><<<blocks, threads, smem, stream>>>(sc, rays, count, hits, counters);
     return cudaGetLastError();
 }

@@ -24,6 +24,9 @@ namespace vkrt {
 #define VKRT_LOCAL_STACK 56  // further entries per thread in local memory
 #define VKRT_POSTPONE_FRACTION 0.2f
 
+// persistent vote-scheduled traversal: a warp fetches new rays once fewer than this many of its lanes are traversing
+constexpr int kVoteRefillLanes = 20;
+
 struct TraceRay {
     float3 org;
     float3 dir;
@@ -203,9 +206,17 @@ constexpr uint32_t kShadowThroughTransmission = 0xFFFFFFFEu;
 // kAlpha 1 (scenes with alpha-tested materials, entry/path/any_hit.slang and entry/shadow/any_hit.slang): a candidate
 // hit on such a material counts only when alphaAccepts it, with the ray's `alphaSeed`; kAlpha 2 (selection and pick
 // rays, entry/select/any_hit.slang): mask cut-outs are dropped (selectionAlphaAccepts).
-template <bool kAnyHit, bool kCount, bool kMeshFilter = false, bool kTransmissive = false, int kAlpha = 0>
+// kRuntime: the any-hit, transmissive and alpha (mode 1) behaviours are also chosen per call by rtAnyHit,
+// rtTransmissive and rtAlpha, so one inlined copy of the traversal serves closest-hit and shadow rays (the megakernel's
+// single trace site); with kRuntime = false the runtime flags are ignored and the template flags alone decide.
+template <bool kAnyHit, bool kCount, bool kMeshFilter = false, bool kTransmissive = false, int kAlpha = 0,
+          bool kRuntime = false>
 VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* smemColumn, uint32_t smemStride,
-                           RenderCounters* counters, uint32_t meshFilter = 0u, uint32_t alphaSeed = 0u) {
+                           RenderCounters* counters, uint32_t meshFilter = 0u, uint32_t alphaSeed = 0u,
+                           bool rtAnyHit = false, bool rtTransmissive = false, bool rtAlpha = false) {
+    const bool anyHit = kAnyHit || (kRuntime && rtAnyHit);
+    const bool transmissive = kTransmissive || (kRuntime && rtTransmissive);
+    const bool alphaTest = kAlpha == 1 || (kRuntime && rtAlpha);
     TraceHit best;
     best.mesh = VKRT_CUDA_INVALID_INDEX;
     best.prim = VKRT_CUDA_INVALID_INDEX;
@@ -281,11 +292,11 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
             if (watertightHit(wr, org, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
                               make_float3(c.x, c.y, c.z), tmin, tmax, t, b1, b2)) {
                 uint32_t gid = __float_as_uint(a.w);
-                if (kAlpha == 1 && !alphaAccepts(sc, __float_as_uint(b.w), __float_as_uint(c.w), b1, b2, alphaSeed, gid))
+                if (alphaTest && !alphaAccepts(sc, __float_as_uint(b.w), __float_as_uint(c.w), b1, b2, alphaSeed, gid))
                     continue;
                 if (kAlpha == 2 && !selectionAlphaAccepts(sc, __float_as_uint(b.w), __float_as_uint(c.w), b1, b2))
                     continue;
-                if (kTransmissive && sc.materials[sc.meshes[__float_as_uint(b.w)].materialIndex].transmission > 0.0f) {
+                if (transmissive && sc.materials[sc.meshes[__float_as_uint(b.w)].materialIndex].transmission > 0.0f) {
                     best.prim = kShadowThroughTransmission;
                     continue;
                 }
@@ -297,7 +308,7 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
                     best.gid = gid;
                     best.mesh = __float_as_uint(b.w);
                     best.prim = __float_as_uint(c.w);
-                    if (kAnyHit) {
+                    if (anyHit) {
                         triGroup.y = 0u;
                         nodeGroup.y = 0u;
                         stack.sp = 0;
@@ -307,7 +318,7 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
             }
         }
         if (overflow) break;
-        if (kAnyHit && best.mesh != VKRT_CUDA_INVALID_INDEX) break;
+        if (anyHit && best.mesh != VKRT_CUDA_INVALID_INDEX) break;
 
         if (nodeGroup.y <= 0x00FFFFFFu) {
             if (stack.sp > 0) {
@@ -318,8 +329,8 @@ VKRT_DEV TraceHit traceBvh(const DeviceScene& sc, const TraceRay& ray, uint2* sm
         }
     }
     if (kCount && counters) {
-        atomicAdd(kAnyHit ? &counters->shadowNodeBytes : &counters->nodeBytes, (unsigned long long)nodeBytes);
-        atomicAdd(kAnyHit ? &counters->shadowTriBytes : &counters->triBytes, (unsigned long long)triBytes);
+        atomicAdd(anyHit ? &counters->shadowNodeBytes : &counters->nodeBytes, (unsigned long long)nodeBytes);
+        atomicAdd(anyHit ? &counters->shadowTriBytes : &counters->triBytes, (unsigned long long)triBytes);
     }
     if (overflow) {
         best.mesh = VKRT_CUDA_INVALID_INDEX;

@@ -54,7 +54,7 @@ enum : uint32_t {
 constexpr uint32_t kPendCache = 16u;        // pendFlags: the path ended at a radiance-cache query
 constexpr uint32_t kPendUnsupported = 32u;  // pendFlags: an NEE shadow ray met a transmissive surface
 constexpr uint32_t kSortMaterial = 1, kSortClass = 2;  // sortByMaterial (0: as traced); 1 sorts by (scene, class)
-constexpr int kRefillLanes = 20;  // a warp refills once fewer of its lanes are still traversing
+constexpr int kRefillLanes = kVoteRefillLanes;  // a warp refills once fewer of its lanes are still traversing
 
 
 struct WfGlobals {

@@ -10,6 +10,11 @@
 * sky_environment(...)  — 1024 x 512 FP32 lat-long map: grey sky gradient 0.2-1.0 plus a 0.5-degree sun disc of
                           radiance 5e3 at a seeded direction.
 All scenes are Z-up like vkrt's default camera (src/core/scene/uniform.c:133-138).
+
+Records (default material and SceneData, camera matrices, vertex packing, light tables) come from a host layer:
+the backend's own host library by default (ProductHost), or any object with the same five methods passed as
+`host=` — the CPU reference run of the benchmark passes the oracle's independent restatement, so it loads no product
+code.
 """
 from __future__ import annotations
 
@@ -18,29 +23,51 @@ import math
 import numpy as np
 
 from . import abi
-from .context import Scene, build_light_tables
+from . import context
+from .context import Scene
 
 
-def default_material(**overrides) -> np.ndarray:
-    m = np.zeros(1, dtype=abi.MATERIAL)
-    abi.load().vkrt_host_default_material(abi.ptr(m))
+class ProductHost:
+    """The backend's host library (vkrt_host_* in libvkrt_gb300.so)."""
+
+    @staticmethod
+    def default_material() -> np.ndarray:
+        m = np.zeros(1, dtype=abi.MATERIAL)
+        abi.load().vkrt_host_default_material(abi.ptr(m))
+        return m
+
+    @staticmethod
+    def default_scene_data(width: int, height: int) -> np.ndarray:
+        sd = np.zeros(1, dtype=abi.SCENE_DATA)
+        abi.load().vkrt_host_default_scene_data(width, height, abi.ptr(sd))
+        return sd
+
+    @staticmethod
+    def camera_matrices(sd: np.ndarray, pos, target, up, vfov: float) -> None:
+        p = np.array(pos, dtype=np.float32)
+        t = np.array(target, dtype=np.float32)
+        u = np.array(up, dtype=np.float32)
+        w, h = int(sd["viewportRect"][0][2]), int(sd["viewportRect"][0][3])
+        abi.load().vkrt_host_camera_matrices(abi.ptr(p), abi.ptr(t), abi.ptr(u), vfov, 0.001, 10000.0, w, h,
+                                             abi.ptr(sd))
+
+    pack_vertices = staticmethod(context.pack_vertices)
+    build_light_tables = staticmethod(context.build_light_tables)
+
+
+def default_material(host=None, **overrides) -> np.ndarray:
+    m = (host or ProductHost).default_material()
     for k, v in overrides.items():
         m[k] = v
     return m
 
 
-def default_scene_data(width: int, height: int) -> np.ndarray:
-    sd = np.zeros(1, dtype=abi.SCENE_DATA)
-    abi.load().vkrt_host_default_scene_data(width, height, abi.ptr(sd))
-    return sd
+def default_scene_data(width: int, height: int, host=None) -> np.ndarray:
+    return (host or ProductHost).default_scene_data(width, height)
 
 
-def set_camera(sd: np.ndarray, pos, target, up=(0.0, 0.0, 1.0), vfov: float = 40.0) -> None:
-    p = np.array(pos, dtype=np.float32)
-    t = np.array(target, dtype=np.float32)
-    u = np.array(up, dtype=np.float32)
-    w, h = int(sd["viewportRect"][0][2]), int(sd["viewportRect"][0][3])
-    abi.load().vkrt_host_camera_matrices(abi.ptr(p), abi.ptr(t), abi.ptr(u), vfov, 0.001, 10000.0, w, h, abi.ptr(sd))
+def set_camera(sd: np.ndarray, pos, target, up=(0.0, 0.0, 1.0), vfov: float = 40.0, host=None) -> None:
+    (host or ProductHost).camera_matrices(sd, pos, target, up, vfov)
 
 
 def _quad(p0, p1, p2, p3, normal):
@@ -80,7 +107,7 @@ def _box(sx, sy, sz):
     return np.concatenate(vs), np.concatenate(ids)
 
 
-def _assemble(parts, materials, scene_data, name) -> Scene:
+def _assemble(parts, materials, scene_data, name, host=None) -> Scene:
     """parts: list of (vertices, mesh-relative indices, material index, position, rotation, scale)."""
     verts, idxs = [], []
     meshes = np.zeros(len(parts), dtype=abi.MESH_INFO)
@@ -101,22 +128,32 @@ def _assemble(parts, materials, scene_data, name) -> Scene:
         ib += len(i)
     s = Scene(vertices=np.concatenate(verts), indices=np.concatenate(idxs), meshes=meshes,
               materials=np.concatenate(materials), scene_data=scene_data, name=name)
-    build_light_tables(s)
+    _finish(s, host)
     return s
 
 
+def _finish(s: Scene, host) -> None:
+    """Light tables, and with a host other than the product library the packed vertices too (so that nothing
+    downstream packs them through the product library)."""
+    host = host or ProductHost
+    host.build_light_tables(s)
+    if host is not ProductHost:
+        s.shader_vertices = host.pack_vertices(s.vertices)
+
+
 def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 8,
-            wall_textures: list | None = None) -> Scene:
+            wall_textures: list | None = None, host=None) -> Scene:
     """The Cornell box. With `wall_textures` (five (albedo, roughness) pairs of float32 (H, W) or (H, W, 3)
     arrays, for floor, ceiling, back, left, right), each wall gets its own material whose base colour (1, 1, 1) is
     multiplied by the albedo texture (slot 2k) and whose roughness 1 by the G channel of a metallic-roughness
     texture (slot 2k + 1); walls stay Lambertian (specular 0), so roughness acts through the dielectric
     directional-albedo attenuation of the Lambert lobe."""
     lamb = dict(metallic=0.0, roughness=1.0, specular=0.0, diffuseRoughness=0.0)
-    mats = [default_material(baseColor=(0.73, 0.73, 0.73), **lamb),
-            default_material(baseColor=(0.65, 0.05, 0.05), **lamb),
-            default_material(baseColor=(0.12, 0.45, 0.15), **lamb),
-            default_material(baseColor=(0.0, 0.0, 0.0), emissionColor=(1.0, 1.0, 1.0), emissionLuminance=15.0, **lamb)]
+    mats = [default_material(host, baseColor=(0.73, 0.73, 0.73), **lamb),
+            default_material(host, baseColor=(0.65, 0.05, 0.05), **lamb),
+            default_material(host, baseColor=(0.12, 0.45, 0.15), **lamb),
+            default_material(host, baseColor=(0.0, 0.0, 0.0), emissionColor=(1.0, 1.0, 1.0), emissionLuminance=15.0,
+                             **lamb)]
     WHITE, RED, GREEN, LIGHT = 0, 1, 2, 3
     textures = {}
     wall_mats = [WHITE, WHITE, WHITE, RED, GREEN]
@@ -126,7 +163,7 @@ def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 
         for k, (alb, rough) in enumerate(wall_textures):
             textures[2 * k] = albedo_texture(alb)
             textures[2 * k + 1] = roughness_texture(rough)
-            mats.append(default_material(baseColor=(1.0, 1.0, 1.0), baseColorTextureIndex=2 * k,
+            mats.append(default_material(host, baseColor=(1.0, 1.0, 1.0), baseColorTextureIndex=2 * k,
                                          metallicRoughnessTextureIndex=2 * k + 1, **lamb))
             wall_mats[k] = len(mats) - 1
     ident = ((0, 0, 0), (0, 0, 0), (1, 1, 1))
@@ -149,13 +186,13 @@ def cornell(width: int = 256, height: int = 256, spp: int = 1, max_depth: int = 
     parts.append((sv, si, WHITE, (0.68, 0.32, 0.0), (0.0, 0.0, -18.0), (1, 1, 1)))
     tv, ti = _box(0.3, 0.3, 0.6)
     parts.append((tv, ti, WHITE, (0.32, 0.65, 0.0), (0.0, 0.0, 18.0), (1, 1, 1)))
-    sd = default_scene_data(width, height)
-    set_camera(sd, (0.5, -1.35, 0.5), (0.5, 0.5, 0.5))
+    sd = default_scene_data(width, height, host)
+    set_camera(sd, (0.5, -1.35, 0.5), (0.5, 0.5, 0.5), host=host)
     sd["samplesPerPixel"] = spp
     sd["rrMaxDepth"] = max_depth
     sd["environmentLight"] = (0.0, 0.0, 0.0, 0.0)
     sd["packedRenderSettings"] = abi.pack_render_settings(abi.TONE_MAPPING_ACES, abi.RENDER_MODE_RGB, abi.SPECTRAL_HERO)
-    scene = _assemble(parts, mats, sd, "cornell")
+    scene = _assemble(parts, mats, sd, "cornell", host)
     scene.textures = textures
     return scene
 
@@ -201,18 +238,24 @@ def inverse_rendering_cornell(width: int = 128, height: int = 128, spp: int = 16
     return s
 
 
-def batch_workload(count: int = 64, seed: int = 2, spp: int = 8, max_depth: int = 10,
-                   tri_range=(10_000, 500_000), resolutions=(256, 512, 768, 1024)) -> list[Scene]:
-    """Uneven batch: `count` icosphere fields built as icosphere_field with triangle counts log-uniform over
-    tri_range (1,280 triangles per sphere), square resolutions drawn uniformly from `resolutions`, RGB transport."""
+def batch_specs(count: int = 64, seed: int = 2, spp: int = 8, max_depth: int = 10,
+                tri_range=(10_000, 500_000), resolutions=(256, 512, 768, 1024)) -> list[dict]:
+    """icosphere_field arguments of the uneven batch's scenes: triangle counts log-uniform over tri_range (1,280
+    triangles per sphere), square resolutions drawn uniformly from `resolutions`, RGB transport."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
         tris = math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))
         res = int(rng.choice(resolutions))
-        out.append(icosphere_field(n_spheres=max(1, int(round(tris / 1280))), width=res, height=res, spp=spp,
-                                   max_depth=max_depth, seed=int(seed * 1000 + k), spectral=False))
+        out.append(dict(n_spheres=max(1, int(round(tris / 1280))), width=res, height=res, spp=spp,
+                        max_depth=max_depth, seed=int(seed * 1000 + k), spectral=False))
     return out
+
+
+def batch_workload(count: int = 64, seed: int = 2, spp: int = 8, max_depth: int = 10,
+                   tri_range=(10_000, 500_000), resolutions=(256, 512, 768, 1024)) -> list[Scene]:
+    """Uneven batch: `count` icosphere fields built as icosphere_field from batch_specs."""
+    return [icosphere_field(**p) for p in batch_specs(count, seed, spp, max_depth, tri_range, resolutions)]
 
 
 def unit_icosphere(subdivisions: int = 3) -> tuple[np.ndarray, np.ndarray]:
@@ -281,7 +324,7 @@ def sky_environment(width: int = 1024, height: int = 512, seed: int = 1, sun_rad
 
 def icosphere_field(n_spheres: int = 800, width: int = 1920, height: int = 1080, spp: int = 16, max_depth: int = 12,
                     seed: int = 1, spectral: bool = True, env_size=(1024, 512), subdivisions: int = 3,
-                    extent: float = 10.0) -> Scene:
+                    extent: float = 10.0, host=None) -> Scene:
     rng = np.random.default_rng(seed)
     centers = rng.uniform(-extent, extent, size=(n_spheres, 3))
     radii = np.exp(rng.uniform(math.log(0.1), math.log(1.0), size=n_spheres))
@@ -313,14 +356,14 @@ def icosphere_field(n_spheres: int = 800, width: int = 1920, height: int = 1080,
     meshes["materialIndex"] = np.arange(n_spheres, dtype=np.uint32)
     meshes["scale"] = 1.0
     meshes["opacity"] = 1.0
-    mats = np.concatenate([default_material() for _ in range(n_spheres)])
+    mats = np.repeat(default_material(host), n_spheres)
     mats["baseColor"] = base_color.astype(np.float32)
     mats["roughness"] = roughness.astype(np.float32)
     mats["metallic"] = metallic
     mats["specular"] = 0.5
     mats["ior"] = 1.5
-    sd = default_scene_data(width, height)
-    set_camera(sd, (0.0, -30.0, 6.0), (0.0, 0.0, 0.0))
+    sd = default_scene_data(width, height, host)
+    set_camera(sd, (0.0, -30.0, 6.0), (0.0, 0.0, 0.0), host=host)
     sd["samplesPerPixel"] = spp
     sd["rrMaxDepth"] = max_depth
     mode = abi.RENDER_MODE_SPECTRAL if spectral else abi.RENDER_MODE_RGB
@@ -330,5 +373,5 @@ def icosphere_field(n_spheres: int = 800, width: int = 1920, height: int = 1080,
     sd["environmentLight"] = (1.0, 1.0, 1.0, 1.0)
     s = Scene(vertices=verts, indices=indices, meshes=meshes, materials=mats, scene_data=sd,
               textures={0: env}, env_texture=0, name=f"icospheres{n_spheres}")
-    build_light_tables(s)
+    _finish(s, host)
     return s
