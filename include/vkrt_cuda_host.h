@@ -73,6 +73,15 @@ void vkrt_host_auto_spp_init(VKRT_CudaAutoSpp* state, uint32_t targetFPS);
  * step limits, in [1, 2048]. Returns 1 when *samplesPerPixel changed, 0 when not, -1 on invalid arguments. */
 int32_t vkrt_host_auto_spp_update(VKRT_CudaAutoSpp* state, float renderMs, uint32_t* samplesPerPixel);
 
+/* Reverses the scanline filters of a PNG image (PNG specification, 2nd ed., section 9: filter method 0, types 0 None,
+ * 1 Sub, 2 Up, 3 Average, 4 Paeth), the step of image decoding that vkrt's texture import leaves to libspng
+ * (src/core/utility/image.c:122-192, decodePNGImage). `src` holds `height` filtered scanlines of 1 + rowBytes bytes,
+ * the filter-type byte first, as inflated from the IDAT stream (one Adam7 pass for interlaced images); `dst`
+ * receives height x rowBytes reconstructed bytes. bytesPerPixel is the byte distance the Sub, Average and Paeth
+ * predictors look back (at least 1). Returns 0, or -1 on an unknown filter type or invalid arguments. */
+int32_t vkrt_host_png_unfilter(const uint8_t* src, uint32_t height, uint64_t rowBytes, uint32_t bytesPerPixel,
+                               uint8_t* dst);
+
 #ifdef __cplusplus
 }
 #endif

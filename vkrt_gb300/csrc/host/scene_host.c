@@ -496,3 +496,52 @@ int32_t vkrt_host_auto_spp_update(VKRT_CudaAutoSpp* state, float renderMs, uint3
     *samplesPerPixel = next;
     return 1;
 }
+
+/* ---- PNG scanline filters (PNG specification, section 9) ----------------------------------------------------- */
+
+static uint8_t paeth_predictor(int a, int b, int c) {
+    int p = a + b - c;
+    int pa = abs(p - a), pb = abs(p - b), pc = abs(p - c);
+    if (pa <= pb && pa <= pc) return (uint8_t)a;
+    return (uint8_t)(pb <= pc ? b : c);
+}
+
+int32_t vkrt_host_png_unfilter(const uint8_t* src, uint32_t height, uint64_t rowBytes, uint32_t bytesPerPixel,
+                               uint8_t* dst) {
+    if ((!src || !dst) && height > 0u) return -1;
+    if (bytesPerPixel == 0u) return -1;
+    const size_t n = (size_t)rowBytes, bpp = bytesPerPixel;
+    for (uint32_t y = 0; y < height; ++y) {
+        const uint8_t* in = src + (size_t)y * (n + 1u);
+        uint8_t* out = dst + (size_t)y * n;
+        const uint8_t* up = y > 0u ? out - n : NULL; /* the previous reconstructed row; zeros above the first */
+        const uint8_t type = in[0];
+        ++in;
+        switch (type) {
+            case 0:
+                memcpy(out, in, n);
+                break;
+            case 1:
+                for (size_t i = 0; i < n; ++i) out[i] = (uint8_t)(in[i] + (i >= bpp ? out[i - bpp] : 0));
+                break;
+            case 2:
+                for (size_t i = 0; i < n; ++i) out[i] = (uint8_t)(in[i] + (up ? up[i] : 0));
+                break;
+            case 3:
+                for (size_t i = 0; i < n; ++i) {
+                    int a = i >= bpp ? out[i - bpp] : 0, b = up ? up[i] : 0;
+                    out[i] = (uint8_t)(in[i] + ((a + b) >> 1));
+                }
+                break;
+            case 4:
+                for (size_t i = 0; i < n; ++i) {
+                    int a = i >= bpp ? out[i - bpp] : 0, b = up ? up[i] : 0, c = (i >= bpp && up) ? up[i - bpp] : 0;
+                    out[i] = (uint8_t)(in[i] + paeth_predictor(a, b, c));
+                }
+                break;
+            default:
+                return -1;
+        }
+    }
+    return 0;
+}
