@@ -8,10 +8,11 @@ import struct
 import numpy as np
 
 
-def write_glb(path, meshes, nodes=None, materials=None):
+def write_glb(path, meshes, nodes=None, materials=None, images=None, textures=None, samplers=None):
     """meshes: list of dicts with 'positions' (n, 3) and optional 'normals', 'uv', 'tangents' (n, 4), 'indices',
     'material'. nodes: list of dicts (glTF node fields: 'mesh', 'translation', 'rotation', 'scale', 'children',
-    'name'); default one node per mesh. materials: list of glTF material dicts."""
+    'name'); default one node per mesh. materials: list of glTF material dicts. images: list of (bytes, MIME type)
+    stored in buffer views, or {'uri': ...} dicts; textures and samplers: glTF dicts."""
     blob = bytearray()
     views, accessors = [], []
 
@@ -52,6 +53,24 @@ def write_glb(path, meshes, nodes=None, materials=None):
            "buffers": [{"byteLength": len(blob)}]}
     if materials:
         doc["materials"] = materials
+    if images:
+        gl_images = []
+        for im in images:
+            if isinstance(im, dict):
+                gl_images.append(im)
+                continue
+            data, mime = im
+            while len(blob) % 4:
+                blob += b"\0"
+            views.append({"buffer": 0, "byteOffset": len(blob), "byteLength": len(data)})
+            blob += data
+            gl_images.append({"bufferView": len(views) - 1, "mimeType": mime})
+        doc["images"] = gl_images
+        doc["buffers"][0]["byteLength"] = len(blob)
+    if textures:
+        doc["textures"] = textures
+    if samplers:
+        doc["samplers"] = samplers
     js = json.dumps(doc).encode()
     js += b" " * (-len(js) % 4)
     while len(blob) % 4:

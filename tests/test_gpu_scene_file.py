@@ -131,3 +131,75 @@ def test_dispersive_prism_scene_matches_oracle(built, tmp_path, integrator):
     s0.rgb2spec, s0.scene_data = s.rgb2spec, s.scene_data.copy()
     ref0, _ = cpu.OracleScene(s0).render(s0.scene_data, rng_mode=abi.RNG_REFERENCE)
     assert (np.abs(ref0[..., :3] - ref[..., :3]).max(-1) > 1e-3).mean() > 0.01
+
+
+def _textured_room(tmp_path):
+    """A floor imported with a textured glTF material (8-bit sRGB base-colour checker, 16-bit metallic-roughness
+    with roughness in G and metallic in B, normal map, clamp / mirror samplers), a metal ball and a light."""
+    from png_writer import encode_png
+    yy, xx = np.mgrid[0:32, 0:32]
+    checker = np.where(((yy // 4) + (xx // 4)) % 2 == 0, 220, 40)
+    base = np.stack([checker, checker // 2 + 60, 255 - checker, np.full_like(checker, 255)], -1)
+    mr = np.zeros((16, 16, 3), np.int64)
+    mr[..., 1] = (np.linspace(0.2, 1.0, 16)[None, :] * 65535).astype(np.int64)   # roughness
+    mr[..., 2] = np.where(np.arange(16)[:, None] < 8, 0, 65535)                   # metallic bands
+    nrm = np.zeros((8, 8, 3), np.int64)
+    nrm[..., 0] = 128 + (np.arange(8)[None, :] - 4) * 12
+    nrm[..., 1] = 128
+    nrm[..., 2] = 240
+    images = [(encode_png(base, 8, 6), "image/png"), (encode_png(mr, 16, 2), "image/png"),
+              (encode_png(nrm, 8, 2), "image/png")]
+    material = {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "metallicRoughnessTexture": {"index": 1},
+                                         "metallicFactor": 1.0, "roughnessFactor": 1.0},
+                "normalTexture": {"index": 2, "scale": 0.8}}
+    floor = plane_mesh()
+    floor["material"] = 0
+    write_glb(tmp_path / "floor.glb", [floor], materials=[material], images=images,
+              textures=[{"source": 0, "sampler": 0}, {"source": 1, "sampler": 1}, {"source": 2}],
+              samplers=[{"wrapS": abi.WRAP_MIRROR, "wrapT": abi.WRAP_CLAMP}, {"wrapS": abi.WRAP_CLAMP}])
+    write_glb(tmp_path / "sphere.glb", [icosphere_mesh(3)])
+    write_glb(tmp_path / "plane.glb", [plane_mesh()])
+    mesh = {"renderBackfaces": False, "opacity": 1, "importLocalIndex": 0}
+    doc = {"format": "vkrt.scene", "version": 1, "meshImports": ["floor.glb", "sphere.glb", "plane.glb"],
+           "materials": [{"index": 2, "name": "ball", "material": {"baseColor": [0.9, 0.8, 0.6], "metallic": 1,
+                                                                   "roughness": 0.2}},
+                         {"index": 3, "name": "light", "material": {"roughness": 1, "emissionLuminance": 12}}],
+           "meshes": [dict(mesh, name="floor", materialIndex=1, hasMaterialAssignment=True, importIndex=0),
+                      dict(mesh, name="ball", materialIndex=2, hasMaterialAssignment=True, importIndex=1),
+                      dict(mesh, name="light", materialIndex=3, hasMaterialAssignment=True, importIndex=2)],
+           "sceneObjects": [{"name": "floor", "parentIndex": None, "meshIndex": 0, "localPosition": [0, 0, -0.5],
+                             "localRotation": [0, 0, 15], "localScale": [1.5, 1.5, 1.5]},
+                            {"name": "ball", "parentIndex": None, "meshIndex": 1, "localPosition": [0.2, 0.1, -0.1],
+                             "localRotation": [0, 0, 0], "localScale": [0.4, 0.4, 0.4]},
+                            {"name": "light", "parentIndex": None, "meshIndex": 2, "localPosition": [0, 0, 1.2],
+                             "localRotation": [180, 0, 0], "localScale": [0.4, 0.4, 0.4]}],
+           "sceneSettings": {"camera": {"position": [0, -3.2, 1.4], "target": [0, 0, -0.4], "up": [0, 0, 1],
+                                        "vfov": 40},
+                             "rrMinDepth": 4, "rrMaxDepth": 8, "toneMappingMode": 1, "renderMode": 0,
+                             "spectralSamplingMode": 1, "exposure": 1, "environmentColor": [0.3, 0.35, 0.4],
+                             "environmentStrength": 1, "environmentRotation": 0, "misNeeEnabled": True}}
+    p = tmp_path / "textured.json"
+    p.write_text(json.dumps(doc))
+    return p
+
+
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
+def test_textured_scene_file_matches_oracle(built, tmp_path, integrator):
+    """Decoded PNG textures (base colour, metallic-roughness, normal map) render per sample as the oracle renders
+    the same texels."""
+    from oracle import cpu
+    s = scene_file.load_scene_file(_textured_room(tmp_path), 96, 80)
+    assert len(s.textures) == 3 and s.materials[1]["baseColorTextureIndex"] == 0
+    sd = s.scene_data.copy()
+    sd["samplesPerPixel"] = 4
+    s.scene_data = sd
+    with RenderContext(rng_mode=abi.RNG_REFERENCE, integrator=integrator) as ctx:
+        ctx.upload_scene(s)
+        ctx.render_frame(sd)
+        gpu = ctx.read_accumulation()
+    ref, _ = cpu.OracleScene(s).render(sd, rng_mode=abi.RNG_REFERENCE)
+    assert_match(None, gpu, ref, 1e-3, 1e-3, max_outside=4)
+    # the checker shows: the floor's pixels spread over a wide range of blue / red ratios
+    floor = gpu[60:, :, :3]
+    ratio = (floor[..., 2] + 1e-3) / (floor[..., 0] + 1e-3)
+    assert np.percentile(ratio, 90) > 2.0 * np.percentile(ratio, 10)

@@ -14,8 +14,15 @@ vkrt's importer (src/app/mesh/loader.c):
   colour x luminance, KHR_materials_ior / specular / transmission / volume / clearcoat / sheen / emissive_strength
   factors, double-sided -> render backfaces, alpha modes.
 
-Textures referenced by materials are not decoded (no image codec in this package): their factors are kept and the
-texture slots stay unbound; `GltfImport.ignored` lists what was skipped.
+* textures (loader.c:309-404, 702-736, 907-1011, 1472-1535): per material in order, the base colour (or
+  specular-glossiness diffuse) texture read as sRGB, the metallic-roughness texture, the normal texture (linear) and
+  the emissive texture (sRGB), each image decoded once per colour space and numbered in registration order; a texture
+  on a texture-coordinate set above 1 is not bound; the sampler's wrap modes (repeat by default), the texture
+  coordinate set, KHR_texture_transform scale / offset / rotation and the normal scale go into the material. Images
+  come from files beside the glTF document or from buffer views (vkrt decodes no data-URI image); PNG is decoded
+  (vkrt_gb300.image_decode), JPEG and EXR images are left unbound.
+
+`GltfImport.ignored` lists what was skipped.
 """
 from __future__ import annotations
 
@@ -50,9 +57,10 @@ class MeshEntry:
 @dataclass
 class GltfImport:
     entries: list
-    materials: np.ndarray         # abi.MATERIAL, one per glTF material
+    materials: np.ndarray         # abi.MATERIAL, one per glTF material; texture indices into `textures`
     node_world: list              # per visited node: 4x4 world matrix (vkrt basis, column vectors)
     ignored: set = field(default_factory=set)
+    textures: list = field(default_factory=list)  # image_decode.DecodedImage, in registration order
 
 
 # ---- container ----------------------------------------------------------------------------------------------------
@@ -304,8 +312,87 @@ def _primitive(doc, buffers, prim, name, node_index, ignored):
                      render_backfaces=1 if material and material.get("doubleSided", False) else 0, node=node_index)
 
 
+# ---- textures -----------------------------------------------------------------------------------------------------
+SLOT_BASE_COLOR, SLOT_METALLIC_ROUGHNESS, SLOT_NORMAL, SLOT_EMISSIVE = 0, 1, 2, 3  # VKRT_MATERIAL_TEXTURE_SLOT_*
+_SLOT_FIELDS = {SLOT_BASE_COLOR: "baseColor", SLOT_METALLIC_ROUGHNESS: "metallicRoughness", SLOT_NORMAL: "normal",
+                SLOT_EMISSIVE: "emissive"}
+
+
+class _Textures:
+    """Decoded images of one document, each registered once per (image, colour space) (registerImportedTexture)."""
+
+    def __init__(self, doc, buffers, base: Path, ignored: set):
+        self.doc, self.buffers, self.base, self.ignored = doc, buffers, base, ignored
+        self.images: list = []
+        self.cache: dict = {}
+
+    @staticmethod
+    def texcoord_set(view) -> int:  # queryTextureViewTexcoordSet (loader.c:380-386)
+        t = view.get("extensions", {}).get("KHR_texture_transform", {})
+        if "texCoord" in t and int(t["texCoord"]) >= 0:
+            return int(t["texCoord"])
+        return max(int(view.get("texCoord", 0)), 0)
+
+    def _bytes(self, image):
+        uri = image.get("uri")
+        if uri and not uri.startswith("data:"):
+            return (self.base / uri).read_bytes(), image.get("mimeType")
+        if "bufferView" in image:
+            bv = self.doc["bufferViews"][image["bufferView"]]
+            off, n = bv.get("byteOffset", 0), bv["byteLength"]
+            return bytes(self.buffers[bv["buffer"]][off:off + n]), image.get("mimeType")
+        return None, None
+
+    def register(self, view, color_space: int):
+        """Import-local texture index of `view`, or None when it does not bind."""
+        from .image_decode import ImageDecodeError, UnsupportedImage, decode_image
+        if not view or "index" not in view:
+            return None
+        if self.texcoord_set(view) > 1:  # textureViewUsesUnsupportedTransform (loader.c:1183-1186)
+            self.ignored.add("textures on texture-coordinate sets above 1")
+            return None
+        tex = self.doc.get("textures", [])[view["index"]]
+        if "source" not in tex:
+            return None
+        key = (tex["source"], color_space)
+        if key not in self.cache:
+            data, mime = self._bytes(self.doc["images"][tex["source"]])
+            if data is None:
+                self.ignored.add("data-URI images")
+                self.cache[key] = None
+            else:
+                try:
+                    self.images.append(decode_image(data, mime, color_space))
+                    self.cache[key] = len(self.images) - 1
+                except (UnsupportedImage, ImageDecodeError) as e:
+                    self.ignored.add(f"textures ({e})")
+                    self.cache[key] = None
+        return self.cache[key]
+
+    def bind(self, m: np.ndarray, slot: int, view, color_space: int) -> None:
+        """Binds `view` to material slot `slot`: index, wrap modes, coordinate set, transform and rotation."""
+        idx = self.register(view, color_space)
+        if idx is None:
+            return
+        f = _SLOT_FIELDS[slot]
+        m[f + "TextureIndex"] = idx
+        sampler = self.doc["samplers"][self.doc["textures"][view["index"]]["sampler"]] \
+            if "sampler" in self.doc["textures"][view["index"]] else {}
+        ws, wt = int(sampler.get("wrapS", abi.WRAP_REPEAT)), int(sampler.get("wrapT", abi.WRAP_REPEAT))
+        m[f + "TextureWrap"] = (ws or abi.WRAP_REPEAT) | ((wt or abi.WRAP_REPEAT) << 16)  # packTextureWrapModes
+        shift = 8 * slot
+        sets = int(m["textureTexcoordSets"][0])
+        m["textureTexcoordSets"] = (sets & ~(0xFF << shift)) | ((self.texcoord_set(view) & 0xFF) << shift)
+        t = view.get("extensions", {}).get("KHR_texture_transform")
+        if t is not None:  # copyTextureTransform (loader.c:388-404)
+            sc, of = t.get("scale", [1.0, 1.0]), t.get("offset", [0.0, 0.0])
+            m[f + "TextureTransform"] = (sc[0], sc[1], of[0], of[1])
+            m["textureRotations"][0, slot] = t.get("rotation", 0.0)
+
+
 # ---- materials ----------------------------------------------------------------------------------------------------
-def _material(src, default, ignored) -> np.ndarray:
+def _material(src, default, ignored, textures: _Textures | None = None) -> np.ndarray:
+    from .abi import COLOR_SPACE_LINEAR, COLOR_SPACE_SRGB
     m = default.copy()
     ext = src.get("extensions", {})
     if "KHR_materials_pbrSpecularGlossiness" in ext:
@@ -314,8 +401,8 @@ def _material(src, default, ignored) -> np.ndarray:
         m["baseColor"] = d[:3]
         m["opacity"] = d[3]
         m["roughness"] = 1.0 - sg.get("glossinessFactor", 1.0)
-        if "diffuseTexture" in sg:
-            ignored.add("textures")
+        if textures is not None:
+            textures.bind(m, SLOT_BASE_COLOR, sg.get("diffuseTexture"), COLOR_SPACE_SRGB)
     elif "pbrMetallicRoughness" in src:  # without it vkrt keeps its default material factors (loader.c:966)
         pbr = src["pbrMetallicRoughness"]
         c = pbr.get("baseColorFactor", [1, 1, 1, 1])
@@ -323,8 +410,9 @@ def _material(src, default, ignored) -> np.ndarray:
         m["opacity"] = c[3]
         m["metallic"] = pbr.get("metallicFactor", 1.0)
         m["roughness"] = pbr.get("roughnessFactor", 1.0)
-        if "baseColorTexture" in pbr or "metallicRoughnessTexture" in pbr:
-            ignored.add("textures")
+        if textures is not None:
+            textures.bind(m, SLOT_BASE_COLOR, pbr.get("baseColorTexture"), COLOR_SPACE_SRGB)
+            textures.bind(m, SLOT_METALLIC_ROUGHNESS, pbr.get("metallicRoughnessTexture"), COLOR_SPACE_LINEAR)
     if "KHR_materials_specular" in ext:
         m["specular"] = ext["KHR_materials_specular"].get("specularFactor", 1.0)
     if "KHR_materials_ior" in ext:
@@ -355,8 +443,15 @@ def _material(src, default, ignored) -> np.ndarray:
     else:
         m["emissionColor"] = 1.0
         m["emissionLuminance"] = 0.0
-    if "normalTexture" in src or "emissiveTexture" in src or "occlusionTexture" in src:
-        ignored.add("textures")
+    if textures is not None:
+        nt = src.get("normalTexture")
+        textures.bind(m, SLOT_NORMAL, nt, COLOR_SPACE_LINEAR)
+        if m["normalTextureIndex"][0] != abi.INVALID_INDEX:
+            scale = float(nt.get("scale", 1.0))
+            m["normalTextureScale"] = scale if scale > 0.0 else 1.0
+        textures.bind(m, SLOT_EMISSIVE, src.get("emissiveTexture"), COLOR_SPACE_SRGB)
+    if "occlusionTexture" in src:
+        ignored.add("occlusion textures")  # vkrt's materials have no occlusion input
     mode = src.get("alphaMode", "OPAQUE")
     if mode == "MASK":
         m["alphaMode"] = ALPHA_MODE_MASK
@@ -383,7 +478,8 @@ def load_gltf(path) -> GltfImport:
         if doc.get(key):
             ignored.add(label)
     base = default_material()
-    materials = (np.concatenate([_material(src, base, ignored) for src in doc.get("materials", [])])
+    textures = _Textures(doc, buffers, path.parent, ignored)
+    materials = (np.concatenate([_material(src, base, ignored, textures) for src in doc.get("materials", [])])
                  if doc.get("materials") else np.zeros(0, dtype=abi.MATERIAL))
     nodes = doc.get("nodes", [])
     scene = doc.get("scene")
@@ -411,4 +507,5 @@ def load_gltf(path) -> GltfImport:
             stack.append((c, world))
     if not entries:
         raise ValueError(f"{path}: no triangle mesh primitives")
-    return GltfImport(entries=entries, materials=materials, node_world=node_world, ignored=ignored)
+    return GltfImport(entries=entries, materials=materials, node_world=node_world, ignored=ignored,
+                      textures=textures.images)

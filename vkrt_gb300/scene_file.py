@@ -2,7 +2,12 @@
 (src/app/scene/controller.c:1528-1595 and the steps it calls):
 
 * meshImports (controller.c:1241-1271): each glTF file, resolved against the scene file's folder, is imported with
-  vkrt_gb300.gltf; its mesh entries are appended in order, its materials after vkrt's default material 0;
+  vkrt_gb300.gltf; its mesh entries are appended in order, its materials after vkrt's default material 0, its
+  textures after the scene's textures so far, its materials' texture indices moved with them
+  (mesh/controller.c:159-181, 394-412);
+* textureImports (controller.c:1274-1300): each standalone image is loaded in its saved colour space and appended;
+  saved materials name textures by their saved index, which is remapped to the new one (controller.c:640-661);
+  images of a format this package does not decode (JPEG, EXR) are left out and noted, where vkrt decodes them;
 * meshes (controller.c:1314-1455): each saved mesh names (importIndex, importLocalIndex); meshes no saved mesh names are
   dropped, the rest keep their import order; name, material (hasMaterialAssignment ? materialIndex : 0), backface
   rendering and opacity are applied;
@@ -165,9 +170,11 @@ def load_scene_file(path, width: int = 1280, height: int = 720, missing: str = "
             or not isinstance(doc.get("meshImports"), list) or not isinstance(doc.get("meshes"), list)
             or not isinstance(doc.get("sceneObjects"), list) or not isinstance(doc.get("sceneSettings"), dict)):
         raise SceneFileError(f"{path}: not a {SCENE_FORMAT} version {SCENE_VERSION} document")
+    from .image_decode import ImageDecodeError, UnsupportedImage, decode_image, texture_texels
     notes = []
     base = gltf.default_material()
     materials = [base.copy()]
+    images = []   # decoded textures in scene order
     batches = []  # per import: (first loaded mesh, entries) or None when skipped
     loaded = []   # loaded mesh entries in import order: (entry, material index, node world)
     for k, rel in enumerate(doc["meshImports"]):
@@ -180,16 +187,38 @@ def load_scene_file(path, width: int = 1280, height: int = 720, missing: str = "
             raise SceneFileError(f"{path}: mesh import {rel} not found")
         imp = gltf.load_gltf(f)
         first_material = len(materials)
-        materials.extend(m.reshape(1) for m in imp.materials)
+        first_texture = len(images)
+        images.extend(imp.textures)
+        for m in imp.materials:
+            m = m.reshape(1).copy()
+            for slot in ("baseColor", "metallicRoughness", "normal", "emissive"):
+                t = int(m[slot + "TextureIndex"][0])
+                if t != abi.INVALID_INDEX:
+                    m[slot + "TextureIndex"] = first_texture + t if t < len(imp.textures) else abi.INVALID_INDEX
+            materials.append(m)
         batches.append((len(loaded), len(imp.entries)))
         for e in imp.entries:
             mat = first_material + e.material if e.material != abi.INVALID_INDEX else 0
             loaded.append((e, mat, imp.node_world[e.node]))
         notes.extend(f"{rel}: {what} ignored" for what in sorted(imp.ignored))
-    if doc.get("textureImports"):
-        notes.append("textureImports ignored (no image decoding)")
+    saved_texture = {}  # saved texture index -> scene texture index
+    for k, to in enumerate(doc.get("textureImports") or []):
+        if not isinstance(to, dict) or not isinstance(to.get("path"), str):
+            raise SceneFileError(f"textureImports {k}: index, colorSpace and path are required")
+        idx, cs = int(to["index"]), int(to["colorSpace"])
+        f = (path.parent / to["path"]).resolve()
+        if not f.exists():
+            if missing == "skip":
+                notes.append(f"texture {to['path']} is missing: skipped")
+                continue
+            raise SceneFileError(f"{path}: texture {to['path']} not found")
+        try:
+            images.append(decode_image(f.read_bytes(), None, cs))
+            saved_texture[idx] = len(images) - 1
+        except (UnsupportedImage, ImageDecodeError) as e:
+            notes.append(f"texture {to['path']} left out ({e})")
     if doc.get("environmentTexturePath"):
-        notes.append("environmentTexturePath ignored (no image decoding)")
+        notes.append("environmentTexturePath ignored (HDR / EXR environment images are not decoded here)")
 
     # saved meshes -> loaded entries
     saved_to_loaded = []
@@ -216,7 +245,12 @@ def load_scene_file(path, width: int = 1280, height: int = 720, missing: str = "
     for k, mo in enumerate(doc.get("materials") or []):
         if not isinstance(mo.get("name"), str):
             raise SceneFileError(f"material {k}: name is required")
-        materials[int(mo.get("index", k))] = parse_material(mo.get("material"), base)
+        m = parse_material(mo.get("material"), base)
+        for slot in ("baseColor", "metallicRoughness", "normal", "emissive"):
+            t = int(m[slot + "TextureIndex"][0])
+            if t in saved_texture:
+                m[slot + "TextureIndex"] = saved_texture[t]
+        materials[int(mo.get("index", k))] = m
     materials = np.concatenate(materials)
 
     mesh_mat = {old: mat for old, (_, mat, _) in enumerate(loaded)}
@@ -276,6 +310,7 @@ def load_scene_file(path, width: int = 1280, height: int = 720, missing: str = "
         raise SceneFileError(f"{path}: no meshes left to render")
     sd = scene_data_from_settings(doc["sceneSettings"], width, height)
     s = Scene(vertices=np.concatenate(verts), indices=np.concatenate(idxs), meshes=meshes, materials=materials,
-              scene_data=sd, name=path.stem, mesh_names=[names[old] for old in keep], notes=notes)
+              scene_data=sd, name=path.stem, mesh_names=[names[old] for old in keep], notes=notes,
+              textures={i: texture_texels(img) for i, img in enumerate(images)})
     build_light_tables(s)
     return s
