@@ -288,6 +288,35 @@ def convergence_measure(local: int, scene, max_frames: int = 96, ref_frames: int
     plain, first = curve(ctx, stream, enabled=0)
     cached, _ = curve(ctx, stream, enabled=1, terminationDepth=2, trainingPaths=65536, trainingSteps=4,
                       learningRate=1e-2, seed=3)
+    cached1, _ = curve(ctx, stream, enabled=1, terminationDepth=1, trainingPaths=65536, trainingSteps=4,
+                       learningRate=1e-2, seed=3)
+
+    # variance by path depth: two independent 8-frame renders per estimator; the variance term of relMSE at 128 spp
+    # is mean((A - B)^2 / (2 (ref^2 + 1e-2))). Paths truncated at depth d (rrMaxDepth = d) show the variance that
+    # the first d bounces carry, which a cache terminating paths there cannot remove.
+    ctx.nrc_configure(enabled=0)
+
+    def variance(max_depth, cache_depth=None):
+        if cache_depth is not None:
+            ctx.nrc_configure(enabled=1, terminationDepth=cache_depth, trainingPaths=65536, trainingSteps=4,
+                              learningRate=1e-2, seed=3)
+        imgs = []
+        for h in range(2):
+            ctx.reset_accumulation()
+            vsd = sd.copy()
+            vsd["rrMaxDepth"] = max_depth
+            for f in range(8):
+                vsd["frameNumber"] = 2_000_000 + h * 1000 + f
+                ctx.render_frame(vsd)
+            imgs.append(ctx.read_accumulation()[..., :3].astype(np.float64))
+        if cache_depth is not None:
+            ctx.nrc_configure(enabled=0)
+        return round(float(np.mean((imgs[0] - imgs[1]) ** 2 / (2.0 * den))), 7)
+
+    full_depth = int(sd["rrMaxDepth"][0])
+    var_by_depth = {"spp": 128, "full": variance(full_depth), "rrMaxDepth_2": variance(2),
+                    "rrMaxDepth_1": variance(1), "cache_depth_2": variance(full_depth, 2),
+                    "cache_depth_1": variance(full_depth, 1)}
     ctx.close()
     mctx, mstream = make(abi.INTEGRATOR_MEGAKERNEL)
     mega, _ = curve(mctx, mstream)
@@ -310,11 +339,14 @@ def convergence_measure(local: int, scene, max_frames: int = 96, ref_frames: int
                          "relmse_estimate": round(ref_err, 7), "seconds": round(ref_s, 1),
                          "fp64_same_seed_check": {"rows": len(rows), "spp": 16, "relmse_vs_oracle_fp64": val}},
            "metric": "relMSE = mean (x - ref)^2 / (ref^2 + 1e-2); reached_trimmed drops the 0.01% worst pixels",
-           "plain_wavefront": plain, "radiance_cache": cached, "plain_megakernel": mega}
+           "plain_wavefront": plain, "radiance_cache": cached, "radiance_cache_depth_1": cached1,
+           "plain_megakernel": mega, "variance_by_depth": var_by_depth}
     if plain["reached"] and mega["reached"]:
         out["wavefront_over_megakernel"] = round(plain["reached"]["ms"] / mega["reached"]["ms"], 4)
     if plain["reached"] and cached["reached"]:
         out["cache_over_plain_wavefront"] = round(cached["reached"]["ms"] / plain["reached"]["ms"], 4)
+    if plain["reached"] and cached1["reached"]:
+        out["cache_depth_1_over_plain_wavefront"] = round(cached1["reached"]["ms"] / plain["reached"]["ms"], 4)
     if cached["reached"] and mega["reached"]:
         out["cache_over_megakernel"] = round(cached["reached"]["ms"] / mega["reached"]["ms"], 4)
     return out
@@ -384,7 +416,7 @@ def batch_measure(local: int) -> dict:
             "speedup_vs_sequential_wavefront": round(wave_ms / batched, 2),
             "autotune_s": round(tune_s, 1),
             "autotuned": {k: int(best[k][0]) for k in ("queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
-                                                       "intersectBlocksPerSM", "shadeBlocksPerSM")}}
+                                                       "intersectBlocksPerSM", "shadeBlocksPerSM", "refillLanes")}}
 
 
 def selection_overlay_measure(ctx, sd, stream, torch) -> dict:
@@ -758,6 +790,10 @@ def run_profile_frame(args) -> dict:
         ctx.set_wavefront_config(profileStages=1)
     if args.shade_blocks:
         ctx.set_wavefront_config(shadeBlocksPerSM=args.shade_blocks)
+    if args.refill:
+        ctx.set_wavefront_config(refillLanes=args.refill)
+    if args.intersect_blocks:
+        ctx.set_wavefront_config(intersectBlocksPerSM=args.intersect_blocks)
     if args.cache:
         ctx.nrc_configure(enabled=1)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -782,7 +818,8 @@ def run_profile_frame(args) -> dict:
     out["workload"] = {"width": args.width, "height": args.height, "spp": args.spp, "depth": args.depth,
                        "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
-                       "cache": args.cache, "shade_blocks": args.shade_blocks}
+                       "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
+                       "intersect_blocks": args.intersect_blocks}
     ctx.close()
     return out
 
@@ -813,6 +850,8 @@ def main():
     prof.add_argument("--rgb", action="store_true", help="RGB transport instead of hero spectral")
     prof.add_argument("--cache", action="store_true", help="render with the radiance cache (wavefront only)")
     prof.add_argument("--shade-blocks", type=int, default=0, help="shade kernel residency (blocks per SM)")
+    prof.add_argument("--refill", type=int, default=0, help="traversal refill threshold (lanes; 0 = default)")
+    prof.add_argument("--intersect-blocks", type=int, default=0, help="traversal kernel residency (blocks per SM)")
     args = ap.parse_args()
     if args.profile_frame:
         print(json.dumps(run_profile_frame(args)))

@@ -50,7 +50,12 @@ typedef struct VKRT_CudaConfig {
     uint32_t threadsPerBlock;     /* megakernel block size, 0 = default (128) */
     uint32_t blocksPerSM;         /* reserved for the megakernel, 0 = default */
     uint32_t integrator;          /* VKRT_CUDA_INTEGRATOR_* */
-    uint32_t reserved[7];
+    uint32_t treeletMinTriangles; /* BVH builds of scenes with at least this many triangles run treelet
+                                     restructuring (Karras & Aila 2013: about 5% fewer node bytes per ray, several
+                                     times the build time); 0 = the default (65,536), 0xFFFFFFFF = never */
+    uint32_t treeletsOnUpdate;    /* 1: rebuilds after mesh-transform edits (vkrt_cuda_update_meshes) restructure too;
+                                     0 (default): they build the plain LBVH, so interactive edits stay fast */
+    uint32_t reserved[5];
 } VKRT_CudaConfig;
 
 /* Wavefront integrator parameters (autotuned by vkrt_cuda_autotune_batch). 64 bytes. */
@@ -66,7 +71,9 @@ typedef struct VKRT_CudaWavefrontConfig {
     uint32_t useGraph;             /* 1: the frame is one CUDA-graph launch (conditional while node) */
     uint32_t profileStages;        /* 1: stage-by-stage launches with device timers and fetch-byte counting (slower;
                                       for profiling), reported in VKRT_CudaStats.stageMs / *FetchBytes */
-    uint32_t reserved[8];
+    uint32_t refillLanes;          /* persistent traversal: a warp fetches new rays once fewer than this many of its
+                                      32 lanes are still traversing; 0 = the default (20), else 1..32 */
+    uint32_t reserved[7];
 } VKRT_CudaWavefrontConfig;
 
 typedef struct VKRT_CudaStats {
@@ -255,8 +262,9 @@ int32_t vkrt_cuda_trace_rays_device(VKRT_CudaContext* context, const VKRT_CudaRa
  * device arrays instead of per-call cudaMalloc buffers, so the call performs no allocation. At most 65,536 rays per
  * call (larger counts return VKRT_CUDA_ERROR_INVALID_ARGUMENT). The arrays (4 MiB) exist once per device and are
  * shared by every call on that device: calls that overlap on the GPU race and must be serialised by the caller.
- * The first call on a device resolves the arrays' addresses; make it before any stream capture. Host arrays;
- * synchronous. */
+ * The first call on a device resolves the arrays' addresses; make it before any stream capture. The resolved
+ * addresses are kept for the life of the process: after a cudaDeviceReset (or anything else that destroys and
+ * re-creates the device's primary context) this entry point must not be called again. Host arrays; synchronous. */
 int32_t vkrt_cuda_trace_rays_noalloc(VKRT_CudaContext* context, const VKRT_CudaRay* rays, uint32_t count,
                                      uint32_t anyHit, VKRT_CudaHit* hits);
 

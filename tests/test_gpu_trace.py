@@ -100,3 +100,39 @@ def test_icosphere_field_bit_exact(built):
         sec = _secondary(scene, hits, rays, 11)
         _check(scene, ctx, sec)
         _check(scene, ctx, sec, any_hit=True)
+
+
+def test_bvh_build_options(built):
+    """Treelet restructuring runs from treeletMinTriangles up (default 65,536) and, after mesh-transform edits, only
+    when treeletsOnUpdate asks; every variant of the tree traces bit for bit like the oracle."""
+    scene = scenes.icosphere_field(n_spheres=60, width=64, height=48, seed=4, spectral=False, env_size=(64, 32))
+    rays = _rays_from_camera(scene, 20000, 13)
+    with RenderContext() as ctx:  # 76,800 triangles: restructured
+        ctx.upload_scene(scene)
+        st = ctx.stats()
+        assert st["bvhSahTreelets"] < st["bvhSahLbvh"]
+        _check(scene, ctx, rays)
+        moved = scene.meshes.copy()
+        moved["position"][::7] += np.float32(0.5)  # a transform edit: rebuilt as the plain LBVH
+        ctx.update_meshes(moved)
+        st = ctx.stats()
+        assert st["bvhSahTreelets"] == st["bvhSahLbvh"]
+        edited = scenes.icosphere_field(n_spheres=60, width=64, height=48, seed=4, spectral=False, env_size=(64, 32))
+        edited.meshes = moved
+        _check(edited, ctx, rays)
+    with RenderContext(treelet_min_triangles=0xFFFFFFFF) as ctx:
+        ctx.upload_scene(scene)
+        st = ctx.stats()
+        assert st["bvhSahTreelets"] == st["bvhSahLbvh"]
+        _check(scene, ctx, rays)
+    with RenderContext(treelets_on_update=True) as ctx:
+        ctx.upload_scene(scene)
+        ctx.update_meshes(moved)
+        st = ctx.stats()
+        assert st["bvhSahTreelets"] < st["bvhSahLbvh"]
+        _check(edited, ctx, rays)
+    small = scenes.cornell(32, 32)
+    with RenderContext() as ctx:  # 36 triangles: no restructuring
+        ctx.upload_scene(small)
+        st = ctx.stats()
+        assert st["bvhSahTreelets"] == st["bvhSahLbvh"]

@@ -74,15 +74,16 @@ HIT = np.dtype({"names": ["instanceIndex", "primitiveIndex", "t", "u", "v", "res
                 "itemsize": 32})
 
 CONFIG = np.dtype({"names": ["deviceIndex", "rngMode", "rngSeed", "environmentSampling", "countRays",
-                             "threadsPerBlock", "blocksPerSM", "integrator", "reserved"],
-                   "formats": ["<i4", "<u4", "<u8", "<u4", "<u4", "<u4", "<u4", "<u4", ("<u4", 7)],
-                   "offsets": [0, 4, 8, 16, 20, 24, 28, 32, 36], "itemsize": 64})
+                             "threadsPerBlock", "blocksPerSM", "integrator", "treeletMinTriangles",
+                             "treeletsOnUpdate", "reserved"],
+                   "formats": ["<i4", "<u4", "<u8", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", ("<u4", 5)],
+                   "offsets": [0, 4, 8, 16, 20, 24, 28, 32, 36, 40, 44], "itemsize": 64})
 
 WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
                                        "intersectBlocksPerSM", "shadeBlocksPerSM", "useGraph", "profileStages",
-                                       "reserved"],
-                             "formats": ["<u4"] * 8 + [("<u4", 8)], "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32],
-                             "itemsize": 64})
+                                       "refillLanes", "reserved"],
+                             "formats": ["<u4"] * 9 + [("<u4", 7)],
+                             "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36], "itemsize": 64})
 
 STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathSamples", "nodeFetchBytes",
                             "triFetchBytes", "bvhNodeCount", "bvhTriangleCount", "bvhBytes", "bvhBuildMs",

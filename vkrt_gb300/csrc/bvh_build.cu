@@ -741,9 +741,11 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
         if (n > 1) kRefit<<<(n + b - 1) / b, b, 0, stream>>>(n, dLeft, dRight, dParent, dLo, dHi, dLeafCount, dCost, dFlags);
         if (n > 2) {
             kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah);
-            cudaMemsetAsync(dFlags, 0, sizeof(uint32_t) * n, stream);
-            kTreelets<<<(n + b - 1) / b, b, 0, stream>>>(n, kTreeletLeaves, dLeft, dRight, dParent, dLo, dHi, dLeafCount,
-                                                         dCost, dFlags);
+            if (in.treelets) {
+                cudaMemsetAsync(dFlags, 0, sizeof(uint32_t) * n, stream);
+                kTreelets<<<(n + b - 1) / b, b, 0, stream>>>(n, kTreeletLeaves, dLeft, dRight, dParent, dLo, dHi,
+                                                             dLeafCount, dCost, dFlags);
+            }
             kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah + 1);
         }
     }

@@ -182,7 +182,8 @@ bool isIdentityTRS(const VKRT_CudaMeshInfo& m) {
            m.scale[2] == 1.0f;
 }
 
-cudaError_t rebuildBvh(VKRT_CudaContext* c) {
+// afterEdit: the rebuild follows a mesh-transform edit (treelets only when the config asks for them there)
+cudaError_t rebuildBvh(VKRT_CudaContext* c, bool afterEdit) {
     std::vector<float> world(size_t(c->hostMeshes.size()) * 16);
     std::vector<uint32_t> ident(c->hostMeshes.size());
     for (size_t i = 0; i < c->hostMeshes.size(); ++i) {
@@ -199,6 +200,8 @@ cudaError_t rebuildBvh(VKRT_CudaContext* c) {
     in.hostIdentity = ident.data();
     in.meshCount = uint32_t(c->hostMeshes.size());
     in.triCount = c->triCount;
+    const uint32_t minTris = c->cfg.treeletMinTriangles ? c->cfg.treeletMinTriangles : 65536u;
+    in.treelets = c->triCount >= minTris && (!afterEdit || c->cfg.treeletsOnUpdate != 0u);
     return buildBvh(in, c->bvh, &c->bvhStats, c->stream);
 }
 
@@ -369,7 +372,8 @@ WfScene makeWfScene(VKRT_CudaContext* c, const VKRT_CudaSceneData& sd, bool spec
 WavefrontConfig engineConfig(const VKRT_CudaContext* c) {
     return WavefrontConfig{c->wfCfg.queueCapacity,  c->wfCfg.tileWidth,           c->wfCfg.tileHeight,
                            c->wfCfg.sortByMaterial, c->wfCfg.intersectBlocksPerSM, c->wfCfg.shadeBlocksPerSM,
-                           c->wfCfg.useGraph,       c->wfCfg.profileStages};
+                           c->wfCfg.useGraph,       c->wfCfg.profileStages,
+                           c->wfCfg.refillLanes ? c->wfCfg.refillLanes : uint32_t(kVoteRefillLanes)};
 }
 
 }  // namespace
@@ -395,7 +399,8 @@ int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** out) 
     VKRT_CudaConfig cfg;
     if (config) cfg = *config;
     else vkrt_cuda_default_config(&cfg);
-    if (cfg.rngMode > VKRT_CUDA_RNG_PCG32 || cfg.environmentSampling > VKRT_CUDA_ENV_IMPORTANCE)
+    if (cfg.rngMode > VKRT_CUDA_RNG_PCG32 || cfg.environmentSampling > VKRT_CUDA_ENV_IMPORTANCE ||
+        cfg.treeletsOnUpdate > 1u)
         return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0 || cfg.deviceIndex < 0 || cfg.deviceIndex >= count)
@@ -521,7 +526,7 @@ int32_t vkrt_cuda_upload_geometry(VKRT_CudaContext* c, const VKRT_CudaShaderVert
     if (!(lo[0] <= hi[0])) lo[0] = lo[1] = lo[2] = hi[0] = hi[1] = hi[2] = 0.0f;
     c->boundsLo = make_float3(lo[0], lo[1], lo[2]);
     c->boundsHi = make_float3(hi[0], hi[1], hi[2]);
-    VKRT_TRY(c, rebuildBvh(c), "BVH build");
+    VKRT_TRY(c, rebuildBvh(c, false), "BVH build");
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -552,7 +557,7 @@ int32_t vkrt_cuda_update_meshes(VKRT_CudaContext* c, const VKRT_CudaMeshInfo* me
         uint64_t tris = 0;
         for (auto& m : c->hostMeshes) tris += m.indexCount / 3u;
         c->triCount = uint32_t(tris);
-        VKRT_TRY(c, rebuildBvh(c), "BVH build");
+        VKRT_TRY(c, rebuildBvh(c, true), "BVH build");
     }
     return VKRT_CUDA_SUCCESS;
 }
@@ -920,6 +925,7 @@ int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* c, const VKRT_CudaWavef
     if (w->queueCapacity > (1u << 26)) return invalid(c, "queue capacity above 64M path slots");
     if (w->profileStages > 1u) return invalid(c, "profileStages is 0 or 1");
     if (w->sortByMaterial > 2u) return invalid(c, "sortByMaterial is 0, 1 or 2");
+    if (w->refillLanes > 32u) return invalid(c, "refillLanes is 0 (default) or 1..32");
     c->wfCfg = *w;
     return VKRT_CUDA_SUCCESS;
 }
@@ -1034,7 +1040,7 @@ int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_C
     std::vector<uint32_t> qs{0u};
     for (uint64_t q = 1u << 21; q < std::min<uint64_t>(pixels * 2u, 1u << 26); q <<= 2) qs.push_back(uint32_t(q));
     const uint32_t tiles[][2] = {{8, 8}, {16, 8}, {32, 4}, {16, 16}, {32, 8}};
-    for (int axis = 0; axis < 5; ++axis) {
+    for (int axis = 0; axis < 6; ++axis) {
         std::vector<VKRT_CudaWavefrontConfig> cands;
         if (axis == 0)
             for (uint32_t q : qs) {
@@ -1059,6 +1065,12 @@ int32_t vkrt_cuda_autotune_batch(VKRT_CudaContext* const* contexts, const VKRT_C
             for (uint32_t b : {4u, 6u, 8u}) {
                 VKRT_CudaWavefrontConfig w = cur;
                 w.intersectBlocksPerSM = b;
+                cands.push_back(w);
+            }
+        if (axis == 5)
+            for (uint32_t l : {12u, 16u, 20u, 24u}) {
+                VKRT_CudaWavefrontConfig w = cur;
+                w.refillLanes = l;
                 cands.push_back(w);
             }
         if (axis == 4)

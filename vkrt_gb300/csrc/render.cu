@@ -168,8 +168,8 @@ __global__ void __launch_bounds__(kDefaultThreads) kTraceRaysPersistent(DeviceSc
                                                                         RenderCounters* counters) {
     extern __shared__ uint2 smemStack[];
     uint32_t nodeVisits = 0u, triTests = 0u;
-    persistentTraceVote<kAnyHit, kVoteRefillLanes, false>(
-        count, &counters->workCursor, smemStack + threadIdx.x, blockDim.x, &counters->errorFlags,
+    persistentTraceVote<kAnyHit, false>(
+        count, &counters->workCursor, smemStack + threadIdx.x, blockDim.x, &counters->errorFlags, kVoteRefillLanes,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             const float4* rp = reinterpret_cast<const float4*>(rays + i);
             const float4 a = __ldg(rp), b = __ldg(rp + 1);

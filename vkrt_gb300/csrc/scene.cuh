@@ -95,5 +95,8 @@ struct RenderCounters {
 
 constexpr uint32_t kErrorStackOverflow = 1u;
 constexpr uint32_t kEnvGuide = 256u;
+// persistent vote-scheduled traversal: by default a warp fetches new rays once fewer than this many of its lanes are
+// still traversing
+constexpr int kVoteRefillLanes = 20;
 
 }  // namespace vkrt

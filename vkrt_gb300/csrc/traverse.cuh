@@ -24,8 +24,6 @@ namespace vkrt {
 #define VKRT_LOCAL_STACK 56  // further entries per thread in local memory
 #define VKRT_POSTPONE_FRACTION 0.2f
 
-// persistent vote-scheduled traversal: a warp fetches new rays once fewer than this many of its lanes are traversing
-constexpr int kVoteRefillLanes = 20;
 
 struct TraceRay {
     float3 org;
@@ -431,12 +429,12 @@ VKRT_DEV bool voteTriangleTest(TravState& s) {
 // Persistent traversal with dynamic fetch and a warp vote per step: every step the warp runs one kind of work only,
 // a node visit on the lanes that hold a node group or one triangle test on the lanes that hold triangles, whichever
 // more lanes want (triangles on ties), so node and triangle code never diverge within a step. Lanes with neither
-// pop their stack or finish; the warp refills once fewer than kRefill lanes are busy. Same tests and tie rule as
+// pop their stack or finish; the warp refills once fewer than `refill` lanes are busy. Same tests and tie rule as
 // traceBvh: closest hits are identical.
-template <bool kAnyHit, int kRefill, bool kCount, class Load, class Store>
+template <bool kAnyHit, bool kCount, class Load, class Store>
 VKRT_DEV void persistentTraceVote(uint32_t n, uint32_t* fetch, uint2* smemColumn, uint32_t smemStride,
-                                  unsigned int* errorFlags, Load load, Store store, uint32_t& nodeVisits,
-                                  uint32_t& triTests) {
+                                  unsigned int* errorFlags, int refill, Load load, Store store,
+                                  uint32_t& nodeVisits, uint32_t& triTests) {
     TraversalStack stack;
     stack.smem = smemColumn;
     stack.stride = smemStride;
@@ -481,7 +479,7 @@ VKRT_DEV void persistentTraceVote(uint32_t n, uint32_t* fetch, uint2* smemColumn
                 }
             }
         }
-        const int minBusy = exhausted ? 1 : kRefill;
+        const int minBusy = exhausted ? 1 : refill;
         for (;;) {
             // lanes without pending work take the next stack entry or finish their ray
             if (busy && s.nodeGroup.y <= 0x00FFFFFFu && s.triGroup.y == 0u) {

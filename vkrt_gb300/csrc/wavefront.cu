@@ -54,7 +54,6 @@ enum : uint32_t {
 constexpr uint32_t kPendCache = 16u;        // pendFlags: the path ended at a radiance-cache query
 constexpr uint32_t kPendUnsupported = 32u;  // pendFlags: an NEE shadow ray met a transmissive surface
 constexpr uint32_t kSortMaterial = 1, kSortClass = 2;  // sortByMaterial (0: as traced); 1 sorts by (scene, class)
-constexpr int kRefillLanes = kVoteRefillLanes;  // a warp refills once fewer of its lanes are still traversing
 
 
 struct WfGlobals {
@@ -68,6 +67,7 @@ struct WfGlobals {
     uint32_t Q;
     uint32_t maxIter;
     uint32_t sort;
+    int refill;  // persistent traversal refill threshold
     uint32_t keyCount;
     uint32_t rngMode;
     uint64_t rngSeed;
@@ -437,8 +437,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
     uint32_t primary = 0, ext = 0, nodeVisits = 0, triTests = 0;
-    persistentTraceVote<false, kRefillLanes, kCount>(
-        n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
+    persistentTraceVote<false, kCount>(
+        n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags, g.refill,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             uint32_t slot = q[i];
             const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
@@ -818,8 +818,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g)
     extern __shared__ uint2 smemStack[];
     const uint32_t n = g.counts[kCntShadow];
     uint32_t traced = 0, nodeVisits = 0, triTests = 0;
-    persistentTraceVote<true, kRefillLanes, kCount>(
-        n, &g.counts[kCntFetchShadow], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags,
+    persistentTraceVote<true, kCount>(
+        n, &g.counts[kCntFetchShadow], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags, g.refill,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             float4 a = g.shadowA[i], b = g.shadowB[i];
             uint32_t slot = __float_as_uint(b.w) & 0x7FFFFFFFu;
@@ -1165,6 +1165,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.Q = Q;
     g.maxIter = maxIter;
     g.sort = cfg.sortByMaterial <= kSortClass ? cfg.sortByMaterial : kSortMaterial;
+    g.refill = int(std::min(std::max(cfg.refillLanes, 1u), 32u));
     g.keyCount = keys;
     g.rngMode = rngMode;
     g.rngSeed = rngSeed;

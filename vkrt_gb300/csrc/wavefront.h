@@ -45,6 +45,7 @@ struct WavefrontConfig {
     uint32_t shadeBlocksPerSM;
     uint32_t useGraph;
     uint32_t profileStages;  // 1: no graph; traversal kernels count fetch bytes; per-stage device times recorded
+    uint32_t refillLanes;    // persistent traversal refill threshold (lanes still traversing), 1..32
 };
 
 // stages of the per-stage device times
