@@ -331,8 +331,16 @@ typedef struct VKRT_CudaNrcConfig {
     uint32_t trainingSteps;    /* optimiser steps per frame over the frame's training records (default 4) */
     float learningRate;        /* Adam step size (default 1e-2; beta1 0.9, beta2 0.99, epsilon 1e-8) */
     uint32_t seed;             /* parameter initialisation and training-pixel selection */
-    uint32_t reserved[10];
+    uint32_t inferenceTensorPath; /* cache inference on VKRT_CUDA_NRC_TCGEN05 (0, default: tcgen05 MMAs with
+                                     tensor-memory accumulators) or VKRT_CUDA_NRC_MMA_SYNC (1: warp-level mma.sync,
+                                     the path training uses); same network, FP16 operands, FP32 accumulation */
+    float inferenceAverage;    /* 0 (default): inference reads the optimiser's current parameters; in (0, 1): it reads
+                                  their exponential moving average, updated after every optimiser step with this
+                                  decay (less frame-to-frame noise in the cache's predictions) */
+    uint32_t reserved[8];
 } VKRT_CudaNrcConfig;
+#define VKRT_CUDA_NRC_TCGEN05 0u
+#define VKRT_CUDA_NRC_MMA_SYNC 1u
 
 /* cache input record: 16 floats (position xyz + roughness, outgoing direction xyz + metallic, shading normal xyz + 0,
  * base colour rgb + 0); outputs are 4 floats per input (linear sRGB radiance, unused) */

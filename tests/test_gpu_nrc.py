@@ -115,3 +115,34 @@ def test_cache_lowers_error_at_equal_samples(built):
         cached, ratio = run(enabled=1, terminationDepth=2, trainingPaths=65536, trainingSteps=4, seed=3)
     assert cached < 0.9 * plain
     assert abs(ratio - 1.0) < 0.01
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 4099, 70001])
+def test_tcgen05_inference_matches_mma_sync_and_fp64(built, n):
+    """Cache inference on the tcgen05 path (128-row tiles, FP32 accumulators in tensor memory) against the mma.sync
+    path on the same FP16 parameters and inputs, and both against the FP64 oracle. The two paths round the same FP32
+    sums to FP16 between layers but may accumulate in another order, so they agree to about 1e-3, not bit for bit."""
+    s = scenes.icosphere_field(n_spheres=20, width=32, height=32, spp=1, max_depth=3, seed=5, spectral=False,
+                               env_size=(64, 32))
+    with RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT) as ctx:
+        ctx.upload_scene(s)
+        ctx.nrc_configure(seed=11, inferenceTensorPath=abi.NRC_MMA_SYNC)
+        w, tb = ctx.nrc_parameters(read_table=True)
+        rng = np.random.default_rng(n)
+        tbf = rng.uniform(-0.5, 0.5, tb.size).astype(np.float16).view(np.uint16)
+        ctx.nrc_parameters(weights=w, table=tbf)
+        oc, lo, hi = _oracle(ctx)
+        x, _ = _records(n, lo, hi, seed=n + 1)
+        outs = {}
+        for path in (abi.NRC_MMA_SYNC, abi.NRC_TCGEN05, abi.NRC_TCGEN05):  # the tcgen05 path twice in a row
+            ctx.nrc_configure(seed=11, inferenceTensorPath=path)
+            ctx.nrc_parameters(weights=w, table=tbf)
+            got = ctx.nrc_infer(x)
+            assert np.isfinite(got).all()
+            if path in outs:
+                np.testing.assert_array_equal(got, outs[path])  # deterministic
+            outs[path] = got
+    ref = outs[abi.NRC_MMA_SYNC][:, :4]
+    assert _rel(outs[abi.NRC_TCGEN05][:, :4], ref) < 5e-3
+    want, _, _ = oc.forward(x)
+    assert _rel(outs[abi.NRC_TCGEN05][:, :3], want[:, :3]) < 2e-2

@@ -106,9 +106,10 @@ MATERIAL_GRADIENT = np.dtype({"names": ["baseColor", "roughness", "emission", "r
 GRADIENT_BASE_COLOR, GRADIENT_ROUGHNESS, GRADIENT_EMISSION = 1, 2, 4
 
 NRC_CONFIG = np.dtype({"names": ["enabled", "terminationDepth", "trainingPaths", "trainingSteps", "learningRate", "seed",
-                                 "reserved"],
-                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", ("<u4", 10)],
-                       "offsets": [0, 4, 8, 12, 16, 20, 24], "itemsize": 64})
+                                 "inferenceTensorPath", "inferenceAverage", "reserved"],
+                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", "<u4", "<f4", ("<u4", 8)],
+                       "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32], "itemsize": 64})
+NRC_TCGEN05, NRC_MMA_SYNC = 0, 1
 NRC_INPUT_FLOATS, NRC_WEIGHTS, NRC_TABLE_HALVES = 16, 21504, 16777216
 
 # constants (src/shared/constants.h)

@@ -1146,7 +1146,8 @@ void vkrt_cuda_default_nrc_config(VKRT_CudaNrcConfig* n) {
 
 int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* c, const VKRT_CudaNrcConfig* n) {
     if (!c || !n) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
-    if (!(n->learningRate >= 0.0f) || n->trainingPaths > (1u << 22) || n->trainingSteps > 64u)
+    if (!(n->learningRate >= 0.0f) || n->trainingPaths > (1u << 22) || n->trainingSteps > 64u ||
+        n->inferenceTensorPath > VKRT_CUDA_NRC_MMA_SYNC || !(n->inferenceAverage >= 0.0f && n->inferenceAverage < 1.0f))
         return invalid(c, "radiance cache configuration out of range");
     cudaSetDevice(c->device);
     if (!c->nrc) c->nrc.reset(new NrcEngine());
@@ -1157,6 +1158,8 @@ int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* c, const VKRT_CudaNrcConfig* n
     float3 lo = make_float3(c->boundsLo.x - pad, c->boundsLo.y - pad, c->boundsLo.z - pad);
     float3 hi = make_float3(c->boundsHi.x + pad, c->boundsHi.y + pad, c->boundsHi.z + pad);
     VKRT_TRY(c, c->nrc->reset(s, lo, hi, c->stream), "radiance cache init");
+    c->nrc->setTensorPath(n->inferenceTensorPath);
+    VKRT_TRY(c, c->nrc->setAverageDecay(n->inferenceAverage, c->stream), "radiance cache init");
     VKRT_TRY(c, cudaStreamSynchronize(c->stream), "radiance cache init");
     c->nrcCfg = *n;
     return VKRT_CUDA_SUCCESS;
@@ -1182,6 +1185,12 @@ int32_t vkrt_cuda_nrc_infer(VKRT_CudaContext* c, const float* inputs, uint32_t n
     VKRT_TRY(c, cudaMemcpyAsync(outputs, c->nrcOut.ptr, sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream),
              "cache outputs");
     VKRT_TRY(c, cudaStreamSynchronize(c->stream), "cache inference");
+    unsigned int err = 0u;
+    VKRT_TRY(c, c->nrc->errorWord(&err, c->stream), "cache inference");
+    if (err) {
+        c->lastError = "cache inference: a tensor-core completion wait ran out";
+        return VKRT_CUDA_ERROR_OPERATION_FAILED;
+    }
     return VKRT_CUDA_SUCCESS;
 }
 

@@ -20,6 +20,7 @@
 #include <cmath>
 
 #include "nrc.h"
+#include "umma.cuh"
 
 namespace vkrt {
 
@@ -238,6 +239,114 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSM)
     if (kTrain && loss) {
         for (int off = 16; off > 0; off >>= 1) lossAcc += __shfl_xor_sync(0xFFFFFFFFu, lossAcc, off);
         if (lane == 0u && lossAcc != 0.0f) atomicAdd(loss, lossAcc / (3.0f * float(max(n, 1u))));
+    }
+}
+
+// Inference on the fifth-generation tensor cores (tcgen05): one 128-record tile per step, the tile's FP16 activations
+// (128 x 64) and all six weight matrices in shared memory in the canonical K-major layout, the FP32 accumulator of a
+// layer in tensor memory (128 lanes = the tile's rows, 64 columns). Per layer one elected thread issues four
+// 128 x N x 16 MMAs (N = 64, then 16 for the output layer) and commits them to an mbarrier; after the wait each warp
+// reads its 32 rows from tensor memory (tcgen05.ld), applies ReLU, rounds to FP16 and writes the next layer's
+// operand. Same network and arithmetic types as kNrcForward<false>; accumulation order inside the tensor core may
+// differ. A wait that does not complete within its bound sets bit 0 of *error and the block stops.
+constexpr uint32_t kUmmaThreads = 128;  // four warps: tensor-memory lanes 32 w .. 32 w + 31 of warp w
+constexpr uint32_t kUmmaRows = 128;
+constexpr uint32_t kUmmaLayerBytes = 64u * 64u * 2u;
+constexpr uint32_t kUmmaWBytes = 5u * kUmmaLayerBytes + 16u * 64u * 2u;  // 43,008
+constexpr uint32_t kUmmaABytes = kUmmaRows * 64u * 2u;                   // 16,384
+constexpr uint32_t kUmmaSmemBytes = kUmmaWBytes + kUmmaABytes + 64u;     // + mbarrier and tensor-memory address
+constexpr uint32_t kUmmaBlocksPerSM = 3;
+constexpr uint32_t kUmmaColumns = 64;
+constexpr uint32_t kUmmaWaitPolls = 1u << 22;
+
+__global__ void __launch_bounds__(kUmmaThreads)
+    kNrcInferUmma(const __half* __restrict__ W, const __half* __restrict__ x0, const uint32_t* count, uint32_t cap,
+                  float4* __restrict__ out, unsigned int* error) {
+    extern __shared__ __align__(128) uint8_t usm[];
+    uint8_t* wsm = usm;
+    uint8_t* act = usm + kUmmaWBytes;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(usm + kUmmaWBytes + kUmmaABytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(usm + kUmmaWBytes + kUmmaABytes + 8u);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t n = count ? min(*count, cap) : cap;
+    // weights: row `row` of the concatenated matrices (5 x 64 rows, then 16), eight 16-byte pieces of 8 inputs
+    for (uint32_t i = tid; i < kNrcWeightCount / 8u; i += blockDim.x) {
+        const uint32_t row = i >> 3, kc = i & 7u;
+        const uint32_t l = min(row >> 6, 5u), o = row - l * 64u;
+        *reinterpret_cast<uint4*>(wsm + l * kUmmaLayerBytes + ummaOffset(o, kc * 8u)) =
+            reinterpret_cast<const uint4*>(W)[i];
+    }
+    if (tid == 0) mbarInit(bar, 1u);
+    if (warp == 0) tmemAlloc(tslot, kUmmaColumns);
+    tcgenFenceBefore();
+    __syncthreads();
+    tcgenFenceAfter();
+    const uint32_t tmem = *tslot;
+    const uint32_t taddr = tmem + ((warp * 32u) << 16);
+    const uint32_t tiles = (n + kUmmaRows - 1u) / kUmmaRows;
+    uint32_t phase = 0u;
+    bool failed = false;
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint32_t row = tile * kUmmaRows + tid;
+#pragma unroll
+        for (uint32_t kc = 0; kc < 8u; ++kc) {
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (row < n) v = reinterpret_cast<const uint4*>(x0 + size_t(row) * 64u)[kc];
+            *reinterpret_cast<uint4*>(act + ummaOffset(tid, kc * 8u)) = v;
+        }
+        for (uint32_t l = 0; l < 6u && !failed; ++l) {
+            fenceProxyAsyncShared();
+            tcgenFenceBefore();
+            __syncthreads();
+            if (tid == 0) {
+                tcgenFenceAfter();
+                const uint32_t idesc = ummaIdescF16(kUmmaRows, l < 5u ? 64u : 16u);
+                const uint32_t aBase = smemAddr(act), bBase = smemAddr(wsm + l * kUmmaLayerBytes);
+#pragma unroll
+                for (uint32_t s = 0; s < 4u; ++s)
+                    ummaF16(tmem, ummaSmemDesc(aBase + 256u * s), ummaSmemDesc(bBase + 256u * s), idesc, s);
+                ummaCommit(bar);
+            }
+            const bool ok = mbarWait(bar, phase, kUmmaWaitPolls);
+            tcgenFenceAfter();
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            if (l < 5u) {
+#pragma unroll
+                for (uint32_t c = 0; c < 64u; c += 16u) {
+                    uint32_t r[16];
+                    tmemLoad16(taddr + c, r);
+                    tmemLoadWait();
+                    uint32_t h[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        h[j] = packHalf2(fmaxf(__uint_as_float(r[2 * j]), 0.0f), fmaxf(__uint_as_float(r[2 * j + 1]), 0.0f));
+                    *reinterpret_cast<uint4*>(act + ummaOffset(tid, c)) = make_uint4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<uint4*>(act + ummaOffset(tid, c + 8u)) = make_uint4(h[4], h[5], h[6], h[7]);
+                }
+            } else {
+                uint32_t r[16];
+                tmemLoad16(taddr, r);
+                tmemLoadWait();
+                if (row < n)
+                    out[row] = make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]),
+                                           __uint_as_float(r[3]));
+            }
+        }
+    }
+    if (failed) {
+        // let the MMAs of the phase that did not complete finish (bounded) before the columns are released
+        if (tid == 0) atomicOr(error, 1u);
+        mbarWait(bar, phase, kUmmaWaitPolls);
+    }
+    tcgenFenceBefore();
+    __syncthreads();
+    if (warp == 0) {
+        tcgenFenceAfter();
+        tmemFree(tmem, kUmmaColumns);
     }
 }
 
@@ -479,6 +588,19 @@ __global__ void kNrcAdam(float* __restrict__ master, float* __restrict__ m, floa
 // Sparse Adam (hash table), four parameters per thread: a parameter whose gradient is zero in this step keeps its
 // value and moments (a step's records touch a small part of the finer levels); the gradient is cleared as it is
 // consumed, so the next step starts from zeros without a separate clear.
+// Parameter average for inference: avg = decay * avg + (1 - decay) * master, in FP32 arithmetic on FP16 storage
+// (decay 0 copies the masters).
+__global__ void kNrcAverage(const float4* __restrict__ master, uint2* __restrict__ avg, uint32_t count4, float decay) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count4; i += gridDim.x * blockDim.x) {
+        const float4 w = master[i];
+        const uint2 a = avg[i];
+        const float2 a0 = unpackHalf2(a.x), a1 = unpackHalf2(a.y);
+        const float k = 1.0f - decay;
+        avg[i] = make_uint2(packHalf2(decay * a0.x + k * w.x, decay * a0.y + k * w.y),
+                            packHalf2(decay * a1.x + k * w.z, decay * a1.y + k * w.w));
+    }
+}
+
 __global__ void kNrcAdamSparse(float4* __restrict__ master, float4* __restrict__ m, float4* __restrict__ v,
                                float4* __restrict__ grad, uint2* __restrict__ half, uint32_t count4, float lr, float b1,
                                float b2, float eps, float bc1, float bc2) {
@@ -524,13 +646,20 @@ uint32_t mlpGrid(uint32_t rows) {
     return std::max(1u, std::min((tiles + warps - 1u) / warps, smCount() * kMlpBlocksPerSM));
 }
 
+// tcgen05 inference: one 128-row tile per block and pass, at most kUmmaBlocksPerSM blocks per SM (192 of the 512
+// tensor-memory columns)
+uint32_t ummaGrid(uint32_t rows) {
+    const uint32_t tiles = (rows + kUmmaRows - 1u) / kUmmaRows;
+    return std::max(1u, std::min(tiles, smCount() * kUmmaBlocksPerSM));
+}
+
 }  // namespace
 
 NrcEngine::NrcEngine() {}
 
 NrcEngine::~NrcEngine() {
-    void* ptrs[] = {wHalf_, wMaster_, wM_, wV_,  wGrad_, table_, tMaster_, tM_,     tV_,
-                    tGrad_, x0_,      acts_, dz_, dy_,   dx0_,   out_,     masks_, x0Infer_};
+    void* ptrs[] = {wHalf_, wMaster_, wM_, wV_,  wGrad_, table_, tMaster_, tM_,     tV_,      tGrad_,
+                    x0_,    acts_,    dz_, dy_,  dx0_,   out_,   masks_,   x0Infer_, error_, wAvg_, tAvg_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -559,6 +688,11 @@ cudaError_t NrcEngine::reset(const NrcSettings& s, float3 lo, float3 hi, cudaStr
         if (e == cudaSuccess) e = alloc(tM_, kNrcTableParams);
         if (e == cudaSuccess) e = alloc(tV_, kNrcTableParams);
         if (e == cudaSuccess) e = alloc(tGrad_, kNrcTableParams);
+        if (e == cudaSuccess) e = alloc(error_, 1);
+        if (e == cudaSuccess) e = alloc(wAvg_, kNrcWeightCount);
+        if (e == cudaSuccess) e = alloc(tAvg_, kNrcTableParams / 2u);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(kNrcInferUmma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUmmaSmemBytes));
         if (e != cudaSuccess) return e;
         e = cudaFuncSetAttribute(kNrcForward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMlpSmemBytes));
         if (e == cudaSuccess)
@@ -569,6 +703,7 @@ cudaError_t NrcEngine::reset(const NrcSettings& s, float3 lo, float3 hi, cudaStr
             e = cudaFuncSetAttribute(kNrcWeightGrad, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kWgSmemBytes));
         if (e != cudaSuccess) return e;
     }
+    cudaMemsetAsync(error_, 0, sizeof(unsigned int), stream);
     cudaMemsetAsync(wM_, 0, sizeof(float) * kNrcWeightCount, stream);
     cudaMemsetAsync(wV_, 0, sizeof(float) * kNrcWeightCount, stream);
     cudaMemsetAsync(wGrad_, 0, sizeof(float) * kNrcWeightCount, stream);
@@ -578,13 +713,22 @@ cudaError_t NrcEngine::reset(const NrcSettings& s, float3 lo, float3 hi, cudaStr
     tGradClear_ = true;
     kNrcInit<<<gridFor(kNrcWeightCount + kNrcTableParams, 256), 256, 0, stream>>>(
         wMaster_, wHalf_, tMaster_, reinterpret_cast<__half*>(table_), s.seed);
-    return cudaGetLastError();
+    return refreshAverage(0.0f, stream);
 }
 
 cudaError_t NrcEngine::syncMasters(cudaStream_t stream) {
     kHalfToFloat<<<gridFor(kNrcWeightCount, 256), 256, 0, stream>>>(wHalf_, wMaster_, kNrcWeightCount);
     kHalfToFloat<<<gridFor(kNrcTableParams, 256), 256, 0, stream>>>(reinterpret_cast<const __half*>(table_), tMaster_,
                                                                     kNrcTableParams);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? refreshAverage(0.0f, stream) : e;
+}
+
+cudaError_t NrcEngine::refreshAverage(float decay, cudaStream_t stream) {
+    kNrcAverage<<<gridFor(kNrcWeightCount / 4u, 256), 256, 0, stream>>>(
+        reinterpret_cast<const float4*>(wMaster_), reinterpret_cast<uint2*>(wAvg_), kNrcWeightCount / 4u, decay);
+    kNrcAverage<<<gridFor(kNrcTableParams / 4u, 256), 256, 0, stream>>>(
+        reinterpret_cast<const float4*>(tMaster_), reinterpret_cast<uint2*>(tAvg_), kNrcTableParams / 4u, decay);
     return cudaGetLastError();
 }
 
@@ -619,9 +763,16 @@ cudaError_t NrcEngine::inferCounted(const NrcInput* inputs, const uint32_t* coun
     if (capacity > (0xFFFFFFFFu >> 4)) return cudaErrorInvalidValue;  // (record, level) indices stay in 32 bits
     cudaError_t e = reserveInference(capacity);
     if (e != cudaSuccess) return e;
-    kNrcEncode<<<gridFor(capacity * 16u, 256), 256, 0, stream>>>(grid_, table_, inputs, count, capacity, x0Infer_);
-    kNrcForward<false><<<mlpGrid(capacity), kMlpThreads, kMlpSmemBytes, stream>>>(
-        wHalf_, x0Infer_, count, capacity, out, nullptr, nullptr, nullptr, nullptr, nullptr);
+    // inference reads the averaged parameters when averaging is on, else the optimiser's current ones
+    const __half2* table = averageDecay_ > 0.0f ? tAvg_ : table_;
+    const __half* weights = averageDecay_ > 0.0f ? wAvg_ : wHalf_;
+    kNrcEncode<<<gridFor(capacity * 16u, 256), 256, 0, stream>>>(grid_, table, inputs, count, capacity, x0Infer_);
+    if (tensorPath_ == kNrcTensorTcgen05)
+        kNrcInferUmma<<<ummaGrid(capacity), kUmmaThreads, kUmmaSmemBytes, stream>>>(weights, x0Infer_, count, capacity,
+                                                                                    out, error_);
+    else
+        kNrcForward<false><<<mlpGrid(capacity), kMlpThreads, kMlpSmemBytes, stream>>>(
+            weights, x0Infer_, count, capacity, out, nullptr, nullptr, nullptr, nullptr, nullptr);
     return cudaGetLastError();
 }
 
@@ -653,8 +804,20 @@ cudaError_t NrcEngine::train(const NrcInput* inputs, const float4* targets, uint
             reinterpret_cast<float4*>(tGrad_), reinterpret_cast<uint2*>(table_), kNrcTableParams / 4u,
             s_.learningRate, s_.beta1, s_.beta2, s_.epsilon, bc1, bc2);
         tGradClear_ = true;
+        if (averageDecay_ > 0.0f) {
+            cudaError_t e2 = refreshAverage(averageDecay_, stream);
+            if (e2 != cudaSuccess) return e2;
+        }
     }
     return cudaGetLastError();
+}
+
+cudaError_t NrcEngine::errorWord(unsigned int* out, cudaStream_t stream) {
+    *out = 0u;
+    if (!error_) return cudaSuccess;
+    cudaError_t e = cudaMemcpyAsync(out, error_, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    return e;
 }
 
 }  // namespace vkrt

@@ -8,6 +8,10 @@
 
 namespace vkrt {
 
+// tensor-core path of cache inference: tcgen05 MMAs with tensor-memory accumulators (kNrcInferUmma), or warp-level
+// mma.sync (kNrcForward, which training always uses)
+enum NrcTensorPath : uint32_t { kNrcTensorTcgen05 = 0, kNrcTensorMmaSync = 1 };
+
 struct NrcSettings {
     float learningRate;
     float beta1, beta2, epsilon;
@@ -48,9 +52,20 @@ public:
     cudaError_t syncMasters(cudaStream_t stream);
     // allocates the inference scratch for `capacity` rows ahead of a graph capture (no allocation while capturing)
     cudaError_t reserveInference(uint32_t capacity);
+    void setTensorPath(uint32_t path) { tensorPath_ = path; }
+    // inference reads an exponential moving average of the parameters (per optimiser step: avg = decay avg +
+    // (1 - decay) param) when decay > 0; the average restarts from the current parameters
+    cudaError_t setAverageDecay(float decay, cudaStream_t stream) {
+        averageDecay_ = decay;
+        return refreshAverage(0.0f, stream);
+    }
+    uint32_t tensorPath() const { return tensorPath_; }
+    // device error word (bit 0: a tcgen05 completion wait ran out), read synchronously on `stream`
+    cudaError_t errorWord(unsigned int* out, cudaStream_t stream);
 
 private:
     cudaError_t ensureScratch(uint32_t n);
+    cudaError_t refreshAverage(float decay, cudaStream_t stream);
     NrcSettings s_{};
     NrcGridInfo grid_{};
     uint32_t step_ = 0;
@@ -68,6 +83,11 @@ private:
     float* dx0_ = nullptr;
     uint32_t* masks_ = nullptr;  // ReLU masks of the forward pass, 5 x tiles x 32 words
     float4* out_ = nullptr;
+    unsigned int* error_ = nullptr;
+    uint32_t tensorPath_ = kNrcTensorTcgen05;
+    float averageDecay_ = 0.0f;
+    __half* wAvg_ = nullptr;   // parameter averages read by inference
+    __half2* tAvg_ = nullptr;
 };
 
 }  // namespace vkrt
