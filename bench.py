@@ -290,6 +290,9 @@ def convergence_measure(local: int, scene, max_frames: int = 96, ref_frames: int
                       learningRate=1e-2, seed=3)
     cached1, _ = curve(ctx, stream, enabled=1, terminationDepth=1, trainingPaths=65536, trainingSteps=4,
                        learningRate=1e-2, seed=3)
+    # area-spread termination (Mueller et al. 2021) with the paper's constant, at most at bounce full_depth
+    spread, _ = curve(ctx, stream, enabled=1, terminationDepth=int(sd["rrMaxDepth"][0]), terminationSpread=0.01,
+                      trainingPaths=65536, trainingSteps=4, learningRate=1e-2, seed=3)
 
     # variance by path depth: two independent 8-frame renders per estimator; the variance term of relMSE at 128 spp
     # is mean((A - B)^2 / (2 (ref^2 + 1e-2))). Paths truncated at depth d (rrMaxDepth = d) show the variance that
@@ -340,13 +343,15 @@ def convergence_measure(local: int, scene, max_frames: int = 96, ref_frames: int
                          "fp64_same_seed_check": {"rows": len(rows), "spp": 16, "relmse_vs_oracle_fp64": val}},
            "metric": "relMSE = mean (x - ref)^2 / (ref^2 + 1e-2); reached_trimmed drops the 0.01% worst pixels",
            "plain_wavefront": plain, "radiance_cache": cached, "radiance_cache_depth_1": cached1,
-           "plain_megakernel": mega, "variance_by_depth": var_by_depth}
+           "radiance_cache_spread": spread, "plain_megakernel": mega, "variance_by_depth": var_by_depth}
     if plain["reached"] and mega["reached"]:
         out["wavefront_over_megakernel"] = round(plain["reached"]["ms"] / mega["reached"]["ms"], 4)
     if plain["reached"] and cached["reached"]:
         out["cache_over_plain_wavefront"] = round(cached["reached"]["ms"] / plain["reached"]["ms"], 4)
     if plain["reached"] and cached1["reached"]:
         out["cache_depth_1_over_plain_wavefront"] = round(cached1["reached"]["ms"] / plain["reached"]["ms"], 4)
+    if plain["reached"] and spread["reached"]:
+        out["cache_spread_over_plain_wavefront"] = round(spread["reached"]["ms"] / plain["reached"]["ms"], 4)
     if cached["reached"] and mega["reached"]:
         out["cache_over_megakernel"] = round(cached["reached"]["ms"] / mega["reached"]["ms"], 4)
     return out
@@ -603,7 +608,11 @@ def run_ours(args) -> dict | None:
                      "algorithmic_bytes_per_launch": int(closest_bytes / max(isect_launches, 1)),
                      "launches": isect_launches,
                      "note": "80 B per node visit + 48 B per triangle test of closest-hit rays / kernel time, "
-                             "profiling frame; the 65 MB BVH is L2-resident, so frac > 1 is possible",
+                             "profiling frame; the 58 MB BVH is L2-resident, so frac > 1 is possible",
+                     "ceiling": "latency and divergence, not bandwidth: in the committed small-case capture the "
+                                "kernel runs at 15% of L2 peak throughput with 13.2 of 32 lanes active per "
+                                "instruction and long-scoreboard stalls first "
+                                "(profiles/kWfIntersect_icosphere1M_640x360x4spp.md)",
                      "shadow_kernel": {"kernel": "kWfShadow",
                                        "achieved": round(shadow_bytes / (shadow_ms * 1e-3) / 1e9, 1),
                                        "frac": round(shadow_bytes / (shadow_ms * 1e-3) / 1e9 / peak, 4)},
@@ -774,7 +783,8 @@ def run_profile_frame(args) -> dict:
     summaries): prints one JSON line with rays by kind, node/triangle fetch bytes (with --stage-launches, which also
     times the wavefront stages one by one), per-stage device milliseconds and the frames' device time. Under ncu the
     kernels of every rendered frame (warm-up included) are captured; --warmup 0 --frames 1 keeps a capture to one
-    frame. --cache renders with the radiance cache, so its training and inference kernels run in every frame."""
+    frame, or ncu's `--nvtx --nvtx-include "measured/"` selects the frames after the warm-up. --cache renders with the
+    radiance cache, so its training and inference kernels run in every frame."""
     import torch
     from vkrt_gb300 import RenderContext, abi, scenes
 
@@ -802,12 +812,15 @@ def run_profile_frame(args) -> dict:
     for f in range(args.warmup + args.frames):
         sd["frameNumber"] = f
         ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if f >= args.warmup:
+            torch.cuda.nvtx.range_push("measured")
         ev[0].record(stream)
         ctx.render_frame(sd)
         ev[1].record(stream)
         ctx.sync()
         st = ctx.stats()
         if f >= args.warmup:
+            torch.cuda.nvtx.range_pop()
             for k in ("primaryRays", "extensionRays", "shadowRays", "nodeFetchBytes", "triFetchBytes",
                       "shadowNodeFetchBytes", "shadowTriFetchBytes", "kernelLaunches", "wavefrontBodies",
                       "cacheTrainingRecords", "errorFlags"):

@@ -73,7 +73,10 @@ typedef struct VKRT_CudaWavefrontConfig {
                                       for profiling), reported in VKRT_CudaStats.stageMs / *FetchBytes */
     uint32_t refillLanes;          /* persistent traversal: a warp fetches new rays once fewer than this many of its
                                       32 lanes are still traversing; 0 = the default (20), else 1..32 */
-    uint32_t reserved[7];
+    uint32_t rayOrder;             /* 1: paths are queued for traversal in 8 bins by the octant of their ray direction,
+                                      so a traversal warp draws rays of one octant; 0: in the order the previous stage
+                                      produced them (camera rays in tile order) */
+    uint32_t reserved[6];
 } VKRT_CudaWavefrontConfig;
 
 typedef struct VKRT_CudaStats {
@@ -337,7 +340,12 @@ typedef struct VKRT_CudaNrcConfig {
     float inferenceAverage;    /* 0 (default): inference reads the optimiser's current parameters; in (0, 1): it reads
                                   their exponential moving average, updated after every optimiser step with this
                                   decay (less frame-to-frame noise in the cache's predictions) */
-    uint32_t reserved[8];
+    float terminationSpread;   /* 0 (default): render paths query the cache at bounce `terminationDepth`; c > 0: they
+                                  also query it at the first vertex where the area spread of the path after its
+                                  primary vertex exceeds c times the primary vertex's footprint seen from the camera
+                                  (Mueller et al. 2021, "Real-time Neural Radiance Caching for Path Tracing", 3.3;
+                                  the paper uses c = 0.01), and at `terminationDepth` at the latest */
+    uint32_t reserved[7];
 } VKRT_CudaNrcConfig;
 #define VKRT_CUDA_NRC_TCGEN05 0u
 #define VKRT_CUDA_NRC_MMA_SYNC 1u

@@ -117,6 +117,49 @@ def test_cache_lowers_error_at_equal_samples(built):
     assert abs(ratio - 1.0) < 0.01
 
 
+def test_spread_termination_limits(built):
+    """Area-spread termination (Mueller et al. 2021, section 3.3) at its two limits, with an untrained cache (no
+    training paths, so every frame is deterministic): a constant no spread exceeds ends every path at
+    terminationDepth, bit for bit the fixed-depth image; a constant every spread exceeds ends every path at its first
+    secondary vertex, bit for bit the image of terminationDepth 1. The paper's c = 0.01 ends some paths at each and
+    gives an image unlike both."""
+    s = scenes.icosphere_field(n_spheres=40, width=64, height=48, spp=4, max_depth=8, seed=7, spectral=True,
+                               env_size=(128, 64))
+    with RenderContext(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE,
+                       integrator=abi.INTEGRATOR_WAVEFRONT) as ctx:
+        s.rgb2spec, info = ctx.generate_rgb2spec(16)
+        s.scene_data["rgb2specSRGB"] = info
+        ctx.upload_scene(s)
+
+        def render(**cache):
+            ctx.nrc_configure(enabled=1, trainingPaths=0, trainingSteps=0, seed=5, **cache)
+            ctx.reset_accumulation()
+            sd = s.scene_data.copy()
+            for f in range(2):
+                sd["frameNumber"] = f
+                ctx.render_frame(sd)
+            assert ctx.stats()["errorFlags"] == 0
+            return ctx.read_accumulation()[..., :3].copy()
+
+        depth3 = render(terminationDepth=3)
+        depth1 = render(terminationDepth=1)
+        never = render(terminationDepth=3, terminationSpread=3.0e38)
+        always = render(terminationDepth=3, terminationSpread=1.0e-38)
+        paper = render(terminationDepth=3, terminationSpread=0.01)
+    assert np.array_equal(never, depth3)
+    assert np.array_equal(always, depth1)
+    assert not np.array_equal(paper, depth3) and not np.array_equal(paper, depth1)
+    assert np.isfinite(paper).all()
+
+
+def test_spread_constant_validated(built):
+    with RenderContext(rng_mode=abi.RNG_PCG32, integrator=abi.INTEGRATOR_WAVEFRONT) as ctx:
+        ctx.upload_scene(scenes.cornell(32, 32, 1, 2))
+        for bad in (-1.0, float("nan"), float("inf")):
+            with pytest.raises(RuntimeError):
+                ctx.nrc_configure(terminationSpread=bad)
+
+
 @pytest.mark.parametrize("n", [1, 127, 128, 129, 4099, 70001])
 def test_tcgen05_inference_matches_mma_sync_and_fp64(built, n):
     """Cache inference on the tcgen05 path (128-row tiles, FP32 accumulators in tensor memory) against the mma.sync

@@ -81,9 +81,9 @@ CONFIG = np.dtype({"names": ["deviceIndex", "rngMode", "rngSeed", "environmentSa
 
 WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
                                        "intersectBlocksPerSM", "shadeBlocksPerSM", "useGraph", "profileStages",
-                                       "refillLanes", "reserved"],
-                             "formats": ["<u4"] * 9 + [("<u4", 7)],
-                             "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36], "itemsize": 64})
+                                       "refillLanes", "rayOrder", "reserved"],
+                             "formats": ["<u4"] * 10 + [("<u4", 6)],
+                             "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40], "itemsize": 64})
 
 STATS = np.dtype({"names": ["primaryRays", "extensionRays", "shadowRays", "pathSamples", "nodeFetchBytes",
                             "triFetchBytes", "bvhNodeCount", "bvhTriangleCount", "bvhBytes", "bvhBuildMs",
@@ -106,9 +106,9 @@ MATERIAL_GRADIENT = np.dtype({"names": ["baseColor", "roughness", "emission", "r
 GRADIENT_BASE_COLOR, GRADIENT_ROUGHNESS, GRADIENT_EMISSION = 1, 2, 4
 
 NRC_CONFIG = np.dtype({"names": ["enabled", "terminationDepth", "trainingPaths", "trainingSteps", "learningRate", "seed",
-                                 "inferenceTensorPath", "inferenceAverage", "reserved"],
-                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", "<u4", "<f4", ("<u4", 8)],
-                       "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32], "itemsize": 64})
+                                 "inferenceTensorPath", "inferenceAverage", "terminationSpread", "reserved"],
+                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", "<u4", "<f4", "<f4", ("<u4", 7)],
+                       "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36], "itemsize": 64})
 NRC_TCGEN05, NRC_MMA_SYNC = 0, 1
 NRC_INPUT_FLOATS, NRC_WEIGHTS, NRC_TABLE_HALVES = 16, 21504, 16777216
 

@@ -373,7 +373,8 @@ WavefrontConfig engineConfig(const VKRT_CudaContext* c) {
     return WavefrontConfig{c->wfCfg.queueCapacity,  c->wfCfg.tileWidth,           c->wfCfg.tileHeight,
                            c->wfCfg.sortByMaterial, c->wfCfg.intersectBlocksPerSM, c->wfCfg.shadeBlocksPerSM,
                            c->wfCfg.useGraph,       c->wfCfg.profileStages,
-                           c->wfCfg.refillLanes ? c->wfCfg.refillLanes : uint32_t(kVoteRefillLanes)};
+                           c->wfCfg.refillLanes ? c->wfCfg.refillLanes : uint32_t(kVoteRefillLanes),
+                           c->wfCfg.rayOrder};
 }
 
 }  // namespace
@@ -926,6 +927,7 @@ int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* c, const VKRT_CudaWavef
     if (w->profileStages > 1u) return invalid(c, "profileStages is 0 or 1");
     if (w->sortByMaterial > 2u) return invalid(c, "sortByMaterial is 0, 1 or 2");
     if (w->refillLanes > 32u) return invalid(c, "refillLanes is 0 (default) or 1..32");
+    if (w->rayOrder > 1u) return invalid(c, "rayOrder is 0 or 1");
     c->wfCfg = *w;
     return VKRT_CUDA_SUCCESS;
 }
@@ -980,7 +982,8 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
         return invalid(c0, "the radiance cache covers RGB and hero-wavelength frames");
     if (useCache)
         cache = WfCacheFrame{c0->nrc.get(), c0->nrcCfg.terminationDepth, c0->nrcCfg.trainingPaths,
-                             c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber};
+                             c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber,
+                             c0->nrcCfg.terminationSpread};
     VKRT_TRY(c0, c0->wavefront->render(scenes, spectral, wc, c0->cfg.rngMode, c0->cfg.rngSeed, c0->counters, c0->stream,
                                        kWavefrontForward, nullptr, useCache ? &cache : nullptr),
              "batch render");
@@ -1147,7 +1150,8 @@ void vkrt_cuda_default_nrc_config(VKRT_CudaNrcConfig* n) {
 int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* c, const VKRT_CudaNrcConfig* n) {
     if (!c || !n) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     if (!(n->learningRate >= 0.0f) || n->trainingPaths > (1u << 22) || n->trainingSteps > 64u ||
-        n->inferenceTensorPath > VKRT_CUDA_NRC_MMA_SYNC || !(n->inferenceAverage >= 0.0f && n->inferenceAverage < 1.0f))
+        n->inferenceTensorPath > VKRT_CUDA_NRC_MMA_SYNC || !(n->inferenceAverage >= 0.0f && n->inferenceAverage < 1.0f) ||
+        !(n->terminationSpread >= 0.0f && n->terminationSpread <= 3.0e38f))
         return invalid(c, "radiance cache configuration out of range");
     cudaSetDevice(c->device);
     if (!c->nrc) c->nrc.reset(new NrcEngine());

@@ -269,12 +269,16 @@ __global__ void __launch_bounds__(kUmmaThreads)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(usm + kUmmaWBytes + kUmmaABytes + 8u);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const uint32_t n = count ? min(*count, cap) : cap;
-    // weights: row `row` of the concatenated matrices (5 x 64 rows, then 16), eight 16-byte pieces of 8 inputs
-    for (uint32_t i = tid; i < kNrcWeightCount / 8u; i += blockDim.x) {
-        const uint32_t row = i >> 3, kc = i & 7u;
+    // the grid follows the capacity; blocks past the device-side count leave before staging anything
+    if (blockIdx.x * kUmmaRows >= n) return;
+    // weights: 16-byte piece kc of row `row` of the concatenated matrices (5 x 64 rows, then 16); rows run fastest
+    // across the threads, so a warp's stores fill whole 128-byte core-matrix rows
+    constexpr uint32_t kRows = kNrcWeightCount / 64u;  // 336
+    for (uint32_t i = tid; i < kRows * 8u; i += blockDim.x) {
+        const uint32_t row = i % kRows, kc = i / kRows;
         const uint32_t l = min(row >> 6, 5u), o = row - l * 64u;
         *reinterpret_cast<uint4*>(wsm + l * kUmmaLayerBytes + ummaOffset(o, kc * 8u)) =
-            reinterpret_cast<const uint4*>(W)[i];
+            reinterpret_cast<const uint4*>(W)[row * 8u + kc];
     }
     if (tid == 0) mbarInit(bar, 1u);
     if (warp == 0) tmemAlloc(tslot, kUmmaColumns);

@@ -35,6 +35,9 @@ struct PathState {
     float prevBsdfPdf;                             // RGB MIS, and the single-wavelength MIS of a collapsed path
     uint32_t depth;
     uint32_t flags;
+    // radiance-cache area-spread rule: the running sum of the footprint square roots after the primary vertex, and
+    // the primary vertex's footprint a0 (set at depth 0; used only when StepConfig::cacheSpread > 0)
+    float spread, spreadA0;
     // full instantiations: hero lanes 1-3 of the technique pdfs (lane 0 in the scalars above; the lanes differ after
     // dispersive interfaces) and the absorption of the medium the path is in (RGB in xyz, the four hero lanes, or the
     // collapsed lane in x). A collapsed path keeps its throughput in thr.x, the XYZ of its hero lanes in
@@ -57,6 +60,7 @@ struct StepConfig {
     uint32_t rngMode;
     uint64_t rngSeed;
     uint32_t cacheDepth = 0xFFFFFFFFu;  // surface vertex depth at which the path queries the radiance cache and ends
+    float cacheSpread = 0.0f;  // > 0: a path also ends in the cache once its area spread exceeds this times a0
     bool single = false;  // spectral mode with one wavelength per path (raygen_spectral_single.slang), full kernels
 };
 
@@ -92,6 +96,8 @@ VKRT_DEV PathState beginPath(const StepConfig& cfg, const VKRT_CudaSceneData& sd
     p.prevBsdfPdf = 0.0f;
     p.depth = 0;
     p.flags = 0;
+    p.spread = 0.0f;
+    p.spreadA0 = 0.0f;
     p.techYZW = f3(1.0f);
     p.prevVertexYZW = f3(0.0f);
     p.prevBsdfYZW = f3(0.0f);
@@ -103,6 +109,26 @@ VKRT_DEV PathState beginPath(const StepConfig& cfg, const VKRT_CudaSceneData& sd
         p.thr = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
     }
     return p;
+}
+
+// Path termination by area spread (Mueller, Rousselle, Novak, Keller 2021, "Real-time Neural Radiance Caching for
+// Path Tracing", section 3.3): the footprint a path's vertices x1..xn cover,
+//   a(x1..xn) = (sum_{i=2..n} sqrt(|x_{i-1} - x_i|^2 / (p(w_i | x_{i-1}) |cos theta_i|)))^2,
+// is compared with the primary vertex's footprint seen from the camera, a0 = |x0 - x1|^2 / (4 pi |cos theta_1|);
+// the path ends in the cache at the first vertex where a > c a0. Narrow (glossy) lobes add little spread and keep a
+// path going, a diffuse bounce usually ends it at the next vertex. `t` is the segment length to this vertex (unit
+// direction), `cosTheta` the cosine between that segment and the geometric normal here, `pdfPrev` the solid-angle
+// pdf with which the previous vertex sampled the segment. Records a0 at depth 0.
+VKRT_DEV bool spreadEndsPath(const StepConfig& cfg, PathState& p, uint32_t depth, float t, float cosTheta,
+                             float pdfPrev) {
+    if (!(cfg.cacheSpread > 0.0f)) return false;
+    if (depth == 0u) {
+        p.spreadA0 = (t * t) / (4.0f * kPi * cosTheta);
+        return false;
+    }
+    const float den = pdfPrev * cosTheta;
+    p.spread += den > 0.0f ? t * rsqrtf(den) : __int_as_float(0x7F800000);
+    return p.spread * p.spread > cfg.cacheSpread * p.spreadA0;
 }
 
 // Sample value of a finished path: linear sRGB, or CIE XYZ in spectral mode (spectral.slang:104-113).
@@ -254,7 +280,9 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
         }
     }
 
-    if (depth == cfg.cacheDepth) {
+    if (depth == cfg.cacheDepth ||
+        spreadEndsPath(cfg, p, depth, h.t, fabsf(dot(s.geometricNormal, p.d)),
+                       kSpectral && !collapsed ? p.prevBsdfTech : p.prevBsdfPdf)) {
         hook.cacheQuery(s, mat);
         return false;
     }
@@ -477,7 +505,9 @@ VKRT_DEV bool shadePathVertexSubset(const DeviceScene& sc, const VKRT_CudaSceneD
     }
 
     // radiance-cache termination: the cache stands for everything the vertex scatters (NEE and continuation)
-    if (depth == cfg.cacheDepth) {
+    if (depth == cfg.cacheDepth ||
+        spreadEndsPath(cfg, p, depth, h.t, fabsf(dot(s.geometricNormal, p.d)),
+                       kSpectral ? p.prevBsdfTech : p.prevBsdfPdf)) {
         hook.cacheQuery(s, mat);
         return false;
     }

@@ -50,6 +50,8 @@ enum : uint32_t {
     kCntFetchShadow = 7,
     kCntClass0 = 8,  // class-partitioned shade queue: misses, dielectric hits, metal hits
     kCntQueries = 11,  // radiance-cache queries of the iteration
+    kCntBin0 = 16,     // with rayOrder: entries per direction-octant bin, kRayBins for queue 0 then for queue 1
+    kCntCount = 32,
 };
 constexpr uint32_t kPendCache = 16u;        // pendFlags: the path ended at a radiance-cache query
 constexpr uint32_t kPendUnsupported = 32u;  // pendFlags: an NEE shadow ray met a transmissive surface
@@ -71,14 +73,9 @@ struct WfGlobals {
     uint32_t keyCount;
     uint32_t rngMode;
     uint64_t rngSeed;
-    // slot state (structure of arrays, Q entries)
-    uint4* rng;
-    float4* o;       // xyz origin, w = depth (bits)
-    float4* d;       // xyz direction, w = flags (bits)
-    float4* thr;
-    float4* rad;
-    float4* mis;     // lamUnit, techPath, prevVertexTech, prevBsdfTech
-    float* pdf;      // prevBsdfPdf
+    // path record: one 128-byte line per slot (kRec* words of 16 bytes), so a record read through a queue of scattered
+    // slots touches one line
+    float4* rec;
     uint32_t* slotScene;
     uint32_t* slotItem;    // (pixel, sample) item within the scene
     float4* sampleBuf;     // one result per item, summed per pixel in sample order by the resolve kernel
@@ -89,8 +86,9 @@ struct WfGlobals {
     float4* pend1;
     uint32_t* pendFlags;  // bit 0/1: request 0/1 pending, bit 2/3: request 0/1 visible
     // queues
-    uint32_t* queue0;
+    uint32_t* queue0;       // traversal queues: Q entries, or kRayBins bins of Q entries with rayOrder
     uint32_t* queue1;
+    uint32_t rayOrder;
     uint32_t* finished;
     uint32_t* sorted;
     uint32_t* classQueue;  // 3 * Q: the shade queue partitioned by class (kSortClass)
@@ -116,6 +114,7 @@ struct WfGlobals {
     float4* adjRatioR;  // (df/droughness) / f (xyz), kAdjFlag* bits (w)
     // radiance cache: paths end at surface depth cacheDepth (0xFFFFFFFF = off) with a query
     uint32_t cacheDepth;
+    float cacheSpread;  // > 0: paths also end at the cache by the area-spread rule with this constant
     NrcInput* nrcQueries;  // Q inputs of the iteration's queries
     uint32_t* slotQuery;   // query position of a slot whose path ended at the cache
     float4* nrcPred;       // predictions, by query position
@@ -177,6 +176,50 @@ VKRT_DEV uint32_t warpAggregatedSlot(uint32_t* counters, uint32_t key) {
     return base + __popc(same & ((1u << lane) - 1u));
 }
 
+constexpr uint32_t kRayBins = 8;  // direction octants
+
+// octant of a direction: bit k set when component k is negative
+VKRT_DEV uint32_t dirOctant(float3 d) {
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+
+// Files slot `slot`, whose next ray has direction `dir`, into traversal queue `queue` when `want`; whole warps call
+// it. With rayOrder the queue is kRayBins bins of Q entries, one per direction octant, and counts[queue] keeps the
+// total.
+VKRT_DEV void queuePush(const WfGlobals& g, uint32_t queue, bool want, uint32_t slot, float3 dir) {
+    uint32_t* q = queue == 0 ? g.queue0 : g.queue1;
+    const uint32_t pos = warpPush(&g.counts[queue], want);
+    if (!want) return;
+    if (!g.rayOrder) {
+        q[pos] = slot;
+        return;
+    }
+    const uint32_t b = dirOctant(dir);
+    q[size_t(b) * g.Q + warpAggregatedSlot(&g.counts[kCntBin0 + kRayBins * queue], b)] = slot;
+}
+
+// The running ends of queue `queue`'s bins, written by thread 0 into `binEnd` (shared memory; the caller
+// synchronises the block before use).
+VKRT_DEV void loadBinEnds(const WfGlobals& g, uint32_t queue, uint32_t* binEnd) {
+    if (threadIdx.x != 0u || !g.rayOrder) return;
+    uint32_t s = 0;
+    for (uint32_t b = 0; b < kRayBins; ++b) {
+        s += g.counts[kCntBin0 + kRayBins * queue + b];
+        binEnd[b] = s;
+    }
+}
+
+// entry i of a traversal queue read as one sequence (bins in octant order with rayOrder)
+VKRT_DEV uint32_t queueEntry(const WfGlobals& g, const uint32_t* q, const uint32_t* binEnd, uint32_t i) {
+    if (!g.rayOrder) return q[i];
+    uint32_t b = 0, start = 0;
+    while (b + 1u < kRayBins && i >= binEnd[b]) {
+        start = binEnd[b];
+        ++b;
+    }
+    return q[size_t(b) * g.Q + (i - start)];
+}
+
 // miss / dielectric / metal
 VKRT_DEV uint32_t hitClass(const DeviceScene& sc, const TraceHit& h) {
     if (h.mesh == VKRT_CUDA_INVALID_INDEX) return 0u;
@@ -195,35 +238,48 @@ VKRT_DEV bool workPixel(const WfScene& S, uint32_t local, int& px, int& py) {
     return true;
 }
 
-VKRT_DEV void storePath(const WfGlobals& g, uint32_t s, const PathState& p) {
-    g.rng[s] = make_uint4(uint32_t(p.rng.state), uint32_t(p.rng.state >> 32), uint32_t(p.rng.inc),
-                          uint32_t(p.rng.inc >> 32));
-    g.o[s] = make_float4(p.o.x, p.o.y, p.o.z, __uint_as_float(p.depth));
-    g.d[s] = make_float4(p.d.x, p.d.y, p.d.z, __uint_as_float(p.flags));
-    g.thr[s] = p.thr;
-    g.rad[s] = p.radiance;
-    g.mis[s] = make_float4(p.lamUnit, p.techPath, p.prevVertexTech, p.prevBsdfTech);
-    g.pdf[s] = p.prevBsdfPdf;
+// words of a slot's record: origin + depth, direction + flags (together one 32-byte sector, all the traversal reads),
+// RNG state, throughput, radiance, MIS terms (lamUnit, techPath, prevVertexTech, prevBsdfTech), previous BSDF pdf with
+// the cache's area-spread terms; the eighth word is unused
+enum : uint32_t { kRecOrigin = 0, kRecDir, kRecRng, kRecThr, kRecRad, kRecMis, kRecPdf, kRecWords = 8 };
+
+VKRT_DEV float4* record(const WfGlobals& g, uint32_t s) { return g.rec + size_t(s) * kRecWords; }
+
+VKRT_DEV void packRecord(float4* r, const PathState& p) {
+    r[kRecRng] = make_float4(__uint_as_float(uint32_t(p.rng.state)), __uint_as_float(uint32_t(p.rng.state >> 32)),
+                             __uint_as_float(uint32_t(p.rng.inc)), __uint_as_float(uint32_t(p.rng.inc >> 32)));
+    r[kRecOrigin] = make_float4(p.o.x, p.o.y, p.o.z, __uint_as_float(p.depth));
+    r[kRecDir] = make_float4(p.d.x, p.d.y, p.d.z, __uint_as_float(p.flags));
+    r[kRecThr] = p.thr;
+    r[kRecRad] = p.radiance;
+    r[kRecMis] = make_float4(p.lamUnit, p.techPath, p.prevVertexTech, p.prevBsdfTech);
+    r[kRecPdf] = make_float4(p.prevBsdfPdf, p.spread, p.spreadA0, 0.0f);
 }
+
+VKRT_DEV void storePath(const WfGlobals& g, uint32_t s, const PathState& p) { packRecord(record(g, s), p); }
 
 VKRT_DEV PathState loadPath(const WfGlobals& g, uint32_t s) {
     PathState p;
-    uint4 r = g.rng[s];
-    p.rng.state = uint64_t(r.x) | (uint64_t(r.y) << 32);
-    p.rng.inc = uint64_t(r.z) | (uint64_t(r.w) << 32);
-    float4 o = g.o[s], d = g.d[s];
+    const float4* rp = record(g, s);
+    const float4 r = rp[kRecRng];
+    p.rng.state = uint64_t(__float_as_uint(r.x)) | (uint64_t(__float_as_uint(r.y)) << 32);
+    p.rng.inc = uint64_t(__float_as_uint(r.z)) | (uint64_t(__float_as_uint(r.w)) << 32);
+    const float4 o = rp[kRecOrigin], d = rp[kRecDir];
     p.o = make_float3(o.x, o.y, o.z);
     p.depth = __float_as_uint(o.w);
     p.d = make_float3(d.x, d.y, d.z);
     p.flags = __float_as_uint(d.w);
-    p.thr = g.thr[s];
-    p.radiance = g.rad[s];
-    float4 m = g.mis[s];
+    p.thr = rp[kRecThr];
+    p.radiance = rp[kRecRad];
+    const float4 m = rp[kRecMis];
     p.lamUnit = m.x;
     p.techPath = m.y;
     p.prevVertexTech = m.z;
     p.prevBsdfTech = m.w;
-    p.prevBsdfPdf = g.pdf[s];
+    const float4 pd = rp[kRecPdf];
+    p.prevBsdfPdf = pd.x;
+    p.spread = pd.y;
+    p.spreadA0 = pd.z;
     return p;
 }
 
@@ -254,6 +310,7 @@ VKRT_DEV void loadPathExt(const WfGlobals& g, uint32_t s, PathState& p) {
 
 VKRT_DEV StepConfig stepConfig(const WfGlobals& g, const WfScene& S) {
     StepConfig cfg{S.spectral != 0u, S.neeEnabled != 0u, S.envNee != 0u, g.rngMode, g.rngSeed, g.cacheDepth};
+    cfg.cacheSpread = g.cacheSpread;
     cfg.single = S.spectral != 0u && singleWavelength(S.sd);
     return cfg;
 }
@@ -265,7 +322,7 @@ VKRT_DEV SpecTable specTable(const WfScene& S) {
 // starts sample `sample` of the slot's pixel; returns false for a padding work item
 template <bool kSpectral>
 VKRT_DEV bool startSample(const WfGlobals& g, const WfScene* scenes, uint32_t slot, uint32_t sceneId, uint32_t work,
-                          uint32_t sample) {
+                          uint32_t sample, PathState* held) {
     const WfScene& S = scenes[sceneId];
     int px, py;
     if (!workPixel(S, work, px, py)) return false;
@@ -274,7 +331,8 @@ VKRT_DEV bool startSample(const WfGlobals& g, const WfScene* scenes, uint32_t sl
     uint32_t first = g.mode == kWavefrontForward ? uint32_t(S.film.accumRead[pix].w + 0.5f) : g.adj.sampleBase;
     StepConfig cfg = stepConfig(g, S);
     PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, first + sample);
-    storePath(g, slot, p);
+    if (held) *held = p;
+    else storePath(g, slot, p);
     storePathExt(g, slot, p);
     g.pendFlags[slot] = 0u;
     if (g.mode == kWavefrontAdjoint) {
@@ -296,15 +354,17 @@ VKRT_DEV uint32_t sceneOfItem(const WfGlobals& g, uint32_t w) {
 }
 
 // Takes (pixel, sample) items from the cursor, starting with `w`, until one lies inside a viewport; false when the
-// batch is exhausted. Items of one pixel are consecutive (item = pixel work index * spp + sample).
+// batch is exhausted. Items of one pixel are consecutive (item = pixel work index * spp + sample). With `held` the
+// new path's record is returned there instead of stored.
 template <bool kSpectral>
-VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t slot, uint32_t w) {
+VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t slot, uint32_t w,
+                          PathState* held = nullptr) {
     for (;;) {
         if (w >= g.totalItems) return false;
         uint32_t sceneId = sceneOfItem(g, w);
         const WfScene& S = scenes[sceneId];
         uint32_t local = w - S.itemBase;
-        if (startSample<kSpectral>(g, scenes, slot, sceneId, local / S.spp, local % S.spp)) {
+        if (startSample<kSpectral>(g, scenes, slot, sceneId, local / S.spp, local % S.spp, held)) {
             g.slotScene[slot] = sceneId;
             g.slotItem[slot] = local;
             if (g.features) {
@@ -319,20 +379,40 @@ VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t sl
 }
 
 __global__ void kWfSetup(WfGlobals g) {
-    if (threadIdx.x < 16u) g.counts[threadIdx.x] = 0u;
+    if (threadIdx.x < kCntCount) g.counts[threadIdx.x] = 0u;
     if (threadIdx.x == 0u) {
         g.counts[kCntCursor] = min(g.Q, g.totalItems);
         atomicAdd(&g.counters->kernelLaunches, (unsigned long long)g.launchesOutsideLoop);
     }
 }
 
+// A warp starts 32 consecutive slots, whose records are one contiguous 4 KB run: the records are assembled in shared
+// memory (rows of kRecWords + 1 words, so the 16-byte writes of 8 lanes fall on distinct banks) and stored as 8
+// coalesced warp-wide stores instead of 8 stores that each touch 32 lines.
 template <bool kSpectral>
 __global__ void __launch_bounds__(kWfThreads) kWfInit(WfGlobals g) {
+    constexpr uint32_t kRow = kRecWords + 1u;
+    __shared__ float4 stage[kWfThreads * kRow];
     const WfScene* scenes = g.scenes;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < g.Q; s += gridDim.x * blockDim.x) {
-        bool ok = acquireItem<kSpectral>(g, scenes, s, s < g.totalItems ? s : g.totalItems);
-        uint32_t pos = warpPush(&g.counts[kCntActive0], ok);
-        if (ok) g.queue0[pos] = s;
+    const uint32_t lane = threadIdx.x & 31u;
+    float4* ws = stage + (threadIdx.x >> 5) * 32u * kRow;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < g.Q; base += stride) {
+        const uint32_t s = base + lane;
+        PathState p;
+        bool ok = false;
+        if (s < g.Q) ok = acquireItem<kSpectral>(g, scenes, s, s < g.totalItems ? s : g.totalItems, &p);
+        if (ok) packRecord(ws + lane * kRow, p);
+        const unsigned okMask = __ballot_sync(0xFFFFFFFFu, ok);
+        __syncwarp();
+        float4* out = g.rec + size_t(base) * kRecWords;
+#pragma unroll
+        for (uint32_t k = 0; k < kRecWords; ++k) {
+            const uint32_t j = k * 32u + lane, owner = j / kRecWords;
+            if ((okMask >> owner) & 1u) out[j] = ws[owner * kRow + j % kRecWords];
+        }
+        __syncwarp();
+        queuePush(g, 0u, ok, s, p.d);
     }
 }
 
@@ -397,6 +477,7 @@ __global__ void kWfBegin(WfGlobals g, uint32_t outQueue) {
         g.counts[kCntFetchShadow] = 0u;
         g.counts[kCntClass0] = g.counts[kCntClass0 + 1] = g.counts[kCntClass0 + 2] = 0u;
         g.counts[kCntQueries] = 0u;
+        for (uint32_t b = 0; b < kRayBins; ++b) g.counts[kCntBin0 + kRayBins * outQueue + b] = 0u;
     }
     if (g.sort == kSortMaterial)
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < g.keyCount; k += gridDim.x * blockDim.x)
@@ -434,15 +515,19 @@ VKRT_DEV void storeHit(const WfGlobals& g, uint32_t i, uint32_t slot, const Trac
 template <bool kCount, int kMinBlocks>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals g, uint32_t inQueue) {
     extern __shared__ uint2 smemStack[];
+    __shared__ uint32_t binEnd[kRayBins];
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
+    loadBinEnds(g, inQueue, binEnd);
+    __syncthreads();
     uint32_t primary = 0, ext = 0, nodeVisits = 0, triTests = 0;
     persistentTraceVote<false, kCount>(
         n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags, g.refill,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
-            uint32_t slot = q[i];
+            uint32_t slot = queueEntry(g, q, binEnd, i);
             const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
-            float4 o = g.o[slot], d = g.d[slot];
+            const float4* rp = record(g, slot);
+            float4 o = rp[kRecOrigin], d = rp[kRecDir];
             r = TraceRay{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
             nodes = sc.nodes;
             tris = sc.tris;
@@ -450,7 +535,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
             if (__float_as_uint(o.w) == 0u) ++primary;
             else ++ext;
         },
-        [&](uint32_t i, const TraceHit& h) { storeHit(g, i, q[i], h); }, nodeVisits, triTests);
+        [&](uint32_t i, const TraceHit& h) { storeHit(g, i, queueEntry(g, q, binEnd, i), h); }, nodeVisits,
+        triTests);
     warpCount(&g.counters->primaryRays, primary);
     warpCount(&g.counters->extensionRays, ext);
     if (kCount) warpCountBytes(&g.counters->nodeBytes, &g.counters->triBytes, nodeVisits, triTests);
@@ -461,16 +547,21 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
 template <bool kCount>
 __global__ void __launch_bounds__(kWfThreads) kWfIntersectAlpha(WfGlobals g, uint32_t inQueue) {
     extern __shared__ uint2 smemStack[];
+    __shared__ uint32_t binEnd[kRayBins];
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
+    loadBinEnds(g, inQueue, binEnd);
+    __syncthreads();
     uint32_t primary = 0, ext = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         if (i < n) {
-            const uint32_t slot = q[i];
+            const uint32_t slot = queueEntry(g, q, binEnd, i);
             const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
-            const float4 o = g.o[slot], d = g.d[slot];
-            const uint4 rs = g.rng[slot];
+            const float4* rp = record(g, slot);
+            const float4 o = rp[kRecOrigin], d = rp[kRecDir], rf = rp[kRecRng];
+            const uint4 rs = make_uint4(__float_as_uint(rf.x), __float_as_uint(rf.y), __float_as_uint(rf.z),
+                                        __float_as_uint(rf.w));
             const TraceRay r{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
             const TraceHit h = traceBvh<false, kCount, false, false, true>(
                 sc, r, smemStack + threadIdx.x, blockDim.x, kCount ? g.counters : nullptr, 0u, rs.x ^ rs.y);
@@ -517,11 +608,14 @@ __global__ void __launch_bounds__(1024) kWfSortScan(WfGlobals g) {
 }
 
 __global__ void kWfSortScatter(WfGlobals g, uint32_t inQueue) {
+    __shared__ uint32_t binEnd[kRayBins];
     const uint32_t* q = inQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
+    loadBinEnds(g, inQueue, binEnd);
+    __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t pos = warpAggregatedSlot(g.keyHist, g.hitKey[i]);
-        g.sorted[pos] = q[i];
+        g.sorted[pos] = queueEntry(g, q, binEnd, i);
     }
 }
 
@@ -718,9 +812,11 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         clearMaterialSmem(smemMat, mc);
         __syncthreads();
     }
+    __shared__ uint32_t binEnd[kRayBins];
     const uint32_t* q = g.sort == kSortMaterial ? g.sorted : (inQueue == 0 ? g.queue0 : g.queue1);
-    uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[inQueue];
+    if (g.sort == 0u) loadBinEnds(g, inQueue, binEnd);
+    __syncthreads();
     const uint32_t nMiss = g.counts[kCntClass0], nDiel = g.counts[kCntClass0 + 1];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t i = base + threadIdx.x;
@@ -730,13 +826,14 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         ShadowRequest sh[2];
         NrcInput query{};
         bool queried = false;
+        float3 nextDir = f3(0.0f);
         if (valid) {
             if (g.sort == kSortClass)  // the three class queues read as one
                 slot = i < nMiss ? g.classQueue[i]
                                  : (i < nMiss + nDiel ? g.classQueue[g.Q + (i - nMiss)]
                                                       : g.classQueue[2u * size_t(g.Q) + (i - nMiss - nDiel)]);
             else
-                slot = q[i];
+                slot = g.sort == 0u ? queueEntry(g, q, binEnd, i) : q[i];
             const WfScene& S = scenes[g.slotScene[slot]];
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
@@ -774,6 +871,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
             }
             storePath(g, slot, p);
             if constexpr (kFull) storePathExt(g, slot, p);
+            nextDir = p.d;
             uint32_t flags = queried ? kPendCache : 0u;
             if (ns > 0) {
                 g.pend0[slot] = sh[0].contribution;
@@ -787,9 +885,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         }
         // continuing paths to the next queue, finished ones to finalize (one atomic per warp and queue)
         __syncwarp();
-        uint32_t pos = warpPush(&g.counts[outQueue], valid && cont);
-        if (valid && cont) outQ[pos] = slot;
-        pos = warpPush(&g.counts[kCntFinished], valid && !cont);
+        queuePush(g, outQueue, valid && cont, slot, nextDir);
+        uint32_t pos = warpPush(&g.counts[kCntFinished], valid && !cont);
         if (valid && !cont) g.finished[pos] = slot;
         if (g.cacheDepth != 0xFFFFFFFFu) {
             pos = warpPush(&g.counts[kCntQueries], valid && queried);
@@ -878,7 +975,6 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
         clearMaterialSmem(smemMat, mc);
         __syncthreads();
     }
-    uint32_t* outQ = outQueue == 0 ? g.queue0 : g.queue1;
     const uint32_t n = g.counts[kCntFinished];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t i = base + threadIdx.x;
@@ -913,8 +1009,9 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             requeue = acquireItem<kSpectral>(g, scenes, slot, w);
         }
         __syncwarp();
-        uint32_t pos = warpPush(&g.counts[outQueue], valid && requeue);
-        if (valid && requeue) outQ[pos] = slot;
+        float3 dir = f3(0.0f);
+        if (g.rayOrder && valid && requeue) dir = xyz(record(g, slot)[kRecDir]);
+        queuePush(g, outQueue, valid && requeue, slot, dir);
         warpCount(&g.counters->pathSamples, samples);
     }
     if constexpr (kAdjoint) {
@@ -965,7 +1062,7 @@ struct WfGraphCache {
 struct WavefrontEngine::Buffers {
     WfGlobals g{};
     size_t capQ = 0, capKeys = 0, capScenes = 0;
-    size_t c_rng = 0, c_o = 0, c_d = 0, c_thr = 0, c_rad = 0, c_mis = 0, c_pdf = 0, c_scene = 0, c_work = 0,
+    size_t c_rec = 0, c_scene = 0, c_work = 0,
            c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
            c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0,
            c_fA = 0, c_fN = 0, c_eA = 0, c_eB = 0, c_eC = 0, c_eD = 0, c_as = 0;
@@ -1004,7 +1101,7 @@ void WavefrontEngine::release() {
         gc.graph = nullptr;
     }
     WfGlobals& g = b_->g;
-    void* ptrs[] = {g.rng, g.o, g.d, g.thr, g.rad, g.mis, g.pdf, g.slotScene, g.slotItem, g.sampleBuf,
+    void* ptrs[] = {g.rec, g.slotScene, g.slotItem, g.sampleBuf,
                     g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
                     g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, b_->bases,
                     g.nrcQueries, g.slotQuery, g.nrcPred, b_->recIn, b_->recTarget, b_->recCount, g.adjDelta,
@@ -1066,13 +1163,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WfGlobals& g = B.g;
 #define WF_GROW(field, cap, n) \
     if (e == cudaSuccess) e = grow(g.field, B.cap, (n))
-    WF_GROW(rng, c_rng, Q);
-    WF_GROW(o, c_o, Q);
-    WF_GROW(d, c_d, Q);
-    WF_GROW(thr, c_thr, Q);
-    WF_GROW(rad, c_rad, Q);
-    WF_GROW(mis, c_mis, Q);
-    WF_GROW(pdf, c_pdf, Q);
+    WF_GROW(rec, c_rec, size_t(kRecWords) * Q);
     WF_GROW(slotScene, c_scene, Q);
     WF_GROW(slotItem, c_work, Q);
     WF_GROW(sampleBuf, c_sum, std::max<size_t>(totalItems, 1));
@@ -1103,15 +1194,15 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(pend0, c_p0, Q);
     WF_GROW(pend1, c_p1, Q);
     WF_GROW(pendFlags, c_pf, Q);
-    WF_GROW(queue0, c_q0, Q);
-    WF_GROW(queue1, c_q1, Q);
+    WF_GROW(queue0, c_q0, size_t(cfg.rayOrder ? kRayBins : 1u) * Q);
+    WF_GROW(queue1, c_q1, size_t(cfg.rayOrder ? kRayBins : 1u) * Q);
     WF_GROW(finished, c_fin, Q);
     WF_GROW(sorted, c_sorted, Q);
     if (cfg.sortByMaterial == kSortClass) WF_GROW(classQueue, c_class, 3 * size_t(Q));
     WF_GROW(shadowA, c_sA, 2 * size_t(Q));
     WF_GROW(shadowB, c_sB, 2 * size_t(Q));
     WF_GROW(keyHist, c_hist, keys);
-    WF_GROW(counts, c_counts, 16);
+    WF_GROW(counts, c_counts, kCntCount);
     if (useCache) {
         WF_GROW(nrcQueries, c_nq, Q);
         WF_GROW(slotQuery, c_sq, Q);
@@ -1156,6 +1247,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.alpha = alpha ? 1u : 0u;
     g.adj = adjoint ? *adjoint : AdjointParams{};
     g.cacheDepth = useCache ? cache->cacheDepth : 0xFFFFFFFFu;
+    g.cacheSpread = useCache ? cache->cacheSpread : 0.0f;
     g.scenes = B.scenes;
     g.itemBases = B.bases;
     g.workBases = B.bases + scenes.size();
@@ -1166,6 +1258,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.maxIter = maxIter;
     g.sort = cfg.sortByMaterial <= kSortClass ? cfg.sortByMaterial : kSortMaterial;
     g.refill = int(std::min(std::max(cfg.refillLanes, 1u), 32u));
+    g.rayOrder = cfg.rayOrder ? 1u : 0u;
     g.keyCount = keys;
     g.rngMode = rngMode;
     g.rngSeed = rngSeed;

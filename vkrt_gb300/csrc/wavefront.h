@@ -46,6 +46,7 @@ struct WavefrontConfig {
     uint32_t useGraph;
     uint32_t profileStages;  // 1: no graph; traversal kernels count fetch bytes; per-stage device times recorded
     uint32_t refillLanes;    // persistent traversal refill threshold (lanes still traversing), 1..32
+    uint32_t rayOrder;       // 1: traversal queues binned by ray-direction octant
 };
 
 // stages of the per-stage device times
@@ -63,6 +64,7 @@ struct WfCacheFrame {
     uint32_t trainingSteps;
     uint32_t seed;
     uint32_t frame;
+    float cacheSpread;  // area-spread constant c (0: paths end at cacheDepth only)
 };
 
 class WavefrontEngine {
