@@ -804,6 +804,8 @@ def run_profile_frame(args) -> dict:
         ctx.set_wavefront_config(refillLanes=args.refill)
     if args.intersect_blocks:
         ctx.set_wavefront_config(intersectBlocksPerSM=args.intersect_blocks)
+    if args.ray_order:
+        ctx.set_wavefront_config(rayOrder=args.ray_order)
     if args.cache:
         ctx.nrc_configure(enabled=1)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -832,7 +834,7 @@ def run_profile_frame(args) -> dict:
                        "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
                        "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
-                       "intersect_blocks": args.intersect_blocks}
+                       "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order}
     ctx.close()
     return out
 
@@ -865,6 +867,7 @@ def main():
     prof.add_argument("--shade-blocks", type=int, default=0, help="shade kernel residency (blocks per SM)")
     prof.add_argument("--refill", type=int, default=0, help="traversal refill threshold (lanes; 0 = default)")
     prof.add_argument("--intersect-blocks", type=int, default=0, help="traversal kernel residency (blocks per SM)")
+    prof.add_argument("--ray-order", type=int, default=0, help="1: traversal queues binned by direction octant")
     args = ap.parse_args()
     if args.profile_frame:
         print(json.dumps(run_profile_frame(args)))

@@ -52,7 +52,9 @@ def test_wavefront_schedule_independence(built):
     base, _ = _render(scene, abi.INTEGRATOR_WAVEFRONT, wf={"queueCapacity": 0}, **kw)
     for wf in ({"sortByMaterial": 1}, {"sortByMaterial": 2}, {"useGraph": 0},
                {"tileWidth": 4, "tileHeight": 4, "queueCapacity": 300, "sortByMaterial": 2},
-               {"queueCapacity": 97, "sortByMaterial": 1, "intersectBlocksPerSM": 2, "shadeBlocksPerSM": 1}):
+               {"queueCapacity": 97, "sortByMaterial": 1, "intersectBlocksPerSM": 2, "shadeBlocksPerSM": 1},
+               {"rayOrder": 1}, {"rayOrder": 1, "sortByMaterial": 0}, {"rayOrder": 1, "sortByMaterial": 1},
+               {"rayOrder": 1, "queueCapacity": 300, "useGraph": 0}):
         got, _ = _render(scene, abi.INTEGRATOR_WAVEFRONT, wf=wf, **kw)
         np.testing.assert_array_equal(got, base, err_msg=str(wf))
     mega, _ = _render(scene, abi.INTEGRATOR_MEGAKERNEL, **kw)
@@ -114,3 +116,13 @@ def test_batch_of_mixed_material_scenes(built):
     finally:
         for c in ctxs:
             c.close()
+
+
+def test_ray_order_with_alpha_and_glass(built):
+    """Direction-octant queue bins feed the alpha-tested traversal and the full-stack kernels the same paths: the
+    images equal the unbinned renders bit for bit."""
+    from tests.test_gpu_materials import alpha_cornell, glass_cornell
+    for s in (alpha_cornell(40, 48, spp=2), glass_cornell(48, 40, spp=2, abbe=30.0, absorb=2.0)):
+        base, _ = _render(s, abi.INTEGRATOR_WAVEFRONT, rng_mode=abi.RNG_PCG32)
+        got, _ = _render(s, abi.INTEGRATOR_WAVEFRONT, wf={"rayOrder": 1}, rng_mode=abi.RNG_PCG32)
+        np.testing.assert_array_equal(got, base)
