@@ -830,6 +830,9 @@ def run_profile_frame(args) -> dict:
             for k, v in zip(abi.WAVEFRONT_STAGES, st["stageMs"]):
                 out.setdefault("stage_ms", {})[k] = round(out.get("stage_ms", {}).get(k, 0.0) + float(v), 3)
             out["frame_ms"] = round(out.get("frame_ms", 0.0) + ev[0].elapsed_time(ev[1]), 3)
+    st = ctx.stats()
+    out["bvh"] = {"nodes": int(st["bvhNodeCount"]), "triangles": int(st["bvhTriangleCount"]),
+                  "build_ms": round(float(st["bvhBuildMs"]), 2)}
     out["workload"] = {"width": args.width, "height": args.height, "spp": args.spp, "depth": args.depth,
                        "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",

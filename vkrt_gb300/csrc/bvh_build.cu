@@ -10,7 +10,8 @@
 //   5. LBVH      : Karras 2012 binary radix tree, ties in the code broken by the sorted position
 //   6. refit     : bottom-up boxes, subtree sizes and SAH cost with one atomic arrival flag per node
 //   7. treelets  : Karras & Aila 2013 treelet restructuring (7 leaves, exhaustive over partitions by DP) in rounds
-//   8. collapse  : binary -> 8-wide compressed nodes, level by level, leaves of up to 3 triangles, children placed in
+//   8. collapse  : binary -> 8-wide compressed nodes, children chosen by the SAH-optimal dynamic program of Ylitie et
+//                  al. 2017, level by level, leaves of up to 3 triangles, children placed in
 //                  octant slots so traversal visits them near to far (Ylitie et al. 2017)
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -467,6 +468,111 @@ __global__ void kRootSah(const float4* nodeLo, const float4* nodeHi, const float
 }
 
 // ---- 8. collapse to 8-wide compressed nodes -------------------------------------------------------------------
+// SAH-optimal collapse (Ylitie, Karras, Laine 2017, section 3.1), bottom-up over the binary tree: C(n, i) is the
+// lowest cost of representing the subtree of binary node n as at most i children of a wide node,
+//   C(n, 1) = min(C_leaf(n), C_internal(n)),  C(n, i) = min(C(n, i - 1), C_distribute(n, i))  for i > 1,
+//   C_distribute(n, j) = min over 0 < k < j of C(left, k) + C(right, j - k),
+//   C_internal(n) = c_node A(n) + C_distribute(n, 8),  C_leaf(n) = c_tri A(n) p(n) when p(n) <= 3 triangles,
+// A the box's half area, p the triangle count. The choices are kept per node in eight bytes: byte 0 is 0 for a leaf
+// or the split k of C_distribute(n, 8) for an internal wide node; byte i - 1 (i > 1) is 0 when C(n, i) = C(n, i - 1)
+// or the split k of C_distribute(n, i).
+constexpr float kWideCostNode = 1.0f;  // a wide node visit (eight box tests)
+constexpr float kWideCostTri = 1.0f;   // one triangle test (a traversal step, like a node visit)
+constexpr uint32_t kWideLeafMax = 3u;  // triangles per leaf child (three triangle-mask bits per child)
+
+__device__ __forceinline__ void wideLeafCost(float a, float* c, uint8_t* d) {
+    for (int i = 0; i < 8; ++i) {
+        c[i] = kWideCostTri * a;
+        d[i] = 0u;
+    }
+}
+
+__global__ void kWideCostLeaves(uint32_t n, const float4* __restrict__ nodeLo, const float4* __restrict__ nodeHi,
+                                float4* __restrict__ wideCost, uint2* __restrict__ wideDec, uint32_t* __restrict__ flags) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n - 1) flags[k] = 0u;
+    if (k >= n) return;
+    const uint32_t node = n - 1 + k;
+    float c[8];
+    uint8_t d[8];
+    wideLeafCost(halfArea(nodeLo[node], nodeHi[node]), c, d);
+    wideCost[2 * node] = make_float4(c[0], c[1], c[2], c[3]);
+    wideCost[2 * node + 1] = make_float4(c[4], c[5], c[6], c[7]);
+    wideDec[node] = make_uint2(0u, 0u);
+}
+
+// one thread per binary leaf walks up; the second arrival at a node computes its costs (as the refit does)
+__global__ void kWideCost(uint32_t n, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                          const uint32_t* __restrict__ parent, const float4* __restrict__ nodeLo,
+                          const float4* __restrict__ nodeHi, const uint32_t* __restrict__ leafCount,
+                          float4* wideCost, uint2* wideDec, uint32_t* flags) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t node = parent[n - 1 + k];
+    while (node != kInvalid) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0u) return;
+        __threadfence();
+        const uint32_t l = left[node], r = right[node];
+        float cl[8], cr[8];
+        const float4 l0 = __ldcg(&wideCost[2 * l]), l1 = __ldcg(&wideCost[2 * l + 1]);
+        const float4 r0 = __ldcg(&wideCost[2 * r]), r1 = __ldcg(&wideCost[2 * r + 1]);
+        cl[0] = l0.x, cl[1] = l0.y, cl[2] = l0.z, cl[3] = l0.w, cl[4] = l1.x, cl[5] = l1.y, cl[6] = l1.z, cl[7] = l1.w;
+        cr[0] = r0.x, cr[1] = r0.y, cr[2] = r0.z, cr[3] = r0.w, cr[4] = r1.x, cr[5] = r1.y, cr[6] = r1.z, cr[7] = r1.w;
+        // C_distribute(node, j) for j = 2..8 (cl[i - 1] = C(left, i))
+        float dist[9];
+        uint8_t split[9];
+        for (int j = 2; j <= 8; ++j) {
+            float best = INFINITY;
+            uint8_t bk = 1u;
+            for (int kk = 1; kk < j; ++kk) {
+                const float v = cl[kk - 1] + cr[j - kk - 1];
+                if (v < best) {
+                    best = v;
+                    bk = uint8_t(kk);
+                }
+            }
+            dist[j] = best;
+            split[j] = bk;
+        }
+        const float a = halfArea(__ldcg(&nodeLo[node]), __ldcg(&nodeHi[node]));
+        const uint32_t cnt = leafCount[node];
+        const float cInternal = kWideCostNode * a + dist[8];
+        const float cLeaf = cnt <= kWideLeafMax ? kWideCostTri * a * float(cnt) : INFINITY;
+        float c[8];
+        uint8_t d[8];
+        if (cnt <= kWideLeafMax && cLeaf <= cInternal) {
+            c[0] = cLeaf;
+            d[0] = 0u;
+        } else {
+            c[0] = cInternal;
+            d[0] = split[8];
+        }
+        for (int i = 2; i <= 8; ++i) {
+            if (c[i - 2] <= dist[i]) {
+                c[i - 1] = c[i - 2];
+                d[i - 1] = 0u;
+            } else {
+                c[i - 1] = dist[i];
+                d[i - 1] = split[i];
+            }
+        }
+        wideCost[2 * node] = make_float4(c[0], c[1], c[2], c[3]);
+        wideCost[2 * node + 1] = make_float4(c[4], c[5], c[6], c[7]);
+        wideDec[node] = make_uint2(uint32_t(d[0]) | (uint32_t(d[1]) << 8) | (uint32_t(d[2]) << 16) |
+                                       (uint32_t(d[3]) << 24),
+                                   uint32_t(d[4]) | (uint32_t(d[5]) << 8) | (uint32_t(d[6]) << 16) |
+                                       (uint32_t(d[7]) << 24));
+        node = parent[node];
+    }
+}
+
+__device__ __forceinline__ uint32_t wideChoice(const uint2* wideDec, uint32_t node, uint32_t i) {
+    const uint2 d = wideDec[node];
+    const uint32_t w = i < 4u ? d.x : d.y;
+    return (w >> ((i & 3u) * 8u)) & 0xFFu;
+}
+
 struct CollapseItem {
     uint32_t binary;  // binary node index
     uint32_t wide;    // wide node slot to fill
@@ -487,7 +593,8 @@ __global__ void kCollapse(uint32_t n, const CollapseItem* __restrict__ in, uint3
                           CollapseItem* __restrict__ out, uint32_t* __restrict__ outCount,
                           const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
                           const float4* __restrict__ nodeLo, const float4* __restrict__ nodeHi,
-                          const uint32_t* __restrict__ leafCount, const uint32_t* __restrict__ sortedIds,
+                          const uint32_t* __restrict__ leafCount, const uint2* __restrict__ wideDec,
+                          const uint32_t* __restrict__ sortedIds,
                           const TriRecord* __restrict__ trisIn, uint32_t* __restrict__ nodeCursor,
                           uint32_t* __restrict__ triCursor, WideNode* __restrict__ nodes,
                           TriRecord* __restrict__ trisOut) {
@@ -498,30 +605,37 @@ __global__ void kCollapse(uint32_t n, const CollapseItem* __restrict__ in, uint3
     uint32_t child[8];
     int cnt = 0;
     auto isLeaf = [&](uint32_t b) { return b >= firstLeaf; };
+    // a child is internal (another wide node) when the collapse chose so, else a leaf of at most three triangles
+    auto isInternal = [&](uint32_t b) { return !isLeaf(b) && wideChoice(wideDec, b, 0u) != 0u; };
     if (isLeaf(item.binary)) {
         child[cnt++] = item.binary;  // single-triangle scene
     } else {
-        child[cnt++] = left[item.binary];
-        child[cnt++] = right[item.binary];
-    }
-    // greedy expansion: split the largest child with more than 3 triangles until 8 children
-    while (cnt < 8) {
-        int best = -1;
-        float bestArea = -1.0f;
-        for (int c = 0; c < cnt; ++c) {
-            if (isLeaf(child[c]) || leafCount[child[c]] <= 3u) continue;
-            float a = halfArea(nodeLo[child[c]], nodeHi[child[c]]);
-            if (a > bestArea) {
-                bestArea = a;
-                best = c;
+        // the roots of C_distribute(item, 8): (node, i) = the subtree of node as at most i children
+        uint32_t stackNode[8], stackI[8];
+        int sp = 0;
+        // the root of a scene of at most three triangles may have chosen to be a leaf: split it 1 + 7
+        const uint32_t k0 = max(wideChoice(wideDec, item.binary, 0u), 1u);
+        stackNode[sp] = right[item.binary], stackI[sp++] = 8u - k0;
+        stackNode[sp] = left[item.binary], stackI[sp++] = k0;
+        while (sp > 0) {
+            uint32_t m = stackNode[--sp], i = stackI[sp];
+            for (;;) {
+                if (i <= 1u || isLeaf(m)) {
+                    child[cnt++] = m;
+                    break;
+                }
+                const uint32_t kk = wideChoice(wideDec, m, i - 1u);
+                if (kk == 0u) {
+                    --i;
+                    continue;
+                }
+                stackNode[sp] = right[m], stackI[sp++] = i - kk;
+                stackNode[sp] = left[m], stackI[sp++] = kk;
+                break;
             }
         }
-        if (best < 0) break;
-        uint32_t b = child[best];
-        child[best] = left[b];
-        child[cnt++] = right[b];
     }
-    // a child with <= 3 triangles becomes a leaf (its triangles are gathered below)
+    // a leaf child's triangles (at most three) are gathered below
     // octant slot assignment: slot s prefers the child furthest along (+-1,+-1,+-1) with bit set = positive
     float4 plo = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), phi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
     float3 cc[8];
@@ -568,7 +682,7 @@ __global__ void kCollapse(uint32_t n, const CollapseItem* __restrict__ in, uint3
         int c = childInSlot[s];
         if (c < 0) continue;
         uint32_t b = child[c];
-        if (!isLeaf(b) && leafCount[b] > 3u) numInternal++;
+        if (isInternal(b)) numInternal++;
         else numTris += isLeaf(b) ? 1u : leafCount[b];
     }
     uint32_t childBase = numInternal ? atomicAdd(nodeCursor, numInternal) : 0u;
@@ -605,7 +719,7 @@ __global__ void kCollapse(uint32_t n, const CollapseItem* __restrict__ in, uint3
             qlo[k][s] = uint8_t(fminf(fmaxf(ql, 0.0f), 255.0f));
             qhi[k][s] = uint8_t(fminf(fmaxf(qh, 0.0f), 255.0f));
         }
-        if (!isLeaf(b) && leafCount[b] > 3u) {
+        if (isInternal(b)) {
             meta[s] = uint8_t((1u << 5) | (24u + uint32_t(s)));
             imask |= 1u << s;
             out[outBase + nextInternal] = CollapseItem{b, childBase + nextInternal};
@@ -697,6 +811,8 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
     uint32_t* dParent = dalloc<uint32_t>(2 * n, err);
     uint32_t* dLeafCount = dalloc<uint32_t>(2 * n, err);
     float* dCost = dalloc<float>(2 * n, err);
+    float4* dWideCost = dalloc<float4>(4 * size_t(n), err);  // C(node, 1..8) as two float4 per binary node
+    uint2* dWideDec = dalloc<uint2>(2 * size_t(n), err);
     uint32_t* dFlags = dalloc<uint32_t>(n, err);
     float* dSah = dalloc<float>(2, err);
     // wide nodes: at most one per internal binary node
@@ -748,6 +864,11 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
             }
             kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah + 1);
         }
+        // SAH-optimal choice of each wide node's children
+        kWideCostLeaves<<<(n + b - 1) / b, b, 0, stream>>>(n, dLo, dHi, dWideCost, dWideDec, dFlags);
+        if (n > 1)
+            kWideCost<<<(n + b - 1) / b, b, 0, stream>>>(n, dLeft, dRight, dParent, dLo, dHi, dLeafCount, dWideCost,
+                                                         dWideDec, dFlags);
     }
     {
         // level-by-level collapse; the root wide node is slot 0
@@ -762,7 +883,8 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
             uint32_t zero = 0u;
             cudaMemcpyAsync(dCounters + 2, &zero, sizeof(zero), cudaMemcpyHostToDevice, stream);
             kCollapse<<<(inCount + 127) / 128, 128, 0, stream>>>(n, dQueue[q], inCount, dQueue[q ^ 1], dCounters + 2,
-                                                                 dLeft, dRight, dLo, dHi, dLeafCount, dVals[0],
+                                                                 dLeft, dRight, dLo, dHi, dLeafCount, dWideDec,
+                                                                 dVals[0],
                                                                  dTrisFlat, dCounters, dCounters + 1, out.nodes,
                                                                  out.tris);
             err = cudaMemcpyAsync(&inCount, dCounters + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
@@ -812,6 +934,8 @@ done:
     cudaFree(dParent);
     cudaFree(dLeafCount);
     cudaFree(dCost);
+    cudaFree(dWideCost);
+    cudaFree(dWideDec);
     cudaFree(dFlags);
     cudaFree(dSah);
     cudaFree(dQueue[0]);

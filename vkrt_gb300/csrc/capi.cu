@@ -101,6 +101,7 @@ struct VKRT_CudaContext {
     bool alphaTested = false;       // some mesh's material (or the mesh) is alpha-tested
     VKRT_CudaRGB2SpecTableInfo rgb2specInfo{};
     DeviceArray<float4> rgb2specCells;  // the table of rgb2specInfo repacked one float4 per cell
+    DeviceArray<uint16_t> rgb2specGuide;  // its brightness guide
 
     // environment distribution
     DeviceArray<float> envMarginal, envConditional, envTexelPdf;
@@ -259,6 +260,7 @@ DeviceScene makeDeviceScene(VKRT_CudaContext* c) {
     s.sheenLtc = c->sheenTable.ptr;
     s.rgb2specCells = c->rgb2specCells.ptr;
     s.rgb2specCellsInfo = c->rgb2specInfo;
+    s.rgb2specGuide = c->rgb2specGuide.ptr;
     s.env.marginal = c->envMarginal.ptr;
     s.env.conditional = c->envConditional.ptr;
     s.env.texelPdf = c->envTexelPdf.ptr;
@@ -452,6 +454,7 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     c->textureTable.release();
     c->rgb2spec.release();
     c->rgb2specCells.release();
+    c->rgb2specGuide.release();
     c->envMarginalGuide.release();
     c->envConditionalGuide.release();
     c->envMarginal.release();
@@ -721,6 +724,9 @@ int32_t vkrt_cuda_upload_rgb2spec(VKRT_CudaContext* c, const float* table, uint3
     VKRT_TRY(c, c->rgb2specCells.reserve(size_t(3) * info->res * info->res * info->res), "rgb2spec cells");
     VKRT_TRY(c, launchRepackRgb2Spec(c->rgb2spec.ptr, info->res, info->dataOffset, c->rgb2specCells.ptr, c->stream),
              "rgb2spec cells");
+    VKRT_TRY(c, c->rgb2specGuide.reserve(kRgb2SpecGuide + 1u), "rgb2spec guide");
+    VKRT_TRY(c, launchRgb2SpecGuide(c->rgb2spec.ptr, info->res, info->scaleOffset, c->rgb2specGuide.ptr, c->stream),
+             "rgb2spec guide");
     return VKRT_CUDA_SUCCESS;
 }
 
@@ -735,6 +741,8 @@ int32_t vkrt_cuda_generate_rgb2spec(VKRT_CudaContext* c, uint32_t res, VKRT_Cuda
     c->rgb2specInfo = VKRT_CudaRGB2SpecTableInfo{res, 0u, res};
     VKRT_TRY(c, c->rgb2specCells.reserve(size_t(3) * res * res * res), "rgb2spec cells");
     VKRT_TRY(c, launchRepackRgb2Spec(c->rgb2spec.ptr, res, res, c->rgb2specCells.ptr, c->stream), "rgb2spec cells");
+    VKRT_TRY(c, c->rgb2specGuide.reserve(kRgb2SpecGuide + 1u), "rgb2spec guide");
+    VKRT_TRY(c, launchRgb2SpecGuide(c->rgb2spec.ptr, res, 0u, c->rgb2specGuide.ptr, c->stream), "rgb2spec guide");
     if (outInfo) *outInfo = c->rgb2specInfo;
     return VKRT_CUDA_SUCCESS;
 }

@@ -512,6 +512,9 @@ VKRT_DEV bool shadePathVertexSubset(const DeviceScene& sc, const VKRT_CudaSceneD
         return false;
     }
 
+    // the spectral stack's direction-independent term, shared by the NEE evaluations and the continuation
+    const float4 vaSub = kSpectral && bsdf.wo.z > 0.0f ? spectralDiffuseTerm(bsdf, tab, lam) : f4(0.0f);
+
     // emissive-triangle NEE (light/direct/light_sampling.slang, rgb_lighting.slang / spectral_lighting.slang)
     if (cfg.neeEnabled && bsdf.wo.z > 0.0f) {
         LightSample ls;
@@ -520,7 +523,7 @@ VKRT_DEV bool shadePathVertexSubset(const DeviceScene& sc, const VKRT_CudaSceneD
             float pdf;
             float4 c = f4(0.0f);
             if (kSpectral) {
-                float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
+                float4 fcos = evalSpectral(bsdf, tab, wl, lam, vaSub, pdf) * fabsf(wl.z);
                 float lt = p.techPath * ls.pdfSA, bt = p.techPath * pdf;
                 float den = 4.0f * lt + 4.0f * bt;
                 float mis = den > 0.0f ? lt / den : 0.0f;
@@ -549,7 +552,7 @@ VKRT_DEV bool shadePathVertexSubset(const DeviceScene& sc, const VKRT_CudaSceneD
             float pdf;
             float4 c = f4(0.0f);
             if (kSpectral) {
-                float4 fcos = evalSpectral(bsdf, tab, wl, lam, pdf) * fabsf(wl.z);
+                float4 fcos = evalSpectral(bsdf, tab, wl, lam, vaSub, pdf) * fabsf(wl.z);
                 float lt = p.techPath * pe, bt = p.techPath * pdf;
                 float den = 4.0f * lt + 4.0f * bt;
                 float mis = den > 0.0f ? lt / den : 0.0f;
@@ -575,7 +578,7 @@ VKRT_DEV bool shadePathVertexSubset(const DeviceScene& sc, const VKRT_CudaSceneD
     if (!sampleDirection(bsdf, p.rng, wl)) return false;
     float pdf;
     if (kSpectral) {
-        float4 val = evalSpectral(bsdf, tab, wl, lam, pdf);
+        float4 val = evalSpectral(bsdf, tab, wl, lam, vaSub, pdf);
         if (!(pdf > 0.0f)) return false;
         float4 weight = val * (fabsf(wl.z) / pdf);
         if (!anyPos(weight)) return false;

@@ -315,6 +315,21 @@ __global__ void kRepackRgb2Spec(const float* table, uint32_t res, uint32_t dataO
     }
 }
 
+// The brightness guide of a table (one block): entry b is the interval of b / kRgb2SpecGuide, found by the binary
+// search itself; every entry is 0xFFFF when the scale is not non-decreasing, so lookups keep the binary search.
+__global__ void __launch_bounds__(1024) kBuildRgb2SpecGuide(const float* table, uint32_t res, uint32_t scaleOffset,
+                                                        uint16_t* guide) {
+    __shared__ int monotone;
+    if (threadIdx.x == 0) monotone = 1;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i + 1u < res; i += blockDim.x)
+        if (!(table[scaleOffset + i] <= table[scaleOffset + i + 1u])) monotone = 0;
+    __syncthreads();
+    const SpecTable tab{table, res, scaleOffset, 0u, nullptr, nullptr};
+    for (uint32_t b = threadIdx.x; b <= kRgb2SpecGuide; b += blockDim.x)
+        guide[b] = monotone ? uint16_t(rgb2specIntervalSearch(tab, float(b) / float(kRgb2SpecGuide))) : 0xFFFFu;
+}
+
 __global__ void kEnvTexelPdf(const double* f, uint32_t W, uint32_t H, const double* total, float* pdf) {
     size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= size_t(W) * H) return;
@@ -525,6 +540,13 @@ cudaError_t launchRepackRgb2Spec(const float* table, uint32_t res, uint32_t data
                                  cudaStream_t stream) {
     const uint32_t n = 3u * res * res * res;
     kRepackRgb2Spec<<<(n + 255u) / 256u, 256, 0, stream>>>(table, res, dataOffset, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launchRgb2SpecGuide(const float* table, uint32_t res, uint32_t scaleOffset, uint16_t* guide,
+                                cudaStream_t stream) {
+    if (res < 2 || res > 0xFFFFu) return cudaErrorInvalidValue;
+    kBuildRgb2SpecGuide<<<1, 1024, 0, stream>>>(table, res, scaleOffset, guide);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,10 @@ cudaError_t launchBuildEnvGuides(const float* marginal, const float* conditional
 cudaError_t launchRepackRgb2Spec(const float* table, uint32_t res, uint32_t dataOffset, float4* cells,
                                  cudaStream_t stream);
 
+// Brightness guide of an rgb2spec table: kRgb2SpecGuide + 1 interval indices (see DeviceScene::rgb2specGuide).
+cudaError_t launchRgb2SpecGuide(const float* table, uint32_t res, uint32_t scaleOffset, uint16_t* guide,
+                                cudaStream_t stream);
+
 // rgb2spec table fit on the device; `table` holds res + 3*res^3*3 floats.
 cudaError_t launchGenerateRgb2Spec(uint32_t res, float* table, cudaStream_t stream);
 

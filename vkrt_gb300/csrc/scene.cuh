@@ -73,6 +73,9 @@ struct DeviceScene {
     uint32_t rgb2specFloatCount;
     // the table selected by rgb2specCellsInfo repacked one float4 (3 coefficients) per cell: [3][res][res][res]
     const float4* rgb2specCells;
+    // for the same table: the brightness interval of z = b / kRgb2SpecGuide for b = 0..kRgb2SpecGuide (0xFFFF in every
+    // entry when the table's scale is not non-decreasing)
+    const uint16_t* rgb2specGuide;
     VKRT_CudaRGB2SpecTableInfo rgb2specCellsInfo;
     EnvDistribution env;
     const float* sheenLtc;  // sheen LTC table (3 x 32 x 32), null until uploaded
@@ -95,6 +98,9 @@ struct RenderCounters {
 
 constexpr uint32_t kErrorStackOverflow = 1u;
 constexpr uint32_t kEnvGuide = 256u;
+// buckets of the rgb2spec brightness guide; a power of two, so b = floor(z * kRgb2SpecGuide) is exact and b / kRgb2SpecGuide
+// never exceeds z
+constexpr uint32_t kRgb2SpecGuide = 1024u;
 // persistent vote-scheduled traversal: by default a warp fetches new rays once fewer than this many of its lanes are
 // still traversing
 constexpr int kVoteRefillLanes = 20;

@@ -254,7 +254,8 @@ VKRT_DEV bool selectionAlphaAccepts(const DeviceScene& sc, uint32_t mesh, uint32
 struct SpecTable {
     const float* t;
     uint32_t res, scaleOffset, dataOffset;
-    const float4* cells;  // the same coefficients one float4 per cell, or null
+    const float4* cells;    // the same coefficients one float4 per cell, or null
+    const uint16_t* guide;  // brightness guide of the same table (DeviceScene::rgb2specGuide), or null
 };
 
 // the frame's table (SceneData.rgb2specSRGB) with its repacked cells when the context holds them for that layout
@@ -262,11 +263,12 @@ VKRT_DEV SpecTable makeSpecTable(const DeviceScene& sc, const VKRT_CudaSceneData
     const VKRT_CudaRGB2SpecTableInfo& i = sd.rgb2specSRGB;
     bool packed = sc.rgb2specCells && sc.rgb2specCellsInfo.res == i.res &&
                   sc.rgb2specCellsInfo.scaleOffset == i.scaleOffset && sc.rgb2specCellsInfo.dataOffset == i.dataOffset;
-    return SpecTable{sc.rgb2spec, i.res, i.scaleOffset, i.dataOffset, packed ? sc.rgb2specCells : nullptr};
+    return SpecTable{sc.rgb2spec, i.res, i.scaleOffset, i.dataOffset, packed ? sc.rgb2specCells : nullptr,
+                     packed ? sc.rgb2specGuide : nullptr};
 }
 
-// Largest i in [0, res - 2] with scale[i] <= x (utility/rgb2spec.slang:14-32).
-VKRT_DEV uint32_t rgb2specInterval(const SpecTable& tab, float x) {
+// Largest i in [0, res - 2] with scale[i] <= x (utility/rgb2spec.slang:14-32), by binary search.
+VKRT_DEV uint32_t rgb2specIntervalSearch(const SpecTable& tab, float x) {
     int left = 0, size = int(tab.res) - 2;
     while (size > 0) {
         int half = size >> 1, middle = left + half + 1;
@@ -278,6 +280,20 @@ VKRT_DEV uint32_t rgb2specInterval(const SpecTable& tab, float x) {
         }
     }
     return min(uint32_t(left), tab.res - 2u);
+}
+
+// The same interval from the brightness guide: the guide holds the interval of b / kRgb2SpecGuide <= x, and on a
+// non-decreasing scale the interval of x is reached by stepping forward from it (usually zero or one step).
+VKRT_DEV uint32_t rgb2specInterval(const SpecTable& tab, float x) {
+    if (tab.guide && x >= 0.0f && x <= 1.0f) {
+        const uint32_t g = __ldg(tab.guide + uint32_t(x * float(kRgb2SpecGuide)));
+        if (g != 0xFFFFu) {
+            uint32_t i = g;
+            while (i + 2u < tab.res && __ldg(tab.t + tab.scaleOffset + i + 1u) <= x) ++i;
+            return i;
+        }
+    }
+    return rgb2specIntervalSearch(tab, x);
 }
 
 VKRT_DEV float3 rgb2specFetch(const SpecTable& tab, float3 rgb) {
@@ -783,8 +799,20 @@ VKRT_DEV float3 evalRgb(const Bsdf& s, float3 wi, float& pdf) {
     return metal * s.mat.metallic + (diel + s.viewAtten * sub) * (1.0f - s.mat.metallic);
 }
 
-// 4-lane spectral stack of the subset (principled/eval_spectral.slang:4-94); all lanes share one technique pdf
-VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, float4 l, float& pdf) {
+// The direction-independent product of the spectral stack, view attenuation x diffuse (both upsampled from RGB):
+// the same for every direction a vertex evaluates, so a vertex computes it once. It is multiplied by
+// (1 - metallic), so a pure metal skips it (the product is finite and would contribute exactly zero).
+VKRT_DEV float4 spectralDiffuseTerm(const Bsdf& s, const SpecTable& tab, float4 l) {
+    if (!(1.0f - s.mat.metallic != 0.0f)) return f4(0.0f);
+    float4 sub = f4(0.0f);
+    if (s.wDiff > 0.0f) sub = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l) * kInvPi;
+    const float4 va = spectral4(tab, sat(s.viewAtten), l);
+    return va * sub;
+}
+
+// 4-lane spectral stack of the subset (principled/eval_spectral.slang:4-94); all lanes share one technique pdf.
+// `vaSub` is spectralDiffuseTerm of the same Bsdf and wavelengths.
+VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, float4 l, float4 vaSub, float& pdf) {
     pdf = 0.0f;
     if (wi.z <= 0.0f) return f4(0.0f);
     float4 metal = f4(0.0f), diel = f4(0.0f);
@@ -807,13 +835,8 @@ VKRT_DEV float4 evalSpectral(const Bsdf& s, const SpecTable& tab, float3 wi, flo
         diel = spectral4(tab, sat(schlick(wom, s.f0Diel)), l) * DG;
         pdf += s.wDiel * reflPdf;
     }
-    float4 sub = f4(0.0f);
-    if (s.wDiff > 0.0f) {
-        sub = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l) * kInvPi;
-        pdf += s.wDiff * (wi.z * kInvPi);
-    }
-    float4 va = spectral4(tab, sat(s.viewAtten), l);
-    return metal * s.mat.metallic + (diel + va * sub) * (1.0f - s.mat.metallic);
+    if (s.wDiff > 0.0f) pdf += s.wDiff * (wi.z * kInvPi);
+    return metal * s.mat.metallic + (diel + vaSub) * (1.0f - s.mat.metallic);
 }
 
 // sampleBSDFDirection (principled/sample.slang:4-51) of the subset: metal, dielectric reflection, diffuse
