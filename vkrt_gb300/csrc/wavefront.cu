@@ -1005,8 +1005,21 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
                 g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
             }
             samples = 1;
-            uint32_t w = atomicAdd(&g.counts[kCntCursor], 1u);
-            requeue = acquireItem<kSpectral>(g, scenes, slot, w);
+        }
+        // the next items for this warp's finished slots: one cursor fetch per warp, none once the cursor is past the
+        // last item (always, with one slot per item); the counter only grows, so a stale read is conservative
+        __syncwarp();
+        const unsigned fin = __ballot_sync(0xFFFFFFFFu, valid);
+        if (fin) {
+            const uint32_t lane = threadIdx.x & 31u, leader = uint32_t(__ffs(fin) - 1);
+            uint32_t item0 = g.totalItems;
+            if (lane == leader && __ldcg(&g.counts[kCntCursor]) < g.totalItems)
+                item0 = atomicAdd(&g.counts[kCntCursor], uint32_t(__popc(fin)));
+            item0 = __shfl_sync(0xFFFFFFFFu, item0, int(leader));
+            if (valid) {
+                const uint32_t w = item0 >= g.totalItems ? g.totalItems : item0 + __popc(fin & ((1u << lane) - 1u));
+                requeue = acquireItem<kSpectral>(g, scenes, slot, w);
+            }
         }
         __syncwarp();
         float3 dir = f3(0.0f);
