@@ -443,21 +443,10 @@ def selection_overlay_measure(ctx, sd, stream, torch) -> dict:
             "ms": round(a.elapsed_time(b) / 5, 3), "mask_pixels": int(ctx.read_selection_mask().sum())}
 
 
-def features_and_materials_measure(ctx, scene, sd, stream, flush, frame, torch, local) -> dict:
-    """Two costs beyond the headline frame, each the mean of 2 timed frames after 1 (CUDA events, L2 flushed):
-    the frame with denoiser feature films (albedo and normal), and the frame with vkrt's full material stack: every
-    third sphere glass (IOR 1.5, Abbe number 40, absorption 0.5 with tint (0.8, 0.9, 1)), every third clear-coated
-    with an Oren-Nayar base, every third subsurface, which runs the full-stack kernels (transmissive interface,
-    media, per-lane hero pdfs, transmission-aware shadow rays)."""
+def full_material_scene(scene):
+    """The scene with vkrt's full material stack: every third sphere glass (IOR 1.5, Abbe number 40, absorption 0.5
+    with tint (0.8, 0.9, 1)), every third clear-coated with an Oren-Nayar base, every third subsurface."""
     import copy
-    from vkrt_gb300 import RenderContext, abi
-    out = {}
-    ctx.set_denoiser_features(True)
-    _device_frames(ctx, sd, stream, flush, frame, 1, torch)
-    fms, frays, _ = _device_frames(ctx, sd, stream, flush, frame, 2, torch)
-    ctx.set_denoiser_features(False)
-    out["features"] = {"ms_per_frame": round(float(np.mean(fms)), 3),
-                       "value": round(frays / (sum(fms) * 1e-3) / 1e6, 2), "unit": "Mrays/s"}
     s = copy.copy(scene)
     m = scene.materials.copy()
     n = len(m)
@@ -474,6 +463,23 @@ def features_and_materials_measure(ctx, scene, sd, stream, flush, frame, torch, 
     m["diffuseRoughness"][coat] = 0.6
     m["subsurface"][sss] = 0.7
     s.materials = m
+    return s
+
+
+def features_and_materials_measure(ctx, scene, sd, stream, flush, frame, torch, local) -> dict:
+    """Two costs beyond the headline frame, each the mean of 2 timed frames after 1 (CUDA events, L2 flushed):
+    the frame with denoiser feature films (albedo and normal), and the frame with vkrt's full material stack
+    (full_material_scene), which runs the full-stack kernels (transmissive interface, media, per-lane hero pdfs,
+    transmission-aware shadow rays)."""
+    from vkrt_gb300 import RenderContext, abi
+    out = {}
+    ctx.set_denoiser_features(True)
+    _device_frames(ctx, sd, stream, flush, frame, 1, torch)
+    fms, frays, _ = _device_frames(ctx, sd, stream, flush, frame, 2, torch)
+    ctx.set_denoiser_features(False)
+    out["features"] = {"ms_per_frame": round(float(np.mean(fms)), 3),
+                       "value": round(frays / (sum(fms) * 1e-3) / 1e6, 2), "unit": "Mrays/s"}
+    s = full_material_scene(scene)
     mctx = RenderContext(device=local, rng_mode=abi.RNG_PCG32, rng_seed=1, environment_sampling=abi.ENV_IMPORTANCE,
                          integrator=abi.INTEGRATOR_WAVEFRONT)
     mctx.upload_scene(s)
@@ -795,6 +801,8 @@ def run_profile_frame(args) -> dict:
     if not args.rgb:
         scene.rgb2spec, info = ctx.generate_rgb2spec(64)
         scene.scene_data["rgb2specSRGB"] = info
+    if args.full_materials:
+        scene = full_material_scene(scene)
     ctx.upload_scene(scene)
     if args.stage_launches:
         ctx.set_wavefront_config(profileStages=1)
@@ -837,7 +845,8 @@ def run_profile_frame(args) -> dict:
                        "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
                        "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
-                       "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order}
+                       "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order,
+                       "full_materials": args.full_materials}
     ctx.close()
     return out
 
@@ -871,6 +880,8 @@ def main():
     prof.add_argument("--refill", type=int, default=0, help="traversal refill threshold (lanes; 0 = default)")
     prof.add_argument("--intersect-blocks", type=int, default=0, help="traversal kernel residency (blocks per SM)")
     prof.add_argument("--ray-order", type=int, default=0, help="1: traversal queues binned by direction octant")
+    prof.add_argument("--full-materials", action="store_true",
+                      help="vkrt's full material stack (glass, clear coat over Oren-Nayar, subsurface)")
     args = ap.parse_args()
     if args.profile_frame:
         print(json.dumps(run_profile_frame(args)))

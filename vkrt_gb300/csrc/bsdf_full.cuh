@@ -279,8 +279,23 @@ VKRT_DEV float3 evalScalarFull(const BsdfFull& s, const SpecTable& tab, float3 w
     return sheenV + (f3(coat) + (metal * s.mat.metallic + (diel + s.viewAtten * sub) * nonMetal) * att) * viewSheen;
 }
 
-// Four hero lanes with one technique pdf per lane in `tp`
-VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi, float4 l, float4& tp) {
+// The hero stack's direction-independent upsampled colours (sheen, diffuse base, view attenuation), the same for
+// every direction a vertex evaluates; each is computed under the condition evalHeroFull uses it.
+struct HeroTerms {
+    float4 sheen, diffuse, viewAtten;
+};
+
+VKRT_DEV HeroTerms heroTerms(const BsdfFull& s, const SpecTable& tab, float4 l) {
+    HeroTerms h{f4(0.0f), f4(0.0f), f4(0.0f)};
+    if (s.wSheen > 0.0f || !s.interior) h.sheen = spectral4(tab, sat(s.sheenColor), l);
+    if (s.wDiff > 0.0f || s.wSub > 0.0f) h.diffuse = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l);
+    if (!s.interior) h.viewAtten = spectral4(tab, sat(s.viewAtten), l);
+    return h;
+}
+
+// Four hero lanes with one technique pdf per lane in `tp`; `ht` is heroTerms of the same BSDF and wavelengths
+VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi, float4 l, const HeroTerms& ht,
+                             float4& tp) {
     tp = f4(0.0f);
     if (wi.z <= 0.0f) {  // evalSpectralDielectricTransmission
         const float4 tc = spectral4(tab, sat(transmissionColor(s.mat)), l) *
@@ -295,7 +310,7 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
     }
     float coat = 0.0f;
     float4 metal = f4(0.0f), diel = f4(0.0f), sub = f4(0.0f), sheenV = f4(0.0f), sc = f4(0.0f);
-    if (s.wSheen > 0.0f || !s.interior) sc = spectral4(tab, sat(s.sheenColor), l);
+    if (s.wSheen > 0.0f || !s.interior) sc = ht.sheen;
     if (s.wSheen > 0.0f) {
         float sp;
         sheenV = sc * evalSheenUnit(s, wi, sp);
@@ -330,7 +345,7 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
         }
     }
     if (s.wDiff > 0.0f || s.wSub > 0.0f) {
-        const float4 dc = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l);
+        const float4 dc = ht.diffuse;
         if (s.wDiff > 0.0f) {
             const float unit = s.mat.diffuseRoughness <= 0.0f ? kInvPi : orenNayar(s.mat.diffuseRoughness, s.wo, wi);
             sub = sub + dc * ((1.0f - s.mat.transmission) * (1.0f - s.mat.subsurface) * unit);
@@ -344,7 +359,7 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
     }
     const float nonMetal = 1.0f - s.mat.metallic;
     if (s.interior) return metal * s.mat.metallic + diel * nonMetal;
-    const float4 va = spectral4(tab, sat(s.viewAtten), l);
+    const float4 va = ht.viewAtten;
     const float att = s.viewCoat * coatAtten(s.mat, wi);
     const float alb = sheenAlbedo(s.sheenLtc, s.wo.z, s.mat.sheenRoughness);
     const float4 viewSheen = make_float4(sat(1.0f - sc.x * alb), sat(1.0f - sc.y * alb), sat(1.0f - sc.z * alb),

@@ -287,6 +287,9 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
         return false;
     }
 
+    // the hero stack's direction-independent colours, shared by the NEE evaluations and the continuation
+    const HeroTerms ht = kSpectral && !collapsed ? heroTerms(bsdf, tab, lam) : HeroTerms{f4(0.0f), f4(0.0f), f4(0.0f)};
+
     const bool neeHere = (p.flags & kPathRefractive) == 0u;  // currentVertexNeeAllowed
     if (cfg.neeEnabled && neeHere && bsdf.wo.z > 0.0f) {
         // sampleDirectLight{Rgb, SpectralHero, SpectralSingle} (light/direct/*.slang): the shadow ray is traced even
@@ -313,7 +316,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
                     }
                 } else {
                     float4 tp;
-                    const float4 fcos = evalHeroFull(bsdf, tab, wl, lam, tp) * fabsf(wl.z);
+                    const float4 fcos = evalHeroFull(bsdf, tab, wl, lam, ht, tp) * fabsf(wl.z);
                     const float4 lt = tech * ls.pdfSA, bt = tech * tp;
                     const float den = sum4f(lt) + sum4f(bt);
                     const float mis = den > 0.0f ? lt.x / den : 0.0f;
@@ -334,7 +337,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
             float4 c = f4(0.0f);
             if (kSpectral) {
                 float4 tp;
-                const float4 fcos = evalHeroFull(bsdf, tab, wl, lam, tp) * fabsf(wl.z);
+                const float4 fcos = evalHeroFull(bsdf, tab, wl, lam, ht, tp) * fabsf(wl.z);
                 const float4 lt = tech * pe, bt = tech * tp;
                 const float den = sum4f(lt) + sum4f(bt);
                 const float mis = den > 0.0f ? lt.x / den : 0.0f;
@@ -376,7 +379,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
         p.prevBsdfPdf = pdf;
     } else {
         float4 tp;
-        const float4 val = evalHeroFull(bsdf, tab, wl, lam, tp);
+        const float4 val = evalHeroFull(bsdf, tab, wl, lam, ht, tp);
         if (!(tp.x > 0.0f)) return false;
         const float4 weight = val * (fabsf(wl.z) / tp.x);
         if (!anyPos(weight)) return false;
