@@ -63,3 +63,24 @@ def test_noalloc_rejects_more_than_the_scratch_holds(built):
         rc, got = _noalloc(ctx, rays[:100])
         assert rc == abi.SUCCESS
         np.testing.assert_array_equal(got["primitiveIndex"], ctx.trace_rays(rays[:100])["primitiveIndex"])
+
+
+def test_noalloc_makes_no_device_allocation(built):
+    """After one warm-up call (the driver may size the kernel's local-memory reservation on its first launch), the
+    entry point leaves the device's free memory unchanged across calls of every size up to the cap."""
+    torch = pytest.importorskip("torch")
+    scene = scenes.cornell(32, 32)
+    with RenderContext() as ctx:
+        ctx.upload_scene(scene)
+        rays = _rays(MAX_RAYS, 5)
+        torch.cuda.mem_get_info()
+        rc, _ = _noalloc(ctx, rays)
+        assert rc == abi.SUCCESS
+        ctx.sync()
+        free0, _ = torch.cuda.mem_get_info()
+        for n, any_hit in ((MAX_RAYS, 0), (1000, 1), (MAX_RAYS, 1), (17, 0)):
+            rc, _ = _noalloc(ctx, rays[:n], any_hit)
+            assert rc == abi.SUCCESS
+        ctx.sync()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, (free0, free1)

@@ -79,8 +79,6 @@ struct WfGlobals {
     uint32_t* slotScene;
     uint32_t* slotItem;    // (pixel, sample) item within the scene
     float4* sampleBuf;     // one result per item, summed per pixel in sample order by the resolve kernel
-    uint4* hitA;     // mesh, prim, t, u
-    float* hitV;
     uint32_t* hitKey;
     float4* pend0;
     float4* pend1;
@@ -240,8 +238,9 @@ VKRT_DEV bool workPixel(const WfScene& S, uint32_t local, int& px, int& py) {
 
 // words of a slot's record: origin + depth, direction + flags (together one 32-byte sector, all the traversal reads),
 // RNG state, throughput, radiance, MIS terms (lamUnit, techPath, prevVertexTech, prevBsdfTech), previous BSDF pdf with
-// the cache's area-spread terms; the eighth word is unused
-enum : uint32_t { kRecOrigin = 0, kRecDir, kRecRng, kRecThr, kRecRad, kRecMis, kRecPdf, kRecWords = 8 };
+// the cache's area-spread terms and the closest hit's v, the closest hit (mesh, primitive, t, u). The traversal writes
+// the hit into the record's last sector, which the shade kernel reads with the path state.
+enum : uint32_t { kRecOrigin = 0, kRecDir, kRecRng, kRecThr, kRecRad, kRecMis, kRecPdf, kRecHit, kRecWords };
 
 VKRT_DEV float4* record(const WfGlobals& g, uint32_t s) { return g.rec + size_t(s) * kRecWords; }
 
@@ -498,8 +497,9 @@ VKRT_DEV void warpCountBytes(unsigned long long* nodeBytes, unsigned long long* 
 // kMinBlocks: resident blocks per SM the register allocation must allow (the launch grid's blocks per SM)
 // The closest hit of queue entry i (slot `slot`): hit records, and the sort key or class queue entry
 VKRT_DEV void storeHit(const WfGlobals& g, uint32_t i, uint32_t slot, const TraceHit& h) {
-    g.hitA[slot] = make_uint4(h.mesh, h.prim, __float_as_uint(h.t), __float_as_uint(h.u));
-    g.hitV[slot] = h.v;
+    float4* r = record(g, slot);
+    r[kRecHit] = make_float4(__uint_as_float(h.mesh), __uint_as_float(h.prim), h.t, h.u);
+    reinterpret_cast<float*>(r + kRecPdf)[3] = h.v;
     if (g.sort == kSortMaterial) {  // histogram of (scene, class) keys for the counting sort
         const uint32_t sceneId = g.slotScene[slot];
         const uint32_t key = 3u * sceneId + hitClass(g.scenes[sceneId].sc, h);
@@ -845,8 +845,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
             }
             if constexpr (kAdjoint) adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
             g.pendFlags[slot] = 0u;
-            uint4 a = g.hitA[slot];
-            TraceHit h{a.x, a.y, 0u, __uint_as_float(a.z), __uint_as_float(a.w), g.hitV[slot]};
+            const float4 a = record(g, slot)[kRecHit];
+            const TraceHit h{__float_as_uint(a.x), __float_as_uint(a.y), 0u, a.z, a.w, record(g, slot)[kRecPdf].w};
             StepConfig cfg = stepConfig(g, S);
             if constexpr (kAdjoint) {
                 AdjVertex av;
@@ -1076,7 +1076,7 @@ struct WavefrontEngine::Buffers {
     WfGlobals g{};
     size_t capQ = 0, capKeys = 0, capScenes = 0;
     size_t c_rec = 0, c_scene = 0, c_work = 0,
-           c_sample = 0, c_sum = 0, c_hitA = 0, c_hitV = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
+           c_sample = 0, c_sum = 0, c_key = 0, c_p0 = 0, c_p1 = 0, c_pf = 0, c_q0 = 0,
            c_q1 = 0, c_fin = 0, c_sorted = 0, c_sA = 0, c_sB = 0, c_hist = 0, c_counts = 0, c_sc = 0, c_class = 0,
            c_fA = 0, c_fN = 0, c_eA = 0, c_eB = 0, c_eC = 0, c_eD = 0, c_as = 0;
     size_t c_aD = 0, c_aT = 0, c_aU = 0, c_aC = 0, c_aR0 = 0, c_aR1 = 0, c_aE0 = 0, c_aE1 = 0, c_aRB = 0, c_aRR = 0;
@@ -1115,7 +1115,7 @@ void WavefrontEngine::release() {
     }
     WfGlobals& g = b_->g;
     void* ptrs[] = {g.rec, g.slotScene, g.slotItem, g.sampleBuf,
-                    g.hitA, g.hitV, g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
+                    g.hitKey, g.pend0, g.pend1, g.pendFlags, g.queue0, g.queue1, g.finished,
                     g.sorted, g.classQueue, g.shadowA, g.shadowB, g.keyHist, g.counts, b_->scenes, b_->bases,
                     g.nrcQueries, g.slotQuery, g.nrcPred, b_->recIn, b_->recTarget, b_->recCount, g.adjDelta,
                     g.adjTotal,
@@ -1201,8 +1201,6 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         WF_GROW(itemFeatA, c_fA, std::max<size_t>(totalItems, 1));
         WF_GROW(itemFeatN, c_fN, std::max<size_t>(totalItems, 1));
     }
-    WF_GROW(hitA, c_hitA, Q);
-    WF_GROW(hitV, c_hitV, Q);
     WF_GROW(hitKey, c_key, Q);
     WF_GROW(pend0, c_p0, Q);
     WF_GROW(pend1, c_p1, Q);
