@@ -57,3 +57,42 @@ def test_host_defaults_read_through_the_layouts(built):
     assert sd["packedRenderSettings"] == abi.pack_render_settings(1, 0, 1)
     # camera at (-0.5, 0.2, -0.2): the inverse view's translation column is the eye position
     assert np.allclose(sd["viewInverse"][0][3, :3], [-0.5, 0.2, -0.2], atol=1e-6)
+
+
+def test_backend_records_match_the_header(tmp_path):
+    """The numpy layouts of the backend's own records (configuration, statistics, rays, hits, gradients) have the
+    field offsets and sizes the C header gives them: a probe compiled against include/vkrt_cuda.h prints offsetof
+    and sizeof for every field abi.py declares."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    records = {"VKRT_CudaConfig": abi.CONFIG, "VKRT_CudaWavefrontConfig": abi.WAVEFRONT_CONFIG,
+               "VKRT_CudaStats": abi.STATS, "VKRT_CudaRay": abi.RAY, "VKRT_CudaHit": abi.HIT,
+               "VKRT_CudaAdjointConfig": abi.ADJOINT_CONFIG, "VKRT_CudaMaterialGradient": abi.MATERIAL_GRADIENT,
+               "VKRT_CudaNrcConfig": abi.NRC_CONFIG}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vkrt_cuda.h"', "int main(void) {"]
+    for rec, dt in records.items():
+        lines.append(f'printf("{rec} size %zu\\n", sizeof({rec}));')
+        for name in dt.names:
+            lines.append(f'printf("{rec} {name} %zu %zu\\n", offsetof({rec}, {name}), sizeof((({rec}*)0)->{name}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-std=c11", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in filter(None, out):
+        parts = line.split()
+        if parts[1] == "size":
+            got[(parts[0], None)] = int(parts[2])
+        else:
+            got[(parts[0], parts[1])] = (int(parts[2]), int(parts[3]))
+    for rec, dt in records.items():
+        assert got[(rec, None)] == dt.itemsize, rec
+        for name in dt.names:
+            off, size = got[(rec, name)]
+            assert (dt.fields[name][1], dt.fields[name][0].itemsize) == (off, size), (rec, name)

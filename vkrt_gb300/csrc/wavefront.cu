@@ -60,6 +60,9 @@ constexpr uint32_t kSortMaterial = 1, kSortClass = 2;  // sortByMaterial (0: as 
 
 struct WfGlobals {
     uint32_t mode;  // WavefrontMode
+    // forward frames with a slot per item (no slot is ever refilled): the shade kernel writes the result of a path
+    // that ends with nothing pending (no shadow ray, no cache query) instead of handing it to the finalize kernel
+    uint32_t directFinish;
     const WfScene* scenes;
     const uint32_t* itemBases;  // scenes[i].itemBase, contiguous for the item -> scene search
     const uint32_t* workBases;  // scenes[i].workBase
@@ -825,7 +828,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         uint32_t slot = 0, ns = 0;
         ShadowRequest sh[2];
         NrcInput query{};
-        bool queried = false;
+        bool queried = false, done = false;
         float3 nextDir = f3(0.0f);
         if (valid) {
             if (g.sort == kSortClass)  // the three class queues read as one
@@ -869,8 +872,17 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                     p.flags |= kPathFeatureDone;
                 }
             }
-            storePath(g, slot, p);
-            if constexpr (kFull) storePathExt(g, slot, p);
+            if constexpr (!kAdjoint) {
+                if (g.directFinish && !cont && ns == 0 && !queried) {  // the sample result, as finalize writes it
+                    const float3 res = pathResult<kSpectral>(cfg, p);
+                    g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
+                    done = true;
+                }
+            }
+            if (!done) {
+                storePath(g, slot, p);
+                if constexpr (kFull) storePathExt(g, slot, p);
+            }
             nextDir = p.d;
             uint32_t flags = queried ? kPendCache : 0u;
             if (ns > 0) {
@@ -886,8 +898,10 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         // continuing paths to the next queue, finished ones to finalize (one atomic per warp and queue)
         __syncwarp();
         queuePush(g, outQueue, valid && cont, slot, nextDir);
-        uint32_t pos = warpPush(&g.counts[kCntFinished], valid && !cont);
-        if (valid && !cont) g.finished[pos] = slot;
+        uint32_t pos = warpPush(&g.counts[kCntFinished], valid && !cont && !done);
+        if (valid && !cont && !done) g.finished[pos] = slot;
+        if constexpr (!kAdjoint)
+            if (g.directFinish) warpCount(&g.counters->pathSamples, done ? 1u : 0u);
         if (g.cacheDepth != 0xFFFFFFFFu) {
             pos = warpPush(&g.counts[kCntQueries], valid && queried);
             if (valid && queried) {
@@ -1253,6 +1267,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         if (e != cudaSuccess) return e;
     }
     g.mode = uint32_t(mode);
+    g.directFinish = mode == kWavefrontForward && Q >= totalItems ? 1u : 0u;
     g.features = features ? 1u : 0u;
     g.transmissive = transmissive ? 1u : 0u;
     g.alpha = alpha ? 1u : 0u;
