@@ -814,6 +814,8 @@ def run_profile_frame(args) -> dict:
         ctx.set_wavefront_config(intersectBlocksPerSM=args.intersect_blocks)
     if args.ray_order:
         ctx.set_wavefront_config(rayOrder=args.ray_order)
+    if args.sort is not None:
+        ctx.set_wavefront_config(sortByMaterial=args.sort)
     if args.cache:
         ctx.nrc_configure(enabled=1)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -846,7 +848,7 @@ def run_profile_frame(args) -> dict:
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
                        "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
                        "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order,
-                       "full_materials": args.full_materials}
+                       "full_materials": args.full_materials, "sort": args.sort}
     ctx.close()
     return out
 
@@ -880,6 +882,7 @@ def main():
     prof.add_argument("--refill", type=int, default=0, help="traversal refill threshold (lanes; 0 = default)")
     prof.add_argument("--intersect-blocks", type=int, default=0, help="traversal kernel residency (blocks per SM)")
     prof.add_argument("--ray-order", type=int, default=0, help="1: traversal queues binned by direction octant")
+    prof.add_argument("--sort", type=int, default=None, help="shade-queue order (sortByMaterial 0-3)")
     prof.add_argument("--full-materials", action="store_true",
                       help="vkrt's full material stack (glass, clear coat over Oren-Nayar, subsurface)")
     args = ap.parse_args()

@@ -63,11 +63,13 @@ typedef struct VKRT_CudaWavefrontConfig {
     uint32_t queueCapacity;        /* path slots; 0 = one per (pixel, sample) item of the batch, capped at 64M */
     uint32_t tileWidth;            /* pixels are handed to path slots in tiles of tileWidth x tileHeight */
     uint32_t tileHeight;
-    uint32_t sortByMaterial;       /* shade-queue order: 0 as traced; 1 counting-sorted by (scene, material);
-                                      2 partitioned into misses, dielectric and metal hits by the intersect kernel */
+    uint32_t sortByMaterial;       /* shade-queue order: 0 as traced; 1 counting-sorted by (scene, hit class);
+                                      2 partitioned into misses, dielectric and metal hits by the intersect kernel;
+                                      3 counting-sorted by material (each warp shades one material's lobes) */
     uint32_t intersectBlocksPerSM; /* persistent grid of the traversal kernels, per SM */
     uint32_t shadeBlocksPerSM;     /* persistent grid of the shading kernels, per SM; also their register budget:
-                                      3 (default) 168 registers, 4: 128, 6: 80, 8: 64 */
+                                      3: 168 registers, 4 (default): 128, 6: 80, 8: 64 (the full-material-stack,
+                                      feature and adjoint kernels keep one budget: 168, 168 and 128) */
     uint32_t useGraph;             /* 1: the frame is one CUDA-graph launch (conditional while node) */
     uint32_t profileStages;        /* 1: stage-by-stage launches with device timers and fetch-byte counting (slower;
                                       for profiling), reported in VKRT_CudaStats.stageMs / *FetchBytes */

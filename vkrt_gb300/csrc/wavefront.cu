@@ -55,14 +55,18 @@ enum : uint32_t {
 };
 constexpr uint32_t kPendCache = 16u;        // pendFlags: the path ended at a radiance-cache query
 constexpr uint32_t kPendUnsupported = 32u;  // pendFlags: an NEE shadow ray met a transmissive surface
-constexpr uint32_t kSortMaterial = 1, kSortClass = 2;  // sortByMaterial (0: as traced); 1 sorts by (scene, class)
+// sortByMaterial (0: as traced); 1 counting-sorts by (scene, class), 3 by material (both kSortMaterial in the
+// kernels, with WfGlobals::keyByMaterial telling the keys apart); 2 files hits into class queues
+constexpr uint32_t kSortMaterial = 1, kSortClass = 2, kSortMaterialIndex = 3;
 
 
 struct WfGlobals {
     uint32_t mode;  // WavefrontMode
-    // forward frames with a slot per item (no slot is ever refilled): the shade kernel writes the result of a path
-    // that ends with nothing pending (no shadow ray, no cache query) instead of handing it to the finalize kernel
+    // forward frames: the shade kernel writes the result of a path that ends with nothing pending (no shadow ray, no
+    // cache query); with refills (fewer slots than items) the slot still goes to the finalize kernel, marked
+    // kFinishedDone, only to take its next item
     uint32_t directFinish;
+    uint32_t refills;
     const WfScene* scenes;
     const uint32_t* itemBases;  // scenes[i].itemBase, contiguous for the item -> scene search
     const uint32_t* workBases;  // scenes[i].workBase
@@ -74,6 +78,7 @@ struct WfGlobals {
     uint32_t sort;
     int refill;  // persistent traversal refill threshold
     uint32_t keyCount;
+    uint32_t keyByMaterial;  // sort keys: 0 (scene, class), 1 0 for misses and 1 + materialKeyBase + material index
     uint32_t rngMode;
     uint64_t rngSeed;
     // path record: one 128-byte line per slot (kRec* words of 16 bytes), so a record read through a queue of scattered
@@ -134,6 +139,9 @@ struct WfGlobals {
     float4* extC;
     float* extD;
 };
+
+// finished-queue entries whose result the shade kernel has written already (slot numbers stay below 2^26)
+constexpr uint32_t kFinishedDone = 0x80000000u;
 
 VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
     unsigned mask = __activemask();
@@ -503,9 +511,13 @@ VKRT_DEV void storeHit(const WfGlobals& g, uint32_t i, uint32_t slot, const Trac
     float4* r = record(g, slot);
     r[kRecHit] = make_float4(__uint_as_float(h.mesh), __uint_as_float(h.prim), h.t, h.u);
     reinterpret_cast<float*>(r + kRecPdf)[3] = h.v;
-    if (g.sort == kSortMaterial) {  // histogram of (scene, class) keys for the counting sort
+    if (g.sort == kSortMaterial) {  // histogram of (scene, class) or material keys for the counting sort
         const uint32_t sceneId = g.slotScene[slot];
-        const uint32_t key = 3u * sceneId + hitClass(g.scenes[sceneId].sc, h);
+        const WfScene& S = g.scenes[sceneId];
+        const uint32_t key = !g.keyByMaterial ? 3u * sceneId + hitClass(S.sc, h)
+                             : h.mesh == VKRT_CUDA_INVALID_INDEX
+                                 ? 0u
+                                 : 1u + S.materialKeyBase + S.sc.meshes[h.mesh].materialIndex;
         g.hitKey[i] = key;
         warpAggregatedSlot(g.keyHist, key);
     } else if (g.sort == kSortClass) {  // filed straight into the class queues
@@ -872,7 +884,8 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                     p.flags |= kPathFeatureDone;
                 }
             }
-            if constexpr (!kAdjoint) {
+            // not in the full-stack kernels: bound by instruction fetch, they ran 10% slower with this code inside
+            if constexpr (!kAdjoint && !kFull) {
                 if (g.directFinish && !cont && ns == 0 && !queried) {  // the sample result, as finalize writes it
                     const float3 res = pathResult<kSpectral>(cfg, p);
                     g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
@@ -898,8 +911,9 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
         // continuing paths to the next queue, finished ones to finalize (one atomic per warp and queue)
         __syncwarp();
         queuePush(g, outQueue, valid && cont, slot, nextDir);
-        uint32_t pos = warpPush(&g.counts[kCntFinished], valid && !cont && !done);
-        if (valid && !cont && !done) g.finished[pos] = slot;
+        const bool toFinalize = valid && !cont && (!done || g.refills);
+        uint32_t pos = warpPush(&g.counts[kCntFinished], toFinalize);
+        if (toFinalize) g.finished[pos] = slot | (done ? kFinishedDone : 0u);
         if constexpr (!kAdjoint)
             if (g.directFinish) warpCount(&g.counters->pathSamples, done ? 1u : 0u);
         if (g.cacheDepth != 0xFFFFFFFFu) {
@@ -995,8 +1009,13 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
         bool valid = i < n;
         bool requeue = false;
         uint32_t slot = 0, samples = 0;
+        bool done = false;  // the shade kernel wrote the result; the slot only takes its next item here
         if (valid) {
             slot = g.finished[i];
+            done = (slot & kFinishedDone) != 0u;
+            slot &= ~kFinishedDone;
+        }
+        if (valid && !done) {
             uint32_t sceneId = g.slotScene[slot];
             const WfScene& S = scenes[sceneId];
             PathState p = loadPath(g, slot);
@@ -1159,7 +1178,14 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     if (sms <= 0) sms = 1;
     std::vector<WfScene> scenes = scenesIn;
     uint32_t total = 0, maxSpp = 1, maxDepth = 1;
-    const uint32_t keys = 3u * uint32_t(scenesIn.size());  // (scene, class) sort keys
+    uint32_t keys = 3u * uint32_t(scenesIn.size());  // (scene, class) sort keys
+    if (cfg.sortByMaterial == kSortMaterialIndex) {   // one key for misses, then one per material of every scene
+        keys = 1u;
+        for (WfScene& S : scenes) {
+            S.materialKeyBase = keys - 1u;
+            keys += S.sc.materialCount;
+        }
+    }
     uint64_t items = 0;
     for (WfScene& S : scenes) {
         S.tileW = std::max(1u, cfg.tileWidth);
@@ -1267,7 +1293,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         if (e != cudaSuccess) return e;
     }
     g.mode = uint32_t(mode);
-    g.directFinish = mode == kWavefrontForward && Q >= totalItems ? 1u : 0u;
+    g.directFinish = mode == kWavefrontForward ? 1u : 0u;
+    g.refills = Q < totalItems ? 1u : 0u;
     g.features = features ? 1u : 0u;
     g.transmissive = transmissive ? 1u : 0u;
     g.alpha = alpha ? 1u : 0u;
@@ -1283,6 +1310,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.Q = Q;
     g.maxIter = maxIter;
     g.sort = cfg.sortByMaterial <= kSortClass ? cfg.sortByMaterial : kSortMaterial;
+    g.keyByMaterial = cfg.sortByMaterial == kSortMaterialIndex ? 1u : 0u;
     g.refill = int(std::min(std::max(cfg.refillLanes, 1u), 32u));
     g.rayOrder = cfg.rayOrder ? 1u : 0u;
     g.keyCount = keys;
@@ -1312,6 +1340,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
 
     const uint32_t gridI = uint32_t(sms) * std::max(1u, cfg.intersectBlocksPerSM);
     const uint32_t gridS = uint32_t(sms) * std::max(1u, cfg.shadeBlocksPerSM);
+    const uint32_t grid3 = uint32_t(sms) * 3u, grid4 = uint32_t(sms) * 4u;
     const uint32_t shadeMin = cfg.shadeBlocksPerSM;
     const size_t smem = size_t(kWfThreads) * VKRT_SMEM_STACK * sizeof(uint2);
 
@@ -1331,13 +1360,13 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         }
         stage(kStageShade, [&] {
             // register budget follows the requested residency: 168 (3 blocks/SM, no spills), 128 (4), 80 (6) or
-            // 64 (8) registers
-            if (adjMode) kWfShade<false, true, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (extended && spectral) kWfShade<true, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (extended) kWfShade<false, false, 3, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+            // 64 (8) registers; kernels compiled for one residency run on a grid of that many blocks per SM
+            if (adjMode) kWfShade<false, true, 4><<<grid4, kWfThreads, 0, stream>>>(g, in, out);
+            else if (extended && spectral) kWfShade<true, false, 3, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
+            else if (extended) kWfShade<false, false, 3, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
             else if (features && spectral)  // reflection-only materials with feature films
-                kWfShade<true, false, 3, false, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
-            else if (features) kWfShade<false, false, 3, false, true><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
+                kWfShade<true, false, 3, false, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
+            else if (features) kWfShade<false, false, 3, false, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 8) kWfShade<true, false, 8><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 6) kWfShade<true, false, 6><<<gridS, kWfThreads, 0, stream>>>(g, in, out);
             else if (spectral && shadeMin >= 4) kWfShade<true, false, 4><<<gridS, kWfThreads, 0, stream>>>(g, in, out);

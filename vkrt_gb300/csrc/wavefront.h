@@ -30,6 +30,7 @@ struct WfScene {
     uint32_t tileW, tileH, tilesX;
     uint32_t workBase, workCount;  // padded pixel work items (tile order)
     uint32_t itemBase;             // first (pixel, sample) item of the scene; items of a pixel are consecutive
+    uint32_t materialKeyBase;      // first shade-order key of the scene's materials (material-ordered shading)
 };
 
 // forward: a frame blended into each scene's film; primal: the same paths, each (pixel, sample) radiance kept in the
