@@ -60,7 +60,8 @@ typedef struct VKRT_CudaConfig {
 
 /* Wavefront integrator parameters (autotuned by vkrt_cuda_autotune_batch). 64 bytes. */
 typedef struct VKRT_CudaWavefrontConfig {
-    uint32_t queueCapacity;        /* path slots; 0 = one per (pixel, sample) item of the batch, capped at 64M */
+    uint32_t queueCapacity;        /* path slots, at most 256M (about 70 GB of slot state); 0 = one per (pixel,
+                                      sample) item of the batch, capped at 64M */
     uint32_t tileWidth;            /* pixels are handed to path slots in tiles of tileWidth x tileHeight */
     uint32_t tileHeight;
     uint32_t sortByMaterial;       /* shade-queue order: 0 as traced; 1 counting-sorted by (scene, hit class);

@@ -932,7 +932,7 @@ int32_t vkrt_cuda_set_wavefront_config(VKRT_CudaContext* c, const VKRT_CudaWavef
     if (w->intersectBlocksPerSM == 0 || w->intersectBlocksPerSM > 16u || w->shadeBlocksPerSM == 0 ||
         w->shadeBlocksPerSM > 16u)
         return invalid(c, "blocks per SM must be in [1, 16]");
-    if (w->queueCapacity > (1u << 26)) return invalid(c, "queue capacity above 64M path slots");
+    if (w->queueCapacity > (1u << 28)) return invalid(c, "queue capacity above 256M path slots");  // ~70 GB
     if (w->profileStages > 1u) return invalid(c, "profileStages is 0 or 1");
     if (w->sortByMaterial > 3u) return invalid(c, "sortByMaterial is 0, 1, 2 or 3");
     if (w->refillLanes > 32u) return invalid(c, "refillLanes is 0 (default) or 1..32");

@@ -1079,6 +1079,8 @@ __global__ void kWfCondition(WfGlobals g, uint32_t useGraph) {
     if (useGraph) cudaGraphSetConditional(g.cond, more ? 1u : 0u);
 }
 
+constexpr uint32_t kSlotsDefault = 1u << 26;  // path slots when the configuration leaves the count open
+
 template <class T>
 cudaError_t grow(T*& p, size_t& cap, size_t n) {
     if (n <= cap && p) return cudaSuccess;
@@ -1202,10 +1204,11 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     }
     if (items >= 0xFFFFFFF0ull) return cudaErrorInvalidValue;  // item indices are 32-bit
     const uint32_t totalItems = uint32_t(items);
-    // default: one slot per item up to 64M slots (about 18 GB of slot state and queues). A slot that is refilled with
+    // default: one slot per item up to 64M slots (about 17 GB of slot state and queues). A slot that is refilled with
     // a new item sits wherever the finished path left it, so refills scatter the slot-indexed state accesses of the
-    // next bounces; with a slot per item there are no refills.
-    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, 1u << 26);
+    // next bounces; with a slot per item there are no refills. (A slot per item for the 266M items of the 64-scene
+    // batch, about 70 GB, measured no faster than 64M refilled slots: 122.3 against 121.8 ms.)
+    uint32_t Q = cfg.queueCapacity ? cfg.queueCapacity : std::min<uint32_t>(totalItems, kSlotsDefault);
     Q = std::max(1u, std::min(Q, std::max(totalItems, 1u)));
     // until the item cursor runs out every slot is busy, so the bounces of all items bound the iteration count;
     // the condition kernel counts two-iteration bodies
@@ -1241,14 +1244,16 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         WF_GROW(itemFeatA, c_fA, std::max<size_t>(totalItems, 1));
         WF_GROW(itemFeatN, c_fN, std::max<size_t>(totalItems, 1));
     }
-    WF_GROW(hitKey, c_key, Q);
+    if (cfg.sortByMaterial == kSortMaterial || cfg.sortByMaterial == kSortMaterialIndex) {
+        WF_GROW(hitKey, c_key, Q);
+        WF_GROW(sorted, c_sorted, Q);
+    }
     WF_GROW(pend0, c_p0, Q);
     WF_GROW(pend1, c_p1, Q);
     WF_GROW(pendFlags, c_pf, Q);
     WF_GROW(queue0, c_q0, size_t(cfg.rayOrder ? kRayBins : 1u) * Q);
     WF_GROW(queue1, c_q1, size_t(cfg.rayOrder ? kRayBins : 1u) * Q);
     WF_GROW(finished, c_fin, Q);
-    WF_GROW(sorted, c_sorted, Q);
     if (cfg.sortByMaterial == kSortClass) WF_GROW(classQueue, c_class, 3 * size_t(Q));
     WF_GROW(shadowA, c_sA, 2 * size_t(Q));
     WF_GROW(shadowB, c_sB, 2 * size_t(Q));
