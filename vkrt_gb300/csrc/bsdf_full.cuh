@@ -287,9 +287,9 @@ struct HeroTerms {
 
 VKRT_DEV HeroTerms heroTerms(const BsdfFull& s, const SpecTable& tab, float4 l) {
     HeroTerms h{f4(0.0f), f4(0.0f), f4(0.0f)};
-    if (s.wSheen > 0.0f || !s.interior) h.sheen = spectral4(tab, sat(s.sheenColor), l);
-    if (s.wDiff > 0.0f || s.wSub > 0.0f) h.diffuse = spectral4(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l);
-    if (!s.interior) h.viewAtten = spectral4(tab, sat(s.viewAtten), l);
+    if (s.wSheen > 0.0f || !s.interior) h.sheen = spectral4Call(tab, sat(s.sheenColor), l);
+    if (s.wDiff > 0.0f || s.wSub > 0.0f) h.diffuse = spectral4Call(tab, sat(s.mat.baseColor * (1.0f - s.mat.metallic)), l);
+    if (!s.interior) h.viewAtten = spectral4Call(tab, sat(s.viewAtten), l);
     return h;
 }
 
@@ -298,7 +298,7 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
                              float4& tp) {
     tp = f4(0.0f);
     if (wi.z <= 0.0f) {  // evalSpectralDielectricTransmission
-        const float4 tc = spectral4(tab, sat(transmissionColor(s.mat)), l) *
+        const float4 tc = spectral4Call(tab, sat(transmissionColor(s.mat)), l) *
                           ((1.0f - s.mat.metallic) * s.mat.transmission);
         float4 v;
         v.x = transmissionLane(s, wi, tc.x, l.x, true, tp.x);
@@ -323,7 +323,7 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
     }
     const ReflGeom g = (s.wMetal > 0.0f || s.wDiel > 0.0f) ? reflGeom(s, wi) : ReflGeom{false, 0.0f, 0.0f, 0.0f};
     if (s.wMetal > 0.0f && g.ok) {
-        metal = spectral4(tab, sat(metalFresnel(s, g.wom)), l) * g.DG;
+        metal = spectral4Call(tab, sat(metalFresnel(s, g.wom)), l) * g.DG;
         tp = tp + f4(s.wMetal * g.reflPdf);
     }
     if (s.wDiel > 0.0f && g.ok && !dielIdentity(s.mat)) {
@@ -339,7 +339,7 @@ VKRT_DEV float4 evalHeroFull(const BsdfFull& s, const SpecTable& tab, float3 wi,
         if (anyPos(lanes)) {
             const float4 color = s.mat.transmission > 0.0f && s.mat.metallic <= 0.0f
                                      ? F
-                                     : spectral4(tab, sat(schlick(g.wom, s.f0Diel)), l);
+                                     : spectral4Call(tab, sat(schlick(g.wom, s.f0Diel)), l);
             diel = color * g.DG;
             tp = tp + lanes * s.wDiel;
         }

@@ -228,7 +228,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
                 const float den = sum4f(bt) + sum4f(lt);
                 w = den > 0.0f ? bt.x / den : 0.0f;
             }
-            p.radiance += p.thr * spectral4(tab, L, lam) * w;
+            p.radiance += p.thr * spectral4Call(tab, L, lam) * w;
         } else {
             float w = 1.0f;
             if (cfg.envNee && prevNee && depth > 0 && p.prevBsdfPdf > 0.0f) {
@@ -263,7 +263,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
                 const float den = sum4f(bt) + sum4f(lt);
                 w = den > 0.0f ? bt.x / den : 0.0f;
             }
-            p.radiance += p.thr * spectral4(tab, mat.emission, lam) * w;
+            p.radiance += p.thr * spectral4Call(tab, mat.emission, lam) * w;
         } else {
             float w = 1.0f;
             if (misNee && p.prevBsdfPdf > 0.0f) {
@@ -320,7 +320,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
                     const float4 lt = tech * ls.pdfSA, bt = tech * tp;
                     const float den = sum4f(lt) + sum4f(bt);
                     const float mis = den > 0.0f ? lt.x / den : 0.0f;
-                    if (mis > 0.0f) c = p.thr * (T * fcos * spectral4(tab, ls.emission, lam) * (mis / ls.pdfSA));
+                    if (mis > 0.0f) c = p.thr * (T * fcos * spectral4Call(tab, ls.emission, lam) * (mis / ls.pdfSA));
                 }
             }
             const float3 off = dot(ls.wi, s.geometricNormal) >= 0.0f ? s.geometricNormal : -s.geometricNormal;
@@ -341,7 +341,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
                 const float4 lt = tech * pe, bt = tech * tp;
                 const float den = sum4f(lt) + sum4f(bt);
                 const float mis = den > 0.0f ? lt.x / den : 0.0f;
-                if (mis > 0.0f) c = p.thr * (fcos * spectral4(tab, envRadiance(sc, sd, wi), lam) * (mis / pe));
+                if (mis > 0.0f) c = p.thr * (fcos * spectral4Call(tab, envRadiance(sc, sd, wi), lam) * (mis / pe));
             } else {
                 float pdf;
                 const float3 f = evalScalarFull<false>(bsdf, tab, wl, 0.0f, pdf);
@@ -422,7 +422,7 @@ VKRT_DEV bool shadePathVertexFull(const DeviceScene& sc, const VKRT_CudaSceneDat
             } else if (collapsed) {
                 p.sigma = f4(absorptionSigma(spectral1(tab, tint, lam.x), k));
             } else {
-                const float4 s4 = spectral4(tab, tint, lam);
+                const float4 s4 = spectral4Call(tab, tint, lam);
                 p.sigma = make_float4(absorptionSigma(s4.x, k), absorptionSigma(s4.y, k), absorptionSigma(s4.z, k),
                                       absorptionSigma(s4.w, k));
             }
