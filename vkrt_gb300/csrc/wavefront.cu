@@ -67,6 +67,9 @@ struct WfGlobals {
     // kFinishedDone, only to take its next item
     uint32_t directFinish;
     uint32_t refills;
+    // every slot holds its own item (a slot per item, no tile padding): the first queue is the slot order itself,
+    // filled without atomics, which keeps the camera rays in tile order for the first traversal
+    uint32_t identityStart;
     const WfScene* scenes;
     const uint32_t* itemBases;  // scenes[i].itemBase, contiguous for the item -> scene search
     const uint32_t* workBases;  // scenes[i].workBase
@@ -391,6 +394,7 @@ VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t sl
 __global__ void kWfSetup(WfGlobals g) {
     if (threadIdx.x < kCntCount) g.counts[threadIdx.x] = 0u;
     if (threadIdx.x == 0u) {
+        if (g.identityStart) g.counts[kCntActive0] = g.Q;
         g.counts[kCntCursor] = min(g.Q, g.totalItems);
         atomicAdd(&g.counters->kernelLaunches, (unsigned long long)g.launchesOutsideLoop);
     }
@@ -422,7 +426,11 @@ __global__ void __launch_bounds__(kWfThreads) kWfInit(WfGlobals g) {
             if ((okMask >> owner) & 1u) out[j] = ws[owner * kRow + j % kRecWords];
         }
         __syncwarp();
-        queuePush(g, 0u, ok, s, p.d);
+        if (g.identityStart) {  // every slot below Q starts its own item
+            if (s < g.Q) g.queue0[s] = s;
+        } else {
+            queuePush(g, 0u, ok, s, p.d);
+        }
     }
 }
 
@@ -1300,6 +1308,10 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.mode = uint32_t(mode);
     g.directFinish = mode == kWavefrontForward ? 1u : 0u;
     g.refills = Q < totalItems ? 1u : 0u;
+    bool padded = false;  // some tile reaches past its viewport, so some items are padding
+    for (const WfScene& S : scenes)
+        if (uint64_t(S.workCount) != uint64_t(S.vw) * S.vh) padded = true;
+    g.identityStart = !padded && Q >= totalItems && !cfg.rayOrder ? 1u : 0u;
     g.features = features ? 1u : 0u;
     g.transmissive = transmissive ? 1u : 0u;
     g.alpha = alpha ? 1u : 0u;
