@@ -817,7 +817,7 @@ def run_profile_frame(args) -> dict:
     if args.sort is not None:
         ctx.set_wavefront_config(sortByMaterial=args.sort)
     if args.cache:
-        ctx.nrc_configure(enabled=1)
+        ctx.nrc_configure(enabled=1, trainingTracer=args.training_tracer)
     stream = torch.cuda.ExternalStream(ctx.stream)
     sd = scene.scene_data.copy()
     out = {}
@@ -878,6 +878,8 @@ def main():
     prof.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
     prof.add_argument("--rgb", action="store_true", help="RGB transport instead of hero spectral")
     prof.add_argument("--cache", action="store_true", help="render with the radiance cache (wavefront only)")
+    prof.add_argument("--training-tracer", type=int, default=0,
+                      help="cache training paths: 0 one thread per path, 1 through the wavefront stages")
     prof.add_argument("--shade-blocks", type=int, default=0, help="shade kernel residency (blocks per SM)")
     prof.add_argument("--refill", type=int, default=0, help="traversal refill threshold (lanes; 0 = default)")
     prof.add_argument("--intersect-blocks", type=int, default=0, help="traversal kernel residency (blocks per SM)")

@@ -348,7 +348,11 @@ typedef struct VKRT_CudaNrcConfig {
                                   primary vertex exceeds c times the primary vertex's footprint seen from the camera
                                   (Mueller et al. 2021, "Real-time Neural Radiance Caching for Path Tracing", 3.3;
                                   the paper uses c = 0.01), and at `terminationDepth` at the latest */
-    uint32_t reserved[7];
+    uint32_t trainingTracer;   /* 0 (default): one thread traces each training path; 1: the training paths run
+                                  through the wavefront stages as a pass of their own before the frame (the same
+                                  paths and records; slower at the default 65,536 paths, which fill a dozen
+                                  bounces of stage launches poorly) */
+    uint32_t reserved[6];
 } VKRT_CudaNrcConfig;
 #define VKRT_CUDA_NRC_TCGEN05 0u
 #define VKRT_CUDA_NRC_MMA_SYNC 1u
@@ -364,6 +368,11 @@ void vkrt_cuda_default_nrc_config(VKRT_CudaNrcConfig* config);
 int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* context, const VKRT_CudaNrcConfig* config);
 /* Predictions for n host input records. Synchronous. */
 int32_t vkrt_cuda_nrc_infer(VKRT_CudaContext* context, const float* inputs, uint32_t n, float* outputs);
+/* The last cache frame's training records, in the order they were written: up to `capacity` inputs (16 floats each)
+ * and targets (4 floats each, linear sRGB in rgb); *count (may be NULL) receives how many the frame wrote.
+ * Synchronous. */
+int32_t vkrt_cuda_nrc_read_training_records(VKRT_CudaContext* context, float* inputs, float* targets,
+                                            uint32_t capacity, uint32_t* count);
 /* One optimiser step on n host records (targets: 4 floats each, rgb used); apply = 0 computes the gradients only.
  * *loss (may be NULL) receives the step's loss. Synchronous. */
 int32_t vkrt_cuda_nrc_train(VKRT_CudaContext* context, const float* inputs, const float* targets, uint32_t n,

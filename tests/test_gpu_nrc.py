@@ -117,6 +117,39 @@ def test_cache_lowers_error_at_equal_samples(built):
     assert abs(ratio - 1.0) < 0.01
 
 
+@pytest.mark.parametrize("spectral", [False, True])
+def test_wavefront_training_paths_match_per_thread_paths(built, spectral):
+    """The training paths traced through the wavefront stages (a pass of their own before the frame) give the same
+    training records as one thread per path: the same pixels, random streams, closest hits and shadow answers, so
+    the same vertices. The two tracers are different compiled kernels, whose inlining fuses different multiply-adds
+    (as between the wavefront and the megakernel), so continuation directions and radiance sums differ in the last
+    bits: most records are equal bit for bit and all agree to float rounding. The order the records are written in
+    differs, so both sets are matched on their positions rounded to 1e-3."""
+    s = scenes.icosphere_field(n_spheres=400, width=48, height=32, spp=1, max_depth=6, seed=9, spectral=spectral,
+                               env_size=(64, 32))
+    with RenderContext(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE,
+                       integrator=abi.INTEGRATOR_WAVEFRONT) as ctx:
+        if spectral:
+            s.rgb2spec, info = ctx.generate_rgb2spec(16)
+            s.scene_data["rgb2specSRGB"] = info
+        ctx.upload_scene(s)
+        sets = []
+        for tracer in (0, 1):
+            ctx.nrc_configure(enabled=1, trainingPaths=4096, trainingSteps=1, seed=21, trainingTracer=tracer)
+            sd = s.scene_data.copy()
+            sd["frameNumber"] = 3
+            ctx.render_frame(sd)
+            x, t = ctx.nrc_training_records()
+            assert ctx.stats()["cacheTrainingRecords"] == len(x)
+            key = np.round(x[:, :3].astype(np.float64), 3)
+            order = np.lexsort((key[:, 2], key[:, 1], key[:, 0]))
+            sets.append((x[order], t[order]))
+    assert len(sets[0][0]) > 1000 and len(sets[1][0]) == len(sets[0][0]), (len(sets[0][0]), len(sets[1][0]))
+    np.testing.assert_allclose(sets[1][0], sets[0][0], rtol=1e-3, atol=1e-4)
+    np.testing.assert_allclose(sets[1][1], sets[0][1], rtol=2e-3, atol=1e-4)
+    assert (sets[1][0] == sets[0][0]).all(axis=1).mean() > 0.9
+
+
 def test_spread_termination_limits(built):
     """Area-spread termination (Mueller et al. 2021, section 3.3) at its two limits, with an untrained cache (no
     training paths, so every frame is deterministic): a constant no spread exceeds ends every path at

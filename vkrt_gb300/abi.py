@@ -106,9 +106,10 @@ MATERIAL_GRADIENT = np.dtype({"names": ["baseColor", "roughness", "emission", "r
 GRADIENT_BASE_COLOR, GRADIENT_ROUGHNESS, GRADIENT_EMISSION = 1, 2, 4
 
 NRC_CONFIG = np.dtype({"names": ["enabled", "terminationDepth", "trainingPaths", "trainingSteps", "learningRate", "seed",
-                                 "inferenceTensorPath", "inferenceAverage", "terminationSpread", "reserved"],
-                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", "<u4", "<f4", "<f4", ("<u4", 7)],
-                       "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36], "itemsize": 64})
+                                 "inferenceTensorPath", "inferenceAverage", "terminationSpread", "trainingTracer",
+                                 "reserved"],
+                       "formats": ["<u4", "<u4", "<u4", "<u4", "<f4", "<u4", "<u4", "<f4", "<f4", "<u4", ("<u4", 6)],
+                       "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40], "itemsize": 64})
 NRC_TCGEN05, NRC_MMA_SYNC = 0, 1
 NRC_INPUT_FLOATS, NRC_WEIGHTS, NRC_TABLE_HALVES = 16, 21504, 16777216
 
@@ -196,6 +197,7 @@ EXPORTS = {
     "vkrt_cuda_default_nrc_config": (None, [_V]),
     "vkrt_cuda_nrc_configure": (_I32, [_V, _V]),
     "vkrt_cuda_nrc_infer": (_I32, [_V, _V, _U32, _V]),
+    "vkrt_cuda_nrc_read_training_records": (_I32, [_V, _V, _V, _U32, _V]),
     "vkrt_cuda_nrc_train": (_I32, [_V, _V, _V, _U32, _U32, _V]),
     "vkrt_cuda_nrc_parameters": (_I32, [_V, _V, _V, _U32]),
     "vkrt_cuda_nrc_gradients": (_I32, [_V, _V, _V]),

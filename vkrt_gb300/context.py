@@ -343,6 +343,16 @@ class RenderContext:
             cfg[k] = v
         self._check(self.lib.vkrt_cuda_nrc_configure(self.handle, abi.ptr(cfg)), "configure radiance cache")
 
+    def nrc_training_records(self, capacity: int = 1 << 20) -> tuple[np.ndarray, np.ndarray]:
+        """The last cache frame's training records: inputs (n, 16) and targets (n, 4), in write order."""
+        x = np.zeros((capacity, abi.NRC_INPUT_FLOATS), np.float32)
+        t = np.zeros((capacity, 4), np.float32)
+        n = np.zeros(1, np.uint32)
+        self._check(self.lib.vkrt_cuda_nrc_read_training_records(self.handle, abi.ptr(x), abi.ptr(t), capacity,
+                                                                 abi.ptr(n)), "read training records")
+        k = min(int(n[0]), capacity)
+        return x[:k], t[:k]
+
     def nrc_infer(self, inputs: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(inputs, dtype=np.float32).reshape(-1, abi.NRC_INPUT_FLOATS)
         out = np.zeros((len(x), 4), np.float32)

@@ -992,7 +992,7 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     if (useCache)
         cache = WfCacheFrame{c0->nrc.get(), c0->nrcCfg.terminationDepth, c0->nrcCfg.trainingPaths,
                              c0->nrcCfg.trainingSteps, c0->nrcCfg.seed, sds[0].frameNumber,
-                             c0->nrcCfg.terminationSpread};
+                             c0->nrcCfg.terminationSpread, c0->nrcCfg.trainingTracer};
     VKRT_TRY(c0, c0->wavefront->render(scenes, spectral, wc, c0->cfg.rngMode, c0->cfg.rngSeed, c0->counters, c0->stream,
                                        kWavefrontForward, nullptr, useCache ? &cache : nullptr),
              "batch render");
@@ -1160,7 +1160,7 @@ int32_t vkrt_cuda_nrc_configure(VKRT_CudaContext* c, const VKRT_CudaNrcConfig* n
     if (!c || !n) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     if (!(n->learningRate >= 0.0f) || n->trainingPaths > (1u << 22) || n->trainingSteps > 64u ||
         n->inferenceTensorPath > VKRT_CUDA_NRC_MMA_SYNC || !(n->inferenceAverage >= 0.0f && n->inferenceAverage < 1.0f) ||
-        !(n->terminationSpread >= 0.0f && n->terminationSpread <= 3.0e38f))
+        !(n->terminationSpread >= 0.0f && n->terminationSpread <= 3.0e38f) || n->trainingTracer > 1u)
         return invalid(c, "radiance cache configuration out of range");
     cudaSetDevice(c->device);
     if (!c->nrc) c->nrc.reset(new NrcEngine());
@@ -1185,6 +1185,17 @@ int32_t nrcReady(VKRT_CudaContext* c) {
     return VKRT_CUDA_SUCCESS;
 }
 }  // namespace
+
+int32_t vkrt_cuda_nrc_read_training_records(VKRT_CudaContext* c, float* inputs, float* targets, uint32_t capacity,
+                                            uint32_t* count) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (capacity && (!inputs || !targets)) return invalid(c, "null training-record buffer");
+    if (count) *count = 0;
+    if (!c->wavefront) return VKRT_CUDA_SUCCESS;
+    cudaSetDevice(c->device);
+    VKRT_TRY(c, c->wavefront->readTrainingRecords(inputs, targets, capacity, count, c->stream), "read training records");
+    return VKRT_CUDA_SUCCESS;
+}
 
 int32_t vkrt_cuda_nrc_infer(VKRT_CudaContext* c, const float* inputs, uint32_t n, float* outputs) {
     int32_t r = nrcReady(c);

@@ -70,6 +70,16 @@ struct WfGlobals {
     // every slot holds its own item (a slot per item, no tile padding): the first queue is the slot order itself,
     // filled without atomics, which keeps the camera rays in tile order for the first traversal
     uint32_t identityStart;
+    // radiance-cache training pass (kWavefrontTrain): per slot up to kNrcTrainVerts surface vertices, then records
+    NrcInput* trainIn;     // Q x kNrcTrainVerts: the cache inputs of each vertex
+    float4* trainThr;      // the throughput that reached each vertex
+    float4* trainRad;      // the path radiance after each vertex's emission, before its light samples
+    uint32_t* trainCount;  // vertices recorded per slot
+    NrcInput* recIn;       // training records of the frame
+    float4* recTarget;
+    uint32_t* recCount;
+    uint32_t maxRecords;
+    uint32_t trainSeed, trainFrame;
     const WfScene* scenes;
     const uint32_t* itemBases;  // scenes[i].itemBase, contiguous for the item -> scene search
     const uint32_t* workBases;  // scenes[i].workBase
@@ -338,12 +348,24 @@ VKRT_DEV bool startSample(const WfGlobals& g, const WfScene* scenes, uint32_t sl
                           uint32_t sample, PathState* held) {
     const WfScene& S = scenes[sceneId];
     int px, py;
-    if (!workPixel(S, work, px, py)) return false;
-    uint32_t pix = uint32_t(py) * S.filmWidth + uint32_t(px);
-    // a frame continues the film's sample count; the primal and adjoint passes replay the samples from sampleBase
-    uint32_t first = g.mode == kWavefrontForward ? uint32_t(S.film.accumRead[pix].w + 0.5f) : g.adj.sampleBase;
-    StepConfig cfg = stepConfig(g, S);
-    PathState p = beginPath<kSpectral>(cfg, S.sd, px, py, first + sample);
+    PathState p;
+    uint32_t pix = 0;
+    if (g.mode == kWavefrontTrain) {
+        // training path `work`: a hashed pixel of the viewport and its own random stream (sample index 2^30 + work),
+        // as the one-thread-per-path training kernel chooses them
+        if (S.vw == 0u || S.vh == 0u) return false;
+        const uint32_t h0 = wellonsHash(g.trainSeed ^ (g.trainFrame * 0x9e3779b9u) ^ (work * 0x85ebca6bu));
+        px = int(S.vx0 + h0 % S.vw);
+        py = int(S.vy0 + wellonsHash(h0) % S.vh);
+        p = beginPath<kSpectral>(stepConfig(g, S), S.sd, px, py, 0x40000000u + work);
+        g.trainCount[slot] = 0u;
+    } else {
+        if (!workPixel(S, work, px, py)) return false;
+        pix = uint32_t(py) * S.filmWidth + uint32_t(px);
+        // a frame continues the film's sample count; the primal and adjoint passes replay the samples from sampleBase
+        uint32_t first = g.mode == kWavefrontForward ? uint32_t(S.film.accumRead[pix].w + 0.5f) : g.adj.sampleBase;
+        p = beginPath<kSpectral>(stepConfig(g, S), S.sd, px, py, first + sample);
+    }
     if (held) *held = p;
     else storePath(g, slot, p);
     storePathExt(g, slot, p);
@@ -824,7 +846,8 @@ VKRT_DEV void adjFinishPending(const WfGlobals& g, const WfScene& S, uint32_t sl
 
 // kFull: vkrt's whole material stack (and alpha tests); kFeatures: the denoiser features (taken when g.features is
 // set). Separate instantiations, so frames that need neither keep the register budget of the plain kernel.
-template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFull = false, bool kFeatures = kFull>
+// kTrain: the cache's training pass, whose surface vertices are recorded for the training records.
+template <bool kSpectral, bool kAdjoint, int kMinBlocks, bool kFull = false, bool kFeatures = kFull, bool kTrain = false>
 __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, uint32_t inQueue, uint32_t outQueue) {
     const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
@@ -879,6 +902,21 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                                                                AdjointHook{&av, xyz(g.adjDelta[slot])});
                 if (g.adj.wantEmission && av.emitted) scatterHitEmission(S.sc, g.adj, smemMat, av);
                 adjStoreVertex(g, slot, av, cont);
+            } else if constexpr (kTrain) {
+                // the vertex's cache inputs, the throughput that reached it and the radiance after its emission
+                NrcInput tin;
+                bool has = false;
+                const float4 thrBefore = p.thr;
+                cont = shadePathVertex<kSpectral, TrainHook, kFull>(S.sc, S.sd, cfg, specTable(S), p, h, sh, ns,
+                                                                    TrainHook{{}, &tin, &has, p.d});
+                const uint32_t nv = g.trainCount[slot];
+                if (has && nv < kNrcTrainVerts) {
+                    const size_t v = size_t(slot) * kNrcTrainVerts + nv;
+                    g.trainIn[v] = tin;
+                    g.trainThr[v] = thrBefore;
+                    g.trainRad[v] = p.radiance;
+                    g.trainCount[slot] = nv + 1u;
+                }
             } else {
                 const bool featDone = (p.flags & kPathFeatureDone) != 0u;
                 DenoiserFeature feat{f3(0.0f), f3(0.0f), featDone ? 1.0f : 0.0f};
@@ -1000,7 +1038,8 @@ __global__ void __launch_bounds__(kWfThreads) kWfShadowScan(WfGlobals g) {
     warpCount(&g.counters->shadowRays, traced);
 }
 
-template <bool kSpectral, bool kAdjoint>
+// kTrain: the cache's training pass, which turns the recorded vertices of a finished path into training records
+template <bool kSpectral, bool kAdjoint, bool kTrain = false>
 __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t outQueue) {
     const WfScene* scenes = g.scenes;
     MaterialGradient* smemMat = nullptr;
@@ -1032,6 +1071,28 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             g.pendFlags[slot] = 0u;
             if constexpr (kAdjoint) {
                 adjFinishPending(g, S, slot, pf, p.radiance, smemMat);
+            } else if constexpr (kTrain) {
+                // each recorded vertex j: the radiance the rest of the path gathered after the vertex's emission,
+                // over the throughput that reached it (hero lanes converted like a sample result), in linear sRGB
+                const float4 total = p.radiance;
+                const uint32_t nv = g.trainCount[slot];
+                for (uint32_t j = 0; j < nv; ++j) {
+                    const size_t v = size_t(slot) * kNrcTrainVerts + j;
+                    const float4 vt = g.trainThr[v], vr = g.trainRad[v];
+                    float4 suf;
+                    suf.x = vt.x > 0.0f ? (total.x - vr.x) / vt.x : 0.0f;
+                    suf.y = vt.y > 0.0f ? (total.y - vr.y) / vt.y : 0.0f;
+                    suf.z = vt.z > 0.0f ? (total.z - vr.z) / vt.z : 0.0f;
+                    suf.w = vt.w > 0.0f ? (total.w - vr.w) / vt.w : 0.0f;
+                    const float3 rgb = kSpectral ? xyzToLinearSrgb(spectral4ToXYZ(suf, heroLambdas(p.lamUnit),
+                                                                                  kLambdaRange))
+                                                 : xyz(suf);
+                    const uint32_t pos = atomicAdd(g.recCount, 1u);
+                    if (pos < g.maxRecords) {
+                        g.recIn[pos] = g.trainIn[v];
+                        g.recTarget[pos] = make_float4(rgb.x, rgb.y, rgb.z, 0.0f);
+                    }
+                }
             } else {
                 if (pf & kPendCache) {  // the cache's radiance times the path throughput completes the path
                     const float3 pred = fmax3(xyz(g.nrcPred[g.slotQuery[slot]]), f3(0.0f));
@@ -1045,7 +1106,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
                 float3 res = pathResult<kSpectral>(cfg, p);
                 g.sampleBuf[size_t(S.itemBase) + g.slotItem[slot]] = make_float4(res.x, res.y, res.z, 0.0f);
             }
-            samples = 1;
+            samples = kTrain ? 0u : 1u;  // training paths are not samples of the frame
         }
         // the next items for this warp's finished slots: one cursor fetch per warp, none once the cursor is past the
         // last item (always, with one slot per item); the counter only grows, so a stale read is conservative
@@ -1126,11 +1187,11 @@ struct WavefrontEngine::Buffers {
     WfScene* scenes = nullptr;
     uint32_t* bases = nullptr;  // itemBase of every scene, then workBase
     size_t c_bases = 0;
-    WfGraphCache graphs[3];
+    WfGraphCache graphs[4];  // by WavefrontMode
     float stageMs[kStageCount] = {};
     uint32_t* hostCount = nullptr;  // pinned word the stage-by-stage loop polls
     // radiance cache: queries, predictions, training records
-    size_t c_nq = 0, c_sq = 0, c_np = 0, c_ri = 0, c_rt = 0, c_rc = 0;
+    size_t c_nq = 0, c_sq = 0, c_np = 0, c_ri = 0, c_rt = 0, c_rc = 0, c_ti = 0, c_tt = 0, c_tr = 0, c_tc = 0;
     NrcInput* recIn = nullptr;
     float4* recTarget = nullptr;
     uint32_t* recCount = nullptr;
@@ -1138,6 +1199,17 @@ struct WavefrontEngine::Buffers {
 };
 
 uint32_t WavefrontEngine::lastCacheRecords() const { return b_->lastRecords; }
+
+cudaError_t WavefrontEngine::readTrainingRecords(void* inputs, void* targets, uint32_t capacity, uint32_t* count,
+                                                 cudaStream_t stream) const {
+    const uint32_t n = std::min(capacity, b_->lastRecords);
+    if (count) *count = b_->lastRecords;
+    if (!n) return cudaSuccess;
+    cudaError_t e = cudaMemcpyAsync(inputs, b_->recIn, sizeof(NrcInput) * n, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(targets, b_->recTarget, sizeof(float4) * n, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    return e;
+}
 
 const float* WavefrontEngine::lastStageMs() const { return b_->stageMs; }
 
@@ -1163,13 +1235,35 @@ void WavefrontEngine::release() {
                     g.nrcQueries, g.slotQuery, g.nrcPred, b_->recIn, b_->recTarget, b_->recCount, g.adjDelta,
                     g.adjTotal,
                     g.adjUv, g.adjColor, g.adjReq0, g.adjReq1, g.adjEm0, g.adjEm1, g.adjRatioB, g.adjRatioR,
-                    g.itemFeatA, g.itemFeatN, g.extA, g.extB, g.extC, g.extD, g.alphaSeed};
+                    g.itemFeatA, g.itemFeatN, g.extA, g.extB, g.extC, g.extD, g.alphaSeed,
+                    g.trainIn, g.trainThr, g.trainRad, g.trainCount};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b_->hostCount) cudaFreeHost(b_->hostCount);
     Buffers* fresh = new Buffers();
     std::swap(*b_, *fresh);
     delete fresh;
+}
+
+// The frame's training records (counted on the device) feed `trainingSteps` optimiser steps over 64K-record batches.
+cudaError_t WavefrontEngine::trainOnRecords(const WfCacheFrame& cache, cudaStream_t stream) {
+    Buffers& B = *b_;
+    const uint32_t maxRecords = cache.trainingPaths * kNrcTrainVerts;
+    cudaError_t e = cudaSuccess;
+    if (!B.hostCount) e = cudaMallocHost(&B.hostCount, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.hostCount, B.recCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return e;
+    const uint32_t records = std::min(*B.hostCount, maxRecords);
+    B.lastRecords = records;
+    const uint32_t batch = std::min<uint32_t>(records, 1u << 16);
+    for (uint32_t k = 0; batch && k < cache.trainingSteps; ++k) {
+        const uint32_t off = uint32_t((uint64_t(k) * batch) % records);
+        const uint32_t n = std::min(batch, records - off);
+        e = cache.engine->train(B.recIn + off, B.recTarget + off, n, nullptr, true, stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool spectral, const WavefrontConfig& cfgIn,
@@ -1181,6 +1275,19 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     if (adjMode && (!adjoint || spectral || scenesIn.size() != 1)) return cudaErrorInvalidValue;
     const bool useCache = cache && cache->engine && cache->engine->ready() && mode == kWavefrontForward;
     if (useCache && scenesIn.size() != 1) return cudaErrorInvalidValue;
+    const bool trainMode = mode == kWavefrontTrain;
+    if (trainMode && (!cache || scenesIn.size() != 1)) return cudaErrorInvalidValue;
+    // a cache frame traces its training paths first, as a wavefront pass of their own over the same scene, and
+    // trains the cache on their records before rendering with it
+    const bool wavefrontTraining = useCache && cache->trainingPaths && cache->trainingTracer == 1u;
+    if (wavefrontTraining) {
+        cudaError_t e = grow(B.recCount, B.c_rc, 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.recCount, 0, sizeof(uint32_t), stream);
+        if (e == cudaSuccess) e = render(scenesIn, spectral, cfgIn, rngMode, rngSeed, counters, stream, kWavefrontTrain,
+                                         nullptr, cache);
+        if (e == cudaSuccess) e = trainOnRecords(*cache, stream);
+        if (e != cudaSuccess) return e;
+    }
     WavefrontConfig cfg = cfgIn;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
@@ -1200,6 +1307,15 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     for (WfScene& S : scenes) {
         S.tileW = std::max(1u, cfg.tileWidth);
         S.tileH = std::max(1u, cfg.tileHeight);
+        if (trainMode) {  // one work item (one sample) per training path
+            S.tilesX = 0;
+            S.workBase = S.itemBase = 0;
+            S.workCount = total = cache->trainingPaths;
+            S.spp = 1;
+            items = S.workCount;
+            maxDepth = std::max(maxDepth, S.sd.rrMaxDepth);
+            continue;
+        }
         S.tilesX = (S.vw + S.tileW - 1) / S.tileW;
         uint32_t tilesY = (S.vh + S.tileH - 1) / S.tileH;
         S.workBase = total;
@@ -1267,6 +1383,16 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     WF_GROW(shadowB, c_sB, 2 * size_t(Q));
     WF_GROW(keyHist, c_hist, keys);
     WF_GROW(counts, c_counts, kCntCount);
+    if (trainMode) {
+        WF_GROW(trainIn, c_ti, size_t(Q) * kNrcTrainVerts);
+        WF_GROW(trainThr, c_tt, size_t(Q) * kNrcTrainVerts);
+        WF_GROW(trainRad, c_tr, size_t(Q) * kNrcTrainVerts);
+        WF_GROW(trainCount, c_tc, Q);
+        const size_t maxRecords = size_t(cache->trainingPaths) * kNrcTrainVerts;
+        if (e == cudaSuccess) e = grow(B.recIn, B.c_ri, maxRecords);
+        if (e == cudaSuccess) e = grow(B.recTarget, B.c_rt, maxRecords);
+        if (e == cudaSuccess) e = grow(B.recCount, B.c_rc, 1);
+    }
     if (useCache) {
         WF_GROW(nrcQueries, c_nq, Q);
         WF_GROW(slotQuery, c_sq, Q);
@@ -1316,6 +1442,12 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     g.transmissive = transmissive ? 1u : 0u;
     g.alpha = alpha ? 1u : 0u;
     g.adj = adjoint ? *adjoint : AdjointParams{};
+    g.recIn = B.recIn;
+    g.recTarget = B.recTarget;
+    g.recCount = B.recCount;
+    g.maxRecords = trainMode ? cache->trainingPaths * kNrcTrainVerts : 0u;
+    g.trainSeed = trainMode ? cache->seed : 0u;
+    g.trainFrame = trainMode ? cache->frame : 0u;
     g.cacheDepth = useCache ? cache->cacheDepth : 0xFFFFFFFFu;
     g.cacheSpread = useCache ? cache->cacheSpread : 0.0f;
     g.scenes = B.scenes;
@@ -1379,6 +1511,13 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             // register budget follows the requested residency: 168 (3 blocks/SM, no spills), 128 (4), 80 (6) or
             // 64 (8) registers; kernels compiled for one residency run on a grid of that many blocks per SM
             if (adjMode) kWfShade<false, true, 4><<<grid4, kWfThreads, 0, stream>>>(g, in, out);
+            else if (trainMode && extended && spectral)
+                kWfShade<true, false, 3, true, false, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
+            else if (trainMode && extended)
+                kWfShade<false, false, 3, true, false, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
+            else if (trainMode && spectral)
+                kWfShade<true, false, 4, false, false, true><<<grid4, kWfThreads, 0, stream>>>(g, in, out);
+            else if (trainMode) kWfShade<false, false, 4, false, false, true><<<grid4, kWfThreads, 0, stream>>>(g, in, out);
             else if (extended && spectral) kWfShade<true, false, 3, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
             else if (extended) kWfShade<false, false, 3, true><<<grid3, kWfThreads, 0, stream>>>(g, in, out);
             else if (features && spectral)  // reflection-only materials with feature films
@@ -1405,6 +1544,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             stage(kStageShade, [&] { cache->engine->inferCounted(g.nrcQueries, g.counts + kCntQueries, Q, g.nrcPred, stream); });
         stage(kStageFinalize, [&] {
             if (adjMode) kWfFinalize<false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
+            else if (trainMode && spectral) kWfFinalize<true, false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
+            else if (trainMode) kWfFinalize<false, false, true><<<gridS, kWfThreads, 0, stream>>>(g, out);
             else if (spectral) kWfFinalize<true, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
             else kWfFinalize<false, false><<<gridS, kWfThreads, 0, stream>>>(g, out);
         });
@@ -1427,9 +1568,9 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
         });
     };
 
-    B.lastRecords = 0;
-    if (useCache) {
-        // train the cache on this frame's training paths before rendering with it
+    if (!wavefrontTraining && !trainMode) B.lastRecords = 0;
+    if (useCache && !wavefrontTraining) {
+        // train the cache on this frame's training paths, one thread per path, before rendering with it
         e = cudaMemsetAsync(B.recCount, 0, sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
         const uint32_t maxRecords = cache->trainingPaths * kNrcTrainVerts;
@@ -1445,19 +1586,8 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
             else VKRT_TRAIN(false, false);
 #undef VKRT_TRAIN
         }
-        if (!B.hostCount) e = cudaMallocHost(&B.hostCount, sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMemcpyAsync(B.hostCount, B.recCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        e = trainOnRecords(*cache, stream);
         if (e != cudaSuccess) return e;
-        const uint32_t records = std::min(*B.hostCount, maxRecords);
-        B.lastRecords = records;
-        const uint32_t batch = std::min<uint32_t>(records, 1u << 16);
-        for (uint32_t k = 0; batch && k < cache->trainingSteps; ++k) {
-            const uint32_t off = uint32_t((uint64_t(k) * batch) % records);
-            const uint32_t n = std::min(batch, records - off);
-            e = cache->engine->train(B.recIn + off, B.recTarget + off, n, nullptr, true, stream);
-            if (e != cudaSuccess) return e;
-        }
     }
 
     if (!cfg.useGraph) {

@@ -35,7 +35,9 @@ struct WfScene {
 
 // forward: a frame blended into each scene's film; primal: the same paths, each (pixel, sample) radiance kept in the
 // engine's sample buffer and the film untouched; adjoint: the primal paths replayed with gradients (one scene)
-enum WavefrontMode : uint32_t { kWavefrontForward = 0, kWavefrontPrimal = 1, kWavefrontAdjoint = 2 };
+// train: the radiance cache's training paths of a cache frame (items are training paths at hashed pixels of the
+// scene; their surface vertices become training records)
+enum WavefrontMode : uint32_t { kWavefrontForward = 0, kWavefrontPrimal = 1, kWavefrontAdjoint = 2, kWavefrontTrain = 3 };
 
 struct WavefrontConfig {
     uint32_t queueCapacity;  // path slots; 0 = one per (pixel, sample) item, capped at 64M
@@ -66,6 +68,7 @@ struct WfCacheFrame {
     uint32_t seed;
     uint32_t frame;
     float cacheSpread;  // area-spread constant c (0: paths end at cacheDepth only)
+    uint32_t trainingTracer;  // 0: one thread per training path; 1: the training paths run as a wavefront pass
 };
 
 class WavefrontEngine {
@@ -84,11 +87,15 @@ public:
                        const WfCacheFrame* cache = nullptr);
     // records and steps of the last cache training
     uint32_t lastCacheRecords() const;
+    // the last cache frame's training records (NrcInput and float4 target each), up to `capacity`; *count = records
+    cudaError_t readTrainingRecords(void* inputs, void* targets, uint32_t capacity, uint32_t* count,
+                                    cudaStream_t stream) const;
     void release();
     // per-stage device milliseconds of the last render call made with profileStages (zeros otherwise)
     const float* lastStageMs() const;
 
 private:
+    cudaError_t trainOnRecords(const WfCacheFrame& cache, cudaStream_t stream);
     struct Buffers;
     Buffers* b_;
 };
