@@ -153,7 +153,7 @@ struct WfGlobals {
     float* extD;
 };
 
-// finished-queue entries whose result the shade kernel has written already (slot numbers stay below 2^26)
+// finished-queue entries whose result the shade kernel has written already (slot numbers stay below 2^28)
 constexpr uint32_t kFinishedDone = 0x80000000u;
 
 VKRT_DEV uint32_t warpPush(uint32_t* counter, bool want) {
