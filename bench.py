@@ -816,6 +816,9 @@ def run_profile_frame(args) -> dict:
         ctx.set_wavefront_config(rayOrder=args.ray_order)
     if args.sort is not None:
         ctx.set_wavefront_config(sortByMaterial=args.sort)
+    if args.tile:
+        tw, th = (int(v) for v in args.tile.split("x"))
+        ctx.set_wavefront_config(tileWidth=tw, tileHeight=th)
     if args.cache:
         ctx.nrc_configure(enabled=1, trainingTracer=args.training_tracer)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -848,7 +851,7 @@ def run_profile_frame(args) -> dict:
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
                        "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
                        "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order,
-                       "full_materials": args.full_materials, "sort": args.sort}
+                       "full_materials": args.full_materials, "sort": args.sort, "tile": args.tile}
     ctx.close()
     return out
 
@@ -885,6 +888,7 @@ def main():
     prof.add_argument("--intersect-blocks", type=int, default=0, help="traversal kernel residency (blocks per SM)")
     prof.add_argument("--ray-order", type=int, default=0, help="1: traversal queues binned by direction octant")
     prof.add_argument("--sort", type=int, default=None, help="shade-queue order (sortByMaterial 0-3)")
+    prof.add_argument("--tile", default="", help="wavefront tile WxH (default 16x8)")
     prof.add_argument("--full-materials", action="store_true",
                       help="vkrt's full material stack (glass, clear coat over Oren-Nayar, subsurface)")
     args = ap.parse_args()

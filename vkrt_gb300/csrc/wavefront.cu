@@ -67,8 +67,8 @@ struct WfGlobals {
     // kFinishedDone, only to take its next item
     uint32_t directFinish;
     uint32_t refills;
-    // every slot holds its own item (a slot per item, no tile padding): the first queue is the slot order itself,
-    // filled without atomics, which keeps the camera rays in tile order for the first traversal
+    // no tile padding, so slot s starts item s for every slot (Q never exceeds the item count): the first queue is the
+    // slot order itself, filled without atomics, which keeps the camera rays in tile order for the first traversal
     uint32_t identityStart;
     // radiance-cache training pass (kWavefrontTrain): per slot up to kNrcTrainVerts surface vertices, then records
     NrcInput* trainIn;     // Q x kNrcTrainVerts: the cache inputs of each vertex
@@ -1437,7 +1437,7 @@ cudaError_t WavefrontEngine::render(const std::vector<WfScene>& scenesIn, bool s
     bool padded = false;  // some tile reaches past its viewport, so some items are padding
     for (const WfScene& S : scenes)
         if (uint64_t(S.workCount) != uint64_t(S.vw) * S.vh) padded = true;
-    g.identityStart = !padded && Q >= totalItems && !cfg.rayOrder ? 1u : 0u;
+    g.identityStart = !padded && totalItems > 0u && !cfg.rayOrder ? 1u : 0u;
     g.features = features ? 1u : 0u;
     g.transmissive = transmissive ? 1u : 0u;
     g.alpha = alpha ? 1u : 0u;
