@@ -797,7 +797,8 @@ def run_profile_frame(args) -> dict:
     scene = scenes.icosphere_field(n_spheres=args.spheres, width=args.width, height=args.height, spp=args.spp,
                                    max_depth=args.depth, seed=1, spectral=not args.rgb)
     integ = abi.INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
-    ctx = RenderContext(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE, integrator=integ)
+    ctx = RenderContext(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE, integrator=integ,
+                        **({"treelet_min_triangles": 0xFFFFFFFF} if args.no_treelets else {}))
     if not args.rgb:
         scene.rgb2spec, info = ctx.generate_rgb2spec(64)
         scene.scene_data["rgb2specSRGB"] = info
@@ -851,7 +852,8 @@ def run_profile_frame(args) -> dict:
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
                        "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
                        "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order,
-                       "full_materials": args.full_materials, "sort": args.sort, "tile": args.tile}
+                       "full_materials": args.full_materials, "sort": args.sort, "tile": args.tile,
+                       "treelets": not args.no_treelets}
     ctx.close()
     return out
 
@@ -889,6 +891,7 @@ def main():
     prof.add_argument("--ray-order", type=int, default=0, help="1: traversal queues binned by direction octant")
     prof.add_argument("--sort", type=int, default=None, help="shade-queue order (sortByMaterial 0-3)")
     prof.add_argument("--tile", default="", help="wavefront tile WxH (default 16x8)")
+    prof.add_argument("--no-treelets", action="store_true", help="BVH without treelet restructuring")
     prof.add_argument("--full-materials", action="store_true",
                       help="vkrt's full material stack (glass, clear coat over Oren-Nayar, subsurface)")
     args = ap.parse_args()
