@@ -846,7 +846,8 @@ def run_profile_frame(args) -> dict:
             out["frame_ms"] = round(out.get("frame_ms", 0.0) + ev[0].elapsed_time(ev[1]), 3)
     st = ctx.stats()
     out["bvh"] = {"nodes": int(st["bvhNodeCount"]), "triangles": int(st["bvhTriangleCount"]),
-                  "build_ms": round(float(st["bvhBuildMs"]), 2)}
+                  "build_ms": round(float(st["bvhBuildMs"]), 2), "sah_lbvh": round(float(st["bvhSahLbvh"]), 2),
+                  "sah_treelets": round(float(st["bvhSahTreelets"]), 2)}
     out["workload"] = {"width": args.width, "height": args.height, "spp": args.spp, "depth": args.depth,
                        "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",

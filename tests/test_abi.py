@@ -59,6 +59,22 @@ def test_host_defaults_read_through_the_layouts(built):
     assert np.allclose(sd["viewInverse"][0][3, :3], [-0.5, 0.2, -0.2], atol=1e-6)
 
 
+def test_context_config_is_validated_before_any_device_call(built):
+    """vkrt_cuda_create refuses out-of-range configuration fields with VKRT_ERROR_INVALID_ARGUMENT before it looks
+    for a device, so this runs without a GPU."""
+    import ctypes as C
+    lib = abi.load()
+    cfg = np.zeros(1, abi.CONFIG)
+    lib.vkrt_cuda_default_config(abi.ptr(cfg))
+    assert cfg["treeletPasses"] == 0 and cfg["treeletMinTriangles"] == 0 and cfg["treeletsOnUpdate"] == 0
+    for field, bad in (("treeletPasses", 9), ("treeletsOnUpdate", 2), ("rngMode", 7), ("environmentSampling", 5)):
+        c = cfg.copy()
+        c[field] = bad
+        handle = C.c_void_p()
+        assert lib.vkrt_cuda_create(abi.ptr(c), C.byref(handle)) == abi.ERROR_INVALID_ARGUMENT, field
+        assert not handle.value
+
+
 def test_backend_records_match_the_header(tmp_path):
     """The numpy layouts of the backend's own records (configuration, statistics, rays, hits, gradients) have the
     field offsets and sizes the C header gives them: a probe compiled against include/vkrt_cuda.h prints offsetof

@@ -103,8 +103,9 @@ def test_icosphere_field_bit_exact(built):
 
 
 def test_bvh_build_options(built):
-    """Treelet restructuring runs from treeletMinTriangles up (default 65,536) and, after mesh-transform edits, only
-    when treeletsOnUpdate asks; every variant of the tree traces bit for bit like the oracle."""
+    """Treelet restructuring runs from treeletMinTriangles up (default 65,536), treeletPasses times, and, after
+    mesh-transform edits, only when treeletsOnUpdate asks; every variant of the tree traces bit for bit like the
+    oracle."""
     scene = scenes.icosphere_field(n_spheres=60, width=64, height=48, seed=4, spectral=False, env_size=(64, 32))
     rays = _rays_from_camera(scene, 20000, 13)
     with RenderContext() as ctx:  # 76,800 triangles: restructured
@@ -131,6 +132,13 @@ def test_bvh_build_options(built):
         st = ctx.stats()
         assert st["bvhSahTreelets"] < st["bvhSahLbvh"]
         _check(edited, ctx, rays)
+    sah = {}
+    for passes in (1, 3):  # repeated bottom-up passes (default 2) never raise the cost and trace the same hits
+        with RenderContext(treelet_passes=passes) as ctx:
+            ctx.upload_scene(scene)
+            sah[passes] = ctx.stats()["bvhSahTreelets"]
+            _check(scene, ctx, rays)
+    assert sah[3] <= sah[1] * (1.0 + 1e-6)
     small = scenes.cornell(32, 32)
     with RenderContext() as ctx:  # 36 triangles: no restructuring
         ctx.upload_scene(small)

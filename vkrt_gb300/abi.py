@@ -75,9 +75,10 @@ HIT = np.dtype({"names": ["instanceIndex", "primitiveIndex", "t", "u", "v", "res
 
 CONFIG = np.dtype({"names": ["deviceIndex", "rngMode", "rngSeed", "environmentSampling", "countRays",
                              "threadsPerBlock", "blocksPerSM", "integrator", "treeletMinTriangles",
-                             "treeletsOnUpdate", "reserved"],
-                   "formats": ["<i4", "<u4", "<u8", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", ("<u4", 5)],
-                   "offsets": [0, 4, 8, 16, 20, 24, 28, 32, 36, 40, 44], "itemsize": 64})
+                             "treeletsOnUpdate", "treeletPasses", "reserved"],
+                   "formats": ["<i4", "<u4", "<u8", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4",
+                               ("<u4", 4)],
+                   "offsets": [0, 4, 8, 16, 20, 24, 28, 32, 36, 40, 44, 48], "itemsize": 64})
 
 WAVEFRONT_CONFIG = np.dtype({"names": ["queueCapacity", "tileWidth", "tileHeight", "sortByMaterial",
                                        "intersectBlocksPerSM", "shadeBlocksPerSM", "useGraph", "profileStages",

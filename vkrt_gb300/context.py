@@ -101,12 +101,13 @@ class RenderContext:
     def __init__(self, device: int = 0, rng_mode: int = abi.RNG_REFERENCE, rng_seed: int = 1,
                  environment_sampling: int = abi.ENV_BSDF_ONLY, count_rays: bool = False,
                  integrator: int = abi.INTEGRATOR_MEGAKERNEL, treelet_min_triangles: int = 0,
-                 treelets_on_update: bool = False):
+                 treelets_on_update: bool = False, treelet_passes: int = 0):
         self.lib = abi.load()
         cfg = np.zeros(1, dtype=abi.CONFIG)
         self.lib.vkrt_cuda_default_config(abi.ptr(cfg))
         cfg["treeletMinTriangles"] = treelet_min_triangles
         cfg["treeletsOnUpdate"] = 1 if treelets_on_update else 0
+        cfg["treeletPasses"] = treelet_passes
         cfg["deviceIndex"] = device
         cfg["rngMode"] = rng_mode
         cfg["rngSeed"] = rng_seed

@@ -9,7 +9,8 @@
 //                  warp-match ranked scatter)
 //   5. LBVH      : Karras 2012 binary radix tree, ties in the code broken by the sorted position
 //   6. refit     : bottom-up boxes, subtree sizes and SAH cost with one atomic arrival flag per node
-//   7. treelets  : Karras & Aila 2013 treelet restructuring (7 leaves, exhaustive over partitions by DP) in rounds
+//   7. treelets  : Karras & Aila 2013 treelet restructuring (7 leaves, exhaustive over partitions by DP), repeated
+//                  bottom-up passes (two by default)
 //   8. collapse  : binary -> 8-wide compressed nodes, children chosen by the SAH-optimal dynamic program of Ylitie et
 //                  al. 2017, level by level, leaves of up to 3 triangles, children placed in
 //                  octant slots so traversal visits them near to far (Ylitie et al. 2017)
@@ -857,7 +858,8 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
         if (n > 1) kRefit<<<(n + b - 1) / b, b, 0, stream>>>(n, dLeft, dRight, dParent, dLo, dHi, dLeafCount, dCost, dFlags);
         if (n > 2) {
             kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah);
-            if (in.treelets) {
+            // each pass rewires parent[] along with the children, so the next one walks the restructured tree
+            for (uint32_t pass = 0; pass < in.treeletPasses; ++pass) {
                 cudaMemsetAsync(dFlags, 0, sizeof(uint32_t) * n, stream);
                 kTreelets<<<(n + b - 1) / b, b, 0, stream>>>(n, kTreeletLeaves, dLeft, dRight, dParent, dLo, dHi,
                                                              dLeafCount, dCost, dFlags);

@@ -17,7 +17,7 @@ struct BvhBuildInput {
     const uint32_t* hostIdentity;           // host, 1 when the mesh transform is the identity
     uint32_t meshCount;
     uint32_t triCount;
-    bool treelets;  // run treelet restructuring after the LBVH
+    uint32_t treeletPasses;  // bottom-up treelet restructuring passes after the LBVH (0: none)
 };
 
 struct BvhBuffers {

@@ -202,7 +202,8 @@ cudaError_t rebuildBvh(VKRT_CudaContext* c, bool afterEdit) {
     in.meshCount = uint32_t(c->hostMeshes.size());
     in.triCount = c->triCount;
     const uint32_t minTris = c->cfg.treeletMinTriangles ? c->cfg.treeletMinTriangles : 65536u;
-    in.treelets = c->triCount >= minTris && (!afterEdit || c->cfg.treeletsOnUpdate != 0u);
+    const bool treelets = c->triCount >= minTris && (!afterEdit || c->cfg.treeletsOnUpdate != 0u);
+    in.treeletPasses = treelets ? (c->cfg.treeletPasses ? c->cfg.treeletPasses : 2u) : 0u;
     return buildBvh(in, c->bvh, &c->bvhStats, c->stream);
 }
 
@@ -403,7 +404,7 @@ int32_t vkrt_cuda_create(const VKRT_CudaConfig* config, VKRT_CudaContext** out) 
     if (config) cfg = *config;
     else vkrt_cuda_default_config(&cfg);
     if (cfg.rngMode > VKRT_CUDA_RNG_PCG32 || cfg.environmentSampling > VKRT_CUDA_ENV_IMPORTANCE ||
-        cfg.treeletsOnUpdate > 1u)
+        cfg.treeletsOnUpdate > 1u || cfg.treeletPasses > 8u)
         return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0 || cfg.deviceIndex < 0 || cfg.deviceIndex >= count)

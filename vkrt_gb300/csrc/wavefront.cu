@@ -242,6 +242,12 @@ VKRT_DEV uint32_t queueEntry(const WfGlobals& g, const uint32_t* q, const uint32
     return q[size_t(b) * g.Q + (i - start)];
 }
 
+// the scene of a slot; frames of one scene neither write nor read the per-slot array (a scattered 4-byte access per
+// item, in front of each shadow ray's traversal)
+VKRT_DEV uint32_t sceneOfSlot(const WfGlobals& g, uint32_t slot) {
+    return g.sceneCount == 1u ? 0u : g.slotScene[slot];
+}
+
 // miss / dielectric / metal
 VKRT_DEV uint32_t hitClass(const DeviceScene& sc, const TraceHit& h) {
     if (h.mesh == VKRT_CUDA_INVALID_INDEX) return 0u;
@@ -400,7 +406,7 @@ VKRT_DEV bool acquireItem(const WfGlobals& g, const WfScene* scenes, uint32_t sl
         const WfScene& S = scenes[sceneId];
         uint32_t local = w - S.itemBase;
         if (startSample<kSpectral>(g, scenes, slot, sceneId, local / S.spp, local % S.spp, held)) {
-            g.slotScene[slot] = sceneId;
+            if (g.sceneCount != 1u) g.slotScene[slot] = sceneId;
             g.slotItem[slot] = local;
             if (g.features) {
                 g.itemFeatA[size_t(S.itemBase) + local] = f4(0.0f);
@@ -542,7 +548,7 @@ VKRT_DEV void storeHit(const WfGlobals& g, uint32_t i, uint32_t slot, const Trac
     r[kRecHit] = make_float4(__uint_as_float(h.mesh), __uint_as_float(h.prim), h.t, h.u);
     reinterpret_cast<float*>(r + kRecPdf)[3] = h.v;
     if (g.sort == kSortMaterial) {  // histogram of (scene, class) or material keys for the counting sort
-        const uint32_t sceneId = g.slotScene[slot];
+        const uint32_t sceneId = sceneOfSlot(g, slot);
         const WfScene& S = g.scenes[sceneId];
         const uint32_t key = !g.keyByMaterial ? 3u * sceneId + hitClass(S.sc, h)
                              : h.mesh == VKRT_CUDA_INVALID_INDEX
@@ -551,7 +557,7 @@ VKRT_DEV void storeHit(const WfGlobals& g, uint32_t i, uint32_t slot, const Trac
         g.hitKey[i] = key;
         warpAggregatedSlot(g.keyHist, key);
     } else if (g.sort == kSortClass) {  // filed straight into the class queues
-        const uint32_t c = hitClass(g.scenes[g.slotScene[slot]].sc, h);
+        const uint32_t c = hitClass(g.scenes[sceneOfSlot(g, slot)].sc, h);
         const uint32_t pos = warpAggregatedSlot(&g.counts[kCntClass0], c);
         g.classQueue[size_t(c) * g.Q + pos] = slot;
     }
@@ -570,7 +576,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfIntersect(WfGlobals
         n, &g.counts[kCntFetchIntersect], smemStack + threadIdx.x, blockDim.x, &g.counters->errorFlags, g.refill,
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             uint32_t slot = queueEntry(g, q, binEnd, i);
-            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            const DeviceScene& sc = g.scenes[sceneOfSlot(g, slot)].sc;
             const float4* rp = record(g, slot);
             float4 o = rp[kRecOrigin], d = rp[kRecDir];
             r = TraceRay{make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), kTMin, kTMax};
@@ -602,7 +608,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfIntersectAlpha(WfGlobals g, uin
         const uint32_t i = base + threadIdx.x;
         if (i < n) {
             const uint32_t slot = queueEntry(g, q, binEnd, i);
-            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            const DeviceScene& sc = g.scenes[sceneOfSlot(g, slot)].sc;
             const float4* rp = record(g, slot);
             const float4 o = rp[kRecOrigin], d = rp[kRecDir], rf = rp[kRecRng];
             const uint4 rs = make_uint4(__float_as_uint(rf.x), __float_as_uint(rf.y), __float_as_uint(rf.z),
@@ -880,7 +886,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShade(WfGlobals g, 
                                                       : g.classQueue[2u * size_t(g.Q) + (i - nMiss - nDiel)]);
             else
                 slot = g.sort == 0u ? queueEntry(g, q, binEnd, i) : q[i];
-            const WfScene& S = scenes[g.slotScene[slot]];
+            const WfScene& S = scenes[sceneOfSlot(g, slot)];
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
             applyPending(g, slot, p.radiance);
@@ -994,7 +1000,7 @@ __global__ void __launch_bounds__(kWfThreads, kMinBlocks) kWfShadow(WfGlobals g)
         [&](uint32_t i, TraceRay& r, const WideNode*& nodes, const TriRecord*& tris, uint32_t& nodeCount) {
             float4 a = g.shadowA[i], b = g.shadowB[i];
             uint32_t slot = __float_as_uint(b.w) & 0x7FFFFFFFu;
-            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            const DeviceScene& sc = g.scenes[sceneOfSlot(g, slot)].sc;
             r = TraceRay{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
             nodes = sc.nodes;
             tris = sc.tris;
@@ -1025,7 +1031,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfShadowScan(WfGlobals g) {
             const float4 a = g.shadowA[i], b = g.shadowB[i];
             const uint32_t tag = __float_as_uint(b.w);
             const uint32_t slot = tag & 0x7FFFFFFFu;
-            const DeviceScene& sc = g.scenes[g.slotScene[slot]].sc;
+            const DeviceScene& sc = g.scenes[sceneOfSlot(g, slot)].sc;
             const TraceRay r{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), kTMin, a.w};
             const TraceHit h = traceBvh<true, kCount, false, true, kAlpha>(
                 sc, r, smemStack + threadIdx.x, blockDim.x, kCount ? g.counters : nullptr, 0u,
@@ -1063,7 +1069,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinalize(WfGlobals g, uint32_t 
             slot &= ~kFinishedDone;
         }
         if (valid && !done) {
-            uint32_t sceneId = g.slotScene[slot];
+            uint32_t sceneId = sceneOfSlot(g, slot);
             const WfScene& S = scenes[sceneId];
             PathState p = loadPath(g, slot);
             const uint32_t pf = g.pendFlags[slot];
