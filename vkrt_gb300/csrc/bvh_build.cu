@@ -9,8 +9,8 @@
 //                  warp-match ranked scatter)
 //   5. LBVH      : Karras 2012 binary radix tree, ties in the code broken by the sorted position
 //   6. refit     : bottom-up boxes, subtree sizes and SAH cost with one atomic arrival flag per node
-//   7. treelets  : Karras & Aila 2013 treelet restructuring (7 leaves, exhaustive over partitions by DP), repeated
-//                  bottom-up passes (two by default)
+//   7. treelets  : Karras & Aila 2013 treelet restructuring (7 leaves, exhaustive over partitions by a dynamic
+//                  program that a whole warp runs), repeated bottom-up passes (two by default)
 //   8. collapse  : binary -> 8-wide compressed nodes, children chosen by the SAH-optimal dynamic program of Ylitie et
 //                  al. 2017, level by level, leaves of up to 3 triangles, children placed in
 //                  octant slots so traversal visits them near to far (Ylitie et al. 2017)
@@ -332,92 +332,165 @@ __global__ void kRefit(uint32_t n, const uint32_t* __restrict__ left, const uint
 
 // ---- 7. treelet restructuring (Karras & Aila 2013) --------------------------------------------------------------
 constexpr int kTreeletLeaves = 7;
+constexpr uint32_t kTreeletSubsets = 1u << kTreeletLeaves;
+constexpr uint32_t kTreeletThreads = 64;
 
-// Optimal binary topology of a treelet rooted at `root`: the root's subtree is expanded into up to 7 treelet
-// leaves (repeatedly opening the internal leaf of largest area); a dynamic program over the 127 leaf subsets finds
-// the SAH-optimal partition tree (every partition of a subset is tried, the lowest leaf fixed on one side); the
-// treelet's internal nodes are rewired to it and refit. The original topology is among the candidates, so the
-// SAH cost never rises.
-__device__ void restructureTreelet(uint32_t n, uint32_t root, uint32_t* left, uint32_t* right, uint32_t* parent,
-                                   float4* nodeLo, float4* nodeHi, uint32_t* leafCount, float* cost) {
-    uint32_t leaves[kTreeletLeaves], internals[kTreeletLeaves - 1];
-    int nl = 2, ni = 1;
-    internals[0] = root;
-    leaves[0] = __ldcg(&left[root]);
-    leaves[1] = __ldcg(&right[root]);
-    while (nl < kTreeletLeaves) {
+// A treelet formed by one lane: the root's subtree expanded into up to 7 treelet leaves by repeatedly opening the
+// internal leaf of largest area (the opened node's left child takes its place, the right child is appended).
+struct TreeletSlot {
+    uint32_t node[kTreeletLeaves];
+    uint32_t internal[kTreeletLeaves - 1];  // the treelet's internal nodes, root first
+    float4 lo[kTreeletLeaves], hi[kTreeletLeaves];
+    uint32_t count[kTreeletLeaves];
+    float cost[kTreeletLeaves];
+    uint32_t leaves;
+};
+
+// One warp's dynamic program over the 127 leaf subsets of a treelet
+struct TreeletDp {
+    float area[kTreeletSubsets];
+    float copt[kTreeletSubsets];
+    unsigned long long best[kTreeletSubsets];  // (cost bits, 255 - partition): the lowest cost, ties to the larger partition
+    float refit[kTreeletSubsets];              // SAH cost of each rebuilt subtree
+    uint8_t part[kTreeletSubsets];
+};
+
+__device__ __forceinline__ float4 boxMin(float4 a, float4 b) {
+    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+}
+__device__ __forceinline__ float4 boxMax(float4 a, float4 b) {
+    return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.0f);
+}
+
+// the low bits of i placed, in order, at the set bits of mask
+__device__ __forceinline__ uint32_t depositBits(uint32_t i, uint32_t mask) {
+    uint32_t r = 0u;
+    for (uint32_t b = 1u; mask != 0u; b <<= 1) {
+        const uint32_t low = mask & (0u - mask);
+        if (i & b) r |= low;
+        mask ^= low;
+    }
+    return r;
+}
+
+// Forms the treelet rooted at `root` into the lane's slot; false when it has fewer than 3 leaves.
+__device__ bool formTreelet(uint32_t n, uint32_t root, const uint32_t* left, const uint32_t* right,
+                            const float4* nodeLo, const float4* nodeHi, const uint32_t* leafCount, const float* cost,
+                            TreeletSlot& T) {
+    float area[kTreeletLeaves];
+    uint32_t nl = 2, ni = 1;
+    T.internal[0] = root;
+    T.node[0] = __ldcg(&left[root]);
+    T.node[1] = __ldcg(&right[root]);
+    for (int i = 0; i < 2; ++i) {
+        T.lo[i] = __ldcg(&nodeLo[T.node[i]]);
+        T.hi[i] = __ldcg(&nodeHi[T.node[i]]);
+    }
+    area[0] = halfArea(T.lo[0], T.hi[0]);
+    area[1] = halfArea(T.lo[1], T.hi[1]);
+    while (nl < uint32_t(kTreeletLeaves)) {
         int best = -1;
         float bestA = -1.0f;
-        for (int i = 0; i < nl; ++i) {
-            uint32_t l = leaves[i];
-            if (l >= n - 1) continue;  // a triangle
-            float a = halfArea(__ldcg(&nodeLo[l]), __ldcg(&nodeHi[l]));
-            if (a > bestA) {
-                bestA = a;
-                best = i;
+        for (uint32_t i = 0; i < nl; ++i) {
+            if (T.node[i] >= n - 1) continue;  // a triangle
+            if (area[i] > bestA) {
+                bestA = area[i];
+                best = int(i);
             }
         }
         if (best < 0) break;
-        uint32_t x = leaves[best];
-        internals[ni++] = x;
-        leaves[best] = __ldcg(&left[x]);
-        leaves[nl++] = __ldcg(&right[x]);
+        const uint32_t x = T.node[best];
+        T.internal[ni++] = x;
+        const uint32_t l = __ldcg(&left[x]), r = __ldcg(&right[x]);
+        T.node[best] = l;
+        T.node[nl] = r;
+        T.lo[best] = __ldcg(&nodeLo[l]);
+        T.hi[best] = __ldcg(&nodeHi[l]);
+        T.lo[nl] = __ldcg(&nodeLo[r]);
+        T.hi[nl] = __ldcg(&nodeHi[r]);
+        area[best] = halfArea(T.lo[best], T.hi[best]);
+        area[nl] = halfArea(T.lo[nl], T.hi[nl]);
+        ++nl;
     }
-    if (nl < 3) return;
-    float4 llo[kTreeletLeaves], lhi[kTreeletLeaves];
-    uint32_t lcnt[kTreeletLeaves];
-    float area[1 << kTreeletLeaves], copt[1 << kTreeletLeaves];
-    uint8_t part[1 << kTreeletLeaves];
-    for (int i = 0; i < nl; ++i) {
-        llo[i] = __ldcg(&nodeLo[leaves[i]]);
-        lhi[i] = __ldcg(&nodeHi[leaves[i]]);
-        lcnt[i] = __ldcg(&leafCount[leaves[i]]);
+    T.leaves = nl;
+    if (nl < 3) return false;
+    for (uint32_t i = 0; i < nl; ++i) {
+        T.count[i] = __ldcg(&leafCount[T.node[i]]);
+        T.cost[i] = __ldcg(&cost[T.node[i]]);
     }
-    const uint32_t full = (1u << nl) - 1u;
-    for (uint32_t s = 1; s <= full; ++s) {
+    return true;
+}
+
+// The SAH-optimal partition tree of a treelet's leaves, by all 32 lanes of a warp: subsets in order of size, every
+// partition of a subset (its lowest leaf fixed on one side) spread over the lanes, the lowest cost kept by a 64-bit
+// shared-memory minimum. Ties go to the larger partition mask, as an enumeration from the largest mask down with a
+// strict comparison would choose.
+__device__ void treeletDp(const TreeletSlot& T, TreeletDp& dp, const uint8_t* bySize, uint32_t lane) {
+    const uint32_t nl = T.leaves, full = (1u << nl) - 1u;
+    for (uint32_t s = lane + 1u; s < kTreeletSubsets; s += 32u) {
+        if (s & ~full) continue;
         float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
-        for (int i = 0; i < nl; ++i)
+        for (uint32_t i = 0; i < nl; ++i)
             if (s & (1u << i)) {
-                lo = make_float4(fminf(lo.x, llo[i].x), fminf(lo.y, llo[i].y), fminf(lo.z, llo[i].z), 0.0f);
-                hi = make_float4(fmaxf(hi.x, lhi[i].x), fmaxf(hi.y, lhi[i].y), fmaxf(hi.z, lhi[i].z), 0.0f);
+                lo = boxMin(lo, T.lo[i]);
+                hi = boxMax(hi, T.hi[i]);
             }
-        area[s] = halfArea(lo, hi);
+        dp.area[s] = halfArea(lo, hi);
+        dp.best[s] = ~0ull;
         if (__popc(s) == 1) {
-            copt[s] = __ldcg(&cost[leaves[__ffs(s) - 1]]);
-            continue;
+            dp.copt[s] = T.cost[__ffs(s) - 1];
+            dp.refit[s] = T.cost[__ffs(s) - 1];
         }
-        const uint32_t low = s & (0u - s);
-        float best = INFINITY;
-        uint32_t bestP = low;
-        for (uint32_t p = (s - 1u) & s; p > 0u; p = (p - 1u) & s) {
-            if (!(p & low)) continue;
-            float c = copt[p] + copt[s ^ p];
-            if (c < best) {
-                best = c;
-                bestP = p;
-            }
-        }
-        copt[s] = kCostNode * area[s] + best;
-        part[s] = uint8_t(bestP);
     }
-    // rewire: internal nodes in depth-first order of the optimal partition tree (parents before children)
+    __syncwarp();
+    // 7-bit subsets of each size k start at bySize[offset[k]]: C(7, k) of them
+    const uint32_t offset[kTreeletLeaves + 1] = {0, 0, 7, 28, 63, 98, 119, 126};
+    const uint32_t number[kTreeletLeaves + 1] = {0, 7, 21, 35, 35, 21, 7, 1};
+#pragma unroll
+    for (uint32_t k = 2; k <= uint32_t(kTreeletLeaves); ++k) {
+        if (k > nl) break;
+        const uint32_t parts = (1u << (k - 1u)) - 1u, items = number[k] * parts;
+        for (uint32_t w = lane; w < items; w += 32u) {
+            const uint32_t s = bySize[offset[k] + w / parts];
+            if (s & ~full) continue;
+            const uint32_t low = s & (0u - s), p = low | depositBits(w % parts, s ^ low);
+            const float c = dp.copt[p] + dp.copt[s ^ p];
+            atomicMin(&dp.best[s], (static_cast<unsigned long long>(__float_as_uint(c)) << 32) | (255u - p));
+        }
+        __syncwarp();
+        for (uint32_t j = lane; j < number[k]; j += 32u) {
+            const uint32_t s = bySize[offset[k] + j];
+            if (s & ~full) continue;
+            const unsigned long long b = dp.best[s];
+            dp.copt[s] = kCostNode * dp.area[s] + __uint_as_float(uint32_t(b >> 32));
+            dp.part[s] = uint8_t(255u - uint32_t(b & 0xFFu));
+        }
+        __syncwarp();
+    }
+}
+
+// Rewires the treelet's internal nodes to the optimal partition tree (depth first, parents before children) and
+// refits them (children before parents). The original topology is among the candidates, so the SAH cost never rises.
+__device__ void rewireTreelet(const TreeletSlot& T, TreeletDp& dp, uint32_t* left, uint32_t* right, uint32_t* parent,
+                              float4* nodeLo, float4* nodeHi, uint32_t* leafCount, float* cost) {
+    const uint32_t nl = T.leaves, full = (1u << nl) - 1u;
     uint32_t order[kTreeletLeaves - 1], subset[kTreeletLeaves - 1];
     uint32_t stackNode[kTreeletLeaves], stackSet[kTreeletLeaves];
     int sp = 0, used = 1, no = 0;
-    stackNode[sp] = internals[0];
+    stackNode[sp] = T.internal[0];
     stackSet[sp++] = full;
     while (sp > 0) {
         --sp;
         const uint32_t node = stackNode[sp], s = stackSet[sp];
         order[no] = node;
         subset[no++] = s;
-        const uint32_t p = part[s], sides[2] = {p, s ^ p};
+        const uint32_t p = dp.part[s], sides[2] = {p, s ^ p};
         uint32_t child[2];
         for (int k = 0; k < 2; ++k) {
             if (__popc(sides[k]) == 1) {
-                child[k] = leaves[__ffs(sides[k]) - 1];
+                child[k] = T.node[__ffs(sides[k]) - 1];
             } else {
-                child[k] = internals[used++];
+                child[k] = T.internal[used++];
                 stackNode[sp] = child[k];
                 stackSet[sp++] = sides[k];
             }
@@ -426,40 +499,76 @@ __device__ void restructureTreelet(uint32_t n, uint32_t root, uint32_t* left, ui
         left[node] = child[0];
         right[node] = child[1];
     }
-    // refit children before parents
     for (int k = no - 1; k >= 0; --k) {
         const uint32_t node = order[k], s = subset[k];
         float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
         uint32_t cnt = 0;
-        for (int i = 0; i < nl; ++i)
+        for (uint32_t i = 0; i < nl; ++i)
             if (s & (1u << i)) {
-                lo = make_float4(fminf(lo.x, llo[i].x), fminf(lo.y, llo[i].y), fminf(lo.z, llo[i].z), 0.0f);
-                hi = make_float4(fmaxf(hi.x, lhi[i].x), fmaxf(hi.y, lhi[i].y), fmaxf(hi.z, lhi[i].z), 0.0f);
-                cnt += lcnt[i];
+                lo = boxMin(lo, T.lo[i]);
+                hi = boxMax(hi, T.hi[i]);
+                cnt += T.count[i];
             }
         nodeLo[node] = lo;
         nodeHi[node] = hi;
         leafCount[node] = cnt;
         const float a = halfArea(lo, hi);
-        const uint32_t l = left[node], r = right[node];
-        cost[node] = fminf(kCostNode * a + __ldcg(&cost[l]) + __ldcg(&cost[r]), kCostTri * a * float(cnt));
+        const uint32_t p = dp.part[s];
+        const float c = fminf(kCostNode * a + dp.refit[p] + dp.refit[s ^ p], kCostTri * a * float(cnt));
+        dp.refit[s] = c;
+        cost[node] = c;
     }
 }
 
-// Bottom-up pass like the refit: a node is restructured once both of its subtrees are final.
-__global__ void kTreelets(uint32_t n, uint32_t minLeaves, uint32_t* left, uint32_t* right, uint32_t* parent,
-                          float4* nodeLo, float4* nodeHi, uint32_t* leafCount, float* cost, uint32_t* flags) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    uint32_t node = __ldcg(&parent[n - 1 + k]);
-    while (node != kInvalid) {
-        __threadfence();
-        if (atomicAdd(&flags[node], 1u) == 0u) return;
-        __threadfence();
-        if (__ldcg(&leafCount[node]) >= minLeaves)
-            restructureTreelet(n, node, left, right, parent, nodeLo, nodeHi, leafCount, cost);
-        __threadfence();
-        node = __ldcg(&parent[node]);
+// Bottom-up pass like the refit: a node is restructured once both of its subtrees are final. Each round, the lanes
+// that arrive second at a node with enough leaves form their treelets at once; the warp then runs their dynamic
+// programs one after another, and the owning lane rewires each.
+__global__ void __launch_bounds__(kTreeletThreads) kTreelets(uint32_t n, uint32_t minLeaves, uint32_t* left,
+                                                             uint32_t* right, uint32_t* parent, float4* nodeLo,
+                                                             float4* nodeHi, uint32_t* leafCount, float* cost,
+                                                             uint32_t* flags) {
+    __shared__ TreeletSlot slots[kTreeletThreads];
+    __shared__ TreeletDp dps[kTreeletThreads / 32];
+    __shared__ uint8_t bySize[kTreeletSubsets];
+    // the 127 non-empty 7-bit subsets ordered by size, ascending within a size
+    for (uint32_t s = threadIdx.x + 1u; s < kTreeletSubsets; s += blockDim.x) {
+        const uint32_t start[kTreeletLeaves + 1] = {0, 0, 7, 28, 63, 98, 119, 126};
+        uint32_t rank = 0;
+        for (uint32_t t = 1; t < s; ++t) rank += __popc(t) == __popc(s) ? 1u : 0u;
+        bySize[start[__popc(s)] + rank] = uint8_t(s);
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    TreeletDp& dp = dps[threadIdx.x >> 5];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t node = k < n ? __ldcg(&parent[n - 1 + k]) : kInvalid;
+    bool active = node != kInvalid;
+    while (__any_sync(0xFFFFFFFFu, active)) {
+        bool work = false;
+        if (active) {
+            __threadfence();
+            if (atomicAdd(&flags[node], 1u) == 0u) {
+                active = false;
+            } else {
+                __threadfence();
+                work = __ldcg(&leafCount[node]) >= minLeaves &&
+                       formTreelet(n, node, left, right, nodeLo, nodeHi, leafCount, cost, slots[threadIdx.x]);
+            }
+        }
+        uint32_t pending = __ballot_sync(0xFFFFFFFFu, work);
+        __syncwarp();  // the slots formed above, visible to the whole warp
+        for (; pending != 0u; pending &= pending - 1u) {
+            const uint32_t leader = __ffs(pending) - 1u;
+            treeletDp(slots[(threadIdx.x & ~31u) + leader], dp, bySize, lane);
+            if (lane == leader)
+                rewireTreelet(slots[threadIdx.x], dp, left, right, parent, nodeLo, nodeHi, leafCount, cost);
+            __syncwarp();
+        }
+        if (active) {
+            __threadfence();
+            node = __ldcg(&parent[node]);
+            active = node != kInvalid;
+        }
     }
 }
 
@@ -861,8 +970,8 @@ cudaError_t buildBvh(const BvhBuildInput& in, BvhBuffers& out, BvhBuildStats* st
             // each pass rewires parent[] along with the children, so the next one walks the restructured tree
             for (uint32_t pass = 0; pass < in.treeletPasses; ++pass) {
                 cudaMemsetAsync(dFlags, 0, sizeof(uint32_t) * n, stream);
-                kTreelets<<<(n + b - 1) / b, b, 0, stream>>>(n, kTreeletLeaves, dLeft, dRight, dParent, dLo, dHi,
-                                                             dLeafCount, dCost, dFlags);
+                kTreelets<<<(n + kTreeletThreads - 1) / kTreeletThreads, kTreeletThreads, 0, stream>>>(
+                    n, kTreeletLeaves, dLeft, dRight, dParent, dLo, dHi, dLeafCount, dCost, dFlags);
             }
             kRootSah<<<1, 1, 0, stream>>>(dLo, dHi, dCost, dSah + 1);
         }
