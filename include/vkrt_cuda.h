@@ -236,6 +236,16 @@ int32_t vkrt_cuda_sync(VKRT_CudaContext* context, uint32_t timeoutMs);
 int32_t vkrt_cuda_read_accumulation(VKRT_CudaContext* context, float* rgba, size_t bytes);
 int32_t vkrt_cuda_read_output(VKRT_CudaContext* context, uint16_t* rgba, size_t bytes);
 
+/* Pipelined readback of the latest accumulation (same contents and size rule as vkrt_cuda_read_accumulation), an
+ * addition of this backend for frame loops that hand every frame to the host: the copy runs on the context's own
+ * copy stream once the frames queued so far are done, while the next frame renders (a frame only reads the
+ * accumulation it blends into; the frame after it, which overwrites that buffer, first waits for the copy).
+ * Returns without waiting; `rgba` must stay valid and untouched until vkrt_cuda_wait_readback returns. With pageable
+ * host memory the copy is correct but does not overlap; pinned memory (cudaHostAlloc) lets it run on a copy engine.
+ * vkrt_cuda_wait_readback waits for every readback started on the context (timeoutMs as for vkrt_cuda_sync). */
+int32_t vkrt_cuda_read_accumulation_async(VKRT_CudaContext* context, float* rgba, size_t bytes);
+int32_t vkrt_cuda_wait_readback(VKRT_CudaContext* context, uint32_t timeoutMs);
+
 int32_t vkrt_cuda_get_stats(VKRT_CudaContext* context, VKRT_CudaStats* stats);
 
 /* Denoiser features (integrator/path/loop.slang:83-111, writeback.slang:87-114): with enabled = 1, forward frames of

@@ -106,6 +106,41 @@ def test_accumulation_running_mean(built):
     assert not np.array_equal(first[..., :3], second[..., :3])
 
 
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
+def test_pipelined_readback_matches_synchronous(built, integrator):
+    """vkrt_cuda_read_accumulation_async: each frame's accumulation, copied on the context's copy stream while the
+    following frames render (the next one blending from it, the one after overwriting its buffer), equals the
+    synchronous read of the same frame in a second context; a film reset and a resize wait for copies in flight."""
+    torch = pytest.importorskip("torch")
+    scene = scenes.cornell(96, 64, spp=2)
+    frames = 5
+    expected = []
+    with RenderContext(integrator=integrator) as ctx:
+        ctx.upload_scene(scene)
+        sd = scene.scene_data.copy()
+        for f in range(frames):
+            sd["frameNumber"] = f
+            ctx.render_frame(sd)
+            expected.append(ctx.read_accumulation().copy())
+    pinned = [torch.empty((64, 96, 4), dtype=torch.float32, pin_memory=True) for _ in range(frames)]
+    with RenderContext(integrator=integrator) as ctx:
+        ctx.upload_scene(scene)
+        sd = scene.scene_data.copy()
+        for f in range(frames):
+            sd["frameNumber"] = f
+            ctx.render_frame(sd)
+            ctx.read_accumulation_async(pinned[f].numpy())
+        ctx.reset_accumulation()
+        ctx.render_frame(sd)
+        ctx.wait_readback()
+        for f in range(frames):
+            np.testing.assert_array_equal(pinned[f].numpy(), expected[f])
+        ctx.read_accumulation_async(pinned[0].numpy())
+        ctx.resize(48, 32)
+        ctx.wait_readback()
+        np.testing.assert_array_equal(pinned[0].numpy()[..., 3], 2.0)  # the frame after the reset
+
+
 def test_frame_validation(built):
     """Frames the backend cannot render as vkrt would are refused, not rendered differently: debug views, unknown
     spectral modes, spectral frames without an rgb2spec table; the context stays usable."""

@@ -176,6 +176,8 @@ EXPORTS = {
     "vkrt_cuda_render_frame": (_I32, [_V, _V]),
     "vkrt_cuda_sync": (_I32, [_V, _U32]),
     "vkrt_cuda_read_accumulation": (_I32, [_V, _V, _SZ]),
+    "vkrt_cuda_read_accumulation_async": (_I32, [_V, _V, _SZ]),
+    "vkrt_cuda_wait_readback": (_I32, [_V, _U32]),
     "vkrt_cuda_read_output": (_I32, [_V, _V, _SZ]),
     "vkrt_cuda_get_stats": (_I32, [_V, _V]),
     "vkrt_cuda_stream": (_V, [_V]),

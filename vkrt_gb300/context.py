@@ -259,6 +259,17 @@ class RenderContext:
         self._check(self.lib.vkrt_cuda_read_accumulation(self.handle, abi.ptr(out), out.nbytes), "read accumulation")
         return out
 
+    def read_accumulation_async(self, out: np.ndarray) -> None:
+        """Starts the pipelined readback of the latest accumulation into `out` (pinned host memory overlaps the copy
+        with the next frame); `out` is complete after wait_readback()."""
+        if out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("read_accumulation_async needs a C-contiguous float32 array")
+        self._check(self.lib.vkrt_cuda_read_accumulation_async(self.handle, abi.ptr(out), out.nbytes),
+                    "read accumulation async")
+
+    def wait_readback(self, timeout_ms: int = 0) -> None:
+        self._check(self.lib.vkrt_cuda_wait_readback(self.handle, timeout_ms), "wait readback")
+
     def read_output(self) -> np.ndarray:
         out = np.empty((self.height, self.width, 4), dtype=np.uint16)
         self._check(self.lib.vkrt_cuda_read_output(self.handle, abi.ptr(out), out.nbytes), "read output")

@@ -117,6 +117,10 @@ struct VKRT_CudaContext {
     DeviceArray<float4> albedo[2], normal[2];
     uint32_t width = 0, height = 0;
     int readIndex = 0;
+    // pipelined readback (vkrt_cuda_read_accumulation_async): copies of accum[b] on copyStream end at copyDone[b]
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t filmReady = nullptr, copyDone[2] = {nullptr, nullptr};
+    bool copyPending[2] = {false, false};
 
     // counters
     RenderCounters* counters = nullptr;
@@ -205,6 +209,22 @@ cudaError_t rebuildBvh(VKRT_CudaContext* c, bool afterEdit) {
     const bool treelets = c->triCount >= minTris && (!afterEdit || c->cfg.treeletsOnUpdate != 0u);
     in.treeletPasses = treelets ? (c->cfg.treeletPasses ? c->cfg.treeletPasses : 2u) : 0u;
     return buildBvh(in, c->bvh, &c->bvhStats, c->stream);
+}
+
+// Work on `stream` that writes accum[b] first waits for a pipelined readback of that buffer still in flight.
+cudaError_t awaitFilmCopy(VKRT_CudaContext* c, int b, cudaStream_t stream) {
+    if (!c->copyPending[b]) return cudaSuccess;
+    c->copyPending[b] = false;
+    return cudaStreamWaitEvent(stream, c->copyDone[b], 0);
+}
+cudaError_t awaitFilmCopies(VKRT_CudaContext* c, cudaStream_t stream) {
+    cudaError_t e = awaitFilmCopy(c, 0, stream);
+    return e != cudaSuccess ? e : awaitFilmCopy(c, 1, stream);
+}
+// before the film buffers are reallocated or freed: no copy may still read them
+cudaError_t drainFilmCopies(VKRT_CudaContext* c) {
+    c->copyPending[0] = c->copyPending[1] = false;
+    return c->copyStream ? cudaStreamSynchronize(c->copyStream) : cudaSuccess;
 }
 
 FilmBuffers filmOf(VKRT_CudaContext* c) {
@@ -440,6 +460,11 @@ void vkrt_cuda_destroy(VKRT_CudaContext* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    drainFilmCopies(c);
+    if (c->copyStream) cudaStreamDestroy(c->copyStream);
+    if (c->filmReady) cudaEventDestroy(c->filmReady);
+    for (cudaEvent_t e : c->copyDone)
+        if (e) cudaEventDestroy(e);
     c->vertices.release();
     c->indices.release();
     c->meshes.release();
@@ -763,6 +788,7 @@ int32_t vkrt_cuda_resize(VKRT_CudaContext* c, uint32_t w, uint32_t h) {
     if (w == 0 || h == 0 || uint64_t(w) * h > (1ull << 31)) return invalid(c, "film size");
     cudaSetDevice(c->device);
     size_t n = size_t(w) * h;
+    VKRT_TRY(c, drainFilmCopies(c), "film readback");
     VKRT_TRY(c, c->accum[0].reserve(n), "film");
     VKRT_TRY(c, c->accum[1].reserve(n), "film");
     VKRT_TRY(c, c->output.reserve(n), "film");
@@ -778,6 +804,7 @@ int32_t vkrt_cuda_reset_accumulation(VKRT_CudaContext* c) {
     if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
     if (!c->width) return invalid(c, "no film");
     cudaSetDevice(c->device);
+    VKRT_TRY(c, awaitFilmCopies(c, c->stream), "film readback");
     VKRT_TRY(c, launchClearFilm(c->accum[0].ptr, c->accum[1].ptr, c->output.ptr, size_t(c->width) * c->height, c->stream),
              "film clear");
     VKRT_TRY(c, clearFeatureFilms(c), "feature films");
@@ -822,6 +849,8 @@ int32_t vkrt_cuda_render_frame(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd
     int32_t v = validateFrame(c, sd);
     if (v != VKRT_CUDA_SUCCESS) return v;
     cudaSetDevice(c->device);
+    if (c->cfg.integrator != VKRT_CUDA_INTEGRATOR_WAVEFRONT)  // the batch path waits for its own contexts
+        VKRT_TRY(c, awaitFilmCopy(c, c->readIndex ^ 1, c->stream), "film readback");
     VKRT_TRY(c, cudaEventRecord(c->frameStart, c->stream), "frame timing");
     if (c->cfg.integrator == VKRT_CUDA_INTEGRATOR_WAVEFRONT) {
         VKRT_CudaContext* one[1] = {c};
@@ -974,6 +1003,7 @@ int32_t vkrt_cuda_render_batch(VKRT_CudaContext* const* contexts, const VKRT_Cud
     for (uint32_t i = 0; i < count; ++i) {
         VKRT_CudaContext* c = contexts[i];
         scenes[i] = makeWfScene(c, sds[i], spectral);
+        VKRT_TRY(c0, awaitFilmCopy(c, c->readIndex ^ 1, c0->stream), "film readback");
         // c0's stream reads this context's buffers: order it after the work already queued on its own stream
         if (c != c0) {
             VKRT_TRY(c0, cudaEventRecord(c->order, c->stream), "batch ordering");
@@ -1144,6 +1174,47 @@ int32_t vkrt_cuda_read_accumulation(VKRT_CudaContext* c, float* rgba, size_t byt
     VKRT_TRY(c, cudaMemcpyAsync(rgba, c->accum[c->readIndex].ptr, need, cudaMemcpyDeviceToHost, c->stream), "read accumulation");
     VKRT_TRY(c, cudaStreamSynchronize(c->stream), "read accumulation");
     return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_read_accumulation_async(VKRT_CudaContext* c, float* rgba, size_t bytes) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    size_t need = size_t(c->width) * c->height * sizeof(float4);
+    if (!rgba || bytes < need || !need) return invalid(c, "accumulation buffer too small");
+    cudaSetDevice(c->device);
+    if (!c->copyStream) {
+        VKRT_TRY(c, cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking), "readback stream");
+        VKRT_TRY(c, cudaEventCreateWithFlags(&c->filmReady, cudaEventDisableTiming), "readback stream");
+        for (cudaEvent_t& e : c->copyDone) VKRT_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "readback stream");
+    }
+    const int b = c->readIndex;
+    VKRT_TRY(c, cudaEventRecord(c->filmReady, c->stream), "read accumulation async");
+    VKRT_TRY(c, cudaStreamWaitEvent(c->copyStream, c->filmReady, 0), "read accumulation async");
+    VKRT_TRY(c, cudaMemcpyAsync(rgba, c->accum[b].ptr, need, cudaMemcpyDeviceToHost, c->copyStream),
+             "read accumulation async");
+    VKRT_TRY(c, cudaEventRecord(c->copyDone[b], c->copyStream), "read accumulation async");
+    c->copyPending[b] = true;
+    return VKRT_CUDA_SUCCESS;
+}
+
+int32_t vkrt_cuda_wait_readback(VKRT_CudaContext* c, uint32_t timeoutMs) {
+    if (!c) return VKRT_CUDA_ERROR_INVALID_ARGUMENT;
+    if (!c->copyStream) return VKRT_CUDA_SUCCESS;
+    cudaSetDevice(c->device);
+    if (timeoutMs == 0) {
+        VKRT_TRY(c, cudaStreamSynchronize(c->copyStream), "wait readback");
+        return VKRT_CUDA_SUCCESS;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(c->copyStream);
+        if (e == cudaSuccess) return VKRT_CUDA_SUCCESS;
+        if (e != cudaErrorNotReady) return fail(c, e, "wait readback");
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeoutMs)) {
+            c->lastError = "wait readback: timed out";
+            return VKRT_CUDA_ERROR_OPERATION_FAILED;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
 }
 
 void vkrt_cuda_default_nrc_config(VKRT_CudaNrcConfig* n) {
@@ -1383,6 +1454,7 @@ int32_t renderAdjoint(VKRT_CudaContext* c, const VKRT_CudaSceneData* sd, const f
     ap.materialGrad = c->materialGrad.ptr;
     ap.emissiveMeshMaterial = c->emissiveMeshMaterial.ptr;
     VKRT_TRY(c, cudaMemsetAsync(c->counters, 0, sizeof(RenderCounters), c->stream), "adjoint");
+    VKRT_TRY(c, awaitFilmCopies(c, c->stream), "film readback");
     if (c->cfg.integrator == VKRT_CUDA_INTEGRATOR_WAVEFRONT) {
         // a primal wavefront pass keeps each (pixel, sample) radiance, the adjoint pass replays those paths
         std::vector<WfScene> scenes(1, makeWfScene(c, *sd, false));
