@@ -47,3 +47,23 @@ def test_oracle_refuses_a_table_smaller_than_its_layout():
     s.scene_data["rgb2specSRGB"] = (8, 0, 8)
     img, _ = cpu.OracleScene(s).render(s.scene_data)
     assert np.isfinite(img).all()
+
+
+def test_clock_sampler_keeps_the_samples_of_the_timed_region(tmp_path, monkeypatch):
+    """The clock record comes from samples taken while the timed region runs: a stand-in nvidia-smi on PATH prints
+    a sample every 50 ms; start() returns once one has arrived and stop() parses the ones after it."""
+    import os
+    import time
+    import bench
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text("#!/bin/sh\nwhile true; do\n"
+                    "  echo '0, 1965, 2070, 700.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active'\n"
+                    "  sleep 0.05\ndone\n")
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", f"{tmp_path}{os.pathsep}{os.environ['PATH']}")
+    sampler = bench.ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    r = sampler.stop()
+    assert r["samples"] >= 3
+    assert r["sm_mhz"] == 1965.0 and r["sm_max_mhz"] == 2070.0 and r["reasons"] == ["sw_power_cap"]
