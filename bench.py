@@ -832,7 +832,9 @@ def run_profile_frame(args) -> dict:
         scene.scene_data["rgb2specSRGB"] = info
     if args.full_materials:
         scene = full_material_scene(scene)
+    torch.cuda.nvtx.range_push("upload")  # the BVH build, for ncu's --nvtx-include "upload/"
     ctx.upload_scene(scene)
+    torch.cuda.nvtx.range_pop()
     if args.stage_launches:
         ctx.set_wavefront_config(profileStages=1)
     if args.shade_blocks:
