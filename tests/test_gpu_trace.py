@@ -144,3 +144,9 @@ def test_bvh_build_options(built):
         ctx.upload_scene(small)
         st = ctx.stats()
         assert st["bvhSahTreelets"] == st["bvhSahLbvh"]
+    small_rays = _rays_from_camera(small, 4096, 17)
+    with RenderContext(treelet_min_triangles=1, treelet_passes=8) as ctx:  # forced: one block, most lanes idle
+        ctx.upload_scene(small)
+        st = ctx.stats()
+        assert st["bvhSahTreelets"] <= st["bvhSahLbvh"]
+        _check(small, ctx, small_rays)
