@@ -851,7 +851,8 @@ def run_profile_frame(args) -> dict:
         tw, th = (int(v) for v in args.tile.split("x"))
         ctx.set_wavefront_config(tileWidth=tw, tileHeight=th)
     if args.cache:
-        ctx.nrc_configure(enabled=1, trainingTracer=args.training_tracer)
+        ctx.nrc_configure(enabled=1, trainingTracer=args.training_tracer,
+                          **({"terminationDepth": args.cache_depth} if args.cache_depth else {}))
     stream = torch.cuda.ExternalStream(ctx.stream)
     sd = scene.scene_data.copy()
     out = {}
@@ -881,7 +882,8 @@ def run_profile_frame(args) -> dict:
     out["workload"] = {"width": args.width, "height": args.height, "spp": args.spp, "depth": args.depth,
                        "spheres": args.spheres, "triangles": scene.triangle_count, "frames": args.frames,
                        "integrator": args.integrator, "mode": "rgb" if args.rgb else "hero-spectral",
-                       "cache": args.cache, "shade_blocks": args.shade_blocks, "refill": args.refill,
+                       "cache": args.cache, "cache_depth": args.cache_depth, "shade_blocks": args.shade_blocks,
+                       "refill": args.refill,
                        "intersect_blocks": args.intersect_blocks, "ray_order": args.ray_order,
                        "full_materials": args.full_materials, "sort": args.sort, "tile": args.tile,
                        "treelets": not args.no_treelets}
@@ -914,6 +916,7 @@ def main():
     prof.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
     prof.add_argument("--rgb", action="store_true", help="RGB transport instead of hero spectral")
     prof.add_argument("--cache", action="store_true", help="render with the radiance cache (wavefront only)")
+    prof.add_argument("--cache-depth", type=int, default=0, help="bounce at which paths end in the cache (default 2)")
     prof.add_argument("--training-tracer", type=int, default=0,
                       help="cache training paths: 0 one thread per path, 1 through the wavefront stages")
     prof.add_argument("--shade-blocks", type=int, default=0, help="shade kernel residency (blocks per SM)")
