@@ -52,7 +52,7 @@ typedef struct VKRT_CudaConfig {
     uint32_t integrator;          /* VKRT_CUDA_INTEGRATOR_* */
     uint32_t treeletMinTriangles; /* BVH builds of scenes with at least this many triangles run treelet
                                      restructuring (Karras & Aila 2013: about 5% fewer node bytes per ray for
-                                     3.9 ms per pass on 1M triangles, against 3.0 ms for the whole plain build);
+                                     2.4 ms per pass on 1M triangles, against 3.0 ms for the whole plain build);
                                      0 = the default (65,536), 0xFFFFFFFF = never */
     uint32_t treeletsOnUpdate;    /* 1: rebuilds after mesh-transform edits (vkrt_cuda_update_meshes) restructure too;
                                      0 (default): they build the plain LBVH, so interactive edits stay fast */

@@ -340,14 +340,15 @@ constexpr uint32_t kTreeletThreads = 64;
 struct TreeletSlot {
     uint32_t node[kTreeletLeaves];
     uint32_t internal[kTreeletLeaves - 1];  // the treelet's internal nodes, root first
-    float4 lo[kTreeletLeaves], hi[kTreeletLeaves];
-    uint32_t count[kTreeletLeaves];
-    float cost[kTreeletLeaves];
     uint32_t leaves;
 };
 
-// One warp's dynamic program over the 127 leaf subsets of a treelet
+// One warp's dynamic program over the 127 leaf subsets of a treelet, with the treelet's leaf boxes, triangle counts
+// and SAH costs
 struct TreeletDp {
+    float4 lo[kTreeletLeaves], hi[kTreeletLeaves];
+    uint32_t count[kTreeletLeaves];
+    float cost[kTreeletLeaves];
     float area[kTreeletSubsets];
     float copt[kTreeletSubsets];
     unsigned long long best[kTreeletSubsets];  // (cost bits, 255 - partition): the lowest cost, ties to the larger partition
@@ -375,19 +376,14 @@ __device__ __forceinline__ uint32_t depositBits(uint32_t i, uint32_t mask) {
 
 // Forms the treelet rooted at `root` into the lane's slot; false when it has fewer than 3 leaves.
 __device__ bool formTreelet(uint32_t n, uint32_t root, const uint32_t* left, const uint32_t* right,
-                            const float4* nodeLo, const float4* nodeHi, const uint32_t* leafCount, const float* cost,
-                            TreeletSlot& T) {
+                            const float4* nodeLo, const float4* nodeHi, TreeletSlot& T) {
     float area[kTreeletLeaves];
     uint32_t nl = 2, ni = 1;
     T.internal[0] = root;
     T.node[0] = __ldcg(&left[root]);
     T.node[1] = __ldcg(&right[root]);
-    for (int i = 0; i < 2; ++i) {
-        T.lo[i] = __ldcg(&nodeLo[T.node[i]]);
-        T.hi[i] = __ldcg(&nodeHi[T.node[i]]);
-    }
-    area[0] = halfArea(T.lo[0], T.hi[0]);
-    area[1] = halfArea(T.lo[1], T.hi[1]);
+    area[0] = halfArea(__ldcg(&nodeLo[T.node[0]]), __ldcg(&nodeHi[T.node[0]]));
+    area[1] = halfArea(__ldcg(&nodeLo[T.node[1]]), __ldcg(&nodeHi[T.node[1]]));
     while (nl < uint32_t(kTreeletLeaves)) {
         int best = -1;
         float bestA = -1.0f;
@@ -404,42 +400,42 @@ __device__ bool formTreelet(uint32_t n, uint32_t root, const uint32_t* left, con
         const uint32_t l = __ldcg(&left[x]), r = __ldcg(&right[x]);
         T.node[best] = l;
         T.node[nl] = r;
-        T.lo[best] = __ldcg(&nodeLo[l]);
-        T.hi[best] = __ldcg(&nodeHi[l]);
-        T.lo[nl] = __ldcg(&nodeLo[r]);
-        T.hi[nl] = __ldcg(&nodeHi[r]);
-        area[best] = halfArea(T.lo[best], T.hi[best]);
-        area[nl] = halfArea(T.lo[nl], T.hi[nl]);
+        area[best] = halfArea(__ldcg(&nodeLo[l]), __ldcg(&nodeHi[l]));
+        area[nl] = halfArea(__ldcg(&nodeLo[r]), __ldcg(&nodeHi[r]));
         ++nl;
     }
     T.leaves = nl;
-    if (nl < 3) return false;
-    for (uint32_t i = 0; i < nl; ++i) {
-        T.count[i] = __ldcg(&leafCount[T.node[i]]);
-        T.cost[i] = __ldcg(&cost[T.node[i]]);
-    }
-    return true;
+    return nl >= 3;
 }
 
 // The SAH-optimal partition tree of a treelet's leaves, by all 32 lanes of a warp: subsets in order of size, every
 // partition of a subset (its lowest leaf fixed on one side) spread over the lanes, the lowest cost kept by a 64-bit
 // shared-memory minimum. Ties go to the larger partition mask, as an enumeration from the largest mask down with a
 // strict comparison would choose.
-__device__ void treeletDp(const TreeletSlot& T, TreeletDp& dp, const uint8_t* bySize, uint32_t lane) {
+__device__ void treeletDp(const TreeletSlot& T, TreeletDp& dp, const uint8_t* bySize, uint32_t lane,
+                          const float4* nodeLo, const float4* nodeHi, const uint32_t* leafCount, const float* cost) {
     const uint32_t nl = T.leaves, full = (1u << nl) - 1u;
+    if (lane < nl) {  // the leaves' boxes, counts and costs, one leaf per lane
+        const uint32_t x = T.node[lane];
+        dp.lo[lane] = __ldcg(&nodeLo[x]);
+        dp.hi[lane] = __ldcg(&nodeHi[x]);
+        dp.count[lane] = __ldcg(&leafCount[x]);
+        dp.cost[lane] = __ldcg(&cost[x]);
+    }
+    __syncwarp();
     for (uint32_t s = lane + 1u; s < kTreeletSubsets; s += 32u) {
         if (s & ~full) continue;
         float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
         for (uint32_t i = 0; i < nl; ++i)
             if (s & (1u << i)) {
-                lo = boxMin(lo, T.lo[i]);
-                hi = boxMax(hi, T.hi[i]);
+                lo = boxMin(lo, dp.lo[i]);
+                hi = boxMax(hi, dp.hi[i]);
             }
         dp.area[s] = halfArea(lo, hi);
         dp.best[s] = ~0ull;
         if (__popc(s) == 1) {
-            dp.copt[s] = T.cost[__ffs(s) - 1];
-            dp.refit[s] = T.cost[__ffs(s) - 1];
+            dp.copt[s] = dp.cost[__ffs(s) - 1];
+            dp.refit[s] = dp.cost[__ffs(s) - 1];
         }
     }
     __syncwarp();
@@ -505,9 +501,9 @@ __device__ void rewireTreelet(const TreeletSlot& T, TreeletDp& dp, uint32_t* lef
         uint32_t cnt = 0;
         for (uint32_t i = 0; i < nl; ++i)
             if (s & (1u << i)) {
-                lo = boxMin(lo, T.lo[i]);
-                hi = boxMax(hi, T.hi[i]);
-                cnt += T.count[i];
+                lo = boxMin(lo, dp.lo[i]);
+                hi = boxMax(hi, dp.hi[i]);
+                cnt += dp.count[i];
             }
         nodeLo[node] = lo;
         nodeHi[node] = hi;
@@ -552,14 +548,16 @@ __global__ void __launch_bounds__(kTreeletThreads) kTreelets(uint32_t n, uint32_
             } else {
                 __threadfence();
                 work = __ldcg(&leafCount[node]) >= minLeaves &&
-                       formTreelet(n, node, left, right, nodeLo, nodeHi, leafCount, cost, slots[threadIdx.x]);
+                       formTreelet(n, node, left, right, nodeLo, nodeHi, slots[threadIdx.x]);
             }
         }
         uint32_t pending = __ballot_sync(0xFFFFFFFFu, work);
         __syncwarp();  // the slots formed above, visible to the whole warp
+        // the leaves' data was final when the owning lane arrived: every lane reads it after a fence of its own
+        if (pending != 0u) __threadfence();
         for (; pending != 0u; pending &= pending - 1u) {
             const uint32_t leader = __ffs(pending) - 1u;
-            treeletDp(slots[(threadIdx.x & ~31u) + leader], dp, bySize, lane);
+            treeletDp(slots[(threadIdx.x & ~31u) + leader], dp, bySize, lane, nodeLo, nodeHi, leafCount, cost);
             if (lane == leader)
                 rewireTreelet(slots[threadIdx.x], dp, left, right, parent, nodeLo, nodeHi, leafCount, cost);
             __syncwarp();
