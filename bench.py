@@ -644,7 +644,7 @@ def run_ours(args) -> dict | None:
                      "note": "80 B per node visit + 48 B per triangle test of closest-hit rays / kernel time, "
                              "profiling frame; the 60 MB BVH is L2-resident, so frac > 1 is possible",
                      "ceiling": "latency and divergence, not bandwidth: in the committed small-case capture the "
-                                "kernel runs at 15% of L2 peak throughput with 13.8 of 32 lanes active per "
+                                "kernel runs at 14% of L2 peak throughput with 13.7 of 32 lanes active per "
                                 "instruction and long-scoreboard stalls first "
                                 "(profiles/kWfIntersect_icosphere1M_640x360x4spp.md)",
                      "shadow_kernel": {"kernel": "kWfShadow",
