@@ -75,6 +75,45 @@ def test_wavefront_viewport_subrect(built):
     assert (wave[:4] == 0).all() and (wave[:, :8] == 0).all()
 
 
+def test_batch_pipelined_readback(built):
+    """vkrt_cuda_read_accumulation_async on every context of a batch: the batch leader's stream waits for each
+    context's copy in flight before a batched frame overwrites that context's buffer, so every copy equals the
+    synchronous read of the same frame in a second batch."""
+    torch = pytest.importorskip("torch")
+    specs = [dict(n_spheres=20, width=48, height=32, seed=1), dict(n_spheres=30, width=64, height=40, seed=2)]
+    ss = [scenes.icosphere_field(spp=2, max_depth=5, spectral=False, env_size=(64, 32), **p) for p in specs]
+    kw = dict(rng_mode=abi.RNG_PCG32, environment_sampling=abi.ENV_IMPORTANCE)
+    frames = 4
+
+    def run(pipelined):
+        ctxs = [RenderContext(integrator=abi.INTEGRATOR_WAVEFRONT, **kw) for _ in ss]
+        try:
+            for c, s in zip(ctxs, ss):
+                c.upload_scene(s)
+            out = [[torch.empty((c.height, c.width, 4), dtype=torch.float32, pin_memory=True).numpy() for c in ctxs]
+                   for _ in range(frames)]
+            sds = np.concatenate([s.scene_data for s in ss])
+            for f in range(frames):
+                sds["frameNumber"] = f
+                render_batch(ctxs, sds)
+                for c, o in zip(ctxs, out[f]):
+                    if pipelined:
+                        c.read_accumulation_async(o)
+                    else:
+                        o[:] = c.read_accumulation()
+            for c in ctxs:
+                c.wait_readback()
+            return out
+        finally:
+            for c in ctxs:
+                c.close()
+
+    want, got = run(False), run(True)
+    for f in range(frames):
+        for g, w in zip(got[f], want[f]):
+            np.testing.assert_array_equal(g, w)
+
+
 def test_batch_of_uneven_scenes(built):
     specs = [dict(n_spheres=20, width=48, height=32, seed=1), dict(n_spheres=60, width=80, height=64, seed=2),
              dict(n_spheres=8, width=32, height=32, seed=3)]
